@@ -1,0 +1,306 @@
+#!/usr/bin/env python
+"""Benchmark: ms/frame of voxelize + mipmap + cone-trace at 1920x1080 with a
+256^3 grid (6-direction anisotropic RGBA8 mips, 9 diffuse + 1 specular + 1
+shadow cone per pixel) on a seeded synthetic scene: a closed box room (10
+triangles) plus a noise-displaced geodesic icosphere of frequency 158
+(499,280 triangles), one point light.
+
+One step = one Renderer::render() frame.  ``value`` is the device time of
+the voxelize + mip + trace stages (the metric's stages; the G-buffer raster is
+reported next to it and included in ``ms_per_step``), timed with CUDA events
+recorded on the renderer's stream; L2 is flushed (256 MB write) between timed
+frames.  ``e2e`` is the same frame through the public C ABI as a user drives
+it: host-side camera/model/light setup, render, and the read-back of the RGBA8
+frame into pinned host memory, wall-clock timed.
+
+``--impl reference`` times the CPU restatement of the reference's algorithm
+(the oracle's FP32 instantiation, every host thread) on the same workload:
+the reference itself is an OpenGL program that cannot run on these machines.
+
+Multi-GPU: the path has no exchange step; N ranks render N independent
+replicas of the frame (weak scaling), no collective on the data path.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "ms/frame 1080p@256³ (voxelize+mip+trace)"
+UNIT = "ms/frame"
+WIDTH, HEIGHT, GRID = 1920, 1080, 256
+SCENE_SEED = 2000
+CPU_ROW_STRIDE = 64
+
+
+def _peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def _dist():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle-reason samples during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 8:
+                continue
+            try:
+                sm.append(float(f[0]))
+                mx = float(f[1])
+            except ValueError:
+                continue
+            for name, v in zip(names, f[4:8]):
+                if v.lower().startswith("active"):
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def _scene():
+    from voxel_cone_tracing_gb300 import scenes
+    return scenes.scene_sphere(seed=SCENE_SEED, width=WIDTH, height=HEIGHT)
+
+
+def _oracle_params(threads):
+    from oracle import oracle as O
+    return O.Params(grid_res=GRID, width=WIDTH, height=HEIGHT, threads=threads)
+
+
+def cpu_frame_ms(scene, threads, row_stride):
+    """FP32 CPU restatement: voxelize + mip of the whole scene, cone trace of
+    every row_stride-th row, trace time scaled by row_stride."""
+    from oracle import oracle as O
+    ms = O.time_frame(scene, _oracle_params(threads), row_stride)
+    return ms[0] + ms[1] + ms[3] * row_stride, ms
+
+
+def _cpu_sample_text(row_stride):
+    return (f"FP32 C++ restatement, voxelize+mip of the full {WIDTH}x{HEIGHT}@{GRID}^3 frame, cone trace of every "
+            f"{row_stride}th pixel row (1/{row_stride} of the pixels), trace time x{row_stride}")
+
+
+def run_reference(args):
+    rank, world, _ = _dist()
+    if rank != 0:
+        return 0
+    threads = os.cpu_count() or 1
+    scene = _scene()
+    stride = CPU_ROW_STRIDE
+    for _ in range(max(args.warmup, 0)):
+        cpu_frame_ms(scene, threads, stride * 4)
+    vals = []
+    for _ in range(args.steps):
+        v, _ms = cpu_frame_ms(scene, threads, stride)
+        vals.append(v)
+    value = statistics.mean(vals)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(value, 3), "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "room + displaced icosphere (499,290 triangles), 1920x1080, 256^3 aniso RGBA8, "
+                               "9 diffuse + 1 specular + 1 shadow cone", "grid": GRID, "width": WIDTH,
+                   "height": HEIGHT, "triangles": scene.n_tris, "parallelism": "host threads"},
+        "cpu_baseline": {"value": round(value, 3), "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": _cpu_sample_text(stride)},
+        "e2e": {"value": round(value, 3), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "reference is an OpenGL 4.5 program (GLSL in the GL driver); no graphics stack exists on this "
+                "box, so its algorithm is timed as the project's CPU restatement",
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def run_ours(args):
+    rank, world, local = _dist()
+    import numpy as np
+    import torch
+
+    import __graft_entry__ as ge
+    from voxel_cone_tracing_gb300 import renderer as R
+
+    if not torch.cuda.is_available():
+        raise SystemExit("bench.py: no CUDA device (the engine has no CPU path)")
+    torch.cuda.set_device(local)
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+        pg = dist
+    ge.build()
+    scene = _scene()
+    r = R.Renderer(WIDTH, HEIGHT, grid_res=GRID)
+    ids = R.load_scene(r, scene)
+    r.set_voxel_view_dir(7, 0.0)  # the UI sets 7 unless the voxel view is on (main.cpp:300)
+    stream = torch.cuda.Stream()
+    r.set_stream(stream.cuda_stream)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+
+    def frame():
+        R.queue_scene(r, scene, ids)
+        r.render()
+
+    for _ in range(max(args.warmup, 3)):
+        frame()
+    r.synchronize()
+    if pg:
+        pg.barrier()
+    torch.cuda.synchronize()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    stages = []
+    with ClockSampler(local) as clk:
+        for k in range(args.steps):
+            with torch.cuda.stream(stream):
+                flush.zero_()          # L2 flush, outside the timed pair
+            starts[k].record(stream)
+            frame()
+            ends[k].record(stream)
+            r.synchronize()
+            stages.append(r.stage_times())
+        torch.cuda.synchronize()
+    if pg:
+        pg.barrier()
+    frame_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    vmt = [st["voxelize"] + st["mipmap"] + st["trace"] for st in stages]
+    value = statistics.mean(vmt)
+    ms_step = statistics.mean(frame_ms)
+    if pg:
+        t = torch.tensor([value, ms_step], device="cuda", dtype=torch.float64)
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        value, ms_step = float(t[0]), float(t[1])
+    mean = lambda k: statistics.mean(st[k] for st in stages)  # noqa: E731
+
+    # ---- end to end through the public API, host buffers -----------------
+    host = torch.empty((HEIGHT, WIDTH, 4), dtype=torch.uint8, pin_memory=True).numpy()
+    view, proj = np.asarray(scene.view, np.float32), np.asarray(scene.proj, np.float32)
+    e2e_steps = args.steps
+    r.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        r.set_camera_transform(view, proj)
+        for mid, model in zip(ids, scene.models):
+            r.set_model_transform(mid, model)
+        R.queue_scene(r, scene, ids)
+        r.render()
+        r.read_frame(R.FRAME_RGBA8, out=host)
+    e2e_ms = (time.perf_counter() - t0) * 1000.0 / e2e_steps
+    h2d = len(ids) * 128 + len(scene.lights) * 0  # instance records (lights travel as kernel parameters)
+    d2h = WIDTH * HEIGHT * 4 + 32
+
+    # ---- roofline of the dominant kernel (cone trace) ----------------------
+    peak, peak_kind = _peaks()
+    nmaps_levels = sum((GRID >> l) ** 3 for l in range(1, 7)) * 6
+    trace_bytes = WIDTH * HEIGHT * (32 + 4) + (GRID ** 3 + nmaps_levels) * 4
+    trace_ms = mean("trace")
+    achieved = trace_bytes / (trace_ms * 1e-3) / 1e9
+    traffic = None
+    tp = os.path.join(ROOT, "profiles", "trace_traffic.json")
+    if os.path.exists(tp):
+        with open(tp) as f:
+            traffic = json.load(f).get("dram_bytes_per_launch")
+
+    line = {
+        "metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": max(args.warmup, 3), "ms_per_step": round(ms_step, 4), "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "room + displaced icosphere (499,290 triangles), 1920x1080, 256^3 aniso RGBA8, "
+                               "9 diffuse + 1 specular + 1 shadow cone", "grid": GRID, "width": WIDTH,
+                   "height": HEIGHT, "triangles": scene.n_tris, "voxelizer": "reference raster 2x",
+                   "sampler": "texture unit", "l2": "flushed between timed frames (256 MB write)",
+                   "parallelism": f"replicas x{world}"},
+        "stages_ms": {"voxelize": round(mean("voxelize"), 4), "mipmap": round(mean("mipmap"), 4),
+                      "gbuffer": round(mean("gbuffer"), 4), "trace": round(trace_ms, 4),
+                      "frame": round(ms_step, 4)},
+        "e2e": {"value": round(e2e_ms, 4), "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "gpu_launches": int(sum(st["kernel_launches"] for st in stages)),
+        "roofline": {"kernel": "k_trace", "bound": "hbm", "achieved": round(achieved, 2), "peak": peak,
+                     "unit": "GB/s", "frac": round(achieved / peak, 5), "traffic": traffic,
+                     "peak_source": peak_kind},
+        "clocks": clk.summary(),
+    }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        v, ms = cpu_frame_ms(scene, threads, CPU_ROW_STRIDE)
+        line["cpu_baseline"] = {"value": round(v, 2), "unit": UNIT, "cores": threads, "kind": "port",
+                                "sample": _cpu_sample_text(CPU_ROW_STRIDE),
+                                "stages_ms": {"voxelize": round(ms[0], 2), "mipmap": round(ms[1], 2),
+                                              "trace": round(ms[3] * CPU_ROW_STRIDE, 2)}}
+    if rank == 0:
+        print(json.dumps(line))
+    r.close()
+    if pg:
+        pg.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,253 @@
+/*
+ * vct.h -- C ABI of the GB300 voxel cone tracing engine.
+ *
+ * Drop-in boundary for the voxelize -> mipmap -> cone-trace path of
+ * latencyhiding/voxel_cone_tracing: every entry point below replaces one
+ * method of `struct Renderer` (src/renderer.h:122-196) or one Texture3D
+ * helper (src/texture_3d.h:6-10).  Plain C types only; matrices are
+ * column-major float[16] exactly as glm::mat4 stores them; GL object names
+ * become opaque handles.  include/vct_renderer.hpp wraps this ABI in a C++
+ * `Renderer` with the reference's method names and signatures.
+ *
+ * All GPU work of a renderer runs on one CUDA stream (its own, or one set
+ * with vct_set_stream).  vct_render() only enqueues work; the read-back
+ * calls and vct_synchronize() wait for it.  A renderer is not thread-safe,
+ * like the reference (single GL context thread).
+ */
+#ifndef VCT_H
+#define VCT_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------ types ---- */
+
+/* model_id_t / shader_id_t / material_id_t are size_t (renderer.h:23-25). */
+typedef uint64_t vct_model_id;
+typedef uint64_t vct_shader_id;
+typedef uint64_t vct_material_id;
+/* INVALID_ID (~0), renderer.h:22. */
+#define VCT_INVALID_ID (~(uint64_t)0)
+
+/* point_light_t, renderer.h:87-92 (28 bytes). */
+typedef struct {
+  float position[3];
+  float color[3];
+  float intensity;
+} vct_point_light;
+
+/* material_data_t, renderer.h:94-120 (packed, 128 bytes). */
+typedef struct {
+  float ambient[4];
+  float diffuse[4];
+  float specular[4];
+  float transmittance[4];
+  float emission[3];
+  float shininess;
+  float ior;
+  float dissolve;
+  int32_t illum;
+  float roughness;
+  float metallic;
+  float sheen;
+  float clearcoat_thickness;
+  float clearcoat_roughness;
+  float anisotropy;
+  float anisotropy_rotation;
+  float pad[2];
+} vct_material_data;
+
+/* vert_data_t, renderer.cpp:23-35 (packed, 32 bytes). */
+typedef struct {
+  float pos[3];
+  float norm[3];
+  float tex[2];
+} vct_vert_data;
+
+/* One draw object of a model: a run of indices drawn with one material
+ * (draw_obj_t, renderer.h:57-64; built in renderer.cpp:519-556). */
+typedef struct {
+  uint32_t first_index;
+  uint32_t index_count;
+  uint32_t material_id;
+} vct_draw_obj;
+
+typedef enum {
+  VCT_OK = 0,
+  VCT_ERR_INVALID_VALUE = 1,   /* bad argument (size, resolution, pointer) */
+  VCT_ERR_INVALID_ID = 2,      /* unknown model / material / texture id    */
+  VCT_ERR_CUDA = 3,            /* CUDA runtime error (see vct_last_error)   */
+  VCT_ERR_OUT_OF_MEMORY = 4,
+  VCT_ERR_IO = 5,              /* file could not be read / parsed          */
+  VCT_ERR_UNSUPPORTED = 6,
+  VCT_ERR_NO_DEVICE = 7
+} vct_status;
+
+enum { VCT_VOX_REF_RASTER2X = 0, VCT_VOX_CONSERVATIVE = 1 };
+enum { VCT_MIP_ANISO = 0, VCT_MIP_ISO = 1 };
+enum { VCT_STORAGE_RGBA8 = 0, VCT_STORAGE_RGBA16F = 1 };
+enum { VCT_SAMPLER_HW = 0, VCT_SAMPLER_EXACT = 1 };
+enum { VCT_CONES_REF9 = 0, VCT_CONES_SIX60 = 1 };
+enum { VCT_FRAME_RGBA8 = 0, VCT_FRAME_RGBA32F = 1 };
+
+/* Engine settings the reference hard-codes (7 mip levels, renderer.cpp:186;
+ * 6-direction mips, mipmap.comp; 9 diffuse cones, voxel_cone_tracing.frag
+ * :168-196) plus the engine's own choices. */
+typedef struct {
+  int32_t grid_res;     /* initial set_grid_resolution (reference: 128)    */
+  int32_t vox_mode;     /* VCT_VOX_*: coverage rule of the voxelizer        */
+  int32_t mip_mode;     /* VCT_MIP_*                                        */
+  int32_t storage;      /* VCT_STORAGE_*: texel format of the voxel maps    */
+  int32_t sampler;      /* VCT_SAMPLER_*: texture-unit or FP32 filtering    */
+  int32_t cone_set;     /* VCT_CONES_*                                      */
+  int32_t keep_counts;  /* keep per-voxel contribution counts (debug)       */
+  int32_t keep_float_frame; /* also write the unclamped RGBA32F frame       */
+  int32_t reserved[8];
+} vct_config;
+
+typedef struct vct_renderer vct_renderer;
+
+/* Per-stage device times of the last rendered frame, milliseconds. */
+typedef struct {
+  float voxelize;   /* clear + bin + voxelize level 0                     */
+  float mipmap;     /* levels 1..L-1                                       */
+  float gbuffer;    /* forward raster + attribute resolve                  */
+  float trace;      /* cone-trace shading                                  */
+  float total;      /* first to last event of the frame                    */
+  uint32_t kernel_launches; /* engine kernels launched for the frame       */
+} vct_stage_times;
+
+/* --------------------------------------------------- error reporting --- */
+
+/* Message of the last failing call on this thread ("" if none). */
+const char* vct_last_error(void);
+const char* vct_status_string(vct_status s);
+
+/* ------------------------------------------------ Renderer lifetime ---- */
+
+void vct_config_default(vct_config* cfg);
+
+/* Renderer::Renderer(int width, int height), renderer.cpp:100-147.
+ * cfg may be NULL (defaults). */
+vct_status vct_renderer_create(int32_t width, int32_t height, const vct_config* cfg,
+                               vct_renderer** out);
+/* Renderer::~Renderer, renderer.cpp:149-165. */
+void vct_renderer_destroy(vct_renderer* r);
+
+/* ----------------------------------------------------- resources ------- */
+
+/* Renderer::load_model, renderer.cpp:407-603, with the OBJ already parsed:
+ * vertices, u32 indices and draw-object runs are copied to the device.
+ * Writes the new model id to *out (VCT_INVALID_ID on failure). */
+vct_status vct_load_mesh(vct_renderer* r, const vct_vert_data* verts, uint32_t n_verts,
+                         const uint32_t* indices, uint32_t n_indices,
+                         const vct_draw_obj* objs, uint32_t n_objs, vct_model_id* out);
+/* Renderer::load_model(const char*), renderer.cpp:407-603: parses a
+ * Wavefront OBJ (+ MTL) file.  Returns VCT_INVALID_ID on failure. */
+vct_model_id vct_load_model(vct_renderer* r, const char* filename);
+/* Renderer::load_shader, renderer.cpp:605-641.  GLSL programs do not exist
+ * here; kept for source compatibility, returns a new id and does nothing. */
+vct_shader_id vct_load_shader(vct_renderer* r, const char* vertex_shader_name,
+                              const char* fragment_shader_name,
+                              const char* geometry_shader_name);
+/* Renderer::add_material, renderer.cpp:653-665. */
+vct_material_id vct_add_material(vct_renderer* r, const vct_material_data* material_data);
+/* Renderer::upload_material_data, renderer.cpp:643-651. */
+vct_status vct_upload_material_data(vct_renderer* r, const vct_material_data* material_data,
+                                    vct_material_id material_id);
+/* Renderer::set_model_material, renderer.cpp:667-677. */
+vct_status vct_set_model_material(vct_renderer* r, vct_material_id material_id,
+                                  vct_model_id model_id);
+/* Renderer::get_model_dimensions, renderer.cpp:173-176. */
+vct_status vct_get_model_dimensions(vct_renderer* r, vct_model_id model, float out[3]);
+/* Renderer::get_material, renderer.cpp:230-233: copies the material data. */
+vct_status vct_get_material(vct_renderer* r, vct_material_id material_id,
+                            vct_material_data* out);
+
+/* ------------------------------------------------------- settings ------ */
+
+/* Renderer::set_grid_resolution, renderer.cpp:178-188 (power of two,
+ * 8..1024; levels = min(7, log2(res)+1)). */
+vct_status vct_set_grid_resolution(vct_renderer* r, uint32_t res);
+/* Renderer::set_grid_size, renderer.cpp:190-193 (cube_size). */
+vct_status vct_set_grid_size(vct_renderer* r, float size);
+/* Renderer::set_camera_transform, renderer.cpp:167-171. */
+vct_status vct_set_camera_transform(vct_renderer* r, const float lookat[16],
+                                    const float projection[16]);
+/* Renderer::set_model_transform, renderer.cpp:225-228. */
+vct_status vct_set_model_transform(vct_renderer* r, vct_model_id model_id,
+                                   const float model_matrix[16]);
+/* Renderer::set_rendering_phases, renderer.cpp:195-201. */
+vct_status vct_set_rendering_phases(vct_renderer* r, int32_t direct, int32_t diffuse,
+                                    int32_t specular, int32_t shadow);
+/* Renderer::set_voxel_view_dir, renderer.cpp:203-207 (dir < 7 shows map
+ * `dir` at `lod`; the constructor default is 0, like the reference). */
+vct_status vct_set_voxel_view_dir(vct_renderer* r, int32_t dir, float lod);
+
+/* --------------------------------------------------------- frame ------- */
+
+/* Renderer::queue_model, renderer.cpp:209-218 (captures the model matrix;
+ * unknown ids are ignored, as in the reference). */
+vct_status vct_queue_model(vct_renderer* r, vct_model_id model_id);
+/* Renderer::queue_point_light, renderer.cpp:220-223. */
+vct_status vct_queue_point_light(vct_renderer* r, const vct_point_light* light);
+/* Renderer::render, renderer.cpp:392-405: voxelize, mipmap, G-buffer,
+ * cone-trace; clears the queues.  Enqueued on the renderer's stream. */
+vct_status vct_render(vct_renderer* r);
+
+/* --------------------------------------- streams, timing, read-back ---- */
+
+/* Use `stream` (a cudaStream_t) for all further work; NULL restores the
+ * renderer's own stream. */
+vct_status vct_set_stream(vct_renderer* r, void* stream);
+vct_status vct_synchronize(vct_renderer* r);
+vct_status vct_get_stage_times(vct_renderer* r, vct_stage_times* out);
+/* The presented frame, W*H texels, row 0 = bottom (glReadPixels order).
+ * VCT_FRAME_RGBA8: 4 bytes per pixel; VCT_FRAME_RGBA32F: 16 bytes (needs
+ * keep_float_frame).  dst is host memory. */
+vct_status vct_read_frame(vct_renderer* r, void* dst, int32_t format);
+/* Device pointer of the RGBA8 frame (valid until the next resize). */
+vct_status vct_frame_device_ptr(vct_renderer* r, void** out);
+/* Voxel map texels of `level` (0 = the shared level 0) of map 0..5
+ * (-x,+x,-y,+y,-z,+z; iso mode: map 0).  (N>>level)^3 texels, x fastest,
+ * 4 bytes (RGBA8) or 8 bytes (RGBA16F) each. */
+vct_status vct_read_voxels(vct_renderer* r, int32_t level, int32_t map, void* dst);
+/* Per-voxel contribution counts of the last frame (N^3 u32; keep_counts). */
+vct_status vct_read_voxel_counts(vct_renderer* r, uint32_t* dst);
+/* G-buffer of the last frame: visible triangle id (0xffffffff = none; ids
+ * count queued triangles in queue order), world position, interpolated
+ * world normal, material id.  Any pointer may be NULL. */
+vct_status vct_read_gbuffer(vct_renderer* r, uint32_t* tri_id, float* pos, float* nrm,
+                            uint32_t* mat);
+/* Grid resolution and mip level count currently in use. */
+vct_status vct_get_grid(vct_renderer* r, int32_t* res, int32_t* levels);
+
+/* ------------------------------------------------------- Texture3D ----- */
+
+typedef uint32_t vct_tex3d;   /* 0 = no texture, like a GL name */
+
+/* create_tex_3d, texture_3d.cpp:3-25: RGBA8, `levels` mip levels,
+ * clamp-to-border, trilinear mip filtering. 0 on failure. */
+vct_tex3d vct_create_tex_3d(int32_t width, int32_t height, int32_t depth, int32_t levels);
+/* destroy_tex_3d, texture_3d.cpp:27-30. */
+void vct_destroy_tex_3d(vct_tex3d tex);
+/* activate_tex_3d, texture_3d.cpp:32-37: texture-unit binding has no
+ * counterpart (kernels take texture objects); validates the handle. */
+vct_status vct_activate_tex_3d(uint32_t program, vct_tex3d tex, uint32_t unit);
+/* clear_tex_3d, texture_3d.cpp:39-44: fills level 0 with clear_color. */
+vct_status vct_clear_tex_3d(vct_tex3d tex, const float clear_color[4]);
+/* mip_tex_3d, texture_3d.cpp:46-51 (glGenerateMipmap): levels 1.. as the
+ * 2x2x2 box mean of the level below. */
+vct_status vct_mip_tex_3d(vct_tex3d tex);
+/* Host <-> level copies (glTexSubImage3D / glGetTexImage counterparts). */
+vct_status vct_tex3d_upload(vct_tex3d tex, int32_t level, const void* rgba8);
+vct_status vct_tex3d_download(vct_tex3d tex, int32_t level, void* rgba8);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* VCT_H */

@@ -1,0 +1,250 @@
+"""ctypes binding of the CPU oracle (oracle/vct_oracle.cpp).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, ``__graft_entry__.smoke()``
+and the CPU-baseline leg of ``bench.py``, as the checker or the timed CPU
+restatement -- never by the product.  Parity unpinned (the reference has no
+golden vectors and cannot run here); see vct_oracle.cpp.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "liboracle_vct.so")
+SRC = os.path.join(_HERE, "vct_oracle.cpp")
+
+VOX_REF_RASTER2X, VOX_CONSERVATIVE = 0, 1
+MIP_ANISO, MIP_ISO = 0, 1
+CONES_REF9, CONES_SIX60 = 0, 1
+
+
+def build(force: bool = False) -> str:
+    """Compile the oracle with g++ (no -march flags, no FMA contraction, so
+    x86-64 and aarch64 give identical coverage decisions)."""
+    if not force and os.path.exists(LIB_PATH) and os.path.getmtime(LIB_PATH) >= max(
+            os.path.getmtime(SRC), os.path.getmtime(os.path.join(_HERE, "vct_oracle.h"))):
+        return LIB_PATH
+    tmp = LIB_PATH + f".tmp{os.getpid()}"
+    subprocess.check_call(["g++", "-O3", "-std=c++17", "-fPIC", "-shared", "-pthread",
+                           "-ffp-contract=off", "-fno-fast-math", "-o", tmp, SRC])
+    os.replace(tmp, LIB_PATH)
+    return LIB_PATH
+
+
+class _Light(C.Structure):
+    _fields_ = [("position", C.c_float * 3), ("color", C.c_float * 3), ("intensity", C.c_float)]
+
+
+class _Instance(C.Structure):
+    _fields_ = [("verts", C.c_void_p), ("indices", C.c_void_p), ("tri_material", C.c_void_p),
+                ("n_verts", C.c_uint32), ("n_tris", C.c_uint32), ("model", C.c_float * 16)]
+
+
+class _Scene(C.Structure):
+    _fields_ = [("instances", C.c_void_p), ("materials", C.c_void_p), ("lights", C.c_void_p),
+                ("n_instances", C.c_uint32), ("n_materials", C.c_uint32), ("n_lights", C.c_uint32),
+                ("cube_size", C.c_float), ("view", C.c_float * 16), ("proj", C.c_float * 16)]
+
+
+class _Params(C.Structure):
+    _fields_ = [("grid_res", C.c_int32), ("levels", C.c_int32), ("vox_mode", C.c_int32),
+                ("mip_mode", C.c_int32), ("width", C.c_int32), ("height", C.c_int32),
+                ("enable_direct", C.c_int32), ("enable_diffuse", C.c_int32),
+                ("enable_specular", C.c_int32), ("enable_shadow", C.c_int32),
+                ("view_voxel_dir", C.c_int32), ("view_voxel_lod", C.c_float),
+                ("cone_set", C.c_int32), ("threads", C.c_int32)]
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = C.CDLL(LIB_PATH)
+        P = C.c_void_p
+        L.orc_chain_texels.restype = C.c_uint64
+        L.orc_chain_texels.argtypes = [C.c_int32, C.c_int32]
+        for f in ("orc_voxelize", "orc_voxelize_f32"):
+            getattr(L, f).restype = C.c_int64
+            getattr(L, f).argtypes = [P, P, P, P]
+        L.orc_mipmap.argtypes = [P, P, P]
+        L.orc_gbuffer.argtypes = [P, P, P, P, P, P]
+        for f in ("orc_trace", "orc_trace_f32"):
+            getattr(L, f).argtypes = [P, P, P, P, P, P, P, P, C.c_int32, P]
+        L.orc_texture_lod.argtypes = [P, P, P, C.c_int32, P, C.c_double, P]
+        L.orc_trace_cone.argtypes = [P, P, P, P, P, C.c_double, C.c_double, P, P]
+        L.orc_time_frame.argtypes = [P, P, C.c_int32, P]
+        _lib = L
+    return _lib
+
+
+def levels_for(n: int) -> int:
+    return min(7, int(np.log2(n)) + 1)
+
+
+def chain_texels(n: int, levels: int) -> int:
+    return int(lib().orc_chain_texels(n, levels))
+
+
+class Params:
+    """Oracle parameters; field names follow the renderer's settings."""
+
+    def __init__(self, grid_res=64, width=64, height=64, vox_mode=VOX_REF_RASTER2X, mip_mode=MIP_ANISO,
+                 enable_direct=True, enable_diffuse=True, enable_specular=True, enable_shadow=True,
+                 view_voxel_dir=7, view_voxel_lod=0.0, cone_set=CONES_REF9, threads=None, levels=None):
+        self.grid_res, self.width, self.height = grid_res, width, height
+        self.levels = levels if levels is not None else levels_for(grid_res)
+        self.vox_mode, self.mip_mode = vox_mode, mip_mode
+        self.enable_direct, self.enable_diffuse = enable_direct, enable_diffuse
+        self.enable_specular, self.enable_shadow = enable_specular, enable_shadow
+        self.view_voxel_dir, self.view_voxel_lod = view_voxel_dir, view_voxel_lod
+        self.cone_set = cone_set
+        self.threads = threads if threads else (os.cpu_count() or 1)
+
+    def c(self) -> _Params:
+        p = _Params()
+        for name, _ in _Params._fields_:
+            setattr(p, name, type(getattr(p, name))(getattr(self, name)))
+        return p
+
+    @property
+    def n_maps(self) -> int:
+        return 1 if self.mip_mode == MIP_ISO else 6
+
+
+class _SceneHold:
+    """Keeps the numpy buffers of a ctypes scene alive."""
+
+    def __init__(self, scene):
+        self.keep = []
+        n = len(scene.meshes)
+        insts = (_Instance * max(n, 1))()
+        for k, (mesh, model) in enumerate(zip(scene.meshes, scene.models)):
+            v = np.ascontiguousarray(mesh.verts, np.float32)
+            ix = np.ascontiguousarray(mesh.indices, np.uint32)
+            tm = np.ascontiguousarray(mesh.tri_material(), np.uint32)
+            self.keep += [v, ix, tm]
+            insts[k].verts, insts[k].indices, insts[k].tri_material = v.ctypes.data, ix.ctypes.data, tm.ctypes.data
+            insts[k].n_verts, insts[k].n_tris = v.shape[0], ix.shape[0]
+            insts[k].model[:] = [float(x) for x in np.asarray(model, np.float32)]
+        mats = np.ascontiguousarray(scene.materials)
+        lights = np.ascontiguousarray(scene.lights)
+        self.keep += [insts, mats, lights]
+        s = _Scene()
+        s.instances = C.addressof(insts)
+        s.materials, s.lights = mats.ctypes.data, lights.ctypes.data
+        s.n_instances, s.n_materials, s.n_lights = n, mats.shape[0], lights.shape[0]
+        s.cube_size = float(scene.cube_size)
+        s.view[:] = [float(x) for x in scene.view]
+        s.proj[:] = [float(x) for x in scene.proj]
+        self.s = s
+
+    @property
+    def ptr(self):
+        return C.addressof(self.s)
+
+
+def _ptr(a):
+    return a.ctypes.data if a is not None else None
+
+
+def voxelize(scene, params: Params, fp32: bool = False):
+    """-> (level0 uint8 (N,N,N,4) indexed [z,y,x], counts uint32 (N,N,N), rejected)."""
+    n = params.grid_res
+    l0 = np.zeros((n, n, n, 4), np.uint8)
+    cnt = np.zeros((n, n, n), np.uint32)
+    sh, pc = _SceneHold(scene), params.c()
+    f = lib().orc_voxelize_f32 if fp32 else lib().orc_voxelize
+    rej = f(sh.ptr, C.addressof(pc), _ptr(l0), _ptr(cnt))
+    return l0, cnt, int(rej)
+
+
+def mipmap(params: Params, level0: np.ndarray) -> np.ndarray:
+    """-> chains uint8 (n_maps, chain_texels, 4)."""
+    l0 = np.ascontiguousarray(level0, np.uint8)
+    ch = np.zeros((params.n_maps, chain_texels(params.grid_res, params.levels), 4), np.uint8)
+    pc = params.c()
+    lib().orc_mipmap(C.addressof(pc), _ptr(l0), _ptr(ch))
+    return ch
+
+
+def chain_level(chains: np.ndarray, n: int, level: int, map_index: int = 0) -> np.ndarray:
+    """View of one level (>= 1) of one map as (s, s, s, 4) indexed [z,y,x]."""
+    off = 0
+    for k in range(1, level):
+        off += (n >> k) ** 3
+    s = n >> level
+    return chains[map_index, off:off + s ** 3].reshape(s, s, s, 4)
+
+
+def gbuffer(scene, params: Params) -> dict:
+    w, h = params.width, params.height
+    out = dict(tri_id=np.zeros((h, w), np.uint32), pos=np.zeros((h, w, 3)), nrm=np.zeros((h, w, 3)),
+               mat=np.zeros((h, w), np.uint32))
+    sh, pc = _SceneHold(scene), params.c()
+    lib().orc_gbuffer(sh.ptr, C.addressof(pc), _ptr(out["tri_id"]), _ptr(out["pos"]), _ptr(out["nrm"]),
+                      _ptr(out["mat"]))
+    return out
+
+
+def trace(scene, params: Params, level0, chains, gb: dict, row_stride: int = 1, fp32: bool = False):
+    """-> float32 frame (H, W, 4), row 0 = bottom.  Untraced rows stay 0."""
+    w, h = params.width, params.height
+    out = np.zeros((h, w, 4), np.float32)
+    sh, pc = _SceneHold(scene), params.c()
+    l0 = np.ascontiguousarray(level0, np.uint8)
+    ch = np.ascontiguousarray(chains, np.uint8)
+    tid = np.ascontiguousarray(gb["tri_id"], np.uint32)
+    pos = np.ascontiguousarray(gb["pos"], np.float64)
+    nrm = np.ascontiguousarray(gb["nrm"], np.float64)
+    mat = np.ascontiguousarray(gb["mat"], np.uint32)
+    f = lib().orc_trace_f32 if fp32 else lib().orc_trace
+    f(sh.ptr, C.addressof(pc), _ptr(l0), _ptr(ch), _ptr(tid), _ptr(pos), _ptr(nrm), _ptr(mat),
+      int(row_stride), _ptr(out))
+    return out
+
+
+def render(scene, params: Params):
+    """Whole frame through the oracle: returns dict with every stage."""
+    l0, cnt, rej = voxelize(scene, params)
+    ch = mipmap(params, l0)
+    gb = gbuffer(scene, params)
+    frame = trace(scene, params, l0, ch, gb)
+    return dict(level0=l0, counts=cnt, rejected=rej, chains=ch, gbuffer=gb, frame=frame)
+
+
+def texture_lod(params: Params, level0, chains, map_index: int, u, lod: float) -> np.ndarray:
+    out = np.zeros(4)
+    uu = np.asarray(u, np.float64)
+    pc = params.c()
+    lib().orc_texture_lod(C.addressof(pc), _ptr(np.ascontiguousarray(level0, np.uint8)),
+                          _ptr(np.ascontiguousarray(chains, np.uint8)), map_index, _ptr(uu), float(lod),
+                          _ptr(out))
+    return out
+
+
+def trace_cone(params: Params, level0, chains, origin, direction, aperture, max_dist):
+    out = np.zeros(4)
+    steps = C.c_int32(0)
+    o = np.asarray(origin, np.float64)
+    d = np.asarray(direction, np.float64)
+    pc = params.c()
+    lib().orc_trace_cone(C.addressof(pc), _ptr(np.ascontiguousarray(level0, np.uint8)),
+                         _ptr(np.ascontiguousarray(chains, np.uint8)), _ptr(o), _ptr(d), float(aperture),
+                         float(max_dist), _ptr(out), C.addressof(steps))
+    return out, steps.value
+
+
+def time_frame(scene, params: Params, row_stride: int) -> np.ndarray:
+    """Timed FP32 CPU restatement: ms for voxelize, mip, gbuffer, trace (the
+    trace over rows y % row_stride == 0 only)."""
+    ms = np.zeros(4)
+    sh, pc = _SceneHold(scene), params.c()
+    lib().orc_time_frame(sh.ptr, C.addressof(pc), int(row_stride), _ptr(ms))
+    return ms

@@ -1,0 +1,266 @@
+// k_mipmap.cu -- the MipBuilder: replaces Renderer::filter (renderer.cpp
+// :283-314) and mipmap.comp.
+//
+// The reference dispatches one compute pass per level with a memory barrier
+// in between, and every pass re-reads the level below from memory.  Here one
+// CTA loads a B^3 region (B = 16) of the source level into shared memory once
+// and produces up to four levels of all six directional maps from it (the
+// intermediate levels never leave shared memory except for their own store).
+// Level 0 is stored once and shared by the six maps, as in the reference
+// (all six textures receive identical level-0 data, voxelize.frag:245-246).
+// A second, tiny pass builds the remaining levels (5, 6) from level 4.
+//
+// RGBA8 texels are evaluated exactly: with texels k/255 the stored value of
+// mean(alpha_blend(front, back)) (mipmap.comp:40-43,59-98) is
+// round(S / 1020) with S = sum over the four pairs of (F*255 + (255-F.a)*B)
+// per channel, ties up, clamped to 255 -- the exact real value of the GLSL
+// expression, rounded to unorm8 as imageStore does.  RGBA16F texels use FP32
+// maths and round-to-nearest-even to half.
+#include <cuda_fp16.h>
+
+#include "vct_internal.h"
+
+namespace vct {
+namespace {
+
+constexpr int kThreads = 256;
+
+// voxel_offsets, mipmap.comp:10-20.
+__constant__ int c_off[8][3] = {{1, 1, 1}, {1, 1, 0}, {1, 0, 1}, {1, 0, 0},
+                                {0, 1, 1}, {0, 1, 0}, {0, 0, 1}, {0, 0, 0}};
+// (front, back) pairs per map (0:-x 1:+x 2:-y 3:+y 4:-z 5:+z), mipmap.comp:59-98.
+__constant__ int c_pairs[6][4][2] = {
+    {{0, 4}, {1, 5}, {2, 6}, {3, 7}}, {{4, 0}, {5, 1}, {6, 2}, {7, 3}},
+    {{0, 2}, {1, 3}, {5, 7}, {4, 6}}, {{2, 0}, {3, 1}, {7, 5}, {6, 4}},
+    {{0, 1}, {2, 3}, {4, 5}, {6, 7}}, {{1, 0}, {3, 2}, {5, 4}, {7, 6}}};
+
+template <int STORAGE> struct Texel;
+template <> struct Texel<VCT_STORAGE_RGBA8> {
+  typedef uint32_t T;
+  static constexpr int kBytes = 4;
+};
+template <> struct Texel<VCT_STORAGE_RGBA16F> {
+  typedef uint2 T;
+  static constexpr int kBytes = 8;
+};
+
+__device__ __forceinline__ uint32_t ch8(uint32_t t, int c) { return (t >> (8 * c)) & 0xffu; }
+
+__device__ __forceinline__ uint32_t aniso_rgba8(const uint32_t* ch, int d) {
+  uint32_t out = 0;
+#pragma unroll
+  for (int c = 0; c < 4; ++c) {
+    uint32_t S = 0;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const uint32_t f = ch[c_pairs[d][q][0]], b = ch[c_pairs[d][q][1]];
+      S += ch8(f, c) * 255u + (255u - ch8(f, 3)) * ch8(b, c);
+    }
+    uint32_t v = (S + 510u) / 1020u;
+    out |= (v > 255u ? 255u : v) << (8 * c);
+  }
+  return out;
+}
+
+__device__ __forceinline__ uint32_t iso_rgba8(const uint32_t* ch) {
+  uint32_t out = 0;
+#pragma unroll
+  for (int c = 0; c < 4; ++c) {
+    uint32_t S = 0;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) S += ch8(ch[i], c);
+    out |= ((S + 4u) >> 3) << (8 * c);
+  }
+  return out;
+}
+
+__device__ __forceinline__ float4 h2f(uint2 t) {
+  __half2 a = *reinterpret_cast<__half2*>(&t.x), b = *reinterpret_cast<__half2*>(&t.y);
+  float2 fa = __half22float2(a), fb = __half22float2(b);
+  return make_float4(fa.x, fa.y, fb.x, fb.y);
+}
+__device__ __forceinline__ uint2 f2h(float4 v) {
+  __half2 a = __floats2half2_rn(v.x, v.y), b = __floats2half2_rn(v.z, v.w);
+  return make_uint2(*reinterpret_cast<uint32_t*>(&a), *reinterpret_cast<uint32_t*>(&b));
+}
+
+__device__ __forceinline__ uint2 aniso_rgba16f(const uint2* ch, int d) {
+  float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const float4 f = h2f(ch[c_pairs[d][q][0]]), b = h2f(ch[c_pairs[d][q][1]]);
+    const float k = 1.0f - f.w;
+    acc.x += f.x + k * b.x; acc.y += f.y + k * b.y; acc.z += f.z + k * b.z; acc.w += f.w + k * b.w;
+  }
+  return f2h(make_float4(acc.x * 0.25f, acc.y * 0.25f, acc.z * 0.25f, acc.w * 0.25f));
+}
+
+__device__ __forceinline__ uint2 iso_rgba16f(const uint2* ch) {
+  float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    const float4 v = h2f(ch[i]);
+    acc.x += v.x; acc.y += v.y; acc.z += v.z; acc.w += v.w;
+  }
+  return f2h(make_float4(acc.x * 0.125f, acc.y * 0.125f, acc.z * 0.125f, acc.w * 0.125f));
+}
+
+template <int STORAGE>
+__device__ __forceinline__ typename Texel<STORAGE>::T reduce(const typename Texel<STORAGE>::T* ch, int d, bool iso) {
+  if constexpr (STORAGE == VCT_STORAGE_RGBA8) return iso ? iso_rgba8(ch) : aniso_rgba8(ch, d);
+  else return iso ? iso_rgba16f(ch) : aniso_rgba16f(ch, d);
+}
+
+// One pass: source level `src_level` (0 = the shared level 0) -> levels
+// src_level+1 .. src_level+K of NMAPS maps, one CTA per B^3 source region.
+template <int NMAPS, bool FROM_L0, int K, int STORAGE>
+__global__ void __launch_bounds__(kThreads) k_mip(MapSet ms, int src_level) {
+  typedef typename Texel<STORAGE>::T T;
+  constexpr int B = 1 << K;
+  constexpr int B3 = B * B * B;
+  constexpr int NSRC = FROM_L0 ? 1 : NMAPS;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T* src = reinterpret_cast<T*>(smem_raw);
+  T* lvl = src + NSRC * B3;  // level buffers follow, NMAPS * (B/2)^3, (B/4)^3, ...
+  const int S = ms.N >> src_level;
+  const int nbx = S / B;
+  const int bx = blockIdx.x % nbx, by = (blockIdx.x / nbx) % nbx, bz = blockIdx.x / (nbx * nbx);
+  const int ox = bx * B, oy = by * B, oz = bz * B;
+  for (int i = threadIdx.x; i < NSRC * B3; i += kThreads) {
+    const int m = i / B3, r = i % B3;
+    const int x = r % B, y = (r / B) % B, z = r / (B * B);
+    const cudaSurfaceObject_t s = FROM_L0 ? ms.l0_surf : ms.surf[m][src_level];
+    T v;
+    surf3Dread(&v, s, (ox + x) * Texel<STORAGE>::kBytes, oy + y, oz + z);
+    src[i] = v;
+  }
+  __syncthreads();
+  const T* cur = src;
+  int cur_b = B;
+  bool cur_shared = FROM_L0;
+  T* out = lvl;
+#pragma unroll 1
+  for (int l = 1; l <= K; ++l) {
+    const int b = B >> l, b3 = b * b * b, cb3 = cur_b * cur_b * cur_b;
+    for (int i = threadIdx.x; i < NMAPS * b3; i += kThreads) {
+      const int d = i / b3, r = i % b3;
+      const int x = r % b, y = (r / b) % b, z = r / (b * b);
+      const T* base = cur + (cur_shared ? 0 : d * cb3);
+      T ch[8];
+#pragma unroll
+      for (int k = 0; k < 8; ++k)
+        ch[k] = base[((2 * z + c_off[k][2]) * cur_b + (2 * y + c_off[k][1])) * cur_b + (2 * x + c_off[k][0])];
+      const T v = reduce<STORAGE>(ch, d, NMAPS == 1);
+      out[i] = v;
+      const int dl = src_level + l;
+      surf3Dwrite(v, ms.surf[d][dl], ((ox >> l) + x) * Texel<STORAGE>::kBytes, (oy >> l) + y, (oz >> l) + z);
+    }
+    __syncthreads();
+    cur = out;
+    cur_b = b;
+    cur_shared = false;
+    out += NMAPS * b3;
+  }
+}
+
+template <int NMAPS, bool FROM_L0, int K, int STORAGE>
+cudaError_t run_pass(const MapSet& ms, int src_level, cudaStream_t st) {
+  typedef typename Texel<STORAGE>::T T;
+  constexpr int B = 1 << K;
+  constexpr int NSRC = FROM_L0 ? 1 : NMAPS;
+  size_t smem = (size_t)NSRC * B * B * B * sizeof(T);
+  for (int l = 1; l <= K; ++l) smem += (size_t)NMAPS * (B >> l) * (B >> l) * (B >> l) * sizeof(T);
+  auto kern = k_mip<NMAPS, FROM_L0, K, STORAGE>;
+  if (smem > 48 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+  }
+  const int S = ms.N >> src_level;
+  const unsigned grid = (unsigned)((S / B) * (S / B) * (S / B));
+  kern<<<grid, kThreads, smem, st>>>(ms, src_level);
+  return cudaGetLastError();
+}
+
+template <int NMAPS, bool FROM_L0, int STORAGE>
+cudaError_t run_pass_k(const MapSet& ms, int src_level, int K, cudaStream_t st) {
+  switch (K) {
+    case 1: return run_pass<NMAPS, FROM_L0, 1, STORAGE>(ms, src_level, st);
+    case 2: return run_pass<NMAPS, FROM_L0, 2, STORAGE>(ms, src_level, st);
+    case 3: return run_pass<NMAPS, FROM_L0, 3, STORAGE>(ms, src_level, st);
+    case 4: return run_pass<NMAPS, FROM_L0, 4, STORAGE>(ms, src_level, st);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+template <int NMAPS, int STORAGE>
+cudaError_t run_all(const MapSet& ms, cudaStream_t st, int* launches) {
+  const int K1 = ms.L - 1 < 4 ? ms.L - 1 : 4;
+  if (K1 < 1) return cudaSuccess;
+  cudaError_t e = run_pass_k<NMAPS, true, STORAGE>(ms, 0, K1, st);
+  if (e != cudaSuccess) return e;
+  if (launches) ++*launches;
+  int done = K1;
+  while (done < ms.L - 1) {
+    int K = ms.L - 1 - done;
+    if (K > 4) K = 4;
+    e = run_pass_k<NMAPS, false, STORAGE>(ms, done, K, st);
+    if (e != cudaSuccess) return e;
+    if (launches) ++*launches;
+    done += K;
+  }
+  return cudaSuccess;
+}
+
+// ---- Texture3D helpers (create/clear/mip of standalone RGBA8 textures) ----
+__global__ void k_fill_rgba8(cudaSurfaceObject_t s, int w, int h, int d, uchar4 v) {
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (size_t)w * h * d) return;
+  const int x = (int)(i % w), y = (int)((i / w) % h), z = (int)(i / ((size_t)w * h));
+  surf3Dwrite(v, s, x * 4, y, z);
+}
+
+// 2x2x2 box mean of the level below (glGenerateMipmap); for odd sizes the
+// children are clamped to the source extent.
+__global__ void k_box_mip_rgba8(cudaSurfaceObject_t src, int sw, int sh, int sd, cudaSurfaceObject_t dst, int dw,
+                                int dh, int dd) {
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (size_t)dw * dh * dd) return;
+  const int x = (int)(i % dw), y = (int)((i / dw) % dh), z = (int)(i / ((size_t)dw * dh));
+  uint32_t S[4] = {0, 0, 0, 0};
+  for (int k = 0; k < 8; ++k) {
+    const int cx = min(2 * x + (k & 1), sw - 1), cy = min(2 * y + ((k >> 1) & 1), sh - 1),
+              cz = min(2 * z + (k >> 2), sd - 1);
+    uchar4 v;
+    surf3Dread(&v, src, cx * 4, cy, cz);
+    S[0] += v.x; S[1] += v.y; S[2] += v.z; S[3] += v.w;
+  }
+  surf3Dwrite(make_uchar4((S[0] + 4) >> 3, (S[1] + 4) >> 3, (S[2] + 4) >> 3, (S[3] + 4) >> 3), dst, x * 4, y, z);
+}
+
+}  // namespace
+
+cudaError_t launch_mipmap(const MapSet& ms, int mip_mode, cudaStream_t st, int* launches) {
+  if (mip_mode == VCT_MIP_ISO) {
+    return ms.storage == VCT_STORAGE_RGBA8 ? run_all<1, VCT_STORAGE_RGBA8>(ms, st, launches)
+                                           : run_all<1, VCT_STORAGE_RGBA16F>(ms, st, launches);
+  }
+  return ms.storage == VCT_STORAGE_RGBA8 ? run_all<6, VCT_STORAGE_RGBA8>(ms, st, launches)
+                                         : run_all<6, VCT_STORAGE_RGBA16F>(ms, st, launches);
+}
+
+cudaError_t launch_fill_rgba8(cudaSurfaceObject_t s, int w, int h, int d, uchar4 v, cudaStream_t st) {
+  const size_t n = (size_t)w * h * d;
+  if (!n) return cudaSuccess;
+  k_fill_rgba8<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(s, w, h, d, v);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_box_mip_rgba8(cudaSurfaceObject_t src, int sw, int sh, int sd, cudaSurfaceObject_t dst, int dw,
+                                 int dh, int dd, cudaStream_t st) {
+  const size_t n = (size_t)dw * dh * dd;
+  if (!n) return cudaSuccess;
+  k_box_mip_rgba8<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(src, sw, sh, sd, dst, dw, dh, dd);
+  return cudaGetLastError();
+}
+
+}  // namespace vct

@@ -1,0 +1,311 @@
+// k_trace.cu -- the ConeTracer: replaces the per-fragment cone marching of
+// voxel_cone_tracing.frag (main :274-303) over the G-buffer.
+//
+// One thread shades one visible pixel; a 16x16 CTA covers a 16x16 pixel tile
+// (each warp a 16x2 strip) so that neighbouring lanes march neighbouring,
+// nearly parallel cones and hit the same texture-cache lines.
+//
+// Texture sampling is GL textureLod with GL_LINEAR_MIPMAP_LINEAR and
+// CLAMP_TO_BORDER(0) over levels 0..L-1 (texture_3d.cpp:10-15).  Level 0 is
+// one texture shared by the six maps (as in the reference, where all six
+// maps hold identical level-0 data), so for lambda < 1 the three per-axis
+// lookups of sample_voxel (:108-114) need one level-0 fetch:
+//   sum_k a_k [(1-f) T0 + f T1_k] = (1-f) T0 sum_k a_k + f sum_k a_k T1_k.
+// Two samplers:
+//   VCT_SAMPLER_HW    -- the texture unit filters (trilinear within a level,
+//                        linear between levels; 8-bit fixed-point weights);
+//   VCT_SAMPLER_EXACT -- FP32 trilinear / mip-linear filtering in software
+//                        from surface reads (the accuracy reference).
+#include <cuda_fp16.h>
+
+#include "vct_internal.h"
+#include "vct_math.cuh"
+
+namespace vct {
+namespace {
+
+__device__ __forceinline__ float4 f4(float x, float y, float z, float w) { return make_float4(x, y, z, w); }
+__device__ __forceinline__ float4 operator+(float4 a, float4 b) { return f4(a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w); }
+__device__ __forceinline__ float4 operator*(float4 a, float s) { return f4(a.x * s, a.y * s, a.z * s, a.w * s); }
+
+constexpr float kTan22_5 = 0.55785173935f;      // TAN_22_5 (:164), kept verbatim
+constexpr float kMaxDistance = 1.73205080757f;  // MAX_DISTANCE (:166)
+
+// ---------------------------------------------------------------- samplers --
+template <int STORAGE>
+__device__ __forceinline__ float4 fetch_texel(cudaSurfaceObject_t s, int x, int y, int z) {
+  if (STORAGE == VCT_STORAGE_RGBA8) {
+    uchar4 v;
+    surf3Dread(&v, s, x * 4, y, z, cudaBoundaryModeZero);
+    const float k = 1.0f / 255.0f;
+    return f4(v.x * k, v.y * k, v.z * k, v.w * k);
+  } else {
+    uint2 v;
+    surf3Dread(&v, s, x * 8, y, z, cudaBoundaryModeZero);
+    const float2 a = __half22float2(*reinterpret_cast<__half2*>(&v.x));
+    const float2 b = __half22float2(*reinterpret_cast<__half2*>(&v.y));
+    return f4(a.x, a.y, b.x, b.y);
+  }
+}
+
+template <int STORAGE>
+__device__ float4 trilinear_exact(const MapSet& m, int level, int map, V3 u) {
+  const int s = m.N >> level;
+  const cudaSurfaceObject_t surf = level == 0 ? m.l0_surf : m.surf[map][level];
+  const float tx = u.x * (float)s - 0.5f, ty = u.y * (float)s - 0.5f, tz = u.z * (float)s - 0.5f;
+  const float fx = floorf(tx), fy = floorf(ty), fz = floorf(tz);
+  const float ax = tx - fx, ay = ty - fy, az = tz - fz;
+  const int ix = (int)fx, iy = (int)fy, iz = (int)fz;
+  float4 acc = f4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+  for (int c = 0; c < 8; ++c) {
+    const int dx = c & 1, dy = (c >> 1) & 1, dz = c >> 2;
+    const float w = (dx ? ax : 1.0f - ax) * (dy ? ay : 1.0f - ay) * (dz ? az : 1.0f - az);
+    const int X = ix + dx, Y = iy + dy, Z = iz + dz;
+    if ((unsigned)X < (unsigned)s && (unsigned)Y < (unsigned)s && (unsigned)Z < (unsigned)s)
+      acc = acc + fetch_texel<STORAGE>(surf, X, Y, Z) * w;
+  }
+  return acc;
+}
+
+__device__ __forceinline__ bool u_sane(V3 u) {
+  return fabsf(u.x) < 1.0e6f && fabsf(u.y) < 1.0e6f && fabsf(u.z) < 1.0e6f;
+}
+
+template <int STORAGE>
+__device__ float4 texture_lod_exact(const MapSet& m, int map, V3 u, float lod) {
+  if (!u_sane(u)) return f4(0.f, 0.f, 0.f, 0.f);
+  if (!(lod > 0.0f)) return trilinear_exact<STORAGE>(m, 0, map, u);
+  const int q = m.L - 1;
+  if (lod >= (float)q) return trilinear_exact<STORAGE>(m, q, map, u);
+  const float fl = floorf(lod);
+  const int d1 = (int)fl;
+  const float f = lod - fl;
+  return trilinear_exact<STORAGE>(m, d1, map, u) * (1.0f - f) + trilinear_exact<STORAGE>(m, d1 + 1, map, u) * f;
+}
+
+// sum_k a_k * textureLod(map idx_k, u, lod), lod >= 0.
+template <int SAMPLER, bool ISO, int STORAGE>
+__device__ __forceinline__ float4 sample_voxel(const MapSet& m, V3 u, int ix, int iy, int iz, V3 ad, float lod) {
+  if (SAMPLER == VCT_SAMPLER_EXACT) {
+    if (ISO) return texture_lod_exact<STORAGE>(m, 0, u, lod) * (ad.x + ad.y + ad.z);
+    return texture_lod_exact<STORAGE>(m, ix, u, lod) * ad.x + texture_lod_exact<STORAGE>(m, iy, u, lod) * ad.y +
+           texture_lod_exact<STORAGE>(m, iz, u, lod) * ad.z;
+  }
+  if (!u_sane(u)) return f4(0.f, 0.f, 0.f, 0.f);
+  const float wsum = ad.x + ad.y + ad.z;
+  if (lod < 1.0f) {
+    const float4 t0 = tex3D<float4>(m.l0_tex, u.x, u.y, u.z);
+    if (!(lod > 0.0f)) return t0 * wsum;
+    float4 t1;
+    if (ISO) t1 = tex3DLod<float4>(m.tex[0], u.x, u.y, u.z, 0.0f) * wsum;
+    else
+      t1 = tex3DLod<float4>(m.tex[ix], u.x, u.y, u.z, 0.0f) * ad.x +
+           tex3DLod<float4>(m.tex[iy], u.x, u.y, u.z, 0.0f) * ad.y +
+           tex3DLod<float4>(m.tex[iz], u.x, u.y, u.z, 0.0f) * ad.z;
+    return t0 * ((1.0f - lod) * wsum) + t1 * lod;
+  }
+  const float l = lod - 1.0f;
+  if (ISO) return tex3DLod<float4>(m.tex[0], u.x, u.y, u.z, l) * wsum;
+  return tex3DLod<float4>(m.tex[ix], u.x, u.y, u.z, l) * ad.x + tex3DLod<float4>(m.tex[iy], u.x, u.y, u.z, l) * ad.y +
+         tex3DLod<float4>(m.tex[iz], u.x, u.y, u.z, l) * ad.z;
+}
+
+// ------------------------------------------------------------ cone march ----
+// trace_cone, voxel_cone_tracing.frag:116-147.
+template <int SAMPLER, bool ISO, int STORAGE>
+__device__ float4 trace_cone(const MapSet& m, V3 origin, V3 dir, float aperture, float max_dist) {
+  dir = normalize(dir);
+  const int ix = dir.x < 0.0f ? 0 : 1, iy = dir.y < 0.0f ? 2 : 3, iz = dir.z < 0.0f ? 4 : 5;
+  const V3 ad = vabs(dir);
+  const float cube_res = (float)m.N;
+  const float voxel_size = 1.0f / cube_res;
+  float4 acc = f4(0.f, 0.f, 0.f, 0.f);
+  float dist = 3.0f * voxel_size;
+  float diam = dist * aperture;
+  V3 sp = dir * dist + origin;
+  while (acc.w < 1.0f && dist < max_dist) {
+    const float mip = fmaxf(log2f(diam * cube_res), 0.0f);
+    const float4 s = sample_voxel<SAMPLER, ISO, STORAGE>(m, sp, ix, iy, iz, ad, mip);
+    acc = acc + s * (1.0f - acc.w);
+    const float step = fmaxf(diam * 0.5f, voxel_size);
+    dist += step;
+    diam = dist * aperture;
+    sp = dir * dist + origin;
+  }
+  return acc;
+}
+
+// tangent, :154-162.
+__device__ __forceinline__ V3 tangent(V3 n) {
+  const V3 t1 = cross(n, v3(0.f, 0.f, 1.f)), t2 = cross(n, v3(0.f, 1.f, 0.f));
+  return length(t1) > length(t2) ? normalize(t1) : normalize(t2);
+}
+__device__ __forceinline__ V3 mixv(V3 a, V3 b, float t) { return a * (1.0f - t) + b * t; }
+
+// trace_diffuse, :168-196 (9 equal-weight cones); cone set SIX60 (no
+// reference counterpart): the normal plus 5 cones 60 degrees off it in the
+// same tangent frame, aperture 2 tan(30 deg), equal weights.
+template <int SAMPLER, bool ISO, int STORAGE>
+__device__ V3 trace_diffuse(const MapSet& m, int cone_set, V3 origin, V3 n) {
+  const V3 o1 = normalize(tangent(n));
+  const V3 o2 = normalize(cross(o1, n));
+  float4 acc = f4(0.f, 0.f, 0.f, 0.f);
+  if (cone_set == VCT_CONES_SIX60) {
+    const float ap = 1.15470053838f;  // 2 tan(30 deg)
+    const V3 nn = normalize(n);
+    acc = trace_cone<SAMPLER, ISO, STORAGE>(m, origin, nn, ap, kMaxDistance);
+#pragma unroll 1
+    for (int k = 0; k < 5; ++k) {
+      float sphi, cphi;
+      sincosf(6.28318530717958648f * (float)k / 5.0f, &sphi, &cphi);
+      const V3 d = nn * 0.5f + (o1 * cphi + o2 * sphi) * 0.86602540378f;
+      acc = acc + trace_cone<SAMPLER, ISO, STORAGE>(m, origin, d, ap, kMaxDistance);
+    }
+    return v3(acc.x, acc.y, acc.z) * (1.0f / 6.0f);
+  }
+  const V3 c1 = (o1 + o2) * 0.5f, c2 = (o1 - o2) * 0.5f;
+  const V3 side[8] = {o1, -o1, o2, -o2, c1, -c1, c2, -c2};
+  acc = trace_cone<SAMPLER, ISO, STORAGE>(m, origin, n, kTan22_5, kMaxDistance);
+#pragma unroll 1
+  for (int k = 0; k < 8; ++k)
+    acc = acc + trace_cone<SAMPLER, ISO, STORAGE>(m, origin, mixv(n, side[k], 0.5f), kTan22_5, kMaxDistance);
+  return v3(acc.x, acc.y, acc.z) * (1.0f / 9.0f);
+}
+
+__device__ __forceinline__ V3 refract(V3 I, V3 N, float eta) {
+  const float d = dot(N, I);
+  const float k = 1.0f - eta * eta * (1.0f - d * d);
+  if (k < 0.0f) return v3(0.f, 0.f, 0.f);
+  return I * eta - N * (eta * d + sqrtf(k));
+}
+__device__ __forceinline__ V3 reflect(V3 I, V3 N) { return I - N * (2.0f * dot(N, I)); }
+
+__device__ __forceinline__ V3 mat3v(const float* f) { return v3(f[0], f[1], f[2]); }
+
+// direct_light, :203-246.
+template <int SAMPLER, bool ISO, int STORAGE>
+__device__ V3 direct_light(const SceneParams& sp, const MapSet& m, int enable_shadow, const vct_material_data& mat,
+                           V3 pos, V3 nrm, V3 view_dir) {
+  V3 result = v3(0.f, 0.f, 0.f);
+  const int nl = min(sp.n_lights, kMaxLights);
+  for (int i = 0; i < nl; ++i) {
+    const vct_point_light& L = sp.lights[i];
+    V3 lp = v3(L.position[0] / sp.cube_size, L.position[1] / sp.cube_size, L.position[2] / sp.cube_size);
+    lp = lp * 0.5f + v3(0.5f, 0.5f, 0.5f);
+    V3 ld = lp - pos;
+    const float d = length(ld);
+    ld = normalize(ld);
+    const float cs = fmaxf(dot(nrm, ld), 0.0f);
+    const V3 lc = v3(L.color[0], L.color[1], L.color[2]) * ((1.0f / (1.0f + d * d)) * cs * L.intensity);
+    float shadow = 1.0f;
+    if (enable_shadow) shadow = fmaxf(0.0f, 1.0f - trace_cone<SAMPLER, ISO, STORAGE>(m, pos, ld, 0.1f, d).w);
+    const float lambert = fmaxf(dot(ld, nrm), 0.0f);
+    float refract_angle = 0.0f;
+    if (mat.dissolve <= 0.1f) {
+      const V3 rf = refract(view_dir, nrm, 1.0f / mat.ior);
+      refract_angle = fmaxf((1.0f - mat.dissolve) * dot(rf, ld), 0.0f);
+    }
+    const V3 hv = normalize(ld + view_dir);
+    float sa = fmaxf(dot(hv, nrm), 0.0f);
+    sa = fmaxf(sa, refract_angle);
+    const float sc = powf(sa, mat.shininess);
+    const V3 term = mat3v(mat.diffuse) * lambert + mat3v(mat.specular) * sc;
+    result = result + mulv(term, lc) * (shadow + 0.04f);
+  }
+  return result + v3(clamp01(mat.emission[0]), clamp01(mat.emission[1]), clamp01(mat.emission[2]));
+}
+
+__device__ __forceinline__ float specular_aperture(float shininess) {  // :248-255
+  const float r = sqrtf(2.0f / (shininess + 2.0f));
+  const float a = tanf(1.57079f * r);
+  return fminf(fmaxf(a, 0.0174533f), 3.14159265f);
+}
+
+__device__ __forceinline__ unsigned char unorm8(float v) {
+  return (unsigned char)__float2uint_rz(clamp01(v) * 255.0f + 0.5f);
+}
+
+template <int SAMPLER, bool ISO, int STORAGE>
+__global__ void __launch_bounds__(256) k_trace(SceneParams sp, CameraParams cp, MapSet m, TraceParams tp,
+                                               const float4* __restrict__ gb_pos, const float4* __restrict__ gb_nrm,
+                                               uchar4* __restrict__ frame, float4* __restrict__ frame_f32) {
+  const int px = blockIdx.x * 16 + (threadIdx.x & 15), py = blockIdx.y * 16 + (threadIdx.x >> 4);
+  if (px >= cp.W || py >= cp.H) return;
+  const size_t p = (size_t)py * cp.W + px;
+  float4 out = f4(0.15f, 0.25f, 0.25f, 1.0f);  // glClearColor, renderer.cpp:398
+  const float4 g0 = gb_pos[p], g1 = gb_nrm[p];
+  if (__float_as_uint(g1.w) != 0xffffffffu) {
+    const V3 world = v3(g0.x, g0.y, g0.z);
+    const V3 nrm = v3(g1.x, g1.y, g1.z);
+    const vct_material_data& mat = sp.materials[__float_as_uint(g0.w)];
+    const V3 pos = v3(world.x / sp.cube_size, world.y / sp.cube_size, world.z / sp.cube_size) * 0.5f +
+                   v3(0.5f, 0.5f, 0.5f);
+    // within_cube(pos, 0) (:278-279): a fragment outside returns without
+    // writing; the pixel keeps the clear colour.
+    if (fabsf(pos.x) < 1.0f && fabsf(pos.y) < 1.0f && fabsf(pos.z) < 1.0f) {
+      if (tp.view_voxel_dir < 7) {  // voxel debug view, :281-285
+        if (tp.view_voxel_dir >= 0 && tp.view_voxel_dir <= 5) {
+          const float lod = fmaxf(tp.view_voxel_lod, 0.0f);
+          const V3 one = v3(1.f, 0.f, 0.f);
+          const int d = ISO ? 0 : tp.view_voxel_dir;
+          out = sample_voxel<SAMPLER, ISO, STORAGE>(m, pos, d, d, d, one, lod);
+        } else {
+          out = f4(0.f, 0.f, 0.f, 0.f);
+        }
+      } else {
+        const V3 cam = v3(cp.cam_pos[0], cp.cam_pos[1], cp.cam_pos[2]);
+        const V3 view_dir = normalize(world - cam);
+        V3 fd = v3(0.f, 0.f, 0.f), fdir = v3(0.f, 0.f, 0.f), fs = v3(0.f, 0.f, 0.f);
+        if (tp.enable_diffuse)
+          fd = mulv(mat3v(mat.diffuse), trace_diffuse<SAMPLER, ISO, STORAGE>(m, tp.cone_set, pos, nrm));
+        if (tp.enable_direct)
+          fdir = direct_light<SAMPLER, ISO, STORAGE>(sp, m, tp.enable_shadow, mat, pos, nrm, view_dir);
+        const float sap = specular_aperture(mat.shininess);
+        if (tp.enable_specular) {
+          const V3 sd = normalize(reflect(-view_dir, nrm));
+          const float4 c = trace_cone<SAMPLER, ISO, STORAGE>(m, pos, sd, sap, kMaxDistance);
+          fs = mulv(mat3v(mat.specular), v3(c.x, c.y, c.z));
+        }
+        V3 f = fs + fd + fdir;
+        if ((mat.illum == 4 || mat.illum == 6 || mat.illum == 7 || mat.illum == 9) && tp.enable_specular) {
+          const V3 rd = refract(view_dir, nrm, 1.0f / mat.ior);
+          const float4 c = trace_cone<SAMPLER, ISO, STORAGE>(m, pos, rd, sap, kMaxDistance);
+          const V3 tr = mulv(mat3v(mat.transmittance), v3(c.x, c.y, c.z));
+          f = tr * (1.0f - mat.dissolve) + f * mat.dissolve;
+        }
+        out = f4(f.x, f.y, f.z, 1.0f);
+      }
+    }
+  }
+  frame[p] = make_uchar4(unorm8(out.x), unorm8(out.y), unorm8(out.z), unorm8(out.w));
+  if (frame_f32) frame_f32[p] = out;
+}
+
+template <int SAMPLER, bool ISO, int STORAGE>
+cudaError_t run(const SceneParams& sp, const CameraParams& cp, const MapSet& ms, const TraceParams& tp,
+                const float4* gb_pos, const float4* gb_nrm, uchar4* frame, float4* frame_f32, cudaStream_t st) {
+  dim3 grid((cp.W + 15) / 16, (cp.H + 15) / 16);
+  k_trace<SAMPLER, ISO, STORAGE><<<grid, 256, 0, st>>>(sp, cp, ms, tp, gb_pos, gb_nrm, frame, frame_f32);
+  return cudaGetLastError();
+}
+
+}  // namespace
+
+cudaError_t launch_trace(const SceneParams& sp, const CameraParams& cp, const MapSet& ms, const TraceParams& tp,
+                         const float4* gb_pos, const float4* gb_nrm, uchar4* frame, float4* frame_f32,
+                         cudaStream_t st, int* launches) {
+  if (launches) ++*launches;
+  const bool iso = tp.mip_mode == VCT_MIP_ISO;
+  if (tp.sampler == VCT_SAMPLER_EXACT) {
+    if (ms.storage == VCT_STORAGE_RGBA8)
+      return iso ? run<VCT_SAMPLER_EXACT, true, VCT_STORAGE_RGBA8>(sp, cp, ms, tp, gb_pos, gb_nrm, frame, frame_f32, st)
+                 : run<VCT_SAMPLER_EXACT, false, VCT_STORAGE_RGBA8>(sp, cp, ms, tp, gb_pos, gb_nrm, frame, frame_f32, st);
+    return iso ? run<VCT_SAMPLER_EXACT, true, VCT_STORAGE_RGBA16F>(sp, cp, ms, tp, gb_pos, gb_nrm, frame, frame_f32, st)
+               : run<VCT_SAMPLER_EXACT, false, VCT_STORAGE_RGBA16F>(sp, cp, ms, tp, gb_pos, gb_nrm, frame, frame_f32, st);
+  }
+  return iso ? run<VCT_SAMPLER_HW, true, VCT_STORAGE_RGBA8>(sp, cp, ms, tp, gb_pos, gb_nrm, frame, frame_f32, st)
+             : run<VCT_SAMPLER_HW, false, VCT_STORAGE_RGBA8>(sp, cp, ms, tp, gb_pos, gb_nrm, frame, frame_f32, st);
+}
+
+}  // namespace vct

@@ -1,0 +1,570 @@
+// k_voxelize.cu -- the Voxelizer: replaces voxelize.vert/.geom/.frag and the
+// level-0 clear of Renderer::voxelize (renderer.cpp:316-353).
+//
+// Pipeline (all stream-ordered, no host synchronisation):
+//   1. k_bin<false>: every queued triangle -> the 8^3-voxel bricks its
+//      (margin-expanded) box test says it may touch; per-brick counts.
+//   2. exclusive scan of the counts -> per-brick list offsets.
+//   3. k_bin<true>: scatter triangle ids into the per-brick lists.
+//   4. k_bricks: one CTA per brick.  Warps take 32 triangles at a time, set
+//      them up in shared memory, expand (triangle, sample|voxel) work items
+//      across lanes, decide coverage with the exact rule of the selected mode,
+//      shade in FP32 (voxelize.frag:208-239) and add fixed-point colour sums
+//      and counts into shared-memory accumulators.  The CTA then writes its
+//      whole brick of level 0 (empty voxels = 0, which is the clear) as RGBA8
+//      or RGBA16F through a surface -- level 0 is written exactly once.
+//
+// Coverage rules (the CPU oracle implements the same ones):
+//   REF_RASTER2X -- the reference's method: dominant-axis projection
+//     (voxelize.geom:58-82) rasterised on the 2N x 2N viewport
+//     (renderer.cpp:339-340): vertices snapped to 1/256 sample pixel,
+//     integer edge functions, top-left fill rule; sample depth = FP32
+//     barycentric interpolation, voxel = int(N*(0.5*c+0.5)) (voxelize.frag
+//     :242-243, truncation).
+//   CONSERVATIVE -- exact separating-axis triangle/box test on vertices
+//     snapped to 1/256 voxel (int64, the plane test in int128), colour at
+//     the triangle point closest to the voxel centre.
+#include <cuda_fp16.h>
+
+#include <climits>
+#include <type_traits>
+
+#include "vct_internal.h"
+#include "vct_math.cuh"
+
+namespace vct {
+namespace {
+
+constexpr int kThreads = 128;
+constexpr int kWarps = kThreads / 32;
+constexpr int kBrickVox = kBrick * kBrick * kBrick;
+constexpr float kBinMargin = 0.25f;   // voxels; >> snapping and FP32 error
+constexpr float kFix = 65535.0f;      // fixed-point scale of one contribution
+
+// ------------------------------------------------------------ triangle load --
+__device__ __forceinline__ int find_instance(const SceneParams& sp, uint32_t t) {
+  int lo = 0, hi = (int)sp.n_instances - 1;
+  while (lo < hi) {
+    int mid = (lo + hi + 1) >> 1;
+    if (sp.inst[mid].tri_base <= t) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+struct TriLoad {
+  float g[3][3];   // grid-space positions (voxelize.vert:26), FP32 fixed order
+  V3 n[3];         // normalize(NM * normal) (voxelize.vert:28)
+  uint32_t mat;
+  bool ok;
+};
+
+template <bool NORMALS>
+__device__ __forceinline__ void load_tri(const SceneParams& sp, uint32_t t, TriLoad& tl) {
+  const DevInstance& in = sp.inst[find_instance(sp, t)];
+  const uint32_t lt = t - in.tri_base;
+  tl.ok = true;
+  for (int k = 0; k < 3; ++k) {
+    const uint32_t vi = __ldg(in.indices + 3 * (size_t)lt + k);
+    const float4* vp = reinterpret_cast<const float4*>(in.verts + vi);
+    const float4 a = __ldg(vp), b = __ldg(vp + 1);
+    for (int r = 0; r < 3; ++r) {
+      float w = xform_row(in.M, r, a.x, a.y, a.z);
+      float gv = rdiv(w, sp.cube_size);
+      tl.g[k][r] = gv;
+      if (!(fabsf(gv) <= 64.0f)) tl.ok = false;
+    }
+    if (NORMALS) tl.n[k] = normalize(nm_mul(in.NM, a.w, b.x, b.y));
+  }
+  if (NORMALS) tl.mat = __ldg(sp.obj_material + __ldg(in.tri_obj + lt));
+}
+
+// ------------------------------------------------ conservative brick test --
+// Triangle / axis-aligned box overlap in FP32 (box normals, plane, 9 edge
+// axes).  Only used for binning, with boxes grown by kBinMargin, so FP32
+// rounding can only add candidates.
+__device__ bool tri_box_f32(const float v[3][3], const float c[3], const float h[3]) {
+  float u[3][3];
+  for (int k = 0; k < 3; ++k)
+    for (int d = 0; d < 3; ++d) u[k][d] = v[k][d] - c[d];
+  for (int d = 0; d < 3; ++d) {
+    float mn = fminf(u[0][d], fminf(u[1][d], u[2][d])), mx = fmaxf(u[0][d], fmaxf(u[1][d], u[2][d]));
+    if (mn > h[d] || mx < -h[d]) return false;
+  }
+  float f[3][3];
+  for (int d = 0; d < 3; ++d) {
+    f[0][d] = u[1][d] - u[0][d];
+    f[1][d] = u[2][d] - u[1][d];
+    f[2][d] = u[0][d] - u[2][d];
+  }
+  float n0 = f[0][1] * f[1][2] - f[0][2] * f[1][1];
+  float n1 = f[0][2] * f[1][0] - f[0][0] * f[1][2];
+  float n2 = f[0][0] * f[1][1] - f[0][1] * f[1][0];
+  float dd = n0 * u[0][0] + n1 * u[0][1] + n2 * u[0][2];
+  float rr = h[0] * fabsf(n0) + h[1] * fabsf(n1) + h[2] * fabsf(n2);
+  if (fabsf(dd) > rr * 1.0001f + 1e-6f) return false;
+  for (int e = 0; e < 3; ++e) {
+    const float fx = f[e][0], fy = f[e][1], fz = f[e][2];
+    float p0, p1, p2, r;
+    p0 = -fz * u[0][1] + fy * u[0][2]; p1 = -fz * u[1][1] + fy * u[1][2]; p2 = -fz * u[2][1] + fy * u[2][2];
+    r = h[1] * fabsf(fz) + h[2] * fabsf(fy);
+    if (fminf(p0, fminf(p1, p2)) > r * 1.0001f || fmaxf(p0, fmaxf(p1, p2)) < -r * 1.0001f) return false;
+    p0 = fz * u[0][0] - fx * u[0][2]; p1 = fz * u[1][0] - fx * u[1][2]; p2 = fz * u[2][0] - fx * u[2][2];
+    r = h[0] * fabsf(fz) + h[2] * fabsf(fx);
+    if (fminf(p0, fminf(p1, p2)) > r * 1.0001f || fmaxf(p0, fmaxf(p1, p2)) < -r * 1.0001f) return false;
+    p0 = -fy * u[0][0] + fx * u[0][1]; p1 = -fy * u[1][0] + fx * u[1][1]; p2 = -fy * u[2][0] + fx * u[2][1];
+    r = h[0] * fabsf(fy) + h[1] * fabsf(fx);
+    if (fminf(p0, fminf(p1, p2)) > r * 1.0001f || fmaxf(p0, fmaxf(p1, p2)) < -r * 1.0001f) return false;
+  }
+  return true;
+}
+
+template <bool FILL>
+__global__ void __launch_bounds__(256) k_bin(SceneParams sp, int N, uint32_t* __restrict__ count,
+                                             uint32_t* __restrict__ cursor, uint32_t* __restrict__ list,
+                                             uint32_t cap, FrameStatus* st) {
+  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= sp.total_tris) return;
+  TriLoad tl;
+  load_tri<false>(sp, t, tl);
+  if (!tl.ok) {
+    if (!FILL) atomicAdd(&st->rejected_tris, 1u);
+    return;
+  }
+  const float hv = 0.5f * (float)N;
+  float v[3][3];
+  for (int k = 0; k < 3; ++k)
+    for (int d = 0; d < 3; ++d) v[k][d] = (tl.g[k][d] + 1.0f) * hv;  // voxel units
+  const int nb = N / kBrick;
+  int blo[3], bhi[3];
+  for (int d = 0; d < 3; ++d) {
+    float lo = fminf(v[0][d], fminf(v[1][d], v[2][d])) - kBinMargin;
+    float hi = fmaxf(v[0][d], fmaxf(v[1][d], v[2][d])) + kBinMargin;
+    // Depth values in (-1, 0) voxel still land in voxel 0 (int() truncates).
+    if (hi <= -1.0f - kBinMargin || lo >= (float)N) return;
+    blo[d] = max(0, (int)floorf(lo / kBrick));
+    bhi[d] = min(nb - 1, (int)floorf(fmaxf(hi, 0.0f) / kBrick));
+  }
+  const bool single = blo[0] == bhi[0] && blo[1] == bhi[1] && blo[2] == bhi[2];
+  for (int bz = blo[2]; bz <= bhi[2]; ++bz)
+    for (int by = blo[1]; by <= bhi[1]; ++by)
+      for (int bx = blo[0]; bx <= bhi[0]; ++bx) {
+        if (!single) {
+          const int b3[3] = {bx, by, bz};
+          float c[3], h[3];
+          for (int d = 0; d < 3; ++d) {
+            float lo = (float)(b3[d] * kBrick) - kBinMargin - (b3[d] == 0 ? 1.0f : 0.0f);
+            float hi = (float)(b3[d] * kBrick + kBrick) + kBinMargin;
+            c[d] = 0.5f * (lo + hi);
+            h[d] = 0.5f * (hi - lo);
+          }
+          if (!tri_box_f32(v, c, h)) continue;
+        }
+        const uint32_t brick = ((uint32_t)bz * nb + by) * nb + bx;
+        if (FILL) {
+          uint32_t slot = atomicAdd(cursor + brick, 1u);
+          if (slot < cap) list[slot] = t;
+        } else {
+          atomicAdd(count + brick, 1u);
+        }
+      }
+}
+
+// ------------------------------------------------------------- shading -----
+// voxelize.frag:208-239 in FP32.
+__device__ __forceinline__ float4 voxel_color(const SceneParams& sp, const vct_material_data& m, V3 pos, V3 nrm) {
+  V3 color = v3(0.f, 0.f, 0.f);
+  const V3 nn = normalize(nrm);
+  const int nl = min(sp.n_lights, kMaxLights);
+  for (int i = 0; i < nl; ++i) {
+    const vct_point_light& L = sp.lights[i];
+    const V3 lp = v3(L.position[0] / sp.cube_size, L.position[1] / sp.cube_size, L.position[2] / sp.cube_size);
+    const V3 dl = lp - pos;
+    const V3 dir = normalize(dl);
+    const float d = length(dl);
+    const float a = 1.0f / (1.0f + d * d);  // attenuate(1, 0, 1, d)
+    const float cs = fmaxf(dot(nn, dir), 0.0f);
+    color = color + v3(L.color[0], L.color[1], L.color[2]) * (cs * a * L.intensity);
+  }
+  color = mulv(v3(m.diffuse[0], m.diffuse[1], m.diffuse[2]), color) + v3(m.emission[0], m.emission[1], m.emission[2]);
+  float alpha = 1.0f;
+  if (m.illum == 4 || m.illum == 6 || m.illum == 7 || m.illum == 9) {
+    color = mulv(color, v3(m.transmittance[0], m.transmittance[1], m.transmittance[2]));
+    alpha = m.dissolve;
+  }
+  return make_float4(clamp01(color.x), clamp01(color.y), clamp01(color.z), clamp01(alpha));
+}
+
+struct Acc {
+  uint32_t c[4][kBrickVox];
+  uint32_t n[kBrickVox];
+};
+
+__device__ __forceinline__ void accumulate(Acc& acc, int v, float4 col) {
+  atomicAdd(&acc.c[0][v], __float2uint_rn(col.x * kFix));
+  atomicAdd(&acc.c[1][v], __float2uint_rn(col.y * kFix));
+  atomicAdd(&acc.c[2][v], __float2uint_rn(col.z * kFix));
+  atomicAdd(&acc.c[3][v], __float2uint_rn(col.w * kFix));
+  atomicAdd(&acc.n[v], 1u);
+}
+
+// -------------------------------------------------- reference raster mode --
+struct SetupRef {
+  long long area;
+  int A[3], B[3];
+  float c[3];
+  float farea;
+  V3 gp[3], gn[3];
+  uint32_t mat;
+  int axis, tl;
+  int i0, ni, j0, nj;
+};
+
+// Returns the number of samples of this triangle inside the brick's columns.
+__device__ int setup_ref(const SceneParams& sp, int N, uint32_t t, const int b3[3], SetupRef& s) {
+  TriLoad tl;
+  load_tri<true>(sp, t, tl);
+  if (!tl.ok) return 0;
+  // Dominant axis, voxelize.geom:58-82 (FP32, fixed order).
+  float e1[3], e2[3];
+  for (int i = 0; i < 3; ++i) { e1[i] = rsub(tl.g[1][i], tl.g[0][i]); e2[i] = rsub(tl.g[2][i], tl.g[0][i]); }
+  const float px = fabsf(rsub(rmul(e1[1], e2[2]), rmul(e2[1], e1[2])));
+  const float py = fabsf(rsub(rmul(e1[2], e2[0]), rmul(e2[2], e1[0])));
+  const float pz = fabsf(rsub(rmul(e1[0], e2[1]), rmul(e2[0], e1[1])));
+  int axis;
+  if (pz > px && pz > py) axis = 2;
+  else if (px > py && px > pz) axis = 0;
+  else axis = 1;
+  const int ia = axis == 2 ? 0 : (axis == 0 ? 1 : 0);
+  const int ib = axis == 2 ? 1 : 2;
+  const double scale = (double)N * 256.0;
+  int idx[3] = {0, 1, 2};
+  long long A[3], B[3];
+  float c[3];
+  for (int k = 0; k < 3; ++k) {
+    A[k] = __double2ll_rn(__dmul_rn(__dadd_rn((double)tl.g[k][ia], 1.0), scale));
+    B[k] = __double2ll_rn(__dmul_rn(__dadd_rn((double)tl.g[k][ib], 1.0), scale));
+    c[k] = tl.g[k][axis];
+  }
+  long long area = (A[1] - A[0]) * (B[2] - B[0]) - (B[1] - B[0]) * (A[2] - A[0]);
+  if (area == 0) return 0;
+  if (area < 0) {
+    long long tA = A[1]; A[1] = A[2]; A[2] = tA;
+    long long tB = B[1]; B[1] = B[2]; B[2] = tB;
+    float tc = c[1]; c[1] = c[2]; c[2] = tc;
+    idx[1] = 2; idx[2] = 1;
+    area = -area;
+  }
+  // Sample window: the triangle's sample bbox inside the brick's columns.
+  const long long minA = min(A[0], min(A[1], A[2])), maxA = max(A[0], max(A[1], A[2]));
+  const long long minB = min(B[0], min(B[1], B[2])), maxB = max(B[0], max(B[1], B[2]));
+  const int sa0 = 2 * kBrick * b3[ia], sb0 = 2 * kBrick * b3[ib];
+  const long long i0 = max((long long)sa0, ceil_div(minA - 128, 256));
+  const long long i1 = min((long long)sa0 + 2 * kBrick - 1, floor_div(maxA - 128, 256));
+  const long long j0 = max((long long)sb0, ceil_div(minB - 128, 256));
+  const long long j1 = min((long long)sb0 + 2 * kBrick - 1, floor_div(maxB - 128, 256));
+  if (i1 < i0 || j1 < j0) return 0;
+  s.area = area;
+  s.farea = __ll2float_rn(area);
+  for (int k = 0; k < 3; ++k) {
+    s.A[k] = (int)A[k];
+    s.B[k] = (int)B[k];
+    s.c[k] = c[k];
+    const int o = idx[k];
+    s.gp[k] = v3(tl.g[o][0], tl.g[o][1], tl.g[o][2]);
+    s.gn[k] = tl.n[o];
+  }
+  s.tl = (top_left(A[1], B[1], A[2], B[2]) ? 1 : 0) | (top_left(A[2], B[2], A[0], B[0]) ? 2 : 0) |
+         (top_left(A[0], B[0], A[1], B[1]) ? 4 : 0);
+  s.mat = tl.mat;
+  s.axis = axis;
+  s.i0 = (int)i0; s.ni = (int)(i1 - i0 + 1);
+  s.j0 = (int)j0; s.nj = (int)(j1 - j0 + 1);
+  return s.ni * s.nj;
+}
+
+__device__ __forceinline__ void item_ref(const SceneParams& sp, int N, const int b3[3], const SetupRef& s, int local,
+                                         Acc& acc) {
+  const int i = s.i0 + local % s.ni, j = s.j0 + local / s.ni;
+  const long long sx = 256LL * i + 128, sy = 256LL * j + 128;
+  const long long w0 = edge_fn(s.A[1], s.B[1], s.A[2], s.B[2], sx, sy);
+  const long long w1 = edge_fn(s.A[2], s.B[2], s.A[0], s.B[0], sx, sy);
+  const long long w2 = edge_fn(s.A[0], s.B[0], s.A[1], s.B[1], sx, sy);
+  if (!(w0 > 0 || (w0 == 0 && (s.tl & 1)))) return;
+  if (!(w1 > 0 || (w1 == 0 && (s.tl & 2)))) return;
+  if (!(w2 > 0 || (w2 == 0 && (s.tl & 4)))) return;
+  const float b1 = rdiv(__ll2float_rn(w1), s.farea), b2 = rdiv(__ll2float_rn(w2), s.farea);
+  float cz = radd(s.c[0], rmul(b1, rsub(s.c[1], s.c[0])));
+  cz = radd(cz, rmul(b2, rsub(s.c[2], s.c[0])));
+  const float Nf = (float)N;
+  const float t = rmul(Nf, radd(rmul(0.5f, cz), 0.5f));
+  if (!(t > -1.0f && t < Nf)) return;
+  const int kd = __float2int_rz(t);
+  int vx, vy, vz;
+  if (s.axis == 2) { vx = i >> 1; vy = j >> 1; vz = kd; }
+  else if (s.axis == 0) { vx = kd; vy = i >> 1; vz = j >> 1; }
+  else { vx = i >> 1; vy = kd; vz = j >> 1; }
+  const int lx = vx - b3[0] * kBrick, ly = vy - b3[1] * kBrick, lz = vz - b3[2] * kBrick;
+  if ((unsigned)lx >= (unsigned)kBrick || (unsigned)ly >= (unsigned)kBrick || (unsigned)lz >= (unsigned)kBrick) return;
+  const float l0 = __ll2float_rn(w0) / s.farea, l1 = __ll2float_rn(w1) / s.farea, l2 = __ll2float_rn(w2) / s.farea;
+  const V3 p = s.gp[0] * l0 + s.gp[1] * l1 + s.gp[2] * l2;
+  const V3 n = s.gn[0] * l0 + s.gn[1] * l1 + s.gn[2] * l2;
+  accumulate(acc, (lz * kBrick + ly) * kBrick + lx, voxel_color(sp, sp.materials[s.mat], p, n));
+}
+
+// ---------------------------------------------------- conservative mode ----
+struct SetupSat {
+  int V[3][3];
+  V3 gp[3], gn[3];
+  uint32_t mat;
+  int x0, nx, y0, ny, z0, nz;
+};
+
+__device__ int setup_sat(const SceneParams& sp, int N, uint32_t t, const int b3[3], SetupSat& s) {
+  TriLoad tl;
+  load_tri<true>(sp, t, tl);
+  if (!tl.ok) return 0;
+  const double scale = (double)N * 128.0;
+  int lo[3], hi[3];
+  for (int d = 0; d < 3; ++d) {
+    long long mn = LLONG_MAX, mx = LLONG_MIN;
+    for (int k = 0; k < 3; ++k) {
+      long long q = __double2ll_rn(__dmul_rn(__dadd_rn((double)tl.g[k][d], 1.0), scale));
+      s.V[k][d] = (int)q;
+      mn = min(mn, q);
+      mx = max(mx, q);
+    }
+    lo[d] = (int)max((long long)b3[d] * kBrick, ceil_div(mn, 256) - 1);
+    hi[d] = (int)min((long long)b3[d] * kBrick + kBrick - 1, floor_div(mx, 256));
+    if (hi[d] < lo[d]) return 0;
+  }
+  for (int k = 0; k < 3; ++k) {
+    s.gp[k] = v3(tl.g[k][0], tl.g[k][1], tl.g[k][2]);
+    s.gn[k] = tl.n[k];
+  }
+  s.mat = tl.mat;
+  s.x0 = lo[0]; s.nx = hi[0] - lo[0] + 1;
+  s.y0 = lo[1]; s.ny = hi[1] - lo[1] + 1;
+  s.z0 = lo[2]; s.nz = hi[2] - lo[2] + 1;
+  return s.nx * s.ny * s.nz;
+}
+
+__device__ __forceinline__ bool axis_sep(long long p0, long long p1, long long p2, long long r) {
+  return min(p0, min(p1, p2)) > r || max(p0, max(p1, p2)) < -r;
+}
+
+// Exact closed-box SAT on integer coordinates (1/256 voxel units).
+__device__ bool sat_exact(const int V[3][3], long long cx, long long cy, long long cz, long long h) {
+  long long u[3][3];
+  const long long c[3] = {cx, cy, cz};
+  for (int k = 0; k < 3; ++k)
+    for (int d = 0; d < 3; ++d) u[k][d] = (long long)V[k][d] - c[d];
+  for (int d = 0; d < 3; ++d) {
+    long long mn = min(u[0][d], min(u[1][d], u[2][d])), mx = max(u[0][d], max(u[1][d], u[2][d]));
+    if (mn > h || mx < -h) return false;
+  }
+  long long f[3][3];
+  for (int d = 0; d < 3; ++d) {
+    f[0][d] = u[1][d] - u[0][d];
+    f[1][d] = u[2][d] - u[1][d];
+    f[2][d] = u[0][d] - u[2][d];
+  }
+  const long long n0 = f[0][1] * f[1][2] - f[0][2] * f[1][1];
+  const long long n1 = f[0][2] * f[1][0] - f[0][0] * f[1][2];
+  const long long n2 = f[0][0] * f[1][1] - f[0][1] * f[1][0];
+  const __int128 dd = (__int128)n0 * u[0][0] + (__int128)n1 * u[0][1] + (__int128)n2 * u[0][2];
+  const __int128 rr = (__int128)h * ((__int128)llabs(n0) + (__int128)llabs(n1) + (__int128)llabs(n2));
+  if (dd > rr || dd < -rr) return false;
+  for (int e = 0; e < 3; ++e) {
+    const long long fx = f[e][0], fy = f[e][1], fz = f[e][2];
+    if (axis_sep(-fz * u[0][1] + fy * u[0][2], -fz * u[1][1] + fy * u[1][2], -fz * u[2][1] + fy * u[2][2],
+                 h * (llabs(fz) + llabs(fy))))
+      return false;
+    if (axis_sep(fz * u[0][0] - fx * u[0][2], fz * u[1][0] - fx * u[1][2], fz * u[2][0] - fx * u[2][2],
+                 h * (llabs(fz) + llabs(fx))))
+      return false;
+    if (axis_sep(-fy * u[0][0] + fx * u[0][1], -fy * u[1][0] + fx * u[1][1], -fy * u[2][0] + fx * u[2][1],
+                 h * (llabs(fy) + llabs(fx))))
+      return false;
+  }
+  return true;
+}
+
+// Barycentric weights of the closest triangle point to p (Voronoi-region
+// classification of vertices, edges and face).
+__device__ void closest_bary(V3 p, V3 a, V3 b, V3 c, float w[3]) {
+  const V3 ab = b - a, ac = c - a, ap = p - a;
+  const float d1 = dot(ab, ap), d2 = dot(ac, ap);
+  if (d1 <= 0.f && d2 <= 0.f) { w[0] = 1.f; w[1] = 0.f; w[2] = 0.f; return; }
+  const V3 bp = p - b;
+  const float d3 = dot(ab, bp), d4 = dot(ac, bp);
+  if (d3 >= 0.f && d4 <= d3) { w[0] = 0.f; w[1] = 1.f; w[2] = 0.f; return; }
+  const float vc = d1 * d4 - d3 * d2;
+  if (vc <= 0.f && d1 >= 0.f && d3 <= 0.f) {
+    const float den = d1 - d3, v = den != 0.f ? d1 / den : 0.f;
+    w[0] = 1.f - v; w[1] = v; w[2] = 0.f; return;
+  }
+  const V3 cp = p - c;
+  const float d5 = dot(ab, cp), d6 = dot(ac, cp);
+  if (d6 >= 0.f && d5 <= d6) { w[0] = 0.f; w[1] = 0.f; w[2] = 1.f; return; }
+  const float vb = d5 * d2 - d1 * d6;
+  if (vb <= 0.f && d2 >= 0.f && d6 <= 0.f) {
+    const float den = d2 - d6, t = den != 0.f ? d2 / den : 0.f;
+    w[0] = 1.f - t; w[1] = 0.f; w[2] = t; return;
+  }
+  const float va = d3 * d6 - d5 * d4;
+  if (va <= 0.f && (d4 - d3) >= 0.f && (d5 - d6) >= 0.f) {
+    const float den = (d4 - d3) + (d5 - d6), t = den != 0.f ? (d4 - d3) / den : 0.f;
+    w[0] = 0.f; w[1] = 1.f - t; w[2] = t; return;
+  }
+  const float sum = va + vb + vc;
+  if (!(sum != 0.f)) { w[0] = 1.f; w[1] = 0.f; w[2] = 0.f; return; }
+  const float v = vb / sum, t = vc / sum;
+  w[0] = 1.f - v - t; w[1] = v; w[2] = t;
+}
+
+__device__ __forceinline__ void item_sat(const SceneParams& sp, int N, const int b3[3], const SetupSat& s, int local,
+                                         Acc& acc) {
+  const int x = s.x0 + local % s.nx;
+  const int y = s.y0 + (local / s.nx) % s.ny;
+  const int z = s.z0 + local / (s.nx * s.ny);
+  if (!sat_exact(s.V, 256LL * x + 128, 256LL * y + 128, 256LL * z + 128, 128)) return;
+  const float inv = 2.0f / (float)N;
+  const V3 vc = v3(((float)x + 0.5f) * inv - 1.0f, ((float)y + 0.5f) * inv - 1.0f, ((float)z + 0.5f) * inv - 1.0f);
+  float w[3];
+  closest_bary(vc, s.gp[0], s.gp[1], s.gp[2], w);
+  const V3 p = s.gp[0] * w[0] + s.gp[1] * w[1] + s.gp[2] * w[2];
+  const V3 n = s.gn[0] * w[0] + s.gn[1] * w[1] + s.gn[2] * w[2];
+  const int lx = x - b3[0] * kBrick, ly = y - b3[1] * kBrick, lz = z - b3[2] * kBrick;
+  accumulate(acc, (lz * kBrick + ly) * kBrick + lx, voxel_color(sp, sp.materials[s.mat], p, n));
+}
+
+// ------------------------------------------------------------ brick CTA ----
+template <int MODE, int STORAGE>
+__global__ void __launch_bounds__(kThreads) k_bricks(SceneParams sp, int N, const uint32_t* __restrict__ offset,
+                                                     const uint32_t* __restrict__ list, uint32_t cap,
+                                                     cudaSurfaceObject_t l0, uint32_t* __restrict__ counts,
+                                                     FrameStatus* st) {
+  typedef typename std::conditional<MODE == VCT_VOX_CONSERVATIVE, SetupSat, SetupRef>::type Setup;
+  __shared__ Acc acc;
+  __shared__ Setup setup[kWarps][32];
+  __shared__ int excl[kWarps][33];
+  const int nb = N / kBrick;
+  const uint32_t brick = blockIdx.x;
+  const int b3[3] = {(int)(brick % nb), (int)((brick / nb) % nb), (int)(brick / ((uint32_t)nb * nb))};
+  for (int i = threadIdx.x; i < kBrickVox; i += kThreads) {
+    acc.c[0][i] = 0; acc.c[1][i] = 0; acc.c[2][i] = 0; acc.c[3][i] = 0; acc.n[i] = 0;
+  }
+  __syncthreads();
+  const uint32_t beg = min(offset[brick], cap), end = min(offset[brick + 1], cap);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (uint32_t base = beg + warp * 32; base < end; base += kWarps * 32) {
+    const uint32_t e = base + lane;
+    int cnt = 0;
+    if (e < end) {
+      if (MODE == VCT_VOX_CONSERVATIVE)
+        cnt = setup_sat(sp, N, __ldg(list + e), b3, reinterpret_cast<SetupSat&>(setup[warp][lane]));
+      else
+        cnt = setup_ref(sp, N, __ldg(list + e), b3, reinterpret_cast<SetupRef&>(setup[warp][lane]));
+    }
+    int incl = cnt;
+    for (int o = 1; o < 32; o <<= 1) {
+      int v = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += v;
+    }
+    excl[warp][lane] = incl - cnt;
+    const int total = __shfl_sync(0xffffffffu, incl, 31);
+    __syncwarp();
+    for (int it = lane; it < total; it += 32) {
+      int lo = 0, hi = 31;  // owner = last lane with excl <= it
+      while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (excl[warp][mid] <= it) lo = mid; else hi = mid - 1;
+      }
+      const int local = it - excl[warp][lo];
+      if (MODE == VCT_VOX_CONSERVATIVE)
+        item_sat(sp, N, b3, reinterpret_cast<const SetupSat&>(setup[warp][lo]), local, acc);
+      else
+        item_ref(sp, N, b3, reinterpret_cast<const SetupRef&>(setup[warp][lo]), local, acc);
+    }
+    __syncwarp();
+  }
+  __syncthreads();
+  // Order-independent mean, round to nearest (ties up); empty voxels = 0.
+  for (int i = threadIdx.x; i < kBrickVox; i += kThreads) {
+    const uint32_t n = acc.n[i];
+    const int lx = i & 7, ly = (i >> 3) & 7, lz = i >> 6;
+    const int x = b3[0] * kBrick + lx, y = b3[1] * kBrick + ly, z = b3[2] * kBrick + lz;
+    if (n > 65535u) atomicAdd(&st->count_saturated, 1u);
+    if (STORAGE == VCT_STORAGE_RGBA8) {
+      uchar4 o = make_uchar4(0, 0, 0, 0);
+      if (n) {
+        const unsigned long long den = 2ull * n * 65535ull;
+        unsigned char q[4];
+        for (int ch = 0; ch < 4; ++ch) {
+          unsigned long long v = ((unsigned long long)acc.c[ch][i] * 510ull + (unsigned long long)n * 65535ull) / den;
+          q[ch] = (unsigned char)(v > 255ull ? 255ull : v);
+        }
+        o = make_uchar4(q[0], q[1], q[2], q[3]);
+      }
+      surf3Dwrite(o, l0, x * 4, y, z);
+    } else {
+      ushort4 o = make_ushort4(0, 0, 0, 0);
+      if (n) {
+        const float inv = 1.0f / ((float)n * kFix);
+        o = make_ushort4(__half_as_ushort(__float2half_rn((float)acc.c[0][i] * inv)),
+                         __half_as_ushort(__float2half_rn((float)acc.c[1][i] * inv)),
+                         __half_as_ushort(__float2half_rn((float)acc.c[2][i] * inv)),
+                         __half_as_ushort(__float2half_rn((float)acc.c[3][i] * inv)));
+      }
+      surf3Dwrite(o, l0, x * 8, y, z);
+    }
+    if (counts) counts[((size_t)z * N + y) * N + x] = n;
+  }
+}
+
+}  // namespace
+
+cudaError_t launch_voxelize(const SceneParams& sp, int N, int mode, int storage, const VoxBuffers& vb,
+                            cudaSurfaceObject_t l0, cudaStream_t st, int* launches) {
+  int nl = 0;
+  const int nb = N / kBrick;
+  const size_t n_bricks = (size_t)nb * nb * nb;
+  cudaError_t e = cudaMemsetAsync(vb.brick_count, 0, n_bricks * sizeof(uint32_t), st);
+  if (e != cudaSuccess) return e;
+  const unsigned tri_blocks = (sp.total_tris + 255) / 256;
+  if (tri_blocks) {
+    k_bin<false><<<tri_blocks, 256, 0, st>>>(sp, N, vb.brick_count, nullptr, nullptr, 0, vb.status);
+    ++nl;
+  }
+  e = launch_exclusive_scan(vb.brick_count, vb.brick_offset, vb.brick_cursor, n_bricks, vb.scan_tmp, st, &nl);
+  if (e != cudaSuccess) return e;
+  // pair_total <- offset[n_bricks]
+  e = cudaMemcpyAsync(&vb.status->pair_total, vb.brick_offset + n_bricks, sizeof(uint32_t),
+                      cudaMemcpyDeviceToDevice, st);
+  if (e != cudaSuccess) return e;
+  if (tri_blocks) {
+    k_bin<true><<<tri_blocks, 256, 0, st>>>(sp, N, nullptr, vb.brick_cursor, vb.pair_list, vb.pair_cap, vb.status);
+    ++nl;
+  }
+  ++nl;  // k_bricks
+  const unsigned grid = (unsigned)n_bricks;
+  if (mode == VCT_VOX_CONSERVATIVE) {
+    if (storage == VCT_STORAGE_RGBA8)
+      k_bricks<VCT_VOX_CONSERVATIVE, VCT_STORAGE_RGBA8><<<grid, kThreads, 0, st>>>(
+          sp, N, vb.brick_offset, vb.pair_list, vb.pair_cap, l0, vb.counts, vb.status);
+    else
+      k_bricks<VCT_VOX_CONSERVATIVE, VCT_STORAGE_RGBA16F><<<grid, kThreads, 0, st>>>(
+          sp, N, vb.brick_offset, vb.pair_list, vb.pair_cap, l0, vb.counts, vb.status);
+  } else {
+    if (storage == VCT_STORAGE_RGBA8)
+      k_bricks<VCT_VOX_REF_RASTER2X, VCT_STORAGE_RGBA8><<<grid, kThreads, 0, st>>>(
+          sp, N, vb.brick_offset, vb.pair_list, vb.pair_cap, l0, vb.counts, vb.status);
+    else
+      k_bricks<VCT_VOX_REF_RASTER2X, VCT_STORAGE_RGBA16F><<<grid, kThreads, 0, st>>>(
+          sp, N, vb.brick_offset, vb.pair_list, vb.pair_cap, l0, vb.counts, vb.status);
+  }
+  if (launches) *launches += nl;
+  return cudaGetLastError();
+}
+
+}  // namespace vct

@@ -1,0 +1,122 @@
+// vct_internal.h -- structures shared by the host renderer and the kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/vct.h"
+
+namespace vct {
+
+constexpr int kMaxLights = 10;   // MAX_POINT_LIGHTS, voxelize.frag:126
+constexpr int kMaxLevels = 7;    // create_tex_3d(res,res,res,7), renderer.cpp:186
+constexpr int kBrick = 8;        // voxelizer brick edge (voxels)
+constexpr int kMaxMaps = 6;
+
+// One queued model instance of the frame (queue_model captures the model
+// matrix, renderer.cpp:209-218).
+struct DevInstance {
+  float M[16];            // column-major model matrix
+  float NM[9];            // mat3(transpose(inverse(M))), row-major
+  uint32_t tri_base;      // first frame-global triangle id
+  uint32_t n_tris;
+  const vct_vert_data* verts;
+  const uint32_t* indices;
+  const uint32_t* tri_obj;  // per-triangle global draw-object id
+  uint32_t n_verts;
+  uint32_t pad;
+};
+
+// Scene data every stage reads; passed by value to kernels.
+struct SceneParams {
+  const DevInstance* inst;
+  const vct_material_data* materials;
+  const uint32_t* obj_material;   // draw object -> material id
+  uint32_t n_instances;
+  uint32_t total_tris;
+  uint32_t n_materials;
+  int32_t n_lights;
+  float cube_size;
+  vct_point_light lights[kMaxLights];
+};
+
+// Device-side status of one frame, copied to pinned host memory at the end.
+struct FrameStatus {
+  uint32_t pair_total;      // (triangle, brick) pairs needed
+  uint32_t big_total;       // raster work records needed
+  uint32_t big_tiles;       // raster tiles of the big-triangle pass
+  uint32_t rejected_tris;   // non-finite / out-of-range triangles
+  uint32_t count_saturated; // voxels with > 65535 contributions
+  uint32_t pad[3];
+};
+
+// The voxel maps of a renderer: level 0 once, plus one chain per map.
+struct MapSet {
+  int N, L, nmaps, storage;
+  cudaSurfaceObject_t l0_surf;
+  cudaTextureObject_t l0_tex;                    // linear, normalized coords, border 0
+  cudaSurfaceObject_t surf[kMaxMaps][kMaxLevels];  // level l >= 1 of map d
+  cudaTextureObject_t tex[kMaxMaps];             // mipmapped chain (base = level 1)
+};
+
+struct VoxBuffers {
+  uint32_t* brick_count;   // n_bricks
+  uint32_t* brick_offset;  // n_bricks + 1
+  uint32_t* brick_cursor;  // n_bricks
+  uint32_t* pair_list;     // capacity
+  uint32_t pair_cap;
+  uint32_t* scan_tmp;      // block sums
+  uint32_t* counts;        // N^3 or nullptr
+  FrameStatus* status;
+};
+
+struct RasterBuffers {
+  unsigned long long* vis;  // W*H (depth bits << 32 | triangle id)
+  void* big;                // raster work records
+  uint32_t big_cap;
+  uint32_t* big_count;      // [0] records, [1] tiles
+  uint32_t* big_offset;     // tile prefix per record (big_cap + 1)
+  uint32_t* scan_tmp;
+  float4* gb_pos;           // world position, material id bits in .w
+  float4* gb_nrm;           // world normal, triangle id bits in .w
+  FrameStatus* status;
+};
+
+struct CameraParams {
+  float PV[16];       // projection * view (FP32, fixed order)
+  float cam_pos[3];   // column 3 of the view matrix (renderer.cpp:279)
+  int W, H;
+};
+
+struct TraceParams {
+  int enable_direct, enable_diffuse, enable_specular, enable_shadow;
+  int view_voxel_dir;
+  float view_voxel_lod;
+  int cone_set;
+  int sampler;
+  int mip_mode;
+};
+
+// ---- launchers (stream-ordered, no host synchronisation) ----------------
+// `launches` (may be null) is incremented by the number of kernels enqueued.
+cudaError_t launch_voxelize(const SceneParams& sp, int N, int mode, int storage, const VoxBuffers& vb,
+                            cudaSurfaceObject_t l0, cudaStream_t st, int* launches);
+cudaError_t launch_mipmap(const MapSet& ms, int mip_mode, cudaStream_t st, int* launches);
+cudaError_t launch_gbuffer(const SceneParams& sp, const CameraParams& cp, const RasterBuffers& rb,
+                           cudaStream_t st, int* launches);
+cudaError_t launch_trace(const SceneParams& sp, const CameraParams& cp, const MapSet& ms, const TraceParams& tp,
+                         const float4* gb_pos, const float4* gb_nrm, uchar4* frame, float4* frame_f32,
+                         cudaStream_t st, int* launches);
+// Exclusive scan of n u32 values into out[0..n] (out[n] = total); tmp must
+// hold scan_tmp_words(n) words.
+size_t scan_tmp_words(size_t n);
+cudaError_t launch_exclusive_scan(const uint32_t* in, uint32_t* out, uint32_t* copy_out, size_t n, uint32_t* tmp,
+                                  cudaStream_t st, int* launches = nullptr);
+// Texture3D helpers.
+cudaError_t launch_fill_rgba8(cudaSurfaceObject_t s, int w, int h, int d, uchar4 v, cudaStream_t st);
+cudaError_t launch_box_mip_rgba8(cudaSurfaceObject_t src, int sw, int sh, int sd, cudaSurfaceObject_t dst, int dw,
+                                 int dh, int dd, cudaStream_t st);
+
+size_t big_record_bytes();
+
+}  // namespace vct
