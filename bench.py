@@ -39,6 +39,14 @@ UNIT = "ms/frame"
 WIDTH, HEIGHT, GRID = 1920, 1080, 256
 SCENE_SEED = 2000
 CPU_ROW_STRIDE = 64
+NUM_SMS = 152
+# Quadrilinear 3D fetches per pixel of this frame: 251.2 cone-march steps per
+# pixel (3 fetches each, +1 level-0 fetch for the 25.2 steps with lod < 1),
+# counted by the instrumented oracle (oracle.trace_stats; checked by
+# tests/test_scenes.py::test_bench_frame_work).
+TRACE_FETCHES_PER_PIXEL = 778.9
+INSTANCE_RECORD_BYTES = 144   # one per queued model (DevInstance)
+STATUS_BYTES = 32             # per-frame status read back with the frame
 
 
 def _peaks():
@@ -240,8 +248,8 @@ def run_ours(args):
         r.render()
         r.read_frame(R.FRAME_RGBA8, out=host)
     e2e_ms = (time.perf_counter() - t0) * 1000.0 / e2e_steps
-    h2d = len(ids) * 128 + len(scene.lights) * 0  # instance records (lights travel as kernel parameters)
-    d2h = WIDTH * HEIGHT * 4 + 32
+    h2d = len(ids) * INSTANCE_RECORD_BYTES  # lights and camera travel as kernel parameters
+    d2h = WIDTH * HEIGHT * 4 + STATUS_BYTES
 
     # ---- roofline of the dominant kernel (cone trace) ----------------------
     peak, peak_kind = _peaks()
@@ -249,11 +257,14 @@ def run_ours(args):
     trace_bytes = WIDTH * HEIGHT * (32 + 4) + (GRID ** 3 + nmaps_levels) * 4
     trace_ms = mean("trace")
     achieved = trace_bytes / (trace_ms * 1e-3) / 1e9
-    traffic = None
+    traffic, tex_pct = None, None
     tp = os.path.join(ROOT, "profiles", "trace_traffic.json")
     if os.path.exists(tp):
         with open(tp) as f:
-            traffic = json.load(f).get("dram_bytes_per_launch")
+            prof = json.load(f)
+        traffic, tex_pct = prof.get("dram_bytes_per_launch"), prof.get("tex_pipe_pct_of_peak")
+    fetches = TRACE_FETCHES_PER_PIXEL * WIDTH * HEIGHT
+    sm_clock_hz = (clk.summary().get("sm_mhz") or 2070.0) * 1e6
 
     line = {
         "metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -271,7 +282,14 @@ def run_ours(args):
         "gpu_launches": int(sum(st["kernel_launches"] for st in stages)),
         "roofline": {"kernel": "k_trace", "bound": "hbm", "achieved": round(achieved, 2), "peak": peak,
                      "unit": "GB/s", "frac": round(achieved / peak, 5), "traffic": traffic,
-                     "peak_source": peak_kind},
+                     "peak_source": peak_kind,
+                     "texture_path": {
+                         "note": "k_trace is texture-pipeline bound, not HBM bound (profiles/k_trace_1080p_256.md)",
+                         "quadrilinear_fetches_per_frame": fetches,
+                         "fetches_per_clock_per_sm": round(fetches / (trace_ms * 1e-3) / sm_clock_hz / NUM_SMS, 3),
+                         "texel_bytes_per_s": round(fetches * 64 / (trace_ms * 1e-3) / 1e12, 3),
+                         "texel_bytes_unit": "TB/s (16 RGBA8 texels per fetch, served by L1)",
+                         "ncu_tex_pipe_pct_of_peak": tex_pct}},
         "clocks": clk.summary(),
     }
     if rank == 0 and world == 1 and not args.no_cpu_baseline:

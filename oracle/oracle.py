@@ -77,6 +77,7 @@ def lib():
         L.orc_gbuffer.argtypes = [P, P, P, P, P, P]
         for f in ("orc_trace", "orc_trace_f32"):
             getattr(L, f).argtypes = [P, P, P, P, P, P, P, P, C.c_int32, P]
+        L.orc_trace_stats.argtypes = [P, P, P, P, P, P, P, P, C.c_int32, P, P]
         L.orc_texture_lod.argtypes = [P, P, P, C.c_int32, P, C.c_double, P]
         L.orc_trace_cone.argtypes = [P, P, P, P, P, C.c_double, C.c_double, P, P]
         L.orc_time_frame.argtypes = [P, P, C.c_int32, P]
@@ -208,6 +209,21 @@ def trace(scene, params: Params, level0, chains, gb: dict, row_stride: int = 1, 
     f(sh.ptr, C.addressof(pc), _ptr(l0), _ptr(ch), _ptr(tid), _ptr(pos), _ptr(nrm), _ptr(mat),
       int(row_stride), _ptr(out))
     return out
+
+
+def trace_stats(scene, params: Params, level0, chains, gb: dict, row_stride: int = 1) -> dict:
+    """Instrumented FP64 trace: cones, march steps and lod<1 steps per cone
+    class over the traced rows (the algorithmic texture work of the trace)."""
+    w, h = params.width, params.height
+    out = np.zeros((h, w, 4), np.float32)
+    st = np.zeros(12, np.uint64)
+    sh, pc = _SceneHold(scene), params.c()
+    args = [np.ascontiguousarray(level0, np.uint8), np.ascontiguousarray(chains, np.uint8),
+            np.ascontiguousarray(gb["tri_id"], np.uint32), np.ascontiguousarray(gb["pos"], np.float64),
+            np.ascontiguousarray(gb["nrm"], np.float64), np.ascontiguousarray(gb["mat"], np.uint32)]
+    lib().orc_trace_stats(sh.ptr, C.addressof(pc), *[_ptr(a) for a in args], int(row_stride), _ptr(out), _ptr(st))
+    names = ["diffuse", "specular", "shadow", "refraction"]
+    return {n: dict(cones=int(st[i]), steps=int(st[4 + i]), lod_lt1=int(st[8 + i])) for i, n in enumerate(names)}
 
 
 def render(scene, params: Params):

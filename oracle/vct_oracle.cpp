@@ -619,6 +619,14 @@ template <class R> static V4<R> texture_lod(const Maps& m, int map, V3<R> u, R l
 // --------------------------------------------------- voxel_cone_tracing ----
 template <class R> struct ConeOut { V4<R> c; int steps; };
 
+// Instrumentation for orc_trace_stats: per cone class (0 diffuse, 1
+// specular, 2 shadow, 3 refraction) the cones traced, the march steps and
+// the steps whose lod is < 1 (those read level 0 plus level 1).
+enum { kStatCones = 0, kStatSteps = 4, kStatLodLt1 = 8, kStatN = 12 };
+static std::atomic<uint64_t> g_stats[kStatN];
+static bool g_stats_on = false;
+static thread_local int t_cone_class = 0;
+
 // trace_cone, voxel_cone_tracing.frag:116-147 (face_indices :99-106,
 // sample_voxel :108-114).
 template <class R>
@@ -632,7 +640,7 @@ static ConeOut<R> trace_cone(const Maps& m, V3<R> origin, V3<R> dir, R aperture,
   R dist = R(3) * voxel_size;
   R diam = dist * aperture;
   V3<R> sp = dir * dist + origin;
-  int steps = 0;
+  int steps = 0, lod_lt1 = 0;
   while (acc.a < R(1) && dist < max_dist) {
     R mip = fmaxr(R(std::log2(diam * cube_res)), R(0));
     V4<R> smp = texture_lod<R>(m, ix, sp, mip) * ad.x + texture_lod<R>(m, iy, sp, mip) * ad.y +
@@ -643,6 +651,12 @@ static ConeOut<R> trace_cone(const Maps& m, V3<R> origin, V3<R> dir, R aperture,
     diam = dist * aperture;
     sp = dir * dist + origin;
     ++steps;
+    if (mip < R(1)) ++lod_lt1;
+  }
+  if (g_stats_on) {
+    g_stats[kStatCones + t_cone_class] += 1;
+    g_stats[kStatSteps + t_cone_class] += (uint64_t)steps;
+    g_stats[kStatLodLt1 + t_cone_class] += (uint64_t)lod_lt1;
   }
   return {acc, steps};
 }
@@ -724,6 +738,7 @@ static V3<R> direct_light(const orc_scene* s, const Maps& m, int enable_shadow, 
     V3<R> lc = V3<R>(R(L.color[0]), R(L.color[1]), R(L.color[2])) *
                ((R(1) / (R(1) + R(0) * d + R(1) * d * d)) * cs * R(L.intensity));
     R shadow = R(1);
+    t_cone_class = 2;
     if (enable_shadow) shadow = fmaxr(R(0), R(1) - trace_cone<R>(m, pos, ld, R(0.1), d).c.a);
     R lambert = fmaxr(dot(ld, nrm), R(0));
     R refract_angle = R(0);
@@ -760,17 +775,20 @@ static V4<R> shade_pixel(const orc_scene* s, const orc_params* p, const Maps& m,
   V3<R> cam(R(s->view[12]), R(s->view[13]), R(s->view[14]));
   V3<R> view_dir = normalize(world - cam);
   V3<R> fd, fdir, fs;
+  t_cone_class = 0;
   if (p->enable_diffuse) fd = mulv(mat_of<R>(mat, 0), trace_diffuse<R>(m, p->cone_set, pos, nrm));
   if (p->enable_direct) fdir = direct_light<R>(s, m, p->enable_shadow, mat, pos, nrm, view_dir);
   R sap = specular_aperture<R>(mat);
   if (p->enable_specular) {
     V3<R> sd = normalize(reflect(-view_dir, nrm));
+    t_cone_class = 1;
     ConeOut<R> c = trace_cone<R>(m, pos, sd, sap, R(kMaxDistance));
     fs = mulv(mat_of<R>(mat, 1), V3<R>(c.c.r, c.c.g, c.c.b));
   }
   V3<R> f = fs + fd + fdir;
   if (illum_transparent(mat.illum) && p->enable_specular) {
     V3<R> rd = refract(view_dir, nrm, R(1) / R(mat.ior));
+    t_cone_class = 3;
     ConeOut<R> c = trace_cone<R>(m, pos, rd, sap, R(kMaxDistance));
     V3<R> tr = mulv(mat_of<R>(mat, 2), V3<R>(c.c.r, c.c.g, c.c.b));
     R a = R(mat.dissolve);
@@ -1031,6 +1049,16 @@ void orc_trace_cone(const orc_params* p, const uint8_t* level0, const uint8_t* c
                                          V3<double>(dir[0], dir[1], dir[2]), aperture, max_dist);
   rgba[0] = c.c.r; rgba[1] = c.c.g; rgba[2] = c.c.b; rgba[3] = c.c.a;
   if (steps) *steps = c.steps;
+}
+
+void orc_trace_stats(const orc_scene* s, const orc_params* p, const uint8_t* level0, const uint8_t* chains,
+                     const uint32_t* tri_id, const double* pos, const double* nrm, const uint32_t* mat,
+                     int32_t row_stride, float* out, uint64_t* stats) {
+  for (auto& g : g_stats) g = 0;
+  g_stats_on = true;
+  trace_impl<double>(s, p, level0, chains, tri_id, pos, nrm, mat, row_stride, out);
+  g_stats_on = false;
+  for (int i = 0; i < kStatN; ++i) stats[i] = g_stats[i].load();
 }
 
 void orc_time_frame(const orc_scene* s, const orc_params* p, int32_t row_stride, double* ms) {

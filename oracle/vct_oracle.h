@@ -126,6 +126,14 @@ void orc_trace_f32(const orc_scene* s, const orc_params* p,
                    const double* nrm, const uint32_t* mat, int32_t row_stride,
                    float* out);
 
+/* orc_trace with instrumentation: stats[0..3] cones, [4..7] march steps,
+ * [8..11] steps with lod < 1, per class (diffuse, specular, shadow,
+ * refraction).  Not thread-safe against concurrent orc_trace_stats. */
+void orc_trace_stats(const orc_scene* s, const orc_params* p, const uint8_t* level0,
+                     const uint8_t* chains, const uint32_t* tri_id, const double* pos,
+                     const double* nrm, const uint32_t* mat, int32_t row_stride,
+                     float* out, uint64_t* stats);
+
 /* One GL texture sample, textureLod(map d, u, lod) with GL_LINEAR_MIPMAP_LINEAR
  * and CLAMP_TO_BORDER(0) (for the known-answer tests). */
 void orc_texture_lod(const orc_params* p, const uint8_t* level0,

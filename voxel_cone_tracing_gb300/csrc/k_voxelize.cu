@@ -118,55 +118,92 @@ __device__ bool tri_box_f32(const float v[3][3], const float c[3], const float h
   return true;
 }
 
+// One (triangle, candidate brick) test of the binning passes.
+template <bool FILL>
+__device__ __forceinline__ void bin_one(const float v[3][3], int bx, int by, int bz, int nb, bool test, uint32_t t,
+                                        uint32_t* __restrict__ count, uint32_t* __restrict__ cursor,
+                                        uint32_t* __restrict__ list, uint32_t cap) {
+  if (test) {
+    const int b3[3] = {bx, by, bz};
+    float c[3], h[3];
+    for (int d = 0; d < 3; ++d) {
+      float lo = (float)(b3[d] * kBrick) - kBinMargin - (b3[d] == 0 ? 1.0f : 0.0f);
+      float hi = (float)(b3[d] * kBrick + kBrick) + kBinMargin;
+      c[d] = 0.5f * (lo + hi);
+      h[d] = 0.5f * (hi - lo);
+    }
+    if (!tri_box_f32(v, c, h)) return;
+  }
+  const uint32_t brick = ((uint32_t)bz * nb + by) * nb + bx;
+  if (FILL) {
+    uint32_t slot = atomicAdd(cursor + brick, 1u);
+    if (slot < cap) list[slot] = t;
+  } else {
+    atomicAdd(count + brick, 1u);
+  }
+}
+
+constexpr int kSoloBricks = 8;  // candidate bricks a lane bins on its own
+
+// Bins every triangle to the bricks it may touch.  A lane handles its own
+// triangle when it has few candidate bricks; triangles with more candidates
+// (room walls span 1024 bricks at 256^3) are binned by the whole warp, the
+// lanes splitting the candidate range, so no lane serialises a long loop of
+// returning atomics.
 template <bool FILL>
 __global__ void __launch_bounds__(256) k_bin(SceneParams sp, int N, uint32_t* __restrict__ count,
                                              uint32_t* __restrict__ cursor, uint32_t* __restrict__ list,
                                              uint32_t cap, FrameStatus* st) {
   const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= sp.total_tris) return;
-  TriLoad tl;
-  load_tri<false>(sp, t, tl);
-  if (!tl.ok) {
-    if (!FILL) atomicAdd(&st->rejected_tris, 1u);
-    return;
-  }
-  const float hv = 0.5f * (float)N;
-  float v[3][3];
-  for (int k = 0; k < 3; ++k)
-    for (int d = 0; d < 3; ++d) v[k][d] = (tl.g[k][d] + 1.0f) * hv;  // voxel units
+  const int lane = threadIdx.x & 31;
   const int nb = N / kBrick;
-  int blo[3], bhi[3];
-  for (int d = 0; d < 3; ++d) {
-    float lo = fminf(v[0][d], fminf(v[1][d], v[2][d])) - kBinMargin;
-    float hi = fmaxf(v[0][d], fmaxf(v[1][d], v[2][d])) + kBinMargin;
-    // Depth values in (-1, 0) voxel still land in voxel 0 (int() truncates).
-    if (hi <= -1.0f - kBinMargin || lo >= (float)N) return;
-    blo[d] = max(0, (int)floorf(lo / kBrick));
-    bhi[d] = min(nb - 1, (int)floorf(fmaxf(hi, 0.0f) / kBrick));
-  }
-  const bool single = blo[0] == bhi[0] && blo[1] == bhi[1] && blo[2] == bhi[2];
-  for (int bz = blo[2]; bz <= bhi[2]; ++bz)
-    for (int by = blo[1]; by <= bhi[1]; ++by)
-      for (int bx = blo[0]; bx <= bhi[0]; ++bx) {
-        if (!single) {
-          const int b3[3] = {bx, by, bz};
-          float c[3], h[3];
-          for (int d = 0; d < 3; ++d) {
-            float lo = (float)(b3[d] * kBrick) - kBinMargin - (b3[d] == 0 ? 1.0f : 0.0f);
-            float hi = (float)(b3[d] * kBrick + kBrick) + kBinMargin;
-            c[d] = 0.5f * (lo + hi);
-            h[d] = 0.5f * (hi - lo);
-          }
-          if (!tri_box_f32(v, c, h)) continue;
-        }
-        const uint32_t brick = ((uint32_t)bz * nb + by) * nb + bx;
-        if (FILL) {
-          uint32_t slot = atomicAdd(cursor + brick, 1u);
-          if (slot < cap) list[slot] = t;
-        } else {
-          atomicAdd(count + brick, 1u);
-        }
+  float v[3][3] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};
+  int blo[3] = {0, 0, 0}, bhi[3] = {-1, -1, -1};
+  int vol = 0;
+  if (t < sp.total_tris) {
+    TriLoad tl;
+    load_tri<false>(sp, t, tl);
+    if (!tl.ok) {
+      if (!FILL) atomicAdd(&st->rejected_tris, 1u);
+    } else {
+      const float hv = 0.5f * (float)N;
+      for (int k = 0; k < 3; ++k)
+        for (int d = 0; d < 3; ++d) v[k][d] = (tl.g[k][d] + 1.0f) * hv;  // voxel units
+      bool inside = true;
+      for (int d = 0; d < 3; ++d) {
+        float lo = fminf(v[0][d], fminf(v[1][d], v[2][d])) - kBinMargin;
+        float hi = fmaxf(v[0][d], fmaxf(v[1][d], v[2][d])) + kBinMargin;
+        // Depth values in (-1, 0) voxel still land in voxel 0 (int() truncates).
+        if (hi <= -1.0f - kBinMargin || lo >= (float)N) inside = false;
+        blo[d] = max(0, (int)floorf(lo / kBrick));
+        bhi[d] = min(nb - 1, (int)floorf(fmaxf(hi, 0.0f) / kBrick));
       }
+      if (inside && bhi[0] >= blo[0] && bhi[1] >= blo[1] && bhi[2] >= blo[2])
+        vol = (bhi[0] - blo[0] + 1) * (bhi[1] - blo[1] + 1) * (bhi[2] - blo[2] + 1);
+    }
+  }
+  if (vol > 0 && vol <= kSoloBricks) {
+    for (int bz = blo[2]; bz <= bhi[2]; ++bz)
+      for (int by = blo[1]; by <= bhi[1]; ++by)
+        for (int bx = blo[0]; bx <= bhi[0]; ++bx)
+          bin_one<FILL>(v, bx, by, bz, nb, vol > 1, t, count, cursor, list, cap);
+  }
+  unsigned big = __ballot_sync(0xffffffffu, vol > kSoloBricks);
+  while (big) {
+    const int src = __ffs(big) - 1;
+    big &= big - 1;
+    float w[3][3];
+    for (int k = 0; k < 3; ++k)
+      for (int d = 0; d < 3; ++d) w[k][d] = __shfl_sync(0xffffffffu, v[k][d], src);
+    const int x0 = __shfl_sync(0xffffffffu, blo[0], src), y0 = __shfl_sync(0xffffffffu, blo[1], src);
+    const int z0 = __shfl_sync(0xffffffffu, blo[2], src);
+    const int nx = __shfl_sync(0xffffffffu, bhi[0], src) - x0 + 1;
+    const int ny = __shfl_sync(0xffffffffu, bhi[1], src) - y0 + 1;
+    const int n = __shfl_sync(0xffffffffu, vol, src);
+    const uint32_t ts = __shfl_sync(0xffffffffu, t, src);
+    for (int i = lane; i < n; i += 32)
+      bin_one<FILL>(w, x0 + i % nx, y0 + (i / nx) % ny, z0 + i / (nx * ny), nb, true, ts, count, cursor, list, cap);
+  }
 }
 
 // ------------------------------------------------------------- shading -----
