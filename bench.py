@@ -174,6 +174,47 @@ def run_reference(args):
     return 0
 
 
+def mlp_leg(r, R, scene, ids, stream, flush, steps, plain_stages):
+    """Learned diffuse term: train on this frame's scene (2^24 cone-traced
+    surface samples, 1000 Adam steps of 2^18), then time frames that
+    evaluate the network instead of the nine diffuse cones, and compare the
+    frame with the cone-traced one (RGBA8, PSNR)."""
+    import numpy as np
+    import torch
+
+    def frame():
+        R.queue_scene(r, scene, ids)
+        r.render()
+
+    r.set_diffuse_mode(R.DIFFUSE_CONES)
+    frame()
+    ref = r.read_frame().astype(np.float64) / 255.0
+    rep = r.mlp_train(R.mlp_desc())
+    r.set_diffuse_mode(R.DIFFUSE_MLP)
+    for _ in range(3):
+        frame()
+    r.synchronize()
+    stages = []
+    for _ in range(steps):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        frame()
+        r.synchronize()
+        stages.append(r.stage_times())
+    got = r.read_frame().astype(np.float64) / 255.0
+    r.set_diffuse_mode(R.DIFFUSE_CONES)
+    mse = float(np.mean((got[..., :3] - ref[..., :3]) ** 2))
+    trace_mlp = statistics.mean(s["trace"] for s in stages)
+    trace_cones = statistics.mean(s["trace"] for s in plain_stages)
+    value = statistics.mean(s["voxelize"] + s["mipmap"] + s["trace"] for s in stages)
+    return {"value": round(value, 4), "unit": UNIT, "trace_ms": round(trace_mlp, 4),
+            "trace_ms_cones": round(trace_cones, 4), "trace_speedup": round(trace_cones / trace_mlp, 3),
+            "psnr_db_vs_cones": round(10 * np.log10(1.0 / mse), 2) if mse > 0 else None,
+            "train": {"samples": rep["n_samples"], "steps": rep["steps"], "loss_first": rep["loss_first"],
+                      "loss_last": rep["loss_last"], "ms_samples": round(rep["ms_samples"], 2),
+                      "ms_train": round(rep["ms_train"], 2)}}
+
+
 def run_ours(args):
     rank, world, local = _dist()
     import numpy as np
@@ -292,6 +333,8 @@ def run_ours(args):
                          "ncu_tex_pipe_pct_of_peak": tex_pct}},
         "clocks": clk.summary(),
     }
+    if not args.no_mlp:
+        line["mlp"] = mlp_leg(r, R, scene, ids, stream, flush, args.steps, stages)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
         v, ms = cpu_frame_ms(scene, threads, CPU_ROW_STRIDE)
@@ -314,6 +357,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-mlp", action="store_true", help="skip the learned-diffuse leg")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

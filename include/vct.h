@@ -226,6 +226,63 @@ vct_status vct_read_gbuffer(vct_renderer* r, uint32_t* tri_id, float* pos, float
 /* Grid resolution and mip level count currently in use. */
 vct_status vct_get_grid(vct_renderer* r, int32_t* res, int32_t* levels);
 
+/* ------------------------------------------- learned diffuse term ----- */
+
+/* No reference counterpart: an engine extension.  A small network (hash
+ * encoding of the surface position + normal + albedo -> 4 x 64 ReLU MLP ->
+ * RGB, BF16 tensor cores, FP32 accumulation) trained on the GPU to predict
+ * trace_diffuse (voxel_cone_tracing.frag:168-196), the average of the nine
+ * diffuse cones; with VCT_DIFFUSE_MLP a frame evaluates it instead of
+ * tracing those cones.  The cone tracer stays the default and the judge. */
+enum { VCT_DIFFUSE_CONES = 0, VCT_DIFFUSE_MLP = 1 };
+
+typedef struct {
+  int32_t levels;       /* hash-grid levels (16)                          */
+  int32_t log2_table;   /* entries per level, log2 (19)                   */
+  int32_t n_min, n_max; /* coarsest / finest level resolution (16, 512)   */
+  uint32_t n_samples;   /* training samples drawn from the scene (2^24)   */
+  uint32_t batch;       /* samples per optimiser step (2^18)              */
+  uint32_t steps;       /* Adam steps (1000)                              */
+  float lr;             /* Adam learning rate (1e-2)                      */
+  uint64_t seed;
+  uint32_t reserved[8];
+} vct_mlp_desc;
+
+typedef struct {
+  float loss_first;     /* MSE of the first step                          */
+  float loss_last;      /* mean MSE over the last tenth of the steps      */
+  float ms_samples;     /* surface sampling + cone-traced targets (device)*/
+  float ms_train;       /* optimiser steps (device)                       */
+  uint32_t steps, n_samples;
+} vct_mlp_report;
+
+void vct_mlp_desc_default(vct_mlp_desc* d);
+/* Allocate and initialise the network (seeded) without training. */
+vct_status vct_mlp_init(vct_renderer* r, const vct_mlp_desc* d);
+/* Train on the scene and voxel maps of the last rendered frame: draw
+ * n_samples surface points (uniform by area), cone-trace their diffuse
+ * targets, run `steps` Adam steps.  Synchronous. */
+vct_status vct_mlp_train(vct_renderer* r, const vct_mlp_desc* d, vct_mlp_report* report);
+/* VCT_DIFFUSE_CONES (default) or VCT_DIFFUSE_MLP (needs a trained network). */
+vct_status vct_set_diffuse_mode(vct_renderer* r, int32_t mode);
+/* Checkpoint: versioned binary file with the configuration, the FP32 hash
+ * table and weights and the Adam state. */
+vct_status vct_mlp_save(vct_renderer* r, const char* path);
+vct_status vct_mlp_load(vct_renderer* r, const char* path);
+/* Host copies of the FP32 parameters: table levels*2^log2_table*2 floats,
+ * weights 5*64*64 floats (W1..W4 [out][in], W5 rows 0..15 then zeros). */
+vct_status vct_mlp_get_params(vct_renderer* r, float* table, float* weights);
+vct_status vct_mlp_set_params(vct_renderer* r, const float* table, const float* weights);
+/* Rows of 12 floats (texture-space position, normal, albedo, target RGB). */
+vct_status vct_mlp_eval(vct_renderer* r, const float* samples, uint32_t n, float* rgb_out);
+/* One forward + backward pass over the rows (no parameter update): MSE
+ * loss and its gradients (same layouts as vct_mlp_get_params). */
+vct_status vct_mlp_gradients(vct_renderer* r, const float* samples, uint32_t n, float* loss,
+                             float* dweights, float* dtable);
+/* Train on explicit rows instead of scene samples. */
+vct_status vct_mlp_train_samples(vct_renderer* r, const float* samples, uint32_t n,
+                                 const vct_mlp_desc* d, vct_mlp_report* report);
+
 /* ------------------------------------------------------- Texture3D ----- */
 
 typedef uint32_t vct_tex3d;   /* 0 = no texture, like a GL name */

@@ -16,6 +16,7 @@ import numpy as np
 _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "liboracle_vct.so")
 SRC = os.path.join(_HERE, "vct_oracle.cpp")
+SRCS = [SRC, os.path.join(_HERE, "vct_oracle_mlp.cpp")]
 
 VOX_REF_RASTER2X, VOX_CONSERVATIVE = 0, 1
 MIP_ANISO, MIP_ISO = 0, 1
@@ -25,12 +26,12 @@ CONES_REF9, CONES_SIX60 = 0, 1
 def build(force: bool = False) -> str:
     """Compile the oracle with g++ (no -march flags, no FMA contraction, so
     x86-64 and aarch64 give identical coverage decisions)."""
-    if not force and os.path.exists(LIB_PATH) and os.path.getmtime(LIB_PATH) >= max(
-            os.path.getmtime(SRC), os.path.getmtime(os.path.join(_HERE, "vct_oracle.h"))):
+    deps = SRCS + [os.path.join(_HERE, "vct_oracle.h")]
+    if not force and os.path.exists(LIB_PATH) and os.path.getmtime(LIB_PATH) >= max(map(os.path.getmtime, deps)):
         return LIB_PATH
     tmp = LIB_PATH + f".tmp{os.getpid()}"
     subprocess.check_call(["g++", "-O3", "-std=c++17", "-fPIC", "-shared", "-pthread",
-                           "-ffp-contract=off", "-fno-fast-math", "-o", tmp, SRC])
+                           "-ffp-contract=off", "-fno-fast-math", "-o", tmp, *SRCS])
     os.replace(tmp, LIB_PATH)
     return LIB_PATH
 
@@ -81,6 +82,11 @@ def lib():
         L.orc_texture_lod.argtypes = [P, P, P, C.c_int32, P, C.c_double, P]
         L.orc_trace_cone.argtypes = [P, P, P, P, P, C.c_double, C.c_double, P, P]
         L.orc_time_frame.argtypes = [P, P, C.c_int32, P]
+        L.orc_mlp_level_res.restype = C.c_int32
+        L.orc_mlp_level_res.argtypes = [P, C.c_int32]
+        L.orc_mlp_forward.argtypes = [P, P, P, C.c_int32, P, P, P, P]
+        L.orc_mlp_grad.restype = C.c_double
+        L.orc_mlp_grad.argtypes = [P, P, P, C.c_int32, P, P, P, P, P, P]
         _lib = L
     return _lib
 
@@ -264,3 +270,37 @@ def time_frame(scene, params: Params, row_stride: int) -> np.ndarray:
     sh, pc = _SceneHold(scene), params.c()
     lib().orc_time_frame(sh.ptr, C.addressof(pc), int(row_stride), _ptr(ms))
     return ms
+
+
+# ------------------------------------------------------------ learned term --
+class MLPConfig(C.Structure):
+    _fields_ = [("levels", C.c_int32), ("log2_table", C.c_int32), ("n_min", C.c_int32), ("n_max", C.c_int32)]
+
+
+def mlp_config(levels=16, log2_table=19, n_min=16, n_max=512) -> MLPConfig:
+    return MLPConfig(levels, log2_table, n_min, n_max)
+
+
+def mlp_level_res(cfg: MLPConfig, level: int) -> int:
+    return int(lib().orc_mlp_level_res(C.byref(cfg), int(level)))
+
+
+def mlp_forward(cfg: MLPConfig, table, weights, pos, nrm, alb) -> np.ndarray:
+    pos, nrm, alb = (np.ascontiguousarray(a, np.float32).reshape(-1, 3) for a in (pos, nrm, alb))
+    t = np.ascontiguousarray(table, np.float32)
+    w = np.ascontiguousarray(weights, np.float32)
+    out = np.zeros((pos.shape[0], 3), np.float32)
+    lib().orc_mlp_forward(C.byref(cfg), _ptr(t), _ptr(w), pos.shape[0], _ptr(pos), _ptr(nrm), _ptr(alb), _ptr(out))
+    return out
+
+
+def mlp_grad(cfg: MLPConfig, table, weights, pos, nrm, alb, target, want_table=True):
+    """-> (loss, dW (5,64,64) float64, dtable (levels, T, 2) float64 or None)."""
+    pos, nrm, alb, tg = (np.ascontiguousarray(a, np.float32).reshape(-1, 3) for a in (pos, nrm, alb, target))
+    t = np.ascontiguousarray(table, np.float32)
+    w = np.ascontiguousarray(weights, np.float32)
+    dW = np.zeros((5, 64, 64))
+    dt = np.zeros((cfg.levels, 1 << cfg.log2_table, 2)) if want_table else None
+    loss = lib().orc_mlp_grad(C.byref(cfg), _ptr(t), _ptr(w), pos.shape[0], _ptr(pos), _ptr(nrm), _ptr(alb),
+                              _ptr(tg), _ptr(dW), _ptr(dt) if dt is not None else None)
+    return float(loss), dW, dt

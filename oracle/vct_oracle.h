@@ -146,6 +146,25 @@ void orc_trace_cone(const orc_params* p, const uint8_t* level0,
                     const double* dir, double aperture, double max_dist,
                     double* rgba, int32_t* steps);
 
+/* ---- learned diffuse term (vct_oracle_mlp.cpp) ----
+ * Hash table: levels x 2^log2_table x 2 floats; weights: 5 x 64 x 64 floats
+ * (W1..W4 [out][in] 64x64, W5 rows 0..15 of [out][in], rows >= 3 unused). */
+typedef struct {
+  int32_t levels;      /* 16 */
+  int32_t log2_table;  /* 19 */
+  int32_t n_min;       /* 16 */
+  int32_t n_max;       /* finest grid resolution */
+} orc_mlp_config;
+
+int32_t orc_mlp_level_res(const orc_mlp_config* c, int32_t level);
+void orc_mlp_forward(const orc_mlp_config* c, const float* table, const float* W, int32_t n,
+                     const float* pos, const float* nrm, const float* alb, float* out);
+/* MSE loss; dW (5*64*64 doubles) and dtable (levels*2^log2_table*2 doubles,
+ * may be NULL) receive d loss / d parameter. */
+double orc_mlp_grad(const orc_mlp_config* c, const float* table, const float* W, int32_t n,
+                    const float* pos, const float* nrm, const float* alb, const float* target,
+                    double* dW, double* dtable);
+
 /* Timed CPU restatement of one frame (FP32 shading, p->threads threads):
  * voxelize + mip over the whole scene, trace over rows y % row_stride == 0.
  * ms[0..3] = voxelize, mip, gbuffer, trace (trace for the sampled rows). */

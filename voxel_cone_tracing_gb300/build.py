@@ -19,6 +19,8 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libvct.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=off", "-I", CSRC]
+# Extra nvcc flags (e.g. -DVCT_TRACE_MIN_BLOCKS=3 for tuning sweeps).
+EXTRA = os.environ.get("VCT_NVCC_FLAGS", "").split()
 
 
 def nvcc() -> str:
@@ -52,7 +54,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
 
     def compile_one(src):
         obj = os.path.join(BUILD, os.path.basename(src) + ".o")
-        cmd = [cc, *ARCH, *FLAGS, "-c", src, "-o", obj]
+        cmd = [cc, *ARCH, *FLAGS, *EXTRA, "-c", src, "-o", obj]
         if verbose:
             cmd.insert(1, "-Xptxas=-v")
         r = subprocess.run(cmd, capture_output=True, text=True)

@@ -28,6 +28,13 @@ __device__ __forceinline__ float4 f4(float x, float y, float z, float w) { retur
 __device__ __forceinline__ float4 operator+(float4 a, float4 b) { return f4(a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w); }
 __device__ __forceinline__ float4 operator*(float4 a, float s) { return f4(a.x * s, a.y * s, a.z * s, a.w * s); }
 
+#ifndef VCT_TRACE_MIN_BLOCKS
+#define VCT_TRACE_MIN_BLOCKS 4
+#endif
+// Resident 256-thread CTAs per SM the texture-unit variant is compiled for
+// (register budget 65536 / (256 * 4) = 64 per thread).
+constexpr int kTraceMinBlocks = VCT_TRACE_MIN_BLOCKS;
+
 constexpr float kTan22_5 = 0.55785173935f;      // TAN_22_5 (:164), kept verbatim
 constexpr float kMaxDistance = 1.73205080757f;  // MAX_DISTANCE (:166)
 
@@ -165,11 +172,15 @@ __device__ V3 trace_diffuse(const MapSet& m, int cone_set, V3 origin, V3 n) {
     return v3(acc.x, acc.y, acc.z) * (1.0f / 6.0f);
   }
   const V3 c1 = (o1 + o2) * 0.5f, c2 = (o1 - o2) * 0.5f;
-  const V3 side[8] = {o1, -o1, o2, -o2, c1, -c1, c2, -c2};
   acc = trace_cone<SAMPLER, ISO, STORAGE>(m, origin, n, kTan22_5, kMaxDistance);
+  // Side cones o1, -o1, o2, -o2, c1, -c1, c2, -c2 (:184-193), selected
+  // arithmetically so that no local-memory array is needed.
 #pragma unroll 1
-  for (int k = 0; k < 8; ++k)
-    acc = acc + trace_cone<SAMPLER, ISO, STORAGE>(m, origin, mixv(n, side[k], 0.5f), kTan22_5, kMaxDistance);
+  for (int k = 0; k < 8; ++k) {
+    const V3 b = k < 2 ? o1 : (k < 4 ? o2 : (k < 6 ? c1 : c2));
+    const V3 side = (k & 1) ? -b : b;
+    acc = acc + trace_cone<SAMPLER, ISO, STORAGE>(m, origin, mixv(n, side, 0.5f), kTan22_5, kMaxDistance);
+  }
   return v3(acc.x, acc.y, acc.z) * (1.0f / 9.0f);
 }
 
@@ -227,7 +238,7 @@ __device__ __forceinline__ unsigned char unorm8(float v) {
 }
 
 template <int SAMPLER, bool ISO, int STORAGE>
-__global__ void __launch_bounds__(256) k_trace(SceneParams sp, CameraParams cp, MapSet m, TraceParams tp,
+__global__ void __launch_bounds__(256, SAMPLER == VCT_SAMPLER_HW ? kTraceMinBlocks : 1) k_trace(SceneParams sp, CameraParams cp, MapSet m, TraceParams tp,
                                                const float4* __restrict__ gb_pos, const float4* __restrict__ gb_nrm,
                                                uchar4* __restrict__ frame, float4* __restrict__ frame_f32) {
   const int px = blockIdx.x * 16 + (threadIdx.x & 15), py = blockIdx.y * 16 + (threadIdx.x >> 4);
@@ -257,8 +268,14 @@ __global__ void __launch_bounds__(256) k_trace(SceneParams sp, CameraParams cp, 
         const V3 cam = v3(cp.cam_pos[0], cp.cam_pos[1], cp.cam_pos[2]);
         const V3 view_dir = normalize(world - cam);
         V3 fd = v3(0.f, 0.f, 0.f), fdir = v3(0.f, 0.f, 0.f), fs = v3(0.f, 0.f, 0.f);
-        if (tp.enable_diffuse)
-          fd = mulv(mat3v(mat.diffuse), trace_diffuse<SAMPLER, ISO, STORAGE>(m, tp.cone_set, pos, nrm));
+        if (tp.enable_diffuse) {
+          if (tp.diffuse_in) {
+            const float4 d = tp.diffuse_in[p];
+            fd = mulv(mat3v(mat.diffuse), v3(d.x, d.y, d.z));
+          } else {
+            fd = mulv(mat3v(mat.diffuse), trace_diffuse<SAMPLER, ISO, STORAGE>(m, tp.cone_set, pos, nrm));
+          }
+        }
         if (tp.enable_direct)
           fdir = direct_light<SAMPLER, ISO, STORAGE>(sp, m, tp.enable_shadow, mat, pos, nrm, view_dir);
         const float sap = specular_aperture(mat.shininess);
@@ -290,7 +307,31 @@ cudaError_t run(const SceneParams& sp, const CameraParams& cp, const MapSet& ms,
   return cudaGetLastError();
 }
 
+// Training targets of the learned term: trace_diffuse (texture-unit sampler)
+// at each sample's texture-space position and normal (rows of 12 floats;
+// writes columns 9..11).
+template <bool ISO>
+__global__ void __launch_bounds__(256) k_trace_points(MapSet m, int cone_set, float* __restrict__ samples, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  float* q = samples + (size_t)i * 12;
+  const V3 pos = v3(q[0], q[1], q[2]), nrm = v3(q[3], q[4], q[5]);
+  const V3 d = trace_diffuse<VCT_SAMPLER_HW, ISO, VCT_STORAGE_RGBA8>(m, cone_set, pos, nrm);
+  q[9] = d.x;
+  q[10] = d.y;
+  q[11] = d.z;
+}
+
 }  // namespace
+
+cudaError_t launch_trace_points(const SceneParams&, const MapSet& ms, int mip_mode, int cone_set, float* samples,
+                                int n, cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  const unsigned grid = (unsigned)((n + 255) / 256);
+  if (mip_mode == VCT_MIP_ISO) k_trace_points<true><<<grid, 256, 0, st>>>(ms, cone_set, samples, n);
+  else k_trace_points<false><<<grid, 256, 0, st>>>(ms, cone_set, samples, n);
+  return cudaGetLastError();
+}
 
 cudaError_t launch_trace(const SceneParams& sp, const CameraParams& cp, const MapSet& ms, const TraceParams& tp,
                          const float4* gb_pos, const float4* gb_nrm, uchar4* frame, float4* frame_f32,

@@ -1,0 +1,485 @@
+// renderer_state.h -- the state behind a vct_renderer handle (shared by the
+// translation units of the C ABI; not a public header).
+#pragma once
+
+#include <cuda_fp16.h>
+
+#include <algorithm>
+#include <cfloat>
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <vector>
+
+#include "api_common.h"
+#include "vct_internal.h"
+
+using namespace vct;
+
+// --------------------------------------------------------- host maths -----
+namespace vct {
+namespace detail {
+
+// P * V in FP32, fixed summation order (the CPU oracle does the same).
+inline void matmul_f32(const float* P, const float* V, float* o) {
+  for (int c = 0; c < 4; ++c)
+    for (int r = 0; r < 4; ++r) {
+      float t = P[0 * 4 + r] * V[c * 4 + 0];
+      t = t + P[1 * 4 + r] * V[c * 4 + 1];
+      t = t + P[2 * 4 + r] * V[c * 4 + 2];
+      o[c * 4 + r] = t + P[3 * 4 + r] * V[c * 4 + 3];
+    }
+}
+
+// mat3(transpose(inverse(M))) (voxelize.vert:28), row-major float[9].
+inline void normal_matrix(const float* mf, float* nm) {
+  double m[16], inv[16];
+  for (int i = 0; i < 16; ++i) m[i] = mf[i];
+  inv[0] = m[5] * m[10] * m[15] - m[5] * m[11] * m[14] - m[9] * m[6] * m[15] + m[9] * m[7] * m[14] + m[13] * m[6] * m[11] - m[13] * m[7] * m[10];
+  inv[4] = -m[4] * m[10] * m[15] + m[4] * m[11] * m[14] + m[8] * m[6] * m[15] - m[8] * m[7] * m[14] - m[12] * m[6] * m[11] + m[12] * m[7] * m[10];
+  inv[8] = m[4] * m[9] * m[15] - m[4] * m[11] * m[13] - m[8] * m[5] * m[15] + m[8] * m[7] * m[13] + m[12] * m[5] * m[11] - m[12] * m[7] * m[9];
+  inv[12] = -m[4] * m[9] * m[14] + m[4] * m[10] * m[13] + m[8] * m[5] * m[14] - m[8] * m[6] * m[13] - m[12] * m[5] * m[10] + m[12] * m[6] * m[9];
+  inv[1] = -m[1] * m[10] * m[15] + m[1] * m[11] * m[14] + m[9] * m[2] * m[15] - m[9] * m[3] * m[14] - m[13] * m[2] * m[11] + m[13] * m[3] * m[10];
+  inv[5] = m[0] * m[10] * m[15] - m[0] * m[11] * m[14] - m[8] * m[2] * m[15] + m[8] * m[3] * m[14] + m[12] * m[2] * m[11] - m[12] * m[3] * m[10];
+  inv[9] = -m[0] * m[9] * m[15] + m[0] * m[11] * m[13] + m[8] * m[1] * m[15] - m[8] * m[3] * m[13] - m[12] * m[1] * m[11] + m[12] * m[3] * m[9];
+  inv[13] = m[0] * m[9] * m[14] - m[0] * m[10] * m[13] - m[8] * m[1] * m[14] + m[8] * m[2] * m[13] + m[12] * m[1] * m[10] - m[12] * m[2] * m[9];
+  inv[2] = m[1] * m[6] * m[15] - m[1] * m[7] * m[14] - m[5] * m[2] * m[15] + m[5] * m[3] * m[14] + m[13] * m[2] * m[7] - m[13] * m[3] * m[6];
+  inv[6] = -m[0] * m[6] * m[15] + m[0] * m[7] * m[14] + m[4] * m[2] * m[15] - m[4] * m[3] * m[14] - m[12] * m[2] * m[7] + m[12] * m[3] * m[6];
+  inv[10] = m[0] * m[5] * m[15] - m[0] * m[7] * m[13] - m[4] * m[1] * m[15] + m[4] * m[3] * m[13] + m[12] * m[1] * m[7] - m[12] * m[3] * m[5];
+  inv[14] = -m[0] * m[5] * m[14] + m[0] * m[6] * m[13] + m[4] * m[1] * m[14] - m[4] * m[2] * m[13] - m[12] * m[1] * m[6] + m[12] * m[2] * m[5];
+  inv[3] = -m[1] * m[6] * m[11] + m[1] * m[7] * m[10] + m[5] * m[2] * m[11] - m[5] * m[3] * m[10] - m[9] * m[2] * m[7] + m[9] * m[3] * m[6];
+  inv[7] = m[0] * m[6] * m[11] - m[0] * m[7] * m[10] - m[4] * m[2] * m[11] + m[4] * m[3] * m[10] + m[8] * m[2] * m[7] - m[8] * m[3] * m[6];
+  inv[11] = -m[0] * m[5] * m[11] + m[0] * m[7] * m[9] + m[4] * m[1] * m[11] - m[4] * m[3] * m[9] - m[8] * m[1] * m[7] + m[8] * m[3] * m[5];
+  inv[15] = m[0] * m[5] * m[10] - m[0] * m[6] * m[9] - m[4] * m[1] * m[10] + m[4] * m[2] * m[9] + m[8] * m[1] * m[6] - m[8] * m[2] * m[5];
+  const double det = m[0] * inv[0] + m[1] * inv[4] + m[2] * inv[8] + m[3] * inv[12];
+  const double id = det != 0.0 ? 1.0 / det : 0.0;
+  for (int r = 0; r < 3; ++r)
+    for (int c = 0; c < 3; ++c) nm[r * 3 + c] = (float)(inv[r * 4 + c] * id);
+}
+
+inline bool is_pow2(uint32_t v) { return v && !(v & (v - 1)); }
+inline int ilog2(uint32_t v) {
+  int l = 0;
+  while ((1u << (l + 1)) <= v) ++l;
+  return l;
+}
+
+struct Model {
+  DevBuf<vct_vert_data> verts;
+  DevBuf<uint32_t> indices;
+  DevBuf<uint32_t> tri_obj;
+  uint32_t n_verts = 0, n_tris = 0;
+  uint32_t obj_start = 0, obj_count = 0;
+  float dims[3] = {0, 0, 0};
+  float matrix[16];
+};
+
+struct Queued {
+  uint64_t model;
+  float M[16];
+};
+
+// Everything a frame reads, captured by vct_render so that a frame can be
+// re-encoded after its work buffers were grown.
+struct FrameInputs {
+  std::vector<Queued> queue;
+  std::vector<vct_point_light> lights;
+  float view[16], proj[16];
+  float cube_size;
+  TraceParams tp;
+};
+
+constexpr float kIdentity[16] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1};
+
+}  // namespace detail
+}  // namespace vct
+
+using namespace vct::detail;
+
+// Parameters, gradients and Adam state of the learned diffuse term.
+struct MlpState {
+  bool ready = false;  // parameters allocated and initialised
+  bool trained = false;
+  int32_t levels = 16, log2_table = 19, n_min = 16, n_max = 512;
+  int adam_t = 0;
+  DevBuf<float> table, table_grad, table_m, table_v;  // levels * T * 2
+  DevBuf<__nv_bfloat16> table_bf;
+  DevBuf<float> w, w_grad, w_m, w_v;  // kMlpWeights
+  DevBuf<__nv_bfloat16> w_bf;
+  DevBuf<float> samples;  // rows of 12 floats
+  uint32_t n_samples = 0;
+  DevBuf<float> loss;     // one slot per optimiser step
+
+  size_t table_floats() const { return (size_t)levels * ((size_t)1 << log2_table) * 2; }
+
+  MlpParams params() const {
+    MlpParams p;
+    std::memset(&p, 0, sizeof(p));
+    p.table_bf = table_bf.p;
+    p.table_grad = reinterpret_cast<float2*>(table_grad.p);
+    p.w_bf = w_bf.p;
+    p.w_grad = w_grad.p;
+    p.log2_table = log2_table;
+    const double b = std::exp((std::log((double)n_max) - std::log((double)n_min)) / (levels - 1));
+    for (int l = 0; l < levels && l < kMlpLevels; ++l) {
+      p.res[l] = (int)std::floor((double)n_min * std::pow(b, l) + 1e-6);
+      const uint64_t r1 = (uint64_t)p.res[l] + 1;
+      if (r1 * r1 * r1 <= ((uint64_t)1 << log2_table)) p.dense_mask |= 1 << l;
+    }
+    return p;
+  }
+};
+
+struct vct_renderer {
+  int W = 0, H = 0;
+  vct_config cfg;
+  // resources (renderer.h:168-171)
+  std::vector<vct_material_data> materials;
+  std::vector<vct_draw_obj> objs;
+  std::vector<std::unique_ptr<Model>> models;
+  uint64_t next_shader = 0;
+  bool materials_dirty = true, objs_dirty = true;
+  // settings (renderer.h:173-186)
+  float view[16], proj[16];
+  float cube_size = 1.0f;
+  uint32_t res = 0;
+  int levels = 0;
+  bool en_shadow = true, en_direct = true, en_diffuse = true, en_specular = true;
+  int view_dir = 0;  // Renderer::Renderer sets m_view_voxel_dir(0), renderer.cpp:107
+  float view_lod = 0.0f;
+  // per frame (renderer.h:190-191)
+  std::vector<Queued> queue;
+  std::vector<vct_point_light> lights;
+  FrameInputs last;
+  bool have_last = false;
+  // GPU state
+  cudaStream_t own_stream = nullptr, stream = nullptr;
+  cudaEvent_t ev[5] = {};
+  cudaEvent_t ev_staged = nullptr;
+  cudaEvent_t ev_done = nullptr;   // after the frame's status copy
+  cudaArray_t l0_arr = nullptr;
+  cudaMipmappedArray_t dir_arr[kMaxMaps] = {};
+  MapSet ms = {};
+  DevBuf<vct_material_data> d_materials;
+  DevBuf<uint32_t> d_obj_material;
+  DevBuf<DevInstance> d_inst;
+  HostBuf<DevInstance> h_inst;
+  DevBuf<uint32_t> brick_count, brick_offset, brick_cursor, pair_list, scan_tmp, counts;
+  DevBuf<FrameStatus> d_status;
+  HostBuf<FrameStatus> h_status;
+  DevBuf<unsigned long long> vis;
+  DevBuf<unsigned char> big;
+  DevBuf<uint32_t> big_count, big_offset;
+  uint32_t big_cap = 0;
+  DevBuf<float4> gb_pos, gb_nrm;
+  DevBuf<uchar4> frame;
+  DevBuf<float4> frame_f32;
+  bool frame_pending = false;
+  bool have_frame = false;
+  int launches = 0;  // engine kernels of the last encoded frame
+  // learned diffuse term
+  int diffuse_mode = VCT_DIFFUSE_CONES;
+  MlpState mlp;
+  DevBuf<float4> diffuse_px;
+  SceneParams last_sp;  // scene of the last encoded frame (training samples come from it)
+  bool have_sp = false;
+
+  ~vct_renderer() {
+    if (stream) cudaStreamSynchronize(stream);
+    free_maps();
+    for (auto& e : ev)
+      if (e) cudaEventDestroy(e);
+    if (ev_staged) cudaEventDestroy(ev_staged);
+    if (ev_done) cudaEventDestroy(ev_done);
+    if (own_stream) cudaStreamDestroy(own_stream);
+  }
+
+  void free_maps() {
+    if (ms.l0_tex) cudaDestroyTextureObject(ms.l0_tex);
+    if (ms.l0_surf) cudaDestroySurfaceObject(ms.l0_surf);
+    for (int d = 0; d < kMaxMaps; ++d) {
+      if (ms.tex[d]) cudaDestroyTextureObject(ms.tex[d]);
+      for (int l = 0; l < kMaxLevels; ++l)
+        if (ms.surf[d][l]) cudaDestroySurfaceObject(ms.surf[d][l]);
+      if (dir_arr[d]) cudaFreeMipmappedArray(dir_arr[d]);
+      dir_arr[d] = nullptr;
+    }
+    if (l0_arr) cudaFreeArray(l0_arr);
+    l0_arr = nullptr;
+    std::memset(&ms, 0, sizeof(ms));
+  }
+
+  cudaChannelFormatDesc texel_desc() const {
+    return cfg.storage == VCT_STORAGE_RGBA16F ? cudaCreateChannelDesc(16, 16, 16, 16, cudaChannelFormatKindFloat)
+                                              : cudaCreateChannelDesc(8, 8, 8, 8, cudaChannelFormatKindUnsigned);
+  }
+
+  // set_grid_resolution (renderer.cpp:178-188): six 3D textures of `levels`
+  // mip levels.  Here: level 0 once + one chain (levels 1..L-1) per map.
+  vct_status alloc_maps(uint32_t r) {
+    if (stream) VCT_CUDA(cudaStreamSynchronize(stream));
+    free_maps();
+    const int L = std::min(kMaxLevels, ilog2(r) + 1);
+    const int nmaps = cfg.mip_mode == VCT_MIP_ISO ? 1 : 6;
+    const cudaChannelFormatDesc desc = texel_desc();
+    VCT_CUDA(cudaMalloc3DArray(&l0_arr, &desc, make_cudaExtent(r, r, r), cudaArraySurfaceLoadStore));
+    cudaResourceDesc rd;
+    std::memset(&rd, 0, sizeof(rd));
+    rd.resType = cudaResourceTypeArray;
+    rd.res.array.array = l0_arr;
+    VCT_CUDA(cudaCreateSurfaceObject(&ms.l0_surf, &rd));
+    cudaTextureDesc td;
+    std::memset(&td, 0, sizeof(td));
+    td.addressMode[0] = td.addressMode[1] = td.addressMode[2] = cudaAddressModeBorder;
+    td.filterMode = cudaFilterModeLinear;
+    td.readMode = cfg.storage == VCT_STORAGE_RGBA16F ? cudaReadModeElementType : cudaReadModeNormalizedFloat;
+    td.normalizedCoords = 1;
+    td.mipmapFilterMode = cudaFilterModeLinear;
+    VCT_CUDA(cudaCreateTextureObject(&ms.l0_tex, &rd, &td, nullptr));
+    for (int d = 0; d < nmaps && L > 1; ++d) {
+      VCT_CUDA(cudaMallocMipmappedArray(&dir_arr[d], &desc, make_cudaExtent(r / 2, r / 2, r / 2), L - 1,
+                                        cudaArraySurfaceLoadStore));
+      for (int l = 1; l < L; ++l) {
+        cudaArray_t la;
+        VCT_CUDA(cudaGetMipmappedArrayLevel(&la, dir_arr[d], l - 1));
+        cudaResourceDesc lr;
+        std::memset(&lr, 0, sizeof(lr));
+        lr.resType = cudaResourceTypeArray;
+        lr.res.array.array = la;
+        VCT_CUDA(cudaCreateSurfaceObject(&ms.surf[d][l], &lr));
+      }
+      cudaResourceDesc mr;
+      std::memset(&mr, 0, sizeof(mr));
+      mr.resType = cudaResourceTypeMipmappedArray;
+      mr.res.mipmap.mipmap = dir_arr[d];
+      cudaTextureDesc mt = td;
+      mt.minMipmapLevelClamp = 0.0f;
+      mt.maxMipmapLevelClamp = (float)(L - 2);
+      VCT_CUDA(cudaCreateTextureObject(&ms.tex[d], &mr, &mt, nullptr));
+    }
+    ms.N = (int)r;
+    ms.L = L;
+    ms.nmaps = nmaps;
+    ms.storage = cfg.storage;
+    res = r;
+    levels = L;
+    const size_t nb = (size_t)(r / kBrick) * (r / kBrick) * (r / kBrick);
+    VCT_CHECK(brick_count.ensure(nb));
+    VCT_CHECK(brick_offset.ensure(nb + 1));
+    VCT_CHECK(brick_cursor.ensure(nb));
+    VCT_CHECK(scan_tmp.ensure(scan_tmp_words(nb)));
+    if (cfg.keep_counts) VCT_CHECK(counts.ensure((size_t)r * r * r));
+    have_frame = false;
+    return VCT_OK;
+  }
+
+  vct_status init(int w, int h, const vct_config* c) {
+    W = w;
+    H = h;
+    if (c) cfg = *c; else vct_config_default(&cfg);
+    std::memcpy(view, kIdentity, sizeof(view));
+    std::memcpy(proj, kIdentity, sizeof(proj));
+    VCT_CUDA(cudaStreamCreateWithFlags(&own_stream, cudaStreamNonBlocking));
+    stream = own_stream;
+    for (auto& e : ev) VCT_CUDA(cudaEventCreate(&e));
+    VCT_CUDA(cudaEventCreateWithFlags(&ev_staged, cudaEventDisableTiming));
+    VCT_CUDA(cudaEventCreateWithFlags(&ev_done, cudaEventDisableTiming));
+    // Default material (renderer.cpp:115-128, fill_default_mat_data :85-98).
+    vct_material_data m;
+    std::memset(&m, 0, sizeof(m));
+    m.ambient[0] = 1; m.ambient[2] = 1;
+    m.diffuse[0] = 1; m.diffuse[2] = 1;
+    m.shininess = 1; m.ior = 1; m.dissolve = 1; m.illum = 0;
+    materials.push_back(m);
+    const size_t px = (size_t)W * H;
+    VCT_CHECK(vis.ensure(px));
+    VCT_CHECK(gb_pos.ensure(px));
+    VCT_CHECK(gb_nrm.ensure(px));
+    VCT_CHECK(frame.ensure(px));
+    if (cfg.keep_float_frame) VCT_CHECK(frame_f32.ensure(px));
+    VCT_CHECK(d_status.ensure(1));
+    VCT_CHECK(h_status.ensure(1));
+    std::memset(h_status.p, 0, sizeof(FrameStatus));
+    VCT_CHECK(big_count.ensure(2));
+    VCT_CHECK(grow_big(1 << 16));
+    return alloc_maps((uint32_t)cfg.grid_res);
+  }
+
+  vct_status grow_big(uint32_t cap) {
+    VCT_CHECK(big.ensure((size_t)cap * big_record_bytes()));
+    VCT_CHECK(big_offset.ensure((size_t)cap + 1));
+    big_cap = cap;
+    return VCT_OK;
+  }
+
+  vct_status upload_tables() {
+    if (materials_dirty) {
+      VCT_CHECK(d_materials.ensure(materials.size()));
+      VCT_CUDA(cudaMemcpyAsync(d_materials.p, materials.data(), materials.size() * sizeof(vct_material_data),
+                               cudaMemcpyHostToDevice, stream));
+      VCT_CUDA(cudaStreamSynchronize(stream));
+      materials_dirty = false;
+    }
+    if (objs_dirty) {
+      std::vector<uint32_t> om(std::max<size_t>(objs.size(), 1), 0);
+      for (size_t i = 0; i < objs.size(); ++i) om[i] = objs[i].material_id;
+      VCT_CHECK(d_obj_material.ensure(om.size()));
+      VCT_CUDA(cudaMemcpyAsync(d_obj_material.p, om.data(), om.size() * sizeof(uint32_t), cudaMemcpyHostToDevice,
+                               stream));
+      VCT_CUDA(cudaStreamSynchronize(stream));
+      objs_dirty = false;
+    }
+    return VCT_OK;
+  }
+
+  vct_status encode(const FrameInputs& fi) {
+    // Material ids of every queued draw object must exist (the reference
+    // indexes m_materials unchecked, renderer.cpp:252).
+    uint64_t total = 0;
+    for (const Queued& q : fi.queue) {
+      const Model& m = *models[q.model];
+      for (uint32_t o = 0; o < m.obj_count; ++o)
+        if (objs[m.obj_start + o].material_id >= materials.size())
+          return set_error(VCT_ERR_INVALID_ID, "draw object %u of model %llu uses material %u (only %zu exist)", o,
+                           (unsigned long long)q.model, objs[m.obj_start + o].material_id, materials.size());
+      total += m.n_tris;
+    }
+    if (total >= 0xffffffffull) return set_error(VCT_ERR_INVALID_VALUE, "too many queued triangles");
+    VCT_CHECK(upload_tables());
+    const size_t ni = std::max<size_t>(fi.queue.size(), 1);
+    VCT_CHECK(d_inst.ensure(ni));
+    VCT_CUDA(cudaEventSynchronize(ev_staged));  // previous upload has left the staging buffer
+    VCT_CHECK(h_inst.ensure(ni));
+    uint32_t base = 0;
+    for (size_t i = 0; i < fi.queue.size(); ++i) {
+      const Model& m = *models[fi.queue[i].model];
+      DevInstance& d = h_inst.p[i];
+      std::memcpy(d.M, fi.queue[i].M, sizeof(d.M));
+      normal_matrix(fi.queue[i].M, d.NM);
+      d.tri_base = base;
+      d.n_tris = m.n_tris;
+      d.verts = m.verts.p;
+      d.indices = m.indices.p;
+      d.tri_obj = m.tri_obj.p;
+      d.n_verts = m.n_verts;
+      d.pad = 0;
+      base += m.n_tris;
+    }
+    if (!fi.queue.empty())
+      VCT_CUDA(cudaMemcpyAsync(d_inst.p, h_inst.p, fi.queue.size() * sizeof(DevInstance), cudaMemcpyHostToDevice,
+                               stream));
+    VCT_CUDA(cudaEventRecord(ev_staged, stream));
+
+    SceneParams sp;
+    std::memset(&sp, 0, sizeof(sp));
+    sp.inst = d_inst.p;
+    sp.materials = d_materials.p;
+    sp.obj_material = d_obj_material.p;
+    sp.n_instances = (uint32_t)fi.queue.size();
+    sp.total_tris = (uint32_t)total;
+    sp.n_materials = (uint32_t)materials.size();
+    sp.n_lights = (int32_t)std::min<size_t>(fi.lights.size(), kMaxLights);
+    sp.cube_size = fi.cube_size;
+    for (int i = 0; i < sp.n_lights; ++i) sp.lights[i] = fi.lights[i];
+
+    CameraParams cp;
+    matmul_f32(fi.proj, fi.view, cp.PV);
+    cp.cam_pos[0] = fi.view[12];  // glm::column(view, 3), renderer.cpp:279
+    cp.cam_pos[1] = fi.view[13];
+    cp.cam_pos[2] = fi.view[14];
+    cp.W = W;
+    cp.H = H;
+
+    const uint32_t pairs_needed = (uint32_t)std::min<uint64_t>(0xffffff00ull, 4ull * total + 65536ull);
+    if (pair_list.n < pairs_needed) VCT_CHECK(pair_list.ensure(pairs_needed));
+
+    VoxBuffers vb;
+    vb.brick_count = brick_count.p;
+    vb.brick_offset = brick_offset.p;
+    vb.brick_cursor = brick_cursor.p;
+    vb.pair_list = pair_list.p;
+    vb.pair_cap = (uint32_t)pair_list.n;
+    vb.scan_tmp = scan_tmp.p;
+    vb.counts = cfg.keep_counts ? counts.p : nullptr;
+    vb.status = d_status.p;
+
+    RasterBuffers rb;
+    rb.vis = vis.p;
+    rb.big = big.p;
+    rb.big_cap = big_cap;
+    rb.big_count = big_count.p;
+    rb.big_offset = big_offset.p;
+    rb.scan_tmp = nullptr;
+    rb.gb_pos = gb_pos.p;
+    rb.gb_nrm = gb_nrm.p;
+    rb.status = d_status.p;
+
+    VCT_CUDA(cudaMemsetAsync(d_status.p, 0, sizeof(FrameStatus), stream));
+    launches = 0;
+    VCT_CUDA(cudaEventRecord(ev[0], stream));
+    VCT_CUDA(launch_voxelize(sp, (int)res, cfg.vox_mode, cfg.storage, vb, ms.l0_surf, stream, &launches));
+    VCT_CUDA(cudaEventRecord(ev[1], stream));
+    VCT_CUDA(launch_mipmap(ms, cfg.mip_mode, stream, &launches));
+    VCT_CUDA(cudaEventRecord(ev[2], stream));
+    VCT_CUDA(launch_gbuffer(sp, cp, rb, stream, &launches));
+    VCT_CUDA(cudaEventRecord(ev[3], stream));
+    TraceParams tp = fi.tp;
+    tp.diffuse_in = nullptr;
+    if (diffuse_mode == VCT_DIFFUSE_MLP && mlp.trained && tp.enable_diffuse && tp.view_voxel_dir >= 7) {
+      // The learned term replaces the nine diffuse cones (its time counts as trace time).
+      VCT_CHECK(diffuse_px.ensure((size_t)W * H));
+      VCT_CUDA(launch_mlp_infer(mlp.params(), sp, gb_pos.p, gb_nrm.p, W * H, diffuse_px.p, stream));
+      ++launches;
+      tp.diffuse_in = diffuse_px.p;
+    }
+    VCT_CUDA(launch_trace(sp, cp, ms, tp, gb_pos.p, gb_nrm.p, frame.p, cfg.keep_float_frame ? frame_f32.p : nullptr,
+                          stream, &launches));
+    last_sp = sp;
+    have_sp = true;
+    VCT_CUDA(cudaEventRecord(ev[4], stream));
+    VCT_CUDA(cudaMemcpyAsync(h_status.p, d_status.p, sizeof(FrameStatus), cudaMemcpyDeviceToHost, stream));
+    VCT_CUDA(cudaEventRecord(ev_done, stream));
+    frame_pending = true;
+    have_frame = true;
+    return VCT_OK;
+  }
+
+  // Wait for the last frame; if a work list overflowed, grow it and encode
+  // the same frame again (results are exact once this returns).
+  vct_status finish() {
+    if (!frame_pending) return VCT_OK;
+    for (int attempt = 0; attempt < 4; ++attempt) {
+      VCT_CUDA(cudaStreamSynchronize(stream));
+      frame_pending = false;
+      const FrameStatus s = *h_status.p;
+      bool redo = false;
+      if (s.pair_total > pair_list.n) {
+        VCT_CHECK(pair_list.ensure((size_t)s.pair_total + s.pair_total / 4 + 4096));
+        redo = true;
+      }
+      if (s.big_total > big_cap) {
+        VCT_CHECK(grow_big(s.big_total + s.big_total / 4 + 1024));
+        redo = true;
+      }
+      if (!redo) return VCT_OK;
+      if (!have_last) return VCT_OK;
+      VCT_CHECK(encode(last));
+    }
+    return set_error(VCT_ERR_CUDA, "frame work lists kept overflowing");
+  }
+
+  TraceParams trace_params() const {
+    TraceParams tp;
+    tp.enable_direct = en_direct;
+    tp.enable_diffuse = en_diffuse;
+    tp.enable_specular = en_specular;
+    tp.enable_shadow = en_shadow;
+    tp.view_voxel_dir = view_dir;
+    tp.view_voxel_lod = view_lod;
+    tp.cone_set = cfg.cone_set;
+    tp.sampler = cfg.sampler;
+    tp.mip_mode = cfg.mip_mode;
+    tp.diffuse_in = nullptr;
+    return tp;
+  }
+};

@@ -1,6 +1,7 @@
 // vct_internal.h -- structures shared by the host renderer and the kernels.
 #pragma once
 
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -95,6 +96,33 @@ struct TraceParams {
   int cone_set;
   int sampler;
   int mip_mode;
+  // Per-pixel trace_diffuse from the learned term (null: trace the cones).
+  const float4* diffuse_in;
+};
+
+// ---- learned diffuse term (k_mlp.cu) --------------------------------------
+constexpr int kMlpLevels = 16;
+constexpr int kMlpWeights = 5 * 64 * 64;  // W1..W4 64x64, W5 16x64 (padded to 64 rows)
+
+struct MlpParams {
+  const void* table_bf;     // [levels][2^log2_table] bf16 feature pairs
+  float2* table_grad;       // [levels][2^log2_table] (training)
+  const __nv_bfloat16* w_bf;  // [5][64][64] [out][in]
+  float* w_grad;            // [5][64][64] (training)
+  int log2_table;
+  int dense_mask;           // bit l: level l is indexed densely
+  int res[kMlpLevels];      // grid resolution of each level
+};
+
+// A training batch: rows of 12 floats (texture-space position, normal,
+// albedo, target RGB), `n` rows starting at row `first` (mod `total`).
+struct MlpBatch {
+  const float* samples;
+  int first, n, total;
+};
+
+struct AdamStep {
+  float lr, beta1, beta2, eps, c1, c2, l2;  // c1 = 1/(1-beta1^t), c2 = 1/(1-beta2^t)
 };
 
 // ---- launchers (stream-ordered, no host synchronisation) ----------------
@@ -118,5 +146,22 @@ cudaError_t launch_box_mip_rgba8(cudaSurfaceObject_t src, int sw, int sh, int sd
                                  int dh, int dd, cudaStream_t st);
 
 size_t big_record_bytes();
+
+// Learned diffuse term.
+cudaError_t launch_mlp_init(float* prm, __nv_bfloat16* prm_bf, size_t n, float scale, uint64_t seed, cudaStream_t st);
+cudaError_t launch_mlp_train(const MlpParams& p, const MlpBatch& b, float* loss, cudaStream_t st);
+cudaError_t launch_adam(float* prm, float* grad, float* m, float* v, __nv_bfloat16* prm_bf, size_t n,
+                        const AdamStep& a, cudaStream_t st);
+cudaError_t launch_mlp_infer(const MlpParams& p, const SceneParams& sp, const float4* gb_pos, const float4* gb_nrm,
+                             int n_px, float4* out, cudaStream_t st);
+cudaError_t launch_mlp_eval(const MlpParams& p, const float* samples, int n, float* out, cudaStream_t st);
+// Training data: world-space area of every queued triangle; surface samples
+// drawn from the area CDF (rows of 12 floats, see MlpBatch); their
+// cone-traced diffuse targets (trace_diffuse with the texture-unit sampler).
+cudaError_t launch_tri_area(const SceneParams& sp, float* area, cudaStream_t st);
+cudaError_t launch_sample_surface(const SceneParams& sp, const float* cdf, int n, uint64_t seed, float* samples,
+                                  cudaStream_t st);
+cudaError_t launch_trace_points(const SceneParams& sp, const MapSet& ms, int mip_mode, int cone_set, float* samples,
+                                int n, cudaStream_t st);
 
 }  // namespace vct

@@ -37,7 +37,31 @@ EXPORTS = [
     "vct_synchronize", "vct_get_stage_times", "vct_read_frame", "vct_frame_device_ptr", "vct_read_voxels",
     "vct_read_voxel_counts", "vct_read_gbuffer", "vct_get_grid", "vct_create_tex_3d", "vct_destroy_tex_3d",
     "vct_activate_tex_3d", "vct_clear_tex_3d", "vct_mip_tex_3d", "vct_tex3d_upload", "vct_tex3d_download",
+    "vct_mlp_desc_default", "vct_mlp_init", "vct_mlp_train", "vct_set_diffuse_mode", "vct_mlp_save",
+    "vct_mlp_load", "vct_mlp_get_params", "vct_mlp_set_params", "vct_mlp_eval", "vct_mlp_gradients",
+    "vct_mlp_train_samples",
 ]
+DIFFUSE_CONES, DIFFUSE_MLP = 0, 1
+MLP_WEIGHTS = 5 * 64 * 64
+
+
+class MLPDesc(C.Structure):
+    _fields_ = [("levels", C.c_int32), ("log2_table", C.c_int32), ("n_min", C.c_int32), ("n_max", C.c_int32),
+                ("n_samples", C.c_uint32), ("batch", C.c_uint32), ("steps", C.c_uint32), ("lr", C.c_float),
+                ("seed", C.c_uint64), ("reserved", C.c_uint32 * 8)]
+
+
+class MLPReport(C.Structure):
+    _fields_ = [("loss_first", C.c_float), ("loss_last", C.c_float), ("ms_samples", C.c_float),
+                ("ms_train", C.c_float), ("steps", C.c_uint32), ("n_samples", C.c_uint32)]
+
+
+def mlp_desc(**kw) -> MLPDesc:
+    d = MLPDesc()
+    lib().vct_mlp_desc_default(C.byref(d))
+    for k, v in kw.items():
+        setattr(d, k, type(getattr(d, k))(v))
+    return d
 
 
 class VCTError(RuntimeError):
@@ -94,6 +118,11 @@ def lib() -> C.CDLL:
             "vct_activate_tex_3d": (I32, [U32, U32, U32]), "vct_clear_tex_3d": (I32, [U32, P]),
             "vct_mip_tex_3d": (I32, [U32]), "vct_tex3d_upload": (I32, [U32, I32, P]),
             "vct_tex3d_download": (I32, [U32, I32, P]),
+            "vct_mlp_desc_default": (None, [P]), "vct_mlp_init": (I32, [P, P]), "vct_mlp_train": (I32, [P, P, P]),
+            "vct_set_diffuse_mode": (I32, [P, I32]), "vct_mlp_save": (I32, [P, C.c_char_p]),
+            "vct_mlp_load": (I32, [P, C.c_char_p]), "vct_mlp_get_params": (I32, [P, P, P]),
+            "vct_mlp_set_params": (I32, [P, P, P]), "vct_mlp_eval": (I32, [P, P, U32, P]),
+            "vct_mlp_gradients": (I32, [P, P, U32, P, P, P]), "vct_mlp_train_samples": (I32, [P, P, U32, P, P]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
@@ -268,6 +297,57 @@ class Renderer:
         out = np.empty((n, n, n), np.uint32)
         _check(lib().vct_read_voxel_counts(self._r, out.ctypes.data))
         return out
+
+    # ---- learned diffuse term (engine extension) -------------------------
+    def mlp_init(self, desc: MLPDesc | None = None) -> None:
+        _check(lib().vct_mlp_init(self._r, C.byref(desc) if desc is not None else None))
+
+    def mlp_train(self, desc: MLPDesc | None = None) -> dict:
+        rep = MLPReport()
+        _check(lib().vct_mlp_train(self._r, C.byref(desc) if desc is not None else None, C.byref(rep)))
+        return {k: getattr(rep, k) for k, _ in MLPReport._fields_}
+
+    def mlp_train_samples(self, samples: np.ndarray, desc: MLPDesc | None = None) -> dict:
+        s = np.ascontiguousarray(samples, np.float32).reshape(-1, 12)
+        rep = MLPReport()
+        _check(lib().vct_mlp_train_samples(self._r, s.ctypes.data, s.shape[0],
+                                           C.byref(desc) if desc is not None else None, C.byref(rep)))
+        return {k: getattr(rep, k) for k, _ in MLPReport._fields_}
+
+    def set_diffuse_mode(self, mode: int) -> None:
+        _check(lib().vct_set_diffuse_mode(self._r, int(mode)))
+
+    def mlp_save(self, path: str) -> None:
+        _check(lib().vct_mlp_save(self._r, path.encode()))
+
+    def mlp_load(self, path: str) -> None:
+        _check(lib().vct_mlp_load(self._r, path.encode()))
+
+    def mlp_get_params(self, levels=16, log2_table=19):
+        t = np.empty((levels, 1 << log2_table, 2), np.float32)
+        w = np.empty((5, 64, 64), np.float32)
+        _check(lib().vct_mlp_get_params(self._r, t.ctypes.data, w.ctypes.data))
+        return t, w
+
+    def mlp_set_params(self, table: np.ndarray, weights: np.ndarray) -> None:
+        t = np.ascontiguousarray(table, np.float32)
+        w = np.ascontiguousarray(weights, np.float32)
+        _check(lib().vct_mlp_set_params(self._r, t.ctypes.data, w.ctypes.data))
+
+    def mlp_eval(self, samples: np.ndarray) -> np.ndarray:
+        s = np.ascontiguousarray(samples, np.float32).reshape(-1, 12)
+        out = np.empty((s.shape[0], 3), np.float32)
+        _check(lib().vct_mlp_eval(self._r, s.ctypes.data, s.shape[0], out.ctypes.data))
+        return out
+
+    def mlp_gradients(self, samples: np.ndarray, levels=16, log2_table=19):
+        s = np.ascontiguousarray(samples, np.float32).reshape(-1, 12)
+        loss = np.zeros(1, np.float32)
+        dw = np.empty((5, 64, 64), np.float32)
+        dt = np.empty((levels, 1 << log2_table, 2), np.float32)
+        _check(lib().vct_mlp_gradients(self._r, s.ctypes.data, s.shape[0], loss.ctypes.data, dw.ctypes.data,
+                                       dt.ctypes.data))
+        return float(loss[0]), dw, dt
 
     def read_gbuffer(self) -> dict:
         h, w = self.height, self.width
