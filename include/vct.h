@@ -283,6 +283,45 @@ vct_status vct_mlp_gradients(vct_renderer* r, const float* samples, uint32_t n, 
 vct_status vct_mlp_train_samples(vct_renderer* r, const float* samples, uint32_t n,
                                  const vct_mlp_desc* d, vct_mlp_report* report);
 
+/* ------------------------------------------ allocation-free voxelizer --- */
+
+/* No counterpart in the reference: an engine addition for callers that
+ * cannot allocate device memory -- applications that own every device
+ * allocation through their own heaps and forbid cudaMalloc / cudaFree inside
+ * their frame loop (those calls can synchronise the device and stall the
+ * frame, or are simply not theirs to make).  Everything below is caller
+ * memory; the voxelizer's intermediates live in a fixed device array inside
+ * the library (about 9 MB per GPU, held while the library is loaded).
+ *
+ * A mesh already on the device: vertices (vert_data_t layout), u32
+ * indices, a material id per triangle (< n_materials), its model matrix. */
+typedef struct {
+  const vct_vert_data* verts;     /* device */
+  const uint32_t* indices;        /* device, 3 per triangle */
+  const uint32_t* tri_material;   /* device, one id per triangle */
+  uint32_t n_verts;
+  uint32_t n_tris;
+  float model[16];                /* column-major, host */
+} vct_device_mesh;
+
+/* Voxelize meshes (host array of descriptors) into level0_rgba8 (device,
+ * grid_res^3 x 4 bytes, x fastest, fully overwritten) with the same kernels
+ * and coverage rules as vct_render's level 0.  materials: device array;
+ * lights: host array (at most 10 used).  Limits: grid_res a power of two in
+ * [8, 256], <= 64 meshes, <= 4096 materials, <= 2^21 (triangle, 8^3-voxel
+ * brick) pairs; beyond them the call fails with VCT_ERR_INVALID_VALUE (the
+ * pair count is known only after binning, so that case fails after the GPU
+ * work and leaves the output incomplete).  The first call on a device looks
+ * up the library's device array once; calls share that array, so calls
+ * whose GPU work overlaps (other streams / threads) race -- serialise them.
+ * Synchronises `stream` (a cudaStream_t, NULL = default stream) before
+ * returning. */
+vct_status vct_voxelize_noalloc(const vct_device_mesh* meshes, uint32_t n_meshes,
+                                const vct_material_data* materials, uint32_t n_materials,
+                                const vct_point_light* lights, uint32_t n_lights,
+                                float cube_size, int32_t grid_res, int32_t vox_mode,
+                                void* level0_rgba8, void* stream);
+
 /* ------------------------------------------------------- Texture3D ----- */
 
 typedef uint32_t vct_tex3d;   /* 0 = no texture, like a GL name */

@@ -559,7 +559,100 @@ __global__ void __launch_bounds__(kThreads) k_bricks(SceneParams sp, int N, cons
   }
 }
 
+// The same brick CTA writing RGBA8 level 0 into linear memory (x fastest)
+// instead of a surface: the output of vct_voxelize_noalloc.
+template <int MODE>
+__global__ void __launch_bounds__(kThreads) k_bricks_linear(SceneParams sp, int N, const uint32_t* __restrict__ offset,
+                                                            const uint32_t* __restrict__ list, uint32_t cap,
+                                                            uchar4* __restrict__ out) {
+  typedef typename std::conditional<MODE == VCT_VOX_CONSERVATIVE, SetupSat, SetupRef>::type Setup;
+  __shared__ Acc acc;
+  __shared__ Setup setup[kWarps][32];
+  __shared__ int excl[kWarps][33];
+  const int nb = N / kBrick;
+  const uint32_t brick = blockIdx.x;
+  const int b3[3] = {(int)(brick % nb), (int)((brick / nb) % nb), (int)(brick / ((uint32_t)nb * nb))};
+  for (int i = threadIdx.x; i < kBrickVox; i += kThreads) {
+    acc.c[0][i] = 0; acc.c[1][i] = 0; acc.c[2][i] = 0; acc.c[3][i] = 0; acc.n[i] = 0;
+  }
+  __syncthreads();
+  const uint32_t beg = min(offset[brick], cap), end = min(offset[brick + 1], cap);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (uint32_t base = beg + warp * 32; base < end; base += kWarps * 32) {
+    const uint32_t e = base + lane;
+    int cnt = 0;
+    if (e < end) {
+      if (MODE == VCT_VOX_CONSERVATIVE)
+        cnt = setup_sat(sp, N, __ldg(list + e), b3, reinterpret_cast<SetupSat&>(setup[warp][lane]));
+      else
+        cnt = setup_ref(sp, N, __ldg(list + e), b3, reinterpret_cast<SetupRef&>(setup[warp][lane]));
+    }
+    int incl = cnt;
+    for (int o = 1; o < 32; o <<= 1) {
+      int v = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += v;
+    }
+    excl[warp][lane] = incl - cnt;
+    const int total = __shfl_sync(0xffffffffu, incl, 31);
+    __syncwarp();
+    for (int it = lane; it < total; it += 32) {
+      int lo = 0, hi = 31;
+      while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (excl[warp][mid] <= it) lo = mid; else hi = mid - 1;
+      }
+      const int local = it - excl[warp][lo];
+      if (MODE == VCT_VOX_CONSERVATIVE)
+        item_sat(sp, N, b3, reinterpret_cast<const SetupSat&>(setup[warp][lo]), local, acc);
+      else
+        item_ref(sp, N, b3, reinterpret_cast<const SetupRef&>(setup[warp][lo]), local, acc);
+    }
+    __syncwarp();
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < kBrickVox; i += kThreads) {
+    const uint32_t n = acc.n[i];
+    const int x = b3[0] * kBrick + (i & 7), y = b3[1] * kBrick + ((i >> 3) & 7), z = b3[2] * kBrick + (i >> 6);
+    uchar4 o = make_uchar4(0, 0, 0, 0);
+    if (n) {
+      const unsigned long long den = 2ull * n * 65535ull;
+      unsigned char q[4];
+      for (int ch = 0; ch < 4; ++ch) {
+        unsigned long long v = ((unsigned long long)acc.c[ch][i] * 510ull + (unsigned long long)n * 65535ull) / den;
+        q[ch] = (unsigned char)(v > 255ull ? 255ull : v);
+      }
+      o = make_uchar4(q[0], q[1], q[2], q[3]);
+    }
+    out[((size_t)z * N + y) * N + x] = o;
+  }
+}
+
 }  // namespace
+
+cudaError_t launch_voxelize_linear(const SceneParams& sp, int N, int mode, const VoxBuffers& vb, uchar4* out,
+                                   cudaStream_t st) {
+  const int nb = N / kBrick;
+  const size_t n_bricks = (size_t)nb * nb * nb;
+  cudaError_t e = cudaMemsetAsync(vb.brick_count, 0, n_bricks * sizeof(uint32_t), st);
+  if (e != cudaSuccess) return e;
+  const unsigned tri_blocks = (sp.total_tris + 255) / 256;
+  if (tri_blocks)
+    k_bin<false><<<tri_blocks, 256, 0, st>>>(sp, N, vb.brick_count, nullptr, nullptr, 0, vb.status);
+  e = launch_exclusive_scan(vb.brick_count, vb.brick_offset, vb.brick_cursor, n_bricks, vb.scan_tmp, st);
+  if (e != cudaSuccess) return e;
+  e = cudaMemcpyAsync(&vb.status->pair_total, vb.brick_offset + n_bricks, sizeof(uint32_t), cudaMemcpyDeviceToDevice,
+                      st);
+  if (e != cudaSuccess) return e;
+  if (tri_blocks)
+    k_bin<true><<<tri_blocks, 256, 0, st>>>(sp, N, nullptr, vb.brick_cursor, vb.pair_list, vb.pair_cap, vb.status);
+  if (mode == VCT_VOX_CONSERVATIVE)
+    k_bricks_linear<VCT_VOX_CONSERVATIVE><<<(unsigned)n_bricks, kThreads, 0, st>>>(sp, N, vb.brick_offset,
+                                                                                 vb.pair_list, vb.pair_cap, out);
+  else
+    k_bricks_linear<VCT_VOX_REF_RASTER2X><<<(unsigned)n_bricks, kThreads, 0, st>>>(sp, N, vb.brick_offset,
+                                                                                 vb.pair_list, vb.pair_cap, out);
+  return cudaGetLastError();
+}
 
 cudaError_t launch_voxelize(const SceneParams& sp, int N, int mode, int storage, const VoxBuffers& vb,
                             cudaSurfaceObject_t l0, cudaStream_t st, int* launches) {

@@ -129,6 +129,9 @@ struct AdamStep {
 // `launches` (may be null) is incremented by the number of kernels enqueued.
 cudaError_t launch_voxelize(const SceneParams& sp, int N, int mode, int storage, const VoxBuffers& vb,
                             cudaSurfaceObject_t l0, cudaStream_t st, int* launches);
+// The voxelizer writing RGBA8 level 0 to linear memory (x fastest).
+cudaError_t launch_voxelize_linear(const SceneParams& sp, int N, int mode, const VoxBuffers& vb, uchar4* out,
+                                   cudaStream_t st);
 cudaError_t launch_mipmap(const MapSet& ms, int mip_mode, cudaStream_t st, int* launches);
 cudaError_t launch_gbuffer(const SceneParams& sp, const CameraParams& cp, const RasterBuffers& rb,
                            cudaStream_t st, int* launches);

@@ -39,7 +39,7 @@ EXPORTS = [
     "vct_activate_tex_3d", "vct_clear_tex_3d", "vct_mip_tex_3d", "vct_tex3d_upload", "vct_tex3d_download",
     "vct_mlp_desc_default", "vct_mlp_init", "vct_mlp_train", "vct_set_diffuse_mode", "vct_mlp_save",
     "vct_mlp_load", "vct_mlp_get_params", "vct_mlp_set_params", "vct_mlp_eval", "vct_mlp_gradients",
-    "vct_mlp_train_samples",
+    "vct_mlp_train_samples", "vct_voxelize_noalloc",
 ]
 DIFFUSE_CONES, DIFFUSE_MLP = 0, 1
 MLP_WEIGHTS = 5 * 64 * 64
@@ -123,6 +123,7 @@ def lib() -> C.CDLL:
             "vct_mlp_load": (I32, [P, C.c_char_p]), "vct_mlp_get_params": (I32, [P, P, P]),
             "vct_mlp_set_params": (I32, [P, P, P]), "vct_mlp_eval": (I32, [P, P, U32, P]),
             "vct_mlp_gradients": (I32, [P, P, U32, P, P, P]), "vct_mlp_train_samples": (I32, [P, P, U32, P, P]),
+            "vct_voxelize_noalloc": (I32, [P, U32, P, U32, P, U32, F, I32, I32, P, P]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
@@ -356,6 +357,25 @@ class Renderer:
         _check(lib().vct_read_gbuffer(self._r, g["tri_id"].ctypes.data, g["pos"].ctypes.data,
                                       g["nrm"].ctypes.data, g["mat"].ctypes.data))
         return g
+
+
+# ------------------------------------------------ allocation-free voxelizer --
+class DeviceMesh(C.Structure):
+    """vct_device_mesh: device pointers of one mesh + its host model matrix."""
+    _fields_ = [("verts", C.c_void_p), ("indices", C.c_void_p), ("tri_material", C.c_void_p),
+                ("n_verts", C.c_uint32), ("n_tris", C.c_uint32), ("model", C.c_float * 16)]
+
+
+def voxelize_noalloc(meshes, materials_ptr: int, n_materials: int, lights: np.ndarray, cube_size: float,
+                     grid_res: int, vox_mode: int, out_ptr: int, stream: int = 0) -> None:
+    """vct_voxelize_noalloc for callers that own all device memory: meshes is
+    a list of DeviceMesh, materials_ptr / out_ptr are device addresses (the
+    output holds grid_res^3 RGBA8 texels, x fastest)."""
+    arr = (DeviceMesh * max(len(meshes), 1))(*meshes)
+    l = np.ascontiguousarray(np.asarray(lights, scenes.LIGHT_DTYPE).reshape(-1))
+    _check(lib().vct_voxelize_noalloc(C.addressof(arr), len(meshes), C.c_void_p(materials_ptr), int(n_materials),
+                                      l.ctypes.data if l.size else None, l.size, float(cube_size), int(grid_res),
+                                      int(vox_mode), C.c_void_p(out_ptr), C.c_void_p(stream or 0)))
 
 
 # --------------------------------------------------------------- Texture3D --
