@@ -304,6 +304,7 @@ extern "C" vct_status vct_render(vct_renderer* r) {
     const FrameStatus s = *r->h_status.p;
     if (s.pair_total > r->pair_list.n) VCT_CHECK(r->pair_list.ensure((size_t)s.pair_total + s.pair_total / 4 + 4096));
     if (s.big_total > r->big_cap) VCT_CHECK(r->grow_big(s.big_total + s.big_total / 4 + 1024));
+    if (s.bigtri_total > r->bin_big_cap) VCT_CHECK(r->grow_bin_big(s.bigtri_total + s.bigtri_total / 4 + 256));
   }
   FrameInputs fi;
   fi.queue.swap(r->queue);

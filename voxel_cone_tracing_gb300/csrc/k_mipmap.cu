@@ -33,6 +33,11 @@ __constant__ int c_pairs[6][4][2] = {
     {{0, 4}, {1, 5}, {2, 6}, {3, 7}}, {{4, 0}, {5, 1}, {6, 2}, {7, 3}},
     {{0, 2}, {1, 3}, {5, 7}, {4, 6}}, {{2, 0}, {3, 1}, {7, 5}, {6, 4}},
     {{0, 1}, {2, 3}, {4, 5}, {6, 7}}, {{1, 0}, {3, 2}, {5, 4}, {7, 6}}};
+// The same table as a compile-time constant for fully unrolled loops.
+__device__ constexpr int c_pairs_h[6][4][2] = {
+    {{0, 4}, {1, 5}, {2, 6}, {3, 7}}, {{4, 0}, {5, 1}, {6, 2}, {7, 3}},
+    {{0, 2}, {1, 3}, {5, 7}, {4, 6}}, {{2, 0}, {3, 1}, {7, 5}, {6, 4}},
+    {{0, 1}, {2, 3}, {4, 5}, {6, 7}}, {{1, 0}, {3, 2}, {5, 4}, {7, 6}}};
 
 template <int STORAGE> struct Texel;
 template <> struct Texel<VCT_STORAGE_RGBA8> {
@@ -111,6 +116,50 @@ __device__ __forceinline__ typename Texel<STORAGE>::T reduce(const typename Texe
   else return iso ? iso_rgba16f(ch) : aniso_rgba16f(ch, d);
 }
 
+// All six directions of one destination texel from the same 8 children
+// (level 1, where every map reads the shared level 0): each child's channels
+// are unpacked once; same exact rule as aniso_rgba8.
+__device__ __forceinline__ void aniso6_rgba8(const uint32_t* ch, uint32_t* out) {
+  uint32_t c[8][4];
+#pragma unroll
+  for (int k = 0; k < 8; ++k)
+#pragma unroll
+    for (int q = 0; q < 4; ++q) c[k][q] = ch8(ch[k], q);
+#pragma unroll
+  for (int d = 0; d < 6; ++d) {
+    uint32_t o = 0;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      uint32_t S = 0;
+#pragma unroll
+      for (int p = 0; p < 4; ++p) {
+        const int f = c_pairs_h[d][p][0], b = c_pairs_h[d][p][1];
+        S += c[f][q] * 255u + (255u - c[f][3]) * c[b][q];
+      }
+      const uint32_t v = (S + 510u) / 1020u;
+      o |= (v > 255u ? 255u : v) << (8 * q);
+    }
+    out[d] = o;
+  }
+}
+
+__device__ __forceinline__ void aniso6_rgba16f(const uint2* ch, uint2* out) {
+  float4 c[8];
+#pragma unroll
+  for (int k = 0; k < 8; ++k) c[k] = h2f(ch[k]);
+#pragma unroll
+  for (int d = 0; d < 6; ++d) {
+    float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+    for (int p = 0; p < 4; ++p) {
+      const float4 f = c[c_pairs_h[d][p][0]], b = c[c_pairs_h[d][p][1]];
+      const float k = 1.0f - f.w;
+      acc.x += f.x + k * b.x; acc.y += f.y + k * b.y; acc.z += f.z + k * b.z; acc.w += f.w + k * b.w;
+    }
+    out[d] = f2h(make_float4(acc.x * 0.25f, acc.y * 0.25f, acc.z * 0.25f, acc.w * 0.25f));
+  }
+}
+
 // One pass: source level `src_level` (0 = the shared level 0) -> levels
 // src_level+1 .. src_level+K of NMAPS maps, one CTA per B^3 source region.
 template <int NMAPS, bool FROM_L0, int K, int STORAGE>
@@ -142,6 +191,31 @@ __global__ void __launch_bounds__(kThreads) k_mip(MapSet ms, int src_level) {
 #pragma unroll 1
   for (int l = 1; l <= K; ++l) {
     const int b = B >> l, b3 = b * b * b, cb3 = cur_b * cur_b * cur_b;
+    if (FROM_L0 && NMAPS == 6 && l == 1) {
+      // The six maps of level 1 read the same children: one thread per
+      // destination texel evaluates all six directions.
+      for (int r = threadIdx.x; r < b3; r += kThreads) {
+        const int x = r % b, y = (r / b) % b, z = r / (b * b);
+        T ch[8], v6[6];
+#pragma unroll
+        for (int k = 0; k < 8; ++k)
+          ch[k] = cur[((2 * z + c_off[k][2]) * cur_b + (2 * y + c_off[k][1])) * cur_b + (2 * x + c_off[k][0])];
+        if constexpr (STORAGE == VCT_STORAGE_RGBA8) aniso6_rgba8(ch, v6);
+        else aniso6_rgba16f(ch, v6);
+        const int dl = src_level + 1;
+#pragma unroll
+        for (int d = 0; d < 6; ++d) {
+          out[d * b3 + r] = v6[d];
+          surf3Dwrite(v6[d], ms.surf[d][dl], ((ox >> 1) + x) * Texel<STORAGE>::kBytes, (oy >> 1) + y, (oz >> 1) + z);
+        }
+      }
+      __syncthreads();
+      cur = out;
+      cur_b = b;
+      cur_shared = false;
+      out += NMAPS * b3;
+      continue;
+    }
     for (int i = threadIdx.x; i < NMAPS * b3; i += kThreads) {
       const int d = i / b3, r = i % b3;
       const int x = r % b, y = (r / b) % b, z = r / (b * b);

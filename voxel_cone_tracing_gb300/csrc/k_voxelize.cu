@@ -144,16 +144,19 @@ __device__ __forceinline__ void bin_one(const float v[3][3], int bx, int by, int
 }
 
 constexpr int kSoloBricks = 8;  // candidate bricks a lane bins on its own
+constexpr int kBigSplit = 8;     // CTAs that share one large triangle
 
 // Bins every triangle to the bricks it may touch.  A lane handles its own
-// triangle when it has few candidate bricks; triangles with more candidates
-// (room walls span 1024 bricks at 256^3) are binned by the whole warp, the
-// lanes splitting the candidate range, so no lane serialises a long loop of
-// returning atomics.
+// triangle when it has few candidate bricks.  A triangle with more
+// candidates (room walls span 1024 bricks at 256^3) is recorded by the
+// counting pass in `big` and binned by k_bin_big, which spreads each record
+// over several CTAs; without a record list (or when it is full) the warp
+// bins it, the lanes splitting the candidate range.
 template <bool FILL>
 __global__ void __launch_bounds__(256) k_bin(SceneParams sp, int N, uint32_t* __restrict__ count,
                                              uint32_t* __restrict__ cursor, uint32_t* __restrict__ list,
-                                             uint32_t cap, FrameStatus* st) {
+                                             uint32_t cap, FrameStatus* st, BinRec* __restrict__ big,
+                                             uint32_t big_cap, uint32_t* __restrict__ big_count) {
   const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
   const int lane = threadIdx.x & 31;
   const int nb = N / kBrick;
@@ -188,10 +191,29 @@ __global__ void __launch_bounds__(256) k_bin(SceneParams sp, int N, uint32_t* __
         for (int bx = blo[0]; bx <= bhi[0]; ++bx)
           bin_one<FILL>(v, bx, by, bz, nb, vol > 1, t, count, cursor, list, cap);
   }
-  unsigned big = __ballot_sync(0xffffffffu, vol > kSoloBricks);
-  while (big) {
-    const int src = __ffs(big) - 1;
-    big &= big - 1;
+  bool in_warp = vol > kSoloBricks;
+  if (in_warp && big) {
+    // Counting pass records it; the filling pass leaves it to k_bin_big.
+    // A full record list is reported (big_total > big_cap) and the frame is
+    // encoded again with a larger one.
+    in_warp = false;
+    if (!FILL) {
+      const uint32_t slot = atomicAdd(big_count, 1u);
+      if (slot < big_cap) {
+        BinRec r;
+        for (int k = 0; k < 3; ++k)
+          for (int d = 0; d < 3; ++d) r.v[k][d] = v[k][d];
+        for (int d = 0; d < 3; ++d) { r.blo[d] = blo[d]; r.bhi[d] = bhi[d]; }
+        r.t = t;
+        r.vol = (uint32_t)vol;
+        big[slot] = r;
+      }
+    }
+  }
+  unsigned warp_big = __ballot_sync(0xffffffffu, in_warp);
+  while (warp_big) {
+    const int src = __ffs(warp_big) - 1;
+    warp_big &= warp_big - 1;
     float w[3][3];
     for (int k = 0; k < 3; ++k)
       for (int d = 0; d < 3; ++d) w[k][d] = __shfl_sync(0xffffffffu, v[k][d], src);
@@ -203,6 +225,27 @@ __global__ void __launch_bounds__(256) k_bin(SceneParams sp, int N, uint32_t* __
     const uint32_t ts = __shfl_sync(0xffffffffu, t, src);
     for (int i = lane; i < n; i += 32)
       bin_one<FILL>(w, x0 + i % nx, y0 + (i / nx) % ny, z0 + i / (nx * ny), nb, true, ts, count, cursor, list, cap);
+  }
+}
+
+// Large-triangle records: CTA (x, y) takes records x, x + gridDim.x, ... and
+// the candidate bricks y*256 + tid, stepping by kBigSplit*256.
+template <bool FILL>
+__global__ void __launch_bounds__(256) k_bin_big(int N, const BinRec* __restrict__ big, uint32_t big_cap,
+                                                 const uint32_t* __restrict__ big_count, uint32_t* __restrict__ count,
+                                                 uint32_t* __restrict__ cursor, uint32_t* __restrict__ list,
+                                                 uint32_t cap) {
+  const uint32_t n = min(*big_count, big_cap);
+  const int nb = N / kBrick;
+  for (uint32_t r = blockIdx.x; r < n; r += gridDim.x) {
+    const BinRec& rec = big[r];
+    float v[3][3];
+    for (int k = 0; k < 3; ++k)
+      for (int d = 0; d < 3; ++d) v[k][d] = rec.v[k][d];
+    const int nx = rec.bhi[0] - rec.blo[0] + 1, ny = rec.bhi[1] - rec.blo[1] + 1;
+    for (uint32_t i = blockIdx.y * blockDim.x + threadIdx.x; i < rec.vol; i += gridDim.y * blockDim.x)
+      bin_one<FILL>(v, rec.blo[0] + (int)(i % nx), rec.blo[1] + (int)((i / nx) % ny), rec.blo[2] + (int)(i / (nx * ny)),
+                    nb, true, rec.t, count, cursor, list, cap);
   }
 }
 
@@ -488,11 +531,22 @@ __global__ void __launch_bounds__(kThreads) k_bricks(SceneParams sp, int N, cons
   const int nb = N / kBrick;
   const uint32_t brick = blockIdx.x;
   const int b3[3] = {(int)(brick % nb), (int)((brick / nb) % nb), (int)(brick / ((uint32_t)nb * nb))};
+  const uint32_t beg = min(offset[brick], cap), end = min(offset[brick + 1], cap);
+  if (beg == end) {
+    // No triangle touches this brick (most of the grid): store cleared texels
+    // without the accumulator or its barriers.
+    for (int i = threadIdx.x; i < kBrickVox; i += kThreads) {
+      const int x = b3[0] * kBrick + (i & 7), y = b3[1] * kBrick + ((i >> 3) & 7), z = b3[2] * kBrick + (i >> 6);
+      if (STORAGE == VCT_STORAGE_RGBA8) surf3Dwrite(make_uchar4(0, 0, 0, 0), l0, x * 4, y, z);
+      else surf3Dwrite(make_ushort4(0, 0, 0, 0), l0, x * 8, y, z);
+      if (counts) counts[((size_t)z * N + y) * N + x] = 0u;
+    }
+    return;
+  }
   for (int i = threadIdx.x; i < kBrickVox; i += kThreads) {
     acc.c[0][i] = 0; acc.c[1][i] = 0; acc.c[2][i] = 0; acc.c[3][i] = 0; acc.n[i] = 0;
   }
   __syncthreads();
-  const uint32_t beg = min(offset[brick], cap), end = min(offset[brick + 1], cap);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   for (uint32_t base = beg + warp * 32; base < end; base += kWarps * 32) {
     const uint32_t e = base + lane;
@@ -637,14 +691,16 @@ cudaError_t launch_voxelize_linear(const SceneParams& sp, int N, int mode, const
   if (e != cudaSuccess) return e;
   const unsigned tri_blocks = (sp.total_tris + 255) / 256;
   if (tri_blocks)
-    k_bin<false><<<tri_blocks, 256, 0, st>>>(sp, N, vb.brick_count, nullptr, nullptr, 0, vb.status);
+    k_bin<false><<<tri_blocks, 256, 0, st>>>(sp, N, vb.brick_count, nullptr, nullptr, 0, vb.status, nullptr, 0,
+                                             nullptr);
   e = launch_exclusive_scan(vb.brick_count, vb.brick_offset, vb.brick_cursor, n_bricks, vb.scan_tmp, st);
   if (e != cudaSuccess) return e;
   e = cudaMemcpyAsync(&vb.status->pair_total, vb.brick_offset + n_bricks, sizeof(uint32_t), cudaMemcpyDeviceToDevice,
                       st);
   if (e != cudaSuccess) return e;
   if (tri_blocks)
-    k_bin<true><<<tri_blocks, 256, 0, st>>>(sp, N, nullptr, vb.brick_cursor, vb.pair_list, vb.pair_cap, vb.status);
+    k_bin<true><<<tri_blocks, 256, 0, st>>>(sp, N, nullptr, vb.brick_cursor, vb.pair_list, vb.pair_cap, vb.status,
+                                            nullptr, 0, nullptr);
   if (mode == VCT_VOX_CONSERVATIVE)
     k_bricks_linear<VCT_VOX_CONSERVATIVE><<<(unsigned)n_bricks, kThreads, 0, st>>>(sp, N, vb.brick_offset,
                                                                                  vb.pair_list, vb.pair_cap, out);
@@ -662,19 +718,40 @@ cudaError_t launch_voxelize(const SceneParams& sp, int N, int mode, int storage,
   cudaError_t e = cudaMemsetAsync(vb.brick_count, 0, n_bricks * sizeof(uint32_t), st);
   if (e != cudaSuccess) return e;
   const unsigned tri_blocks = (sp.total_tris + 255) / 256;
+  const dim3 big_grid(128, kBigSplit);
+  if (vb.big) {
+    e = cudaMemsetAsync(vb.big_count, 0, sizeof(uint32_t), st);
+    if (e != cudaSuccess) return e;
+  }
   if (tri_blocks) {
-    k_bin<false><<<tri_blocks, 256, 0, st>>>(sp, N, vb.brick_count, nullptr, nullptr, 0, vb.status);
+    k_bin<false><<<tri_blocks, 256, 0, st>>>(sp, N, vb.brick_count, nullptr, nullptr, 0, vb.status, vb.big,
+                                             vb.big_cap, vb.big_count);
     ++nl;
+    if (vb.big) {
+      k_bin_big<false><<<big_grid, 256, 0, st>>>(N, vb.big, vb.big_cap, vb.big_count, vb.brick_count, nullptr, nullptr,
+                                                 0);
+      ++nl;
+    }
   }
   e = launch_exclusive_scan(vb.brick_count, vb.brick_offset, vb.brick_cursor, n_bricks, vb.scan_tmp, st, &nl);
   if (e != cudaSuccess) return e;
-  // pair_total <- offset[n_bricks]
+  // pair_total <- offset[n_bricks]; bigtri_total <- records needed
   e = cudaMemcpyAsync(&vb.status->pair_total, vb.brick_offset + n_bricks, sizeof(uint32_t),
                       cudaMemcpyDeviceToDevice, st);
   if (e != cudaSuccess) return e;
+  if (vb.big) {
+    e = cudaMemcpyAsync(&vb.status->bigtri_total, vb.big_count, sizeof(uint32_t), cudaMemcpyDeviceToDevice, st);
+    if (e != cudaSuccess) return e;
+  }
   if (tri_blocks) {
-    k_bin<true><<<tri_blocks, 256, 0, st>>>(sp, N, nullptr, vb.brick_cursor, vb.pair_list, vb.pair_cap, vb.status);
+    k_bin<true><<<tri_blocks, 256, 0, st>>>(sp, N, nullptr, vb.brick_cursor, vb.pair_list, vb.pair_cap, vb.status,
+                                            vb.big, vb.big_cap, vb.big_count);
     ++nl;
+    if (vb.big) {
+      k_bin_big<true><<<big_grid, 256, 0, st>>>(N, vb.big, vb.big_cap, vb.big_count, nullptr, vb.brick_cursor,
+                                                vb.pair_list, vb.pair_cap);
+      ++nl;
+    }
   }
   ++nl;  // k_bricks
   const unsigned grid = (unsigned)n_bricks;

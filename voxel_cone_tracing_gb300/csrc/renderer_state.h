@@ -165,6 +165,9 @@ struct vct_renderer {
   DevBuf<DevInstance> d_inst;
   HostBuf<DevInstance> h_inst;
   DevBuf<uint32_t> brick_count, brick_offset, brick_cursor, pair_list, scan_tmp, counts;
+  DevBuf<BinRec> bin_big;           // large-triangle binning records
+  DevBuf<uint32_t> bin_big_count;
+  uint32_t bin_big_cap = 0;
   DevBuf<FrameStatus> d_status;
   HostBuf<FrameStatus> h_status;
   DevBuf<unsigned long long> vis;
@@ -302,7 +305,15 @@ struct vct_renderer {
     std::memset(h_status.p, 0, sizeof(FrameStatus));
     VCT_CHECK(big_count.ensure(2));
     VCT_CHECK(grow_big(1 << 16));
+    VCT_CHECK(grow_bin_big(1 << 12));
     return alloc_maps((uint32_t)cfg.grid_res);
+  }
+
+  vct_status grow_bin_big(uint32_t cap) {
+    VCT_CHECK(bin_big.ensure(cap));
+    VCT_CHECK(bin_big_count.ensure(1));
+    bin_big_cap = cap;
+    return VCT_OK;
   }
 
   vct_status grow_big(uint32_t cap) {
@@ -402,6 +413,9 @@ struct vct_renderer {
     vb.scan_tmp = scan_tmp.p;
     vb.counts = cfg.keep_counts ? counts.p : nullptr;
     vb.status = d_status.p;
+    vb.big = bin_big.p;
+    vb.big_cap = bin_big_cap;
+    vb.big_count = bin_big_count.p;
 
     RasterBuffers rb;
     rb.vis = vis.p;
@@ -459,6 +473,10 @@ struct vct_renderer {
       }
       if (s.big_total > big_cap) {
         VCT_CHECK(grow_big(s.big_total + s.big_total / 4 + 1024));
+        redo = true;
+      }
+      if (s.bigtri_total > bin_big_cap) {
+        VCT_CHECK(grow_bin_big(s.bigtri_total + s.bigtri_total / 4 + 256));
         redo = true;
       }
       if (!redo) return VCT_OK;

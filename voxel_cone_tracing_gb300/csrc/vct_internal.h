@@ -48,7 +48,15 @@ struct FrameStatus {
   uint32_t big_tiles;       // raster tiles of the big-triangle pass
   uint32_t rejected_tris;   // non-finite / out-of-range triangles
   uint32_t count_saturated; // voxels with > 65535 contributions
-  uint32_t pad[3];
+  uint32_t bigtri_total;    // large-triangle binning records needed
+  uint32_t pad[2];
+};
+
+// A triangle with many candidate bricks, binned by k_bin_big.
+struct BinRec {
+  float v[3][3];    // vertices in voxel units
+  int blo[3], bhi[3];
+  uint32_t t, vol;  // frame triangle id, candidate bricks
 };
 
 // The voxel maps of a renderer: level 0 once, plus one chain per map.
@@ -69,6 +77,9 @@ struct VoxBuffers {
   uint32_t* scan_tmp;      // block sums
   uint32_t* counts;        // N^3 or nullptr
   FrameStatus* status;
+  BinRec* big;             // large-triangle records (nullptr: bin them in-warp)
+  uint32_t big_cap;
+  uint32_t* big_count;
 };
 
 struct RasterBuffers {
