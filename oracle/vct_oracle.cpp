@@ -621,8 +621,10 @@ template <class R> struct ConeOut { V4<R> c; int steps; };
 
 // Instrumentation for orc_trace_stats: per cone class (0 diffuse, 1
 // specular, 2 shadow, 3 refraction) the cones traced, the march steps and
-// the steps whose lod is < 1 (those read level 0 plus level 1).
-enum { kStatCones = 0, kStatSteps = 4, kStatLodLt1 = 8, kStatN = 12 };
+// the steps whose lod is < 1 (those read level 0 plus level 1); then, over
+// all classes, the steps whose lod lies in [k, k+1) for k = 0..6 (k = 7:
+// lod >= 7).
+enum { kStatCones = 0, kStatSteps = 4, kStatLodLt1 = 8, kStatLodBand = 12, kStatN = 20 };
 static std::atomic<uint64_t> g_stats[kStatN];
 static bool g_stats_on = false;
 static thread_local int t_cone_class = 0;
@@ -652,6 +654,7 @@ static ConeOut<R> trace_cone(const Maps& m, V3<R> origin, V3<R> dir, R aperture,
     sp = dir * dist + origin;
     ++steps;
     if (mip < R(1)) ++lod_lt1;
+    if (g_stats_on) g_stats[kStatLodBand + (mip >= R(7) ? 7 : (int)mip)] += 1;
   }
   if (g_stats_on) {
     g_stats[kStatCones + t_cone_class] += 1;

@@ -64,7 +64,9 @@ def test_bench_frame_work(oracle):
     gb = oracle.gbuffer(s, p)
     st = oracle.trace_stats(s, p, l0, ch, gb, row_stride=32)
     px = len(range(0, bench.HEIGHT, 32)) * bench.WIDTH
+    bands = st.pop("lod_bands")
     steps = sum(v["steps"] for v in st.values()) / px
     lt1 = sum(v["lod_lt1"] for v in st.values()) / px
+    assert sum(bands) == sum(v["steps"] for v in st.values())
     assert st["diffuse"]["cones"] == 9 * px
     assert 3 * steps + lt1 == pytest.approx(bench.TRACE_FETCHES_PER_PIXEL, rel=0.02)

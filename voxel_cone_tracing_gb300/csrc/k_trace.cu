@@ -91,6 +91,18 @@ __device__ float4 texture_lod_exact(const MapSet& m, int map, V3 u, float lod) {
   return trilinear_exact<STORAGE>(m, d1, map, u) * (1.0f - f) + trilinear_exact<STORAGE>(m, d1 + 1, map, u) * f;
 }
 
+// sum_k a_k * textureLod(chain idx_k, u, l) from the texture unit.  A map
+// whose weight is exactly 0 is not fetched: its term 0 * texel is 0 for every
+// finite texel, so the sum is unchanged.  Cones along an axis-aligned normal
+// (every wall pixel) have one or two such weights.
+__device__ __forceinline__ float4 aniso_fetch(const MapSet& m, V3 u, int ix, int iy, int iz, V3 ad, float l) {
+  float4 r = f4(0.f, 0.f, 0.f, 0.f);
+  if (ad.x != 0.0f) r = tex3DLod<float4>(m.tex[ix], u.x, u.y, u.z, l) * ad.x;
+  if (ad.y != 0.0f) r = r + tex3DLod<float4>(m.tex[iy], u.x, u.y, u.z, l) * ad.y;
+  if (ad.z != 0.0f) r = r + tex3DLod<float4>(m.tex[iz], u.x, u.y, u.z, l) * ad.z;
+  return r;
+}
+
 // sum_k a_k * textureLod(map idx_k, u, lod), lod >= 0.
 template <int SAMPLER, bool ISO, int STORAGE>
 __device__ __forceinline__ float4 sample_voxel(const MapSet& m, V3 u, int ix, int iy, int iz, V3 ad, float lod) {
@@ -106,16 +118,12 @@ __device__ __forceinline__ float4 sample_voxel(const MapSet& m, V3 u, int ix, in
     if (!(lod > 0.0f)) return t0 * wsum;
     float4 t1;
     if (ISO) t1 = tex3DLod<float4>(m.tex[0], u.x, u.y, u.z, 0.0f) * wsum;
-    else
-      t1 = tex3DLod<float4>(m.tex[ix], u.x, u.y, u.z, 0.0f) * ad.x +
-           tex3DLod<float4>(m.tex[iy], u.x, u.y, u.z, 0.0f) * ad.y +
-           tex3DLod<float4>(m.tex[iz], u.x, u.y, u.z, 0.0f) * ad.z;
+    else t1 = aniso_fetch(m, u, ix, iy, iz, ad, 0.0f);
     return t0 * ((1.0f - lod) * wsum) + t1 * lod;
   }
   const float l = lod - 1.0f;
   if (ISO) return tex3DLod<float4>(m.tex[0], u.x, u.y, u.z, l) * wsum;
-  return tex3DLod<float4>(m.tex[ix], u.x, u.y, u.z, l) * ad.x + tex3DLod<float4>(m.tex[iy], u.x, u.y, u.z, l) * ad.y +
-         tex3DLod<float4>(m.tex[iz], u.x, u.y, u.z, l) * ad.z;
+  return aniso_fetch(m, u, ix, iy, iz, ad, l);
 }
 
 // ------------------------------------------------------------ cone march ----
