@@ -215,6 +215,43 @@ def mlp_leg(r, R, scene, ids, stream, flush, steps, plain_stages):
                       "ms_train": round(rep["ms_train"], 2)}}
 
 
+def precision_leg(R, torch, steps, flush_mb=256):
+    """Precision workload: 512^3 grid with RGBA16F maps (radiance clamped to
+    [0, 16]), the conservative (exact SAT) voxelizer, 1,997,514 triangles
+    (room + 4 displaced icospheres + 32 cuboids), 1080p.  Per-stage device
+    times of `steps` frames (L2 flushed between frames); the per-stage error
+    against the FP64 oracle is checked by tests/test_gpu_hdr.py."""
+    from voxel_cone_tracing_gb300 import scenes
+    scene = scenes.scene_hdr(width=WIDTH, height=HEIGHT)
+    r = R.Renderer(WIDTH, HEIGHT, grid_res=512, storage=R.STORAGE_RGBA16F, radiance_max=scenes.HDR_RADIANCE_MAX,
+                   vox_mode=R.VOX_CONSERVATIVE)
+    ids = R.load_scene(r, scene)
+    r.set_voxel_view_dir(7, 0.0)
+    stream = torch.cuda.Stream()
+    r.set_stream(stream.cuda_stream)
+    flush = torch.empty(flush_mb << 20, dtype=torch.uint8, device="cuda")
+    for _ in range(3):
+        R.queue_scene(r, scene, ids)
+        r.render()
+    r.synchronize()
+    stages = []
+    for _ in range(steps):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        R.queue_scene(r, scene, ids)
+        r.render()
+        r.synchronize()
+        stages.append(r.stage_times())
+    mean = lambda k: statistics.mean(st[k] for st in stages)  # noqa: E731
+    out = {"workload": f"{scene.name} ({scene.n_tris} triangles), {WIDTH}x{HEIGHT}, 512^3 aniso RGBA16F, "
+                       "radiance [0,16], conservative SAT voxelizer, 9 diffuse + 1 specular + 1 shadow cone",
+           "value": round(mean("voxelize") + mean("mipmap") + mean("trace"), 4), "unit": UNIT,
+           "stages_ms": {k: round(mean(k), 4) for k in ("voxelize", "mipmap", "gbuffer", "trace", "total")},
+           "steps": steps, "gpu_launches": int(sum(st["kernel_launches"] for st in stages))}
+    r.close()
+    return out
+
+
 def run_ours(args):
     rank, world, local = _dist()
     import numpy as np
@@ -335,6 +372,8 @@ def run_ours(args):
     }
     if not args.no_mlp:
         line["mlp"] = mlp_leg(r, R, scene, ids, stream, flush, args.steps, stages)
+    if not args.no_precision:
+        line["precision"] = precision_leg(R, torch, args.steps)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
         v, ms = cpu_frame_ms(scene, threads, CPU_ROW_STRIDE)
@@ -358,6 +397,7 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-mlp", action="store_true", help="skip the learned-diffuse leg")
+    ap.add_argument("--no-precision", action="store_true", help="skip the 512^3 RGBA16F HDR leg")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

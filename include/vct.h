@@ -106,7 +106,10 @@ typedef struct {
   int32_t cone_set;     /* VCT_CONES_*                                      */
   int32_t keep_counts;  /* keep per-voxel contribution counts (debug)       */
   int32_t keep_float_frame; /* also write the unclamped RGBA32F frame       */
-  int32_t reserved[8];
+  float radiance_max;   /* upper clamp of voxel radiance (voxelize.frag:239
+                         * clamps to 1).  0 or 1: the reference's clamp;
+                         * > 1 (HDR, e.g. 16) needs VCT_STORAGE_RGBA16F      */
+  int32_t reserved[7];
 } vct_config;
 
 typedef struct vct_renderer vct_renderer;

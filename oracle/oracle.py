@@ -57,7 +57,7 @@ class _Params(C.Structure):
                 ("enable_direct", C.c_int32), ("enable_diffuse", C.c_int32),
                 ("enable_specular", C.c_int32), ("enable_shadow", C.c_int32),
                 ("view_voxel_dir", C.c_int32), ("view_voxel_lod", C.c_float),
-                ("cone_set", C.c_int32), ("threads", C.c_int32)]
+                ("cone_set", C.c_int32), ("threads", C.c_int32), ("radiance_max", C.c_float)]
 
 
 _lib = None
@@ -75,6 +75,10 @@ def lib():
             getattr(L, f).restype = C.c_int64
             getattr(L, f).argtypes = [P, P, P, P]
         L.orc_mipmap.argtypes = [P, P, P]
+        L.orc_voxelize_hdr.restype = C.c_int64
+        L.orc_voxelize_hdr.argtypes = [P, P, P, P]
+        L.orc_mip_level_f.argtypes = [C.c_int32, C.c_int32, P, C.c_int32, P]
+        L.orc_trace_hdr.argtypes = [P, P, P, P, P, P, P, P, C.c_int32, P]
         L.orc_gbuffer.argtypes = [P, P, P, P, P, P]
         for f in ("orc_trace", "orc_trace_f32"):
             getattr(L, f).argtypes = [P, P, P, P, P, P, P, P, C.c_int32, P]
@@ -104,7 +108,8 @@ class Params:
 
     def __init__(self, grid_res=64, width=64, height=64, vox_mode=VOX_REF_RASTER2X, mip_mode=MIP_ANISO,
                  enable_direct=True, enable_diffuse=True, enable_specular=True, enable_shadow=True,
-                 view_voxel_dir=7, view_voxel_lod=0.0, cone_set=CONES_REF9, threads=None, levels=None):
+                 view_voxel_dir=7, view_voxel_lod=0.0, cone_set=CONES_REF9, threads=None, levels=None,
+                 radiance_max=1.0):
         self.grid_res, self.width, self.height = grid_res, width, height
         self.levels = levels if levels is not None else levels_for(grid_res)
         self.vox_mode, self.mip_mode = vox_mode, mip_mode
@@ -113,6 +118,7 @@ class Params:
         self.view_voxel_dir, self.view_voxel_lod = view_voxel_dir, view_voxel_lod
         self.cone_set = cone_set
         self.threads = threads if threads else (os.cpu_count() or 1)
+        self.radiance_max = radiance_max
 
     def c(self) -> _Params:
         p = _Params()
@@ -170,6 +176,45 @@ def voxelize(scene, params: Params, fp32: bool = False):
     f = lib().orc_voxelize_f32 if fp32 else lib().orc_voxelize
     rej = f(sh.ptr, C.addressof(pc), _ptr(l0), _ptr(cnt))
     return l0, cnt, int(rej)
+
+
+def voxelize_hdr(scene, params: Params):
+    """FP64 voxelize keeping the unrounded mean (HDR storage):
+    -> (level0 float32 (N,N,N,4) [z,y,x], counts, rejected)."""
+    n = params.grid_res
+    l0 = np.zeros((n, n, n, 4), np.float32)
+    cnt = np.zeros((n, n, n), np.uint32)
+    sh, pc = _SceneHold(scene), params.c()
+    rej = lib().orc_voxelize_hdr(sh.ptr, C.addressof(pc), _ptr(l0), _ptr(cnt))
+    return l0, cnt, int(rej)
+
+
+def mip_level_f(src: np.ndarray, mip_mode: int) -> np.ndarray:
+    """One FP64 mip level from float texels.  src: (s,s,s,4) (the shared
+    level 0) or (6,s,s,s,4); -> (n_maps, s/2, s/2, s/2, 4) float32."""
+    src = np.ascontiguousarray(src, np.float32)
+    maps = 1 if src.ndim == 4 else src.shape[0]
+    n = src.shape[-2]
+    out = np.zeros((1 if mip_mode == MIP_ISO else 6, n // 2, n // 2, n // 2, 4), np.float32)
+    lib().orc_mip_level_f(n, maps, _ptr(src), int(mip_mode), _ptr(out))
+    return out
+
+
+def trace_hdr(scene, params: Params, level0, chains, gb: dict, row_stride: int = 1):
+    """FP64 trace over float maps: level0 (N,N,N,4), chains (n_maps,
+    chain_texels, 4) float32.  -> float32 frame (H, W, 4)."""
+    w, h = params.width, params.height
+    out = np.zeros((h, w, 4), np.float32)
+    sh, pc = _SceneHold(scene), params.c()
+    l0 = np.ascontiguousarray(level0, np.float32)
+    ch = np.ascontiguousarray(chains, np.float32)
+    tid = np.ascontiguousarray(gb["tri_id"], np.uint32)
+    pos = np.ascontiguousarray(gb["pos"], np.float64)
+    nrm = np.ascontiguousarray(gb["nrm"], np.float64)
+    mat = np.ascontiguousarray(gb["mat"], np.uint32)
+    lib().orc_trace_hdr(sh.ptr, C.addressof(pc), _ptr(l0), _ptr(ch), _ptr(tid), _ptr(pos), _ptr(nrm), _ptr(mat),
+                        int(row_stride), _ptr(out))
+    return out
 
 
 def mipmap(params: Params, level0: np.ndarray) -> np.ndarray:

@@ -157,6 +157,11 @@ template <class R> static inline V3<R> mat_of(const orc_material& m, int which) 
 static inline bool illum_transparent(int illum) { return illum == 4 || illum == 6 || illum == 7 || illum == 9; }
 
 // --------------------------------------------------------- voxelize.frag --
+// Upper clamp of the voxel colour: 1 in the reference (voxelize.frag:239);
+// orc_params.radiance_max for HDR storage.  Set by voxelize_impl before its
+// worker threads start (the oracle runs one call at a time).
+static double g_radiance_max = 1.0;
+
 // Per-fragment colour, voxelize.frag:208-239.  pos is in grid space
 // ([-1,1]^3 = world / cube_size), nrm the interpolated vertex normal.
 template <class R>
@@ -180,7 +185,9 @@ static V4<R> voxel_fragment_color(const orc_scene* s, const orc_material& mat, V
   R alpha = R(1);
   if (illum_transparent(mat.illum)) { trans = mat_of<R>(mat, 2); alpha = R(mat.dissolve); }  // :231-237
   V3<R> c = mulv(trans, color);
-  return V4<R>(clamp01(c.x), clamp01(c.y), clamp01(c.z), clamp01(alpha));  // :239
+  const R hi = R(g_radiance_max);
+  auto cl = [hi](R v) { return v < R(0) ? R(0) : (v > hi ? hi : v); };
+  return V4<R>(cl(c.x), cl(c.y), cl(c.z), clamp01(alpha));  // :239
 }
 
 // One voxel contribution: voxel index + clamped colour.
@@ -439,8 +446,10 @@ static inline void tri_verts(const orc_scene* s, const orc_instance& in, uint32_
 // triangle chunks and summed per voxel in global triangle order, so the
 // result does not depend on the thread count.
 template <class R>
-static int64_t voxelize_impl(const orc_scene* s, const orc_params* p, uint8_t* level0, uint32_t* counts) {
+static int64_t voxelize_impl(const orc_scene* s, const orc_params* p, uint8_t* level0, uint32_t* counts,
+                             float* level0f = nullptr) {
   const int N = p->grid_res;
+  g_radiance_max = p->radiance_max > 0.0f ? (double)p->radiance_max : 1.0;
   std::vector<TriRef> tris;
   std::vector<std::vector<double>> nms(s->n_instances, std::vector<double>(9));
   for (uint32_t i = 0; i < s->n_instances; ++i) {
@@ -479,8 +488,12 @@ static int64_t voxelize_impl(const orc_scene* s, const orc_params* p, uint8_t* l
         cnt[o]++;
       }
     for (size_t o = 0; o < ve - vb; ++o) {
-      uint8_t* t = level0 + 4 * (vb + o);
       if (counts) counts[vb + o] = cnt[o];
+      if (level0f) {  // HDR storage: the mean itself
+        for (int q = 0; q < 4; ++q) level0f[4 * (vb + o) + q] = cnt[o] ? (float)(sum[4 * o + q] / R(cnt[o])) : 0.0f;
+        continue;
+      }
+      uint8_t* t = level0 + 4 * (vb + o);
       for (int q = 0; q < 4; ++q) {
         if (!cnt[o]) { t[q] = 0; continue; }
         R mean = sum[4 * o + q] / R(cnt[o]);
@@ -563,6 +576,41 @@ static void mipmap_impl(const orc_params* p, const uint8_t* level0, uint8_t* cha
   }
 }
 
+// One level of float maps in FP64: the same pairs / box mean as above
+// without unorm8 rounding (RGBA16F storage).
+static void mip_level_f(int n_src, int src_maps, const float* src, int mip_mode, float* dst, int threads) {
+  const int s = n_src / 2;
+  const int nmaps = mip_mode == ORC_MIP_ISO ? 1 : 6;
+  const size_t src_n = (size_t)n_src * n_src * n_src, dst_n = (size_t)s * s * s;
+  parallel_for(std::max(1, threads), s, [&](int z) {
+    for (int y = 0; y < s; ++y)
+      for (int x = 0; x < s; ++x)
+        for (int d = 0; d < nmaps; ++d) {
+          const float* base = src + 4 * (src_maps == 1 ? 0 : d) * src_n;
+          const float* child[8];
+          for (int i = 0; i < 8; ++i) {
+            int cx = 2 * x + kOff[i][0], cy = 2 * y + kOff[i][1], cz = 2 * z + kOff[i][2];
+            child[i] = base + 4 * (((size_t)cz * n_src + cy) * n_src + cx);
+          }
+          float* o = dst + 4 * (d * dst_n + ((size_t)z * s + y) * s + x);
+          for (int ch = 0; ch < 4; ++ch) {
+            double S = 0.0;
+            if (nmaps == 6) {
+              for (int q = 0; q < 4; ++q) {
+                const float* f = child[kPairs[d][q][0]];
+                const float* b = child[kPairs[d][q][1]];
+                S += (double)f[ch] + (1.0 - (double)f[3]) * (double)b[ch];
+              }
+              o[ch] = (float)(S * 0.25);
+            } else {
+              for (int i = 0; i < 8; ++i) S += child[i][ch];
+              o[ch] = (float)(S * 0.125);
+            }
+          }
+        }
+  });
+}
+
 // -------------------------------------------------- GL texture sampling ----
 struct Maps {
   const uint8_t* level0;
@@ -570,11 +618,19 @@ struct Maps {
   int N, L;
   uint64_t chain;
   bool iso;
+  const float* level0f = nullptr;  // float maps (HDR storage) instead of RGBA8
+  const float* chainsf = nullptr;
 };
 
 template <class R> static inline V4<R> texel(const Maps& m, int l, int map, int x, int y, int z) {
   int s = m.N >> l;
   if (x < 0 || y < 0 || z < 0 || x >= s || y >= s || z >= s) return V4<R>();  // CLAMP_TO_BORDER(0)
+  if (m.level0f) {
+    const float* f;
+    if (l == 0) f = m.level0f + 4 * (((size_t)z * s + y) * s + x);
+    else f = m.chainsf + 4 * ((m.iso ? 0 : map) * m.chain + level_offset(m.N, l) + ((size_t)z * s + y) * s + x);
+    return V4<R>(R(f[0]), R(f[1]), R(f[2]), R(f[3]));
+  }
   const uint8_t* t;
   if (l == 0) t = m.level0 + 4 * (((size_t)z * s + y) * s + x);
   else t = m.chains + 4 * ((m.iso ? 0 : map) * m.chain + level_offset(m.N, l) + ((size_t)z * s + y) * s + x);
@@ -805,8 +861,9 @@ static const float kClear[4] = {0.15f, 0.25f, 0.25f, 1.0f};  // renderer.cpp:398
 template <class R>
 static void trace_impl(const orc_scene* s, const orc_params* p, const uint8_t* level0, const uint8_t* chains,
                        const uint32_t* tri_id, const double* pos, const double* nrm, const uint32_t* mat,
-                       int row_stride, float* out) {
-  Maps m{level0, chains, p->grid_res, p->levels, orc_chain_texels(p->grid_res, p->levels), p->mip_mode == ORC_MIP_ISO};
+                       int row_stride, float* out, const float* level0f = nullptr, const float* chainsf = nullptr) {
+  Maps m{level0, chains, p->grid_res, p->levels, orc_chain_texels(p->grid_res, p->levels), p->mip_mode == ORC_MIP_ISO,
+         level0f, chainsf};
   const int W = p->width, H = p->height;
   if (row_stride < 1) row_stride = 1;
   const int rows = (H + row_stride - 1) / row_stride;
@@ -1021,6 +1078,20 @@ int64_t orc_voxelize_f32(const orc_scene* s, const orc_params* p, uint8_t* level
 }
 
 void orc_mipmap(const orc_params* p, const uint8_t* level0, uint8_t* chains) { mipmap_impl(p, level0, chains); }
+
+int64_t orc_voxelize_hdr(const orc_scene* s, const orc_params* p, float* level0, uint32_t* counts) {
+  return voxelize_impl<double>(s, p, nullptr, counts, level0);
+}
+
+void orc_mip_level_f(int32_t n_src, int32_t src_maps, const float* src, int32_t mip_mode, float* dst) {
+  mip_level_f(n_src, src_maps, src, mip_mode, dst, (int)std::thread::hardware_concurrency());
+}
+
+void orc_trace_hdr(const orc_scene* s, const orc_params* p, const float* level0, const float* chains,
+                   const uint32_t* tri_id, const double* pos, const double* nrm, const uint32_t* mat,
+                   int32_t row_stride, float* out) {
+  trace_impl<double>(s, p, nullptr, nullptr, tri_id, pos, nrm, mat, row_stride, out, level0, chains);
+}
 
 void orc_gbuffer(const orc_scene* s, const orc_params* p, uint32_t* tri_id, double* pos, double* nrm,
                  uint32_t* mat) {

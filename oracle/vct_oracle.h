@@ -92,6 +92,8 @@ typedef struct {
   float view_voxel_lod;
   int32_t cone_set;         /* ORC_CONES_* */
   int32_t threads;          /* host threads, >= 1 */
+  float radiance_max;       /* voxel colour clamp: rgb to [0, radiance_max]
+                             * (<= 0 means 1, the reference's clamp) */
 } orc_params;
 
 /* Number of texels in one directional chain (levels 1..L-1). */
@@ -105,6 +107,24 @@ int64_t orc_voxelize(const orc_scene* s, const orc_params* p,
 /* Voxelize with FP32 shading (the timed CPU restatement).  counts may be 0. */
 int64_t orc_voxelize_f32(const orc_scene* s, const orc_params* p,
                          uint8_t* level0, uint32_t* counts);
+
+/* Voxelize, FP64, writing the unrounded mean as float RGBA (HDR storage:
+ * the GPU rounds the same mean to half). */
+int64_t orc_voxelize_hdr(const orc_scene* s, const orc_params* p,
+                         float* level0, uint32_t* counts);
+
+/* One mip level in FP64 from float texels: src holds src_maps (1 = the shared
+ * level 0, or 6) maps of edge `n_src`; dst receives 6 maps (aniso) or 1 map
+ * (iso) of edge n_src/2. */
+void orc_mip_level_f(int32_t n_src, int32_t src_maps, const float* src,
+                     int32_t mip_mode, float* dst);
+
+/* orc_trace over float voxel maps (level 0: N^3 RGBA floats; chains in the
+ * layout above, RGBA floats). */
+void orc_trace_hdr(const orc_scene* s, const orc_params* p, const float* level0,
+                   const float* chains, const uint32_t* tri_id, const double* pos,
+                   const double* nrm, const uint32_t* mat, int32_t row_stride,
+                   float* out);
 
 /* Mip chains from level 0: aniso -> 6 chains, iso -> 1 chain. */
 void orc_mipmap(const orc_params* p, const uint8_t* level0, uint8_t* chains);

@@ -139,6 +139,7 @@ extern "C" vct_status vct_voxelize_noalloc(const vct_device_mesh* meshes, uint32
   sp.n_materials = n_materials;
   sp.n_lights = (int32_t)std::min<uint32_t>(n_lights, kMaxLights);
   sp.cube_size = cube_size;
+  sp.radiance_max = 1.0f;
   for (int i = 0; i < sp.n_lights; ++i) sp.lights[i] = lights[i];
 
   VoxBuffers vb;

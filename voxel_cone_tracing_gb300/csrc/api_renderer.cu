@@ -79,11 +79,16 @@ extern "C" void vct_config_default(vct_config* cfg) {
   cfg->storage = VCT_STORAGE_RGBA8;
   cfg->sampler = VCT_SAMPLER_HW;
   cfg->cone_set = VCT_CONES_REF9;
+  cfg->radiance_max = 1.0f;
 }
 
 static vct_status check_config(const vct_config& c) {
   if (!is_pow2((uint32_t)c.grid_res) || c.grid_res < 8 || c.grid_res > 1024)
     return set_error(VCT_ERR_INVALID_VALUE, "grid_res %d: need a power of two in [8, 1024]", c.grid_res);
+  if (!(c.radiance_max >= 0.0f && c.radiance_max <= 65504.0f))
+    return set_error(VCT_ERR_INVALID_VALUE, "radiance_max %g: need 0 <= radiance_max <= 65504", c.radiance_max);
+  if (c.radiance_max > 1.0f && c.storage != VCT_STORAGE_RGBA16F)
+    return set_error(VCT_ERR_INVALID_VALUE, "radiance_max %g > 1 needs RGBA16F storage", c.radiance_max);
   if (c.vox_mode < 0 || c.vox_mode > 1 || c.mip_mode < 0 || c.mip_mode > 1 || c.storage < 0 || c.storage > 1 ||
       c.sampler < 0 || c.sampler > 1 || c.cone_set < 0 || c.cone_set > 1)
     return set_error(VCT_ERR_INVALID_VALUE, "config field out of range");

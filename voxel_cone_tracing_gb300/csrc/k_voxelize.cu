@@ -271,21 +271,44 @@ __device__ __forceinline__ float4 voxel_color(const SceneParams& sp, const vct_m
     color = mulv(color, v3(m.transmittance[0], m.transmittance[1], m.transmittance[2]));
     alpha = m.dissolve;
   }
-  return make_float4(clamp01(color.x), clamp01(color.y), clamp01(color.z), clamp01(alpha));
+  // clamp(vec4, 0, 1) (:239); with HDR storage the colour clamps to
+  // [0, radiance_max] instead (radiance_max = 1 is the reference).
+  const float hi = sp.radiance_max;
+  return make_float4(fminf(fmaxf(color.x, 0.0f), hi), fminf(fmaxf(color.y, 0.0f), hi),
+                     fminf(fmaxf(color.z, 0.0f), hi), clamp01(alpha));
 }
 
-struct Acc {
+// Per-brick sums of the contributions.  RGBA8: 16-bit fixed point per
+// contribution in u32 (exact for the 1/255 result).  RGBA16F: the colour
+// divided by radiance_max in 32-bit fixed point, summed in u64, so the sum
+// is exact, order-independent and far finer than half precision.
+template <int STORAGE> struct AccT;
+template <> struct AccT<VCT_STORAGE_RGBA8> {
   uint32_t c[4][kBrickVox];
   uint32_t n[kBrickVox];
+  __device__ __forceinline__ void clear(int i) { c[0][i] = 0; c[1][i] = 0; c[2][i] = 0; c[3][i] = 0; n[i] = 0; }
+  __device__ __forceinline__ void add(const SceneParams&, int v, float4 col) {
+    atomicAdd(&c[0][v], __float2uint_rn(col.x * kFix));
+    atomicAdd(&c[1][v], __float2uint_rn(col.y * kFix));
+    atomicAdd(&c[2][v], __float2uint_rn(col.z * kFix));
+    atomicAdd(&c[3][v], __float2uint_rn(col.w * kFix));
+    atomicAdd(&n[v], 1u);
+  }
 };
-
-__device__ __forceinline__ void accumulate(Acc& acc, int v, float4 col) {
-  atomicAdd(&acc.c[0][v], __float2uint_rn(col.x * kFix));
-  atomicAdd(&acc.c[1][v], __float2uint_rn(col.y * kFix));
-  atomicAdd(&acc.c[2][v], __float2uint_rn(col.z * kFix));
-  atomicAdd(&acc.c[3][v], __float2uint_rn(col.w * kFix));
-  atomicAdd(&acc.n[v], 1u);
-}
+template <> struct AccT<VCT_STORAGE_RGBA16F> {
+  unsigned long long c[4][kBrickVox];
+  uint32_t n[kBrickVox];
+  __device__ __forceinline__ void clear(int i) { c[0][i] = 0; c[1][i] = 0; c[2][i] = 0; c[3][i] = 0; n[i] = 0; }
+  __device__ __forceinline__ void add(const SceneParams& sp, int v, float4 col) {
+    const float k = 4294967296.0f / sp.radiance_max;
+    atomicAdd(&c[0][v], __float2ull_rn(col.x * k));
+    atomicAdd(&c[1][v], __float2ull_rn(col.y * k));
+    atomicAdd(&c[2][v], __float2ull_rn(col.z * k));
+    atomicAdd(&c[3][v], __float2ull_rn(col.w * 4294967296.0f));
+    atomicAdd(&n[v], 1u);
+  }
+};
+typedef AccT<VCT_STORAGE_RGBA8> Acc;
 
 // -------------------------------------------------- reference raster mode --
 struct SetupRef {
@@ -362,8 +385,9 @@ __device__ int setup_ref(const SceneParams& sp, int N, uint32_t t, const int b3[
   return s.ni * s.nj;
 }
 
+template <class A>
 __device__ __forceinline__ void item_ref(const SceneParams& sp, int N, const int b3[3], const SetupRef& s, int local,
-                                         Acc& acc) {
+                                         A& acc) {
   const int i = s.i0 + local % s.ni, j = s.j0 + local / s.ni;
   const long long sx = 256LL * i + 128, sy = 256LL * j + 128;
   const long long w0 = edge_fn(s.A[1], s.B[1], s.A[2], s.B[2], sx, sy);
@@ -388,7 +412,7 @@ __device__ __forceinline__ void item_ref(const SceneParams& sp, int N, const int
   const float l0 = __ll2float_rn(w0) / s.farea, l1 = __ll2float_rn(w1) / s.farea, l2 = __ll2float_rn(w2) / s.farea;
   const V3 p = s.gp[0] * l0 + s.gp[1] * l1 + s.gp[2] * l2;
   const V3 n = s.gn[0] * l0 + s.gn[1] * l1 + s.gn[2] * l2;
-  accumulate(acc, (lz * kBrick + ly) * kBrick + lx, voxel_color(sp, sp.materials[s.mat], p, n));
+  acc.add(sp, (lz * kBrick + ly) * kBrick + lx, voxel_color(sp, sp.materials[s.mat], p, n));
 }
 
 // ---------------------------------------------------- conservative mode ----
@@ -502,8 +526,9 @@ __device__ void closest_bary(V3 p, V3 a, V3 b, V3 c, float w[3]) {
   w[0] = 1.f - v - t; w[1] = v; w[2] = t;
 }
 
+template <class A>
 __device__ __forceinline__ void item_sat(const SceneParams& sp, int N, const int b3[3], const SetupSat& s, int local,
-                                         Acc& acc) {
+                                         A& acc) {
   const int x = s.x0 + local % s.nx;
   const int y = s.y0 + (local / s.nx) % s.ny;
   const int z = s.z0 + local / (s.nx * s.ny);
@@ -515,7 +540,7 @@ __device__ __forceinline__ void item_sat(const SceneParams& sp, int N, const int
   const V3 p = s.gp[0] * w[0] + s.gp[1] * w[1] + s.gp[2] * w[2];
   const V3 n = s.gn[0] * w[0] + s.gn[1] * w[1] + s.gn[2] * w[2];
   const int lx = x - b3[0] * kBrick, ly = y - b3[1] * kBrick, lz = z - b3[2] * kBrick;
-  accumulate(acc, (lz * kBrick + ly) * kBrick + lx, voxel_color(sp, sp.materials[s.mat], p, n));
+  acc.add(sp, (lz * kBrick + ly) * kBrick + lx, voxel_color(sp, sp.materials[s.mat], p, n));
 }
 
 // ------------------------------------------------------------ brick CTA ----
@@ -525,7 +550,7 @@ __global__ void __launch_bounds__(kThreads) k_bricks(SceneParams sp, int N, cons
                                                      cudaSurfaceObject_t l0, uint32_t* __restrict__ counts,
                                                      FrameStatus* st) {
   typedef typename std::conditional<MODE == VCT_VOX_CONSERVATIVE, SetupSat, SetupRef>::type Setup;
-  __shared__ Acc acc;
+  __shared__ AccT<STORAGE> acc;
   __shared__ Setup setup[kWarps][32];
   __shared__ int excl[kWarps][33];
   const int nb = N / kBrick;
@@ -543,9 +568,7 @@ __global__ void __launch_bounds__(kThreads) k_bricks(SceneParams sp, int N, cons
     }
     return;
   }
-  for (int i = threadIdx.x; i < kBrickVox; i += kThreads) {
-    acc.c[0][i] = 0; acc.c[1][i] = 0; acc.c[2][i] = 0; acc.c[3][i] = 0; acc.n[i] = 0;
-  }
+  for (int i = threadIdx.x; i < kBrickVox; i += kThreads) acc.clear(i);
   __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   for (uint32_t base = beg + warp * 32; base < end; base += kWarps * 32) {
@@ -601,10 +624,10 @@ __global__ void __launch_bounds__(kThreads) k_bricks(SceneParams sp, int N, cons
     } else {
       ushort4 o = make_ushort4(0, 0, 0, 0);
       if (n) {
-        const float inv = 1.0f / ((float)n * kFix);
-        o = make_ushort4(__half_as_ushort(__float2half_rn((float)acc.c[0][i] * inv)),
-                         __half_as_ushort(__float2half_rn((float)acc.c[1][i] * inv)),
-                         __half_as_ushort(__float2half_rn((float)acc.c[2][i] * inv)),
+        const float inv = 1.0f / ((float)n * 4294967296.0f), k = inv * sp.radiance_max;
+        o = make_ushort4(__half_as_ushort(__float2half_rn((float)acc.c[0][i] * k)),
+                         __half_as_ushort(__float2half_rn((float)acc.c[1][i] * k)),
+                         __half_as_ushort(__float2half_rn((float)acc.c[2][i] * k)),
                          __half_as_ushort(__float2half_rn((float)acc.c[3][i] * inv)));
       }
       surf3Dwrite(o, l0, x * 8, y, z);
@@ -626,9 +649,7 @@ __global__ void __launch_bounds__(kThreads) k_bricks_linear(SceneParams sp, int 
   const int nb = N / kBrick;
   const uint32_t brick = blockIdx.x;
   const int b3[3] = {(int)(brick % nb), (int)((brick / nb) % nb), (int)(brick / ((uint32_t)nb * nb))};
-  for (int i = threadIdx.x; i < kBrickVox; i += kThreads) {
-    acc.c[0][i] = 0; acc.c[1][i] = 0; acc.c[2][i] = 0; acc.c[3][i] = 0; acc.n[i] = 0;
-  }
+  for (int i = threadIdx.x; i < kBrickVox; i += kThreads) acc.clear(i);
   __syncthreads();
   const uint32_t beg = min(offset[brick], cap), end = min(offset[brick + 1], cap);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;

@@ -391,6 +391,7 @@ struct vct_renderer {
     sp.n_materials = (uint32_t)materials.size();
     sp.n_lights = (int32_t)std::min<size_t>(fi.lights.size(), kMaxLights);
     sp.cube_size = fi.cube_size;
+    sp.radiance_max = cfg.radiance_max > 0.0f ? cfg.radiance_max : 1.0f;
     for (int i = 0; i < sp.n_lights; ++i) sp.lights[i] = fi.lights[i];
 
     CameraParams cp;

@@ -38,6 +38,7 @@ struct SceneParams {
   uint32_t n_materials;
   int32_t n_lights;
   float cube_size;
+  float radiance_max;  // clamp of voxel radiance (1 = the reference's)
   vct_point_light lights[kMaxLights];
 };
 

@@ -73,7 +73,8 @@ class VCTError(RuntimeError):
 class Config(C.Structure):
     _fields_ = [("grid_res", C.c_int32), ("vox_mode", C.c_int32), ("mip_mode", C.c_int32),
                 ("storage", C.c_int32), ("sampler", C.c_int32), ("cone_set", C.c_int32),
-                ("keep_counts", C.c_int32), ("keep_float_frame", C.c_int32), ("reserved", C.c_int32 * 8)]
+                ("keep_counts", C.c_int32), ("keep_float_frame", C.c_int32), ("radiance_max", C.c_float),
+                ("reserved", C.c_int32 * 7)]
 
 
 class StageTimes(C.Structure):
@@ -150,7 +151,7 @@ def default_config(**kw) -> Config:
     c = Config()
     lib().vct_config_default(C.byref(c))
     for k, v in kw.items():
-        setattr(c, k, int(v))
+        setattr(c, k, float(v) if k == "radiance_max" else int(v))
     return c
 
 

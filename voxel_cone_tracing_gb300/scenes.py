@@ -338,3 +338,40 @@ def scene_sphere(seed: int = 2000, freq: int = 158, width: int = 1920, height: i
     return Scene([room, sphere], [mat_identity(), model], np.array(mats, MATERIAL_DTYPE),
                  np.array([point_light((0.0, 0.4, 0.05))], LIGHT_DTYPE), view, proj, ROOM_CUBE_SIZE,
                  name=f"room+icosphere{freq}")
+
+
+HDR_RADIANCE_MAX = 16.0
+
+
+def scene_hdr(seed: int = 3000, freq: int = 158, n_spheres: int = 4, n_cuboids: int = 32, width: int = 1920,
+              height: int = 1080) -> Scene:
+    """HDR precision scene: the room, ``n_spheres`` noise-displaced geodesic
+    spheres (20*freq^2 triangles each; 4 x 158 gives 1,997,120) and
+    ``n_cuboids`` randomly rotated cuboids, a bright point light (intensity
+    12) and emissive cuboids (emission up to 20), so that voxel radiance
+    covers [0, 16] before the clamp."""
+    rng = np.random.default_rng(seed)
+    mats = [default_material()]
+    for _ in range(5):
+        mats.append(make_material(rng.uniform(0.2, 0.9, 3), roughness=rng.uniform(0.3, 1.0)))
+    meshes, models = [box_room(list(range(1, 6)))], [mat_identity()]
+    for k in range(n_spheres):
+        base = len(mats)
+        for _ in range(20):
+            mats.append(make_material(rng.uniform(0.0, 1.0, 3), roughness=rng.uniform(0.0, 1.0)))
+        meshes.append(geodesic_sphere(freq, seed + 1 + k, 0.05, material_base=base))
+        models.append(trs(translate=rng.uniform([-0.3, -0.35, -0.35], [0.3, 0.0, 0.0]),
+                          scale=np.full(3, rng.uniform(0.08, 0.16))))
+    for _ in range(n_cuboids):
+        ids = []
+        for _ in range(6):
+            emit = rng.uniform(0.0, 20.0, 3) if rng.uniform() < 0.3 else (0.0, 0.0, 0.0)
+            mats.append(make_material(rng.uniform(0.1, 0.9, 3), roughness=rng.uniform(0.2, 1.0), emission=emit))
+            ids.append(len(mats) - 1)
+        meshes.append(cuboid(ids))
+        models.append(trs(translate=rng.uniform([-0.42, -0.45, -0.45], [0.42, 0.35, 0.1]),
+                          rot=random_rotation(rng), scale=rng.uniform(0.02, 0.1, 3)))
+    view, proj = _camera(width, height)
+    return Scene(meshes, models, np.array(mats, MATERIAL_DTYPE),
+                 np.array([point_light((0.0, 0.38, 0.05), intensity=12.0)], LIGHT_DTYPE), view, proj,
+                 ROOM_CUBE_SIZE, name=f"room+{n_spheres}icospheres{freq}+{n_cuboids}cuboids")
