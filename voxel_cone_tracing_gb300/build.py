@@ -17,6 +17,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libvct.so")
+DEMO_SRC = os.path.join(HERE, "demo", "vct_demo.cpp")
+DEMO = os.path.join(HERE, "vct_demo")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=off", "-I", CSRC]
 # Extra nvcc flags (e.g. -DVCT_TRACE_MIN_BLOCKS=3 for tuning sweeps).
@@ -46,8 +48,25 @@ def up_to_date() -> bool:
     return all(os.path.getmtime(d) <= t for d in _deps())
 
 
+def build_demo(force: bool = False) -> str:
+    """The headless demo executable (C++ host over include/vct_renderer.hpp),
+    linked against libvct.so next to it."""
+    deps = [DEMO_SRC, LIB] + glob.glob(os.path.join(HERE, "..", "include", "*"))
+    if not force and os.path.exists(DEMO) and os.path.getmtime(DEMO) >= max(map(os.path.getmtime, deps)):
+        return DEMO
+    tmp = DEMO + f".tmp{os.getpid()}"
+    cmd = [shutil.which("g++") or "g++", "-O2", "-std=c++17", "-I", os.path.join(HERE, "..", "include"), DEMO_SRC,
+           "-L", HERE, "-lvct", "-Wl,-rpath,$ORIGIN", "-o", tmp]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"demo build failed:\n{r.stderr}")
+    os.replace(tmp, DEMO)
+    return DEMO
+
+
 def build(force: bool = False, verbose: bool = False) -> str:
     if not force and up_to_date():
+        build_demo()
         return LIB
     os.makedirs(BUILD, exist_ok=True)
     cc = nvcc()
@@ -73,6 +92,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stderr}")
     os.replace(tmp, LIB)
+    build_demo(force=True)
     return LIB
 
 
