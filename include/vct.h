@@ -346,6 +346,80 @@ vct_status vct_mip_tex_3d(vct_tex3d tex);
 vct_status vct_tex3d_upload(vct_tex3d tex, int32_t level, const void* rgba8);
 vct_status vct_tex3d_download(vct_tex3d tex, int32_t level, void* rgba8);
 
+/* ------------------------------------------------- Batched rendering --- */
+/* No reference counterpart: the reference renders one scene per frame
+ * (Renderer::render, renderer.cpp:392-405).  A batch renders many
+ * independent scenes of different grid, mesh and frame sizes per frame with
+ * the same maths as a Renderer (each scene's frame and voxel maps equal a
+ * Renderer's on the same scene, bit for bit), but each stage pass is one
+ * persistent kernel launch over all scenes, and the frame can be captured
+ * once in a CUDA graph and replayed.  Geometry, materials and lights are
+ * fixed at creation; cameras can change every frame.  RGBA8 anisotropic
+ * maps, texture-unit sampler. */
+
+typedef struct {
+  const vct_vert_data* verts;
+  uint32_t n_verts;
+  const uint32_t* indices;       /* 3 * n_tris */
+  uint32_t n_tris;
+  const uint32_t* tri_material;  /* per triangle, index into the scene's materials */
+  float model[16];               /* column-major model matrix */
+} vct_batch_mesh;
+
+typedef struct {
+  int32_t width, height;
+  int32_t grid_res;              /* power of two, 16..256 */
+  int32_t cone_set;              /* VCT_CONES_REF9 (9 cones) or VCT_CONES_SIX60 (6) */
+  float cube_size;
+  const vct_batch_mesh* meshes;
+  uint32_t n_meshes;
+  const vct_material_data* materials;  /* >= 1 */
+  uint32_t n_materials;
+  const vct_point_light* lights;       /* <= 10 */
+  uint32_t n_lights;
+  float view[16], proj[16];
+} vct_batch_scene;
+
+typedef struct {
+  int32_t vox_mode;   /* VCT_VOX_* for every scene */
+  int32_t use_graph;  /* capture the frame once in a CUDA graph, then replay it */
+  int32_t reserved[6];
+} vct_batch_config;
+
+/* Launch shapes of the batched kernels: persistent CTAs per SM of the
+ * binning, brick and trace launches, and the trace's tile scheduling
+ * (1 = atomic tile queue, 0 = static stride). */
+typedef struct {
+  int32_t bin_ctas_per_sm;
+  int32_t bricks_ctas_per_sm;
+  int32_t trace_ctas_per_sm;
+  int32_t trace_dynamic;
+} vct_batch_shape;
+
+typedef struct vct_batch vct_batch;
+
+vct_status vct_batch_create(const vct_batch_scene* scenes, uint32_t n_scenes, const vct_batch_config* cfg,
+                            vct_batch** out);
+void vct_batch_destroy(vct_batch* b);
+vct_status vct_batch_set_camera(vct_batch* b, uint32_t scene, const float view[16], const float proj[16]);
+/* One frame of every scene, enqueued on the batch's stream. */
+vct_status vct_batch_render(vct_batch* b);
+vct_status vct_batch_synchronize(vct_batch* b);
+vct_status vct_batch_set_stream(vct_batch* b, void* stream);
+/* RGBA8 frame of one scene, row 0 = bottom. */
+vct_status vct_batch_read_frame(vct_batch* b, uint32_t scene, void* rgba8);
+/* One level of one voxel map of one scene (level 0: map ignored). */
+vct_status vct_batch_read_voxels(vct_batch* b, uint32_t scene, int32_t level, int32_t map, void* rgba8);
+/* Stage times of the last frame, all scenes together. */
+vct_status vct_batch_stage_times(vct_batch* b, vct_stage_times* out);
+vct_status vct_batch_get_shape(vct_batch* b, vct_batch_shape* out);
+vct_status vct_batch_set_shape(vct_batch* b, const vct_batch_shape* shape);
+/* The autotuner: times `frames` frames of each candidate launch shape on
+ * this batch (coordinate search over the fields of vct_batch_shape), keeps
+ * the fastest, and reports it with the frame times before and after. */
+vct_status vct_batch_autotune(vct_batch* b, int32_t frames, vct_batch_shape* best, float* ms_before,
+                              float* ms_after);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,126 @@
+"""Batched rendering (vct_batch_*): every scene of a batch of uneven grid,
+mesh and frame sizes renders exactly what a Renderer renders on the same
+scene (frames, level 0 and the directional mips bit-exact), eagerly and as
+a replayed CUDA graph, before and after autotuning, and when a work list
+overflows and is grown."""
+import numpy as np
+import pytest
+
+from voxel_cone_tracing_gb300 import scenes
+
+CONES = {9: 0, 6: 1}
+
+
+def _items():
+    out = []
+    for k, (seed, w, h, grid, cones) in enumerate([(11, 64, 48, 16, 9), (12, 96, 64, 32, 6), (13, 40, 40, 64, 9),
+                                                    (14, 80, 30, 32, 9)]):
+        out.append((scenes.scene_small(seed=seed, width=w, height=h), w, h, grid, CONES[cones]))
+    out.append((scenes.scene_sphere(seed=21, freq=8, width=128, height=96), 128, 96, 64, CONES[9]))
+    empty = scenes.scene_small(seed=15, width=24, height=16)
+    empty.meshes, empty.models = [], []
+    out.append((empty, 24, 16, 32, CONES[6]))
+    return out
+
+
+def _single(vct, scene, w, h, grid, cones, vox_mode=0, view=None):
+    r = vct.Renderer(w, h, grid_res=grid, cone_set=cones, vox_mode=vox_mode)
+    ids = vct.load_scene(r, scene)
+    if view is not None:
+        r.set_camera_transform(view, scene.proj)
+    r.set_voxel_view_dir(7, 0.0)
+    vct.queue_scene(r, scene, ids)
+    r.render()
+    return r
+
+
+def _check_scene(vct, b, i, item, vox_mode=0, view=None):
+    scene, w, h, grid, cones = item
+    r = _single(vct, scene, w, h, grid, cones, vox_mode, view)
+    np.testing.assert_array_equal(b.read_frame(i), r.read_frame(), err_msg=f"scene {i} frame")
+    np.testing.assert_array_equal(b.read_voxels(i, 0), r.read_voxels(0), err_msg=f"scene {i} level 0")
+    n, levels = r.grid()
+    for lvl in (1, levels - 1):
+        for m in range(6):
+            np.testing.assert_array_equal(b.read_voxels(i, lvl, m), r.read_voxels(lvl, m),
+                                          err_msg=f"scene {i} level {lvl} map {m}")
+
+
+def test_batch_rejects_bad_scenes(vct):
+    s = scenes.scene_small(width=16, height=16)
+    with pytest.raises(vct.VCTError):
+        vct.Batch([(s, 16, 16, 100, 0)])   # grid not a power of two
+    with pytest.raises(vct.VCTError):
+        vct.Batch([(s, 16, 16, 512, 0)])   # above the batch limit
+    with pytest.raises(vct.VCTError):
+        vct.Batch([(s, 16, 16, 32, 7)])    # no such cone set
+    with pytest.raises(vct.VCTError):
+        vct.Batch([])
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("use_graph", [False, True], ids=["eager", "graph"])
+def test_batch_matches_renderer(vct, use_graph):
+    items = _items()
+    b = vct.Batch(items, use_graph=use_graph)
+    b.render()
+    b.render()  # a second frame (a graph replay) gives the same result
+    t = b.stage_times()
+    assert t["kernel_launches"] > 0 and t["total"] > 0
+    for i, item in enumerate(items):
+        _check_scene(vct, b, i, item)
+
+
+@pytest.mark.gpu
+def test_batch_conservative_voxelizer(vct):
+    items = _items()[:3]
+    b = vct.Batch(items, vox_mode=1)
+    b.render()
+    for i, item in enumerate(items):
+        _check_scene(vct, b, i, item, vox_mode=1)
+
+
+@pytest.mark.gpu
+def test_batch_camera_update_under_graph(vct):
+    items = _items()[:4]
+    b = vct.Batch(items, use_graph=True)
+    b.render()
+    scene = items[2][0]
+    view = scenes.look_at((0.1, 0.05, 0.45), (0.0, -0.1, -0.5))
+    b.set_camera(2, view, scene.proj)
+    b.render()
+    _check_scene(vct, b, 2, items[2], view=view)
+    _check_scene(vct, b, 1, items[1])
+
+
+@pytest.mark.gpu
+def test_batch_autotune_keeps_results(vct):
+    items = _items()
+    b = vct.Batch(items, use_graph=True)
+    b.render()
+    before = [b.read_frame(i).copy() for i in range(len(items))]
+    rep = b.autotune(frames=1)
+    assert rep["shape"] == b.shape
+    assert rep["ms_after"] <= rep["ms_before"] + 1e-6
+    assert rep["shape"]["trace_ctas_per_sm"] in (2, 3, 4) and rep["shape"]["trace_dynamic"] in (0, 1)
+    b.render()
+    for i in range(len(items)):
+        np.testing.assert_array_equal(b.read_frame(i), before[i])
+
+
+@pytest.mark.gpu
+def test_batch_work_lists_grow(vct):
+    """64 large random triangles in a 256^3 grid need more (triangle, brick)
+    pairs than the initial list holds: the batch grows it and renders the
+    frame again, like a Renderer."""
+    rng = np.random.default_rng(5)
+    tris = rng.uniform(-0.9, 0.9, (64, 3, 3)).astype(np.float32)
+    from tests.helpers import tri_scene
+    s = tri_scene(tris, lights=[((0.0, 0.5, 0.0),)], cube_size=1.0,
+                  view=scenes.look_at((0.0, 0.0, 0.95), (0.0, 0.0, 0.0)),
+                  proj=scenes.perspective(1.0, 1.0, 0.01, 10.0))
+    items = [(s, 48, 48, 256, 0), _items()[0]]
+    b = vct.Batch(items, use_graph=True)
+    b.render()
+    for i, item in enumerate(items):
+        _check_scene(vct, b, i, item)

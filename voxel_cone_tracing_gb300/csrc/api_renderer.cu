@@ -231,7 +231,7 @@ extern "C" vct_status vct_set_grid_resolution(vct_renderer* r, uint32_t res) {
   if (!r) return set_error(VCT_ERR_INVALID_VALUE, "NULL renderer");
   if (!is_pow2(res) || res < 8 || res > 1024)
     return set_error(VCT_ERR_INVALID_VALUE, "grid resolution %u: need a power of two in [8, 1024]", res);
-  if (res == r->res && r->l0_arr) return VCT_OK;
+  if (res == r->res && r->maps.l0_arr) return VCT_OK;
   VCT_CHECK(r->finish());
   r->cfg.grid_res = (int32_t)res;
   return r->alloc_maps(res);
@@ -388,8 +388,8 @@ extern "C" vct_status vct_read_voxels(vct_renderer* r, int32_t level, int32_t ma
   if (level < 0 || level >= r->levels) return set_error(VCT_ERR_INVALID_VALUE, "level %d of %d", level, r->levels);
   if (map < 0 || map >= r->ms.nmaps) return set_error(VCT_ERR_INVALID_VALUE, "map %d of %d", map, r->ms.nmaps);
   VCT_CHECK(r->finish());
-  cudaArray_t a = r->l0_arr;
-  if (level > 0) VCT_CUDA(cudaGetMipmappedArrayLevel(&a, r->dir_arr[map], level - 1));
+  cudaArray_t a = r->maps.l0_arr;
+  if (level > 0) VCT_CUDA(cudaGetMipmappedArrayLevel(&a, r->maps.dir_arr[map], level - 1));
   const size_t s = r->res >> level;
   const size_t bpt = r->cfg.storage == VCT_STORAGE_RGBA16F ? 8 : 4;
   cudaMemcpy3DParms p;

@@ -18,6 +18,8 @@
 // maths and round-to-nearest-even to half.
 #include <cuda_fp16.h>
 
+#include <algorithm>
+
 #include "vct_internal.h"
 
 namespace vct {
@@ -163,17 +165,16 @@ __device__ __forceinline__ void aniso6_rgba16f(const uint2* ch, uint2* out) {
 // One pass: source level `src_level` (0 = the shared level 0) -> levels
 // src_level+1 .. src_level+K of NMAPS maps, one CTA per B^3 source region.
 template <int NMAPS, bool FROM_L0, int K, int STORAGE>
-__global__ void __launch_bounds__(kThreads) k_mip(MapSet ms, int src_level) {
+__device__ __forceinline__ void mip_region(const MapSet& ms, int src_level, uint32_t region, unsigned char* smem_raw) {
   typedef typename Texel<STORAGE>::T T;
   constexpr int B = 1 << K;
   constexpr int B3 = B * B * B;
   constexpr int NSRC = FROM_L0 ? 1 : NMAPS;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
   T* src = reinterpret_cast<T*>(smem_raw);
   T* lvl = src + NSRC * B3;  // level buffers follow, NMAPS * (B/2)^3, (B/4)^3, ...
   const int S = ms.N >> src_level;
   const int nbx = S / B;
-  const int bx = blockIdx.x % nbx, by = (blockIdx.x / nbx) % nbx, bz = blockIdx.x / (nbx * nbx);
+  const int bx = region % nbx, by = (region / nbx) % nbx, bz = region / (nbx * nbx);
   const int ox = bx * B, oy = by * B, oz = bz * B;
   for (int i = threadIdx.x; i < NSRC * B3; i += kThreads) {
     const int m = i / B3, r = i % B3;
@@ -235,6 +236,79 @@ __global__ void __launch_bounds__(kThreads) k_mip(MapSet ms, int src_level) {
     cur_shared = false;
     out += NMAPS * b3;
   }
+}
+
+// One pass: source level `src_level` (0 = the shared level 0) -> levels
+// src_level+1 .. src_level+K of NMAPS maps, one CTA per B^3 source region.
+template <int NMAPS, bool FROM_L0, int K, int STORAGE>
+__global__ void __launch_bounds__(kThreads) k_mip(MapSet ms, int src_level) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  mip_region<NMAPS, FROM_L0, K, STORAGE>(ms, src_level, blockIdx.x, smem_raw);
+}
+
+// The first pass (level 0 -> levels 1..4) of every scene of a batch in one
+// persistent launch.
+template <int NMAPS, int STORAGE>
+__global__ void __launch_bounds__(kThreads) k_mip_batch(BatchWork w) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  for (uint32_t g = blockIdx.x; g < w.total; g += gridDim.x) {
+    const int s = batch_scene_of(w, g);
+    mip_region<NMAPS, true, 4, STORAGE>(w.scenes[s].ms, 0, g - __ldg(w.prefix + s), smem_raw);
+    __syncthreads();  // the next region overwrites the shared buffers
+  }
+}
+
+// Level `level` (>= 2) of every scene of a batch from its level - 1, one
+// thread per destination texel of every map (the small last levels).
+template <int NMAPS, int STORAGE>
+__global__ void __launch_bounds__(kThreads) k_mip_level_batch(BatchWork w, int level) {
+  typedef typename Texel<STORAGE>::T T;
+  for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < w.total; g += gridDim.x * blockDim.x) {
+    const int s = batch_scene_of(w, g);
+    const MapSet& ms = w.scenes[s].ms;
+    const uint32_t i = g - __ldg(w.prefix + s);
+    const int n = ms.N >> level;
+    const uint32_t n3 = (uint32_t)n * n * n;
+    const int d = (int)(i / n3);
+    const uint32_t r = i % n3;
+    const int x = (int)(r % n), y = (int)((r / n) % n), z = (int)(r / ((uint32_t)n * n));
+    T ch[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k)
+      surf3Dread(&ch[k], ms.surf[d][level - 1], (2 * x + c_off[k][0]) * Texel<STORAGE>::kBytes, 2 * y + c_off[k][1],
+                 2 * z + c_off[k][2]);
+    const T v = reduce<STORAGE>(ch, d, NMAPS == 1);
+    surf3Dwrite(v, ms.surf[d][level], x * Texel<STORAGE>::kBytes, y, z);
+  }
+}
+
+template <int NMAPS, int STORAGE>
+cudaError_t run_batch(const BatchWork& regions, const BatchWork* tail, int n_tail, cudaStream_t st, int* launches) {
+  typedef typename Texel<STORAGE>::T T;
+  constexpr int B = 16;
+  size_t smem = (size_t)B * B * B * sizeof(T);
+  for (int l = 1; l <= 4; ++l) smem += (size_t)NMAPS * (B >> l) * (B >> l) * (B >> l) * sizeof(T);
+  auto kern = k_mip_batch<NMAPS, STORAGE>;
+  if (smem > 48 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+  }
+  int dev = 0, sms = 148, per_sm = 1;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kThreads, smem);
+  if (regions.total) {
+    const unsigned grid = (unsigned)std::max(1, std::min<int>(sms * std::max(per_sm, 1), (int)regions.total));
+    kern<<<grid, kThreads, smem, st>>>(regions);
+    if (launches) ++*launches;
+  }
+  for (int t = 0; t < n_tail; ++t) {
+    if (!tail[t].total) continue;
+    const unsigned grid = (unsigned)std::min<uint32_t>((tail[t].total + kThreads - 1) / kThreads, (uint32_t)sms * 8);
+    k_mip_level_batch<NMAPS, STORAGE><<<grid, kThreads, 0, st>>>(tail[t], 5 + t);
+    if (launches) ++*launches;
+  }
+  return cudaGetLastError();
 }
 
 template <int NMAPS, bool FROM_L0, int K, int STORAGE>
@@ -320,6 +394,14 @@ cudaError_t launch_mipmap(const MapSet& ms, int mip_mode, cudaStream_t st, int* 
   }
   return ms.storage == VCT_STORAGE_RGBA8 ? run_all<6, VCT_STORAGE_RGBA8>(ms, st, launches)
                                          : run_all<6, VCT_STORAGE_RGBA16F>(ms, st, launches);
+}
+
+cudaError_t launch_mipmap_batch(const BatchWork& regions, const BatchWork* tail, int n_tail, int storage,
+                                cudaStream_t st, int* launches) {
+  // Every scene of a batch is anisotropic (6 maps); levels 1..4 in the first
+  // launch, levels 5 and 6 (where a scene has them) in one launch each.
+  return storage == VCT_STORAGE_RGBA8 ? run_batch<6, VCT_STORAGE_RGBA8>(regions, tail, n_tail, st, launches)
+                                      : run_batch<6, VCT_STORAGE_RGBA16F>(regions, tail, n_tail, st, launches);
 }
 
 cudaError_t launch_fill_rgba8(cudaSurfaceObject_t s, int w, int h, int d, uchar4 v, cudaStream_t st) {

@@ -20,6 +20,8 @@
 //   k_gb_resolve -- per pixel: perspective-correct barycentrics of the
 //                  visible triangle -> world position, interpolated world
 //                  normal (not renormalised), material id.
+#include <algorithm>
+
 #include "vct_internal.h"
 #include "vct_math.cuh"
 
@@ -39,7 +41,7 @@ struct BigRec {
   int tl;
   int x0, y0, x1, y1;  // pixel bbox (inclusive)
   int tw;              // tiles across
-  int pad;
+  uint32_t scene;      // scene of a batch (0 for one renderer)
 };
 
 __device__ __forceinline__ int find_instance(const SceneParams& sp, uint32_t t) {
@@ -101,7 +103,8 @@ __device__ __forceinline__ void pixel_test(const BigRec& r, unsigned long long* 
 }
 
 // Set up one (possibly clipped) screen triangle; raster it here if small.
-__device__ void raster_subtri(const CV v[3], const CameraParams& cp, uint32_t tri, const RasterBuffers& rb) {
+__device__ void raster_subtri(const CV v[3], const CameraParams& cp, uint32_t tri, const RasterBuffers& rb,
+                              uint32_t scene) {
   BigRec r;
   long long X[3], Y[3];
   for (int k = 0; k < 3; ++k) {
@@ -139,13 +142,13 @@ __device__ void raster_subtri(const CV v[3], const CameraParams& cp, uint32_t tr
     return;
   }
   r.tw = (r.x1 - r.x0 + kTile) / kTile;
-  r.pad = 0;
+  r.scene = scene;
   const uint32_t slot = atomicAdd(&rb.big_count[0], 1u);
   if (slot < rb.big_cap) reinterpret_cast<BigRec*>(rb.big)[slot] = r;
 }
 
-__global__ void __launch_bounds__(256) k_gb_setup(SceneParams sp, CameraParams cp, RasterBuffers rb) {
-  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void setup_tri(const SceneParams& sp, const CameraParams& cp, const RasterBuffers& rb,
+                                          uint32_t t, uint32_t scene) {
   if (t >= sp.total_tris) return;
   const DevInstance& in = sp.inst[find_instance(sp, t)];
   const uint32_t lt = t - in.tri_base;
@@ -157,7 +160,7 @@ __global__ void __launch_bounds__(256) k_gb_setup(SceneParams sp, CameraParams c
     for (int k = 0; k < 3; ++k)
       if (!(plane_eval(pl, cv[k]) >= 0.0f)) all_in = false;
   if (all_in) {
-    raster_subtri(cv, cp, t, rb);
+    raster_subtri(cv, cp, t, rb, scene);
     return;
   }
   CV a[10], b[10];
@@ -183,7 +186,28 @@ __global__ void __launch_bounds__(256) k_gb_setup(SceneParams sp, CameraParams c
   }
   for (int k = 1; k + 1 < n; ++k) {
     const CV tri3[3] = {a[0], a[k], a[k + 1]};
-    raster_subtri(tri3, cp, t, rb);
+    raster_subtri(tri3, cp, t, rb, scene);
+  }
+}
+
+__global__ void __launch_bounds__(256) k_gb_setup(SceneParams sp, CameraParams cp, RasterBuffers rb) {
+  setup_tri(sp, cp, rb, blockIdx.x * blockDim.x + threadIdx.x, 0u);
+}
+
+// The pixel slice of one batch scene in the batch-wide raster buffers.
+__device__ __forceinline__ RasterBuffers scene_rb(const RasterBuffers& rb, const BatchScene& S) {
+  RasterBuffers r = rb;
+  r.vis = rb.vis + S.px_base;
+  r.gb_pos = rb.gb_pos + S.px_base;
+  r.gb_nrm = rb.gb_nrm + S.px_base;
+  return r;
+}
+
+__global__ void __launch_bounds__(256) k_gb_setup_batch(BatchWork w, RasterBuffers rb) {
+  for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < w.total; g += gridDim.x * blockDim.x) {
+    const int s = batch_scene_of(w, g);
+    const BatchScene& S = w.scenes[s];
+    setup_tri(S.sp, w.cams[s], scene_rb(rb, S), g - __ldg(w.prefix + s), (uint32_t)s);
   }
 }
 
@@ -230,7 +254,7 @@ __global__ void __launch_bounds__(1024) k_gb_big_scan(RasterBuffers rb) {
   }
 }
 
-__global__ void __launch_bounds__(kTile * kTile) k_gb_big(RasterBuffers rb, int W) {
+__global__ void __launch_bounds__(kTile * kTile) k_gb_big(RasterBuffers rb, int W, const BatchScene* scenes) {
   const uint32_t n = min(rb.big_count[0], rb.big_cap);
   const uint32_t total = rb.big_count[1];
   const BigRec* rec = reinterpret_cast<const BigRec*>(rb.big);
@@ -244,12 +268,18 @@ __global__ void __launch_bounds__(kTile * kTile) k_gb_big(RasterBuffers rb, int 
     const uint32_t lt = t - rb.big_offset[lo];
     const int tx = (int)(lt % (uint32_t)r.tw), ty = (int)(lt / (uint32_t)r.tw);
     const int px = r.x0 + tx * kTile + (threadIdx.x % kTile), py = r.y0 + ty * kTile + (threadIdx.x / kTile);
-    if (px <= r.x1 && py <= r.y1) pixel_test(r, rb.vis, W, px, py);
+    unsigned long long* vis = rb.vis;
+    int w = W;
+    if (scenes) {  // a batch: the record's scene
+      vis += scenes[r.scene].px_base;
+      w = scenes[r.scene].W;
+    }
+    if (px <= r.x1 && py <= r.y1) pixel_test(r, vis, w, px, py);
   }
 }
 
-__global__ void __launch_bounds__(256) k_gb_resolve(SceneParams sp, CameraParams cp, RasterBuffers rb) {
-  const int px = blockIdx.x * 16 + (threadIdx.x & 15), py = blockIdx.y * 16 + (threadIdx.x >> 4);
+__device__ __forceinline__ void resolve_px(const SceneParams& sp, const CameraParams& cp, const RasterBuffers& rb,
+                                           int px, int py) {
   if (px >= cp.W || py >= cp.H) return;
   const size_t p = (size_t)py * cp.W + px;
   const unsigned long long key = rb.vis[p];
@@ -294,6 +324,21 @@ __global__ void __launch_bounds__(256) k_gb_resolve(SceneParams sp, CameraParams
   rb.gb_nrm[p] = make_float4(nrm.x, nrm.y, nrm.z, __uint_as_float(t));
 }
 
+__global__ void __launch_bounds__(256) k_gb_resolve(SceneParams sp, CameraParams cp, RasterBuffers rb) {
+  resolve_px(sp, cp, rb, blockIdx.x * 16 + (threadIdx.x & 15), blockIdx.y * 16 + (threadIdx.x >> 4));
+}
+
+// 16x16-pixel tiles of every batch scene.
+__global__ void __launch_bounds__(256) k_gb_resolve_batch(BatchWork w, RasterBuffers rb) {
+  for (uint32_t g = blockIdx.x; g < w.total; g += gridDim.x) {
+    const int s = batch_scene_of(w, g);
+    const BatchScene& S = w.scenes[s];
+    const uint32_t lt = g - __ldg(w.prefix + s), tiles_x = (uint32_t)(S.W + 15) / 16;
+    resolve_px(S.sp, w.cams[s], scene_rb(rb, S), (int)(lt % tiles_x) * 16 + (threadIdx.x & 15),
+               (int)(lt / tiles_x) * 16 + (threadIdx.x >> 4));
+  }
+}
+
 }  // namespace
 
 size_t big_record_bytes() { return sizeof(BigRec); }
@@ -309,10 +354,32 @@ cudaError_t launch_gbuffer(const SceneParams& sp, const CameraParams& cp, const 
   int dev = 0, sms = 148;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  k_gb_big<<<sms * 8, kTile * kTile, 0, st>>>(rb, cp.W);
+  k_gb_big<<<sms * 8, kTile * kTile, 0, st>>>(rb, cp.W, nullptr);
   dim3 grid((cp.W + 15) / 16, (cp.H + 15) / 16);
   k_gb_resolve<<<grid, 256, 0, st>>>(sp, cp, rb);
   if (launches) *launches += (sp.total_tris ? 1 : 0) + 3;
+  return cudaGetLastError();
+}
+
+cudaError_t launch_gbuffer_batch(const BatchWork& tris, const BatchWork& tiles, size_t total_px,
+                                 const BatchBuffers& bb, int sms, cudaStream_t st, int* launches) {
+  const RasterBuffers& rb = bb.rb;
+  cudaError_t e = cudaMemsetAsync(rb.vis, 0xff, total_px * sizeof(unsigned long long), st);
+  if (e != cudaSuccess) return e;
+  e = cudaMemsetAsync(rb.big_count, 0, 2 * sizeof(uint32_t), st);
+  if (e != cudaSuccess) return e;
+  int nl = 0;
+  if (tris.total) {
+    const unsigned grid = (unsigned)std::max(1, std::min<int>(sms * 4, (int)((tris.total + 255) / 256)));
+    k_gb_setup_batch<<<grid, 256, 0, st>>>(tris, rb);
+    ++nl;
+  }
+  k_gb_big_scan<<<1, 1024, 0, st>>>(rb);
+  k_gb_big<<<sms * 8, kTile * kTile, 0, st>>>(rb, 0, tris.scenes);
+  const unsigned rgrid = (unsigned)std::max(1, std::min<int>(sms * 8, (int)tiles.total));
+  k_gb_resolve_batch<<<rgrid, 256, 0, st>>>(tiles, rb);
+  nl += 3;
+  if (launches) *launches += nl;
   return cudaGetLastError();
 }
 

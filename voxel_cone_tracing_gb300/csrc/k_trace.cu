@@ -18,6 +18,8 @@
 //                        from surface reads (the accuracy reference).
 #include <cuda_fp16.h>
 
+#include <algorithm>
+
 #include "vct_internal.h"
 #include "vct_math.cuh"
 
@@ -245,11 +247,12 @@ __device__ __forceinline__ unsigned char unorm8(float v) {
   return (unsigned char)__float2uint_rz(clamp01(v) * 255.0f + 0.5f);
 }
 
+// Shades pixel (px, py) of one frame (main, voxel_cone_tracing.frag:274-303).
 template <int SAMPLER, bool ISO, int STORAGE>
-__global__ void __launch_bounds__(256, SAMPLER == VCT_SAMPLER_HW ? kTraceMinBlocks : 1) k_trace(SceneParams sp, CameraParams cp, MapSet m, TraceParams tp,
-                                               const float4* __restrict__ gb_pos, const float4* __restrict__ gb_nrm,
-                                               uchar4* __restrict__ frame, float4* __restrict__ frame_f32) {
-  const int px = blockIdx.x * 16 + (threadIdx.x & 15), py = blockIdx.y * 16 + (threadIdx.x >> 4);
+__device__ __forceinline__ void trace_px(const SceneParams& sp, const CameraParams& cp, const MapSet& m,
+                                         const TraceParams& tp, const float4* __restrict__ gb_pos,
+                                         const float4* __restrict__ gb_nrm, uchar4* __restrict__ frame,
+                                         float4* __restrict__ frame_f32, int px, int py) {
   if (px >= cp.W || py >= cp.H) return;
   const size_t p = (size_t)py * cp.W + px;
   float4 out = f4(0.15f, 0.25f, 0.25f, 1.0f);  // glClearColor, renderer.cpp:398
@@ -308,6 +311,64 @@ __global__ void __launch_bounds__(256, SAMPLER == VCT_SAMPLER_HW ? kTraceMinBloc
 }
 
 template <int SAMPLER, bool ISO, int STORAGE>
+__global__ void __launch_bounds__(256, SAMPLER == VCT_SAMPLER_HW ? kTraceMinBlocks : 1)
+    k_trace(SceneParams sp, CameraParams cp, MapSet m, TraceParams tp, const float4* __restrict__ gb_pos,
+            const float4* __restrict__ gb_nrm, uchar4* __restrict__ frame, float4* __restrict__ frame_f32) {
+  trace_px<SAMPLER, ISO, STORAGE>(sp, cp, m, tp, gb_pos, gb_nrm, frame, frame_f32,
+                                  blockIdx.x * 16 + (threadIdx.x & 15), blockIdx.y * 16 + (threadIdx.x >> 4));
+}
+
+// The 16x16 tiles of every scene of a batch in one persistent launch.  With
+// w.queue a CTA takes its next tile from an atomic counter (uneven scenes
+// balance across SMs); without, tiles are strided by the grid.  The CTA
+// keeps its current scene's descriptor and camera in shared memory, so the
+// shading code addresses them at fixed offsets (as kernel parameters are in
+// the one-scene kernel) instead of holding pointers in registers.
+template <bool ISO>
+__global__ void __launch_bounds__(256, kTraceMinBlocks) k_trace_batch(BatchWork w, BatchBuffers bb) {
+  __shared__ uint32_t s_next;
+  __shared__ int s_cur;
+  __shared__ BatchScene s_sc;
+  __shared__ CameraParams s_cam;
+  static_assert(sizeof(BatchScene) % 4 == 0 && sizeof(CameraParams) % 4 == 0, "word copies");
+  uint32_t g = blockIdx.x;
+  if (threadIdx.x == 0) s_cur = -1;
+  if (w.queue) {
+    if (threadIdx.x == 0) s_next = atomicAdd(w.queue, 1u);
+    __syncthreads();
+    g = s_next;
+  }
+  __syncthreads();
+  while (g < w.total) {
+    const int s = batch_scene_of(w, g);
+    if (s != s_cur) {  // CTA-uniform
+      __syncthreads();  // the previous tile is done with the old scene
+      const uint32_t* src = reinterpret_cast<const uint32_t*>(w.scenes + s);
+      for (int i = threadIdx.x; i < (int)(sizeof(BatchScene) / 4); i += blockDim.x)
+        reinterpret_cast<uint32_t*>(&s_sc)[i] = __ldg(src + i);
+      const uint32_t* csrc = reinterpret_cast<const uint32_t*>(w.cams + s);
+      for (int i = threadIdx.x; i < (int)(sizeof(CameraParams) / 4); i += blockDim.x)
+        reinterpret_cast<uint32_t*>(&s_cam)[i] = __ldg(csrc + i);
+      __syncthreads();
+      if (threadIdx.x == 0) s_cur = s;
+    }
+    const uint32_t lt = g - __ldg(w.prefix + s), tiles_x = (uint32_t)(s_sc.W + 15) / 16;
+    trace_px<VCT_SAMPLER_HW, ISO, VCT_STORAGE_RGBA8>(
+        s_sc.sp, s_cam, s_sc.ms, s_sc.tp, bb.rb.gb_pos + s_sc.px_base, bb.rb.gb_nrm + s_sc.px_base,
+        bb.frame + s_sc.px_base, nullptr, (int)(lt % tiles_x) * 16 + (threadIdx.x & 15),
+        (int)(lt / tiles_x) * 16 + (threadIdx.x >> 4));
+    if (w.queue) {
+      __syncthreads();  // every thread has read s_next
+      if (threadIdx.x == 0) s_next = atomicAdd(w.queue, 1u);
+      __syncthreads();
+      g = s_next;
+    } else {
+      g += gridDim.x;
+    }
+  }
+}
+
+template <int SAMPLER, bool ISO, int STORAGE>
 cudaError_t run(const SceneParams& sp, const CameraParams& cp, const MapSet& ms, const TraceParams& tp,
                 const float4* gb_pos, const float4* gb_nrm, uchar4* frame, float4* frame_f32, cudaStream_t st) {
   dim3 grid((cp.W + 15) / 16, (cp.H + 15) / 16);
@@ -338,6 +399,22 @@ cudaError_t launch_trace_points(const SceneParams&, const MapSet& ms, int mip_mo
   const unsigned grid = (unsigned)((n + 255) / 256);
   if (mip_mode == VCT_MIP_ISO) k_trace_points<true><<<grid, 256, 0, st>>>(ms, cone_set, samples, n);
   else k_trace_points<false><<<grid, 256, 0, st>>>(ms, cone_set, samples, n);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_trace_batch(const BatchWork& tiles, const BatchBuffers& bb, const BatchShape& shape, int sms,
+                               cudaStream_t st, int* launches) {
+  if (!tiles.total) return cudaSuccess;
+  BatchWork w = tiles;
+  if (!shape.trace_dynamic) w.queue = nullptr;
+  else {
+    cudaError_t e = cudaMemsetAsync(w.queue, 0, sizeof(uint32_t), st);
+    if (e != cudaSuccess) return e;
+  }
+  const int per_sm = std::min(std::max(shape.trace_ctas_per_sm, 1), kTraceMinBlocks);
+  const unsigned grid = (unsigned)std::max(1, std::min<int>(sms * per_sm, (int)tiles.total));
+  k_trace_batch<false><<<grid, 256, 0, st>>>(w, bb);
+  if (launches) ++*launches;
   return cudaGetLastError();
 }
 

@@ -26,6 +26,7 @@
 //     the triangle point closest to the voxel centre.
 #include <cuda_fp16.h>
 
+#include <algorithm>
 #include <climits>
 #include <type_traits>
 
@@ -152,12 +153,13 @@ constexpr int kBigSplit = 8;     // CTAs that share one large triangle
 // counting pass in `big` and binned by k_bin_big, which spreads each record
 // over several CTAs; without a record list (or when it is full) the warp
 // bins it, the lanes splitting the candidate range.
+// All 32 lanes of a warp call it together (each with its own triangle t of
+// the same scene; t >= total_tris is an idle lane).
 template <bool FILL>
-__global__ void __launch_bounds__(256) k_bin(SceneParams sp, int N, uint32_t* __restrict__ count,
-                                             uint32_t* __restrict__ cursor, uint32_t* __restrict__ list,
-                                             uint32_t cap, FrameStatus* st, BinRec* __restrict__ big,
-                                             uint32_t big_cap, uint32_t* __restrict__ big_count) {
-  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void bin_tri(const SceneParams& sp, int N, uint32_t t, uint32_t* __restrict__ count,
+                                        uint32_t* __restrict__ cursor, uint32_t* __restrict__ list, uint32_t cap,
+                                        FrameStatus* st, BinRec* __restrict__ big, uint32_t big_cap,
+                                        uint32_t* __restrict__ big_count, uint32_t scene) {
   const int lane = threadIdx.x & 31;
   const int nb = N / kBrick;
   float v[3][3] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};
@@ -206,6 +208,8 @@ __global__ void __launch_bounds__(256) k_bin(SceneParams sp, int N, uint32_t* __
         for (int d = 0; d < 3; ++d) { r.blo[d] = blo[d]; r.bhi[d] = bhi[d]; }
         r.t = t;
         r.vol = (uint32_t)vol;
+        r.scene = scene;
+        r.pad = 0;
         big[slot] = r;
       }
     }
@@ -228,24 +232,55 @@ __global__ void __launch_bounds__(256) k_bin(SceneParams sp, int N, uint32_t* __
   }
 }
 
+template <bool FILL>
+__global__ void __launch_bounds__(256) k_bin(SceneParams sp, int N, uint32_t* __restrict__ count,
+                                             uint32_t* __restrict__ cursor, uint32_t* __restrict__ list,
+                                             uint32_t cap, FrameStatus* st, BinRec* __restrict__ big,
+                                             uint32_t big_cap, uint32_t* __restrict__ big_count) {
+  bin_tri<FILL>(sp, N, blockIdx.x * blockDim.x + threadIdx.x, count, cursor, list, cap, st, big, big_cap, big_count,
+                0u);
+}
+
+// Every scene's triangles in one persistent launch; scene triangle ranges
+// are padded to multiples of 32, so a warp bins one scene.
+template <bool FILL>
+__global__ void __launch_bounds__(256) k_bin_batch(BatchWork w, BatchBuffers bb) {
+  for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < w.total; g += gridDim.x * blockDim.x) {
+    const int s = batch_scene_of(w, g);
+    const BatchScene& S = w.scenes[s];
+    bin_tri<FILL>(S.sp, S.N, g - __ldg(w.prefix + s), FILL ? nullptr : bb.brick_count + S.brick_base,
+                  FILL ? bb.brick_cursor + S.brick_base : nullptr, bb.pair_list, bb.pair_cap, bb.status, bb.big,
+                  bb.big_cap, bb.big_count, (uint32_t)s);
+  }
+}
+
 // Large-triangle records: CTA (x, y) takes records x, x + gridDim.x, ... and
-// the candidate bricks y*256 + tid, stepping by kBigSplit*256.
+// the candidate bricks y*256 + tid, stepping by kBigSplit*256.  With
+// `scenes` (a batch) each record bins into its own scene's brick slice.
 template <bool FILL>
 __global__ void __launch_bounds__(256) k_bin_big(int N, const BinRec* __restrict__ big, uint32_t big_cap,
                                                  const uint32_t* __restrict__ big_count, uint32_t* __restrict__ count,
                                                  uint32_t* __restrict__ cursor, uint32_t* __restrict__ list,
-                                                 uint32_t cap) {
+                                                 uint32_t cap, const BatchScene* __restrict__ scenes) {
   const uint32_t n = min(*big_count, big_cap);
-  const int nb = N / kBrick;
   for (uint32_t r = blockIdx.x; r < n; r += gridDim.x) {
     const BinRec& rec = big[r];
+    int nb = N / kBrick;
+    uint32_t* cnt = count;
+    uint32_t* cur = cursor;
+    if (scenes) {
+      const BatchScene& S = scenes[rec.scene];
+      nb = S.N / kBrick;
+      if (cnt) cnt += S.brick_base;
+      if (cur) cur += S.brick_base;
+    }
     float v[3][3];
     for (int k = 0; k < 3; ++k)
       for (int d = 0; d < 3; ++d) v[k][d] = rec.v[k][d];
     const int nx = rec.bhi[0] - rec.blo[0] + 1, ny = rec.bhi[1] - rec.blo[1] + 1;
     for (uint32_t i = blockIdx.y * blockDim.x + threadIdx.x; i < rec.vol; i += gridDim.y * blockDim.x)
       bin_one<FILL>(v, rec.blo[0] + (int)(i % nx), rec.blo[1] + (int)((i / nx) % ny), rec.blo[2] + (int)(i / (nx * ny)),
-                    nb, true, rec.t, count, cursor, list, cap);
+                    nb, true, rec.t, cnt, cur, list, cap);
   }
 }
 
@@ -544,17 +579,18 @@ __device__ __forceinline__ void item_sat(const SceneParams& sp, int N, const int
 }
 
 // ------------------------------------------------------------ brick CTA ----
+template <int MODE>
+using SetupOf = typename std::conditional<MODE == VCT_VOX_CONSERVATIVE, SetupSat, SetupRef>::type;
+
+// One brick, all threads of the CTA (the shared-memory arrays come from the
+// caller, so that a persistent CTA reuses them brick after brick).
 template <int MODE, int STORAGE>
-__global__ void __launch_bounds__(kThreads) k_bricks(SceneParams sp, int N, const uint32_t* __restrict__ offset,
-                                                     const uint32_t* __restrict__ list, uint32_t cap,
-                                                     cudaSurfaceObject_t l0, uint32_t* __restrict__ counts,
-                                                     FrameStatus* st) {
-  typedef typename std::conditional<MODE == VCT_VOX_CONSERVATIVE, SetupSat, SetupRef>::type Setup;
-  __shared__ AccT<STORAGE> acc;
-  __shared__ Setup setup[kWarps][32];
-  __shared__ int excl[kWarps][33];
+__device__ __forceinline__ void brick_body(const SceneParams& sp, int N, uint32_t brick,
+                                           const uint32_t* __restrict__ offset, const uint32_t* __restrict__ list,
+                                           uint32_t cap, cudaSurfaceObject_t l0, uint32_t* __restrict__ counts,
+                                           FrameStatus* st, AccT<STORAGE>& acc, SetupOf<MODE> (&setup)[kWarps][32],
+                                           int (&excl)[kWarps][33]) {
   const int nb = N / kBrick;
-  const uint32_t brick = blockIdx.x;
   const int b3[3] = {(int)(brick % nb), (int)((brick / nb) % nb), (int)(brick / ((uint32_t)nb * nb))};
   const uint32_t beg = min(offset[brick], cap), end = min(offset[brick + 1], cap);
   if (beg == end) {
@@ -633,6 +669,32 @@ __global__ void __launch_bounds__(kThreads) k_bricks(SceneParams sp, int N, cons
       surf3Dwrite(o, l0, x * 8, y, z);
     }
     if (counts) counts[((size_t)z * N + y) * N + x] = n;
+  }
+}
+
+template <int MODE, int STORAGE>
+__global__ void __launch_bounds__(kThreads) k_bricks(SceneParams sp, int N, const uint32_t* __restrict__ offset,
+                                                     const uint32_t* __restrict__ list, uint32_t cap,
+                                                     cudaSurfaceObject_t l0, uint32_t* __restrict__ counts,
+                                                     FrameStatus* st) {
+  __shared__ AccT<STORAGE> acc;
+  __shared__ SetupOf<MODE> setup[kWarps][32];
+  __shared__ int excl[kWarps][33];
+  brick_body<MODE, STORAGE>(sp, N, blockIdx.x, offset, list, cap, l0, counts, st, acc, setup, excl);
+}
+
+// Every scene's bricks in one persistent launch.
+template <int MODE, int STORAGE>
+__global__ void __launch_bounds__(kThreads) k_bricks_batch(BatchWork w, BatchBuffers bb) {
+  __shared__ AccT<STORAGE> acc;
+  __shared__ SetupOf<MODE> setup[kWarps][32];
+  __shared__ int excl[kWarps][33];
+  for (uint32_t g = blockIdx.x; g < w.total; g += gridDim.x) {
+    const int s = batch_scene_of(w, g);
+    const BatchScene& S = w.scenes[s];
+    brick_body<MODE, STORAGE>(S.sp, S.N, g - __ldg(w.prefix + s), bb.brick_offset + S.brick_base, bb.pair_list,
+                              bb.pair_cap, S.ms.l0_surf, nullptr, bb.status, acc, setup, excl);
+    __syncthreads();  // the next brick clears the accumulators
   }
 }
 
@@ -750,7 +812,7 @@ cudaError_t launch_voxelize(const SceneParams& sp, int N, int mode, int storage,
     ++nl;
     if (vb.big) {
       k_bin_big<false><<<big_grid, 256, 0, st>>>(N, vb.big, vb.big_cap, vb.big_count, vb.brick_count, nullptr, nullptr,
-                                                 0);
+                                                 0, nullptr);
       ++nl;
     }
   }
@@ -770,7 +832,7 @@ cudaError_t launch_voxelize(const SceneParams& sp, int N, int mode, int storage,
     ++nl;
     if (vb.big) {
       k_bin_big<true><<<big_grid, 256, 0, st>>>(N, vb.big, vb.big_cap, vb.big_count, nullptr, vb.brick_cursor,
-                                                vb.pair_list, vb.pair_cap);
+                                                vb.pair_list, vb.pair_cap, nullptr);
       ++nl;
     }
   }
@@ -791,6 +853,60 @@ cudaError_t launch_voxelize(const SceneParams& sp, int N, int mode, int storage,
       k_bricks<VCT_VOX_REF_RASTER2X, VCT_STORAGE_RGBA16F><<<grid, kThreads, 0, st>>>(
           sp, N, vb.brick_offset, vb.pair_list, vb.pair_cap, l0, vb.counts, vb.status);
   }
+  if (launches) *launches += nl;
+  return cudaGetLastError();
+}
+
+}  // namespace vct
+
+namespace vct {
+
+// Batched voxelizer: the same passes as launch_voxelize, each one launch
+// over every scene of the batch (brick arrays concatenated, one scan).
+cudaError_t launch_voxelize_batch(const BatchWork& tris, const BatchWork& bricks, uint32_t total_bricks, int mode,
+                                  int storage, const BatchBuffers& bb, uint32_t* scan_tmp, const BatchShape& shape,
+                                  int sms, cudaStream_t st, int* launches) {
+  int nl = 0;
+  cudaError_t e = cudaMemsetAsync(bb.brick_count, 0, (size_t)total_bricks * sizeof(uint32_t), st);
+  if (e != cudaSuccess) return e;
+  e = cudaMemsetAsync(bb.big_count, 0, sizeof(uint32_t), st);
+  if (e != cudaSuccess) return e;
+  const unsigned bin_grid =
+      (unsigned)std::max(1, std::min<int>(sms * std::max(shape.bin_ctas_per_sm, 1), (int)((tris.total + 255) / 256)));
+  const dim3 big_grid(128, kBigSplit);
+  if (tris.total) {
+    k_bin_batch<false><<<bin_grid, 256, 0, st>>>(tris, bb);
+    k_bin_big<false><<<big_grid, 256, 0, st>>>(0, bb.big, bb.big_cap, bb.big_count, bb.brick_count, nullptr, nullptr,
+                                               0, tris.scenes);
+    nl += 2;
+  }
+  e = launch_exclusive_scan(bb.brick_count, bb.brick_offset, bb.brick_cursor, total_bricks, scan_tmp, st, &nl);
+  if (e != cudaSuccess) return e;
+  e = cudaMemcpyAsync(&bb.status->pair_total, bb.brick_offset + total_bricks, sizeof(uint32_t),
+                      cudaMemcpyDeviceToDevice, st);
+  if (e != cudaSuccess) return e;
+  e = cudaMemcpyAsync(&bb.status->bigtri_total, bb.big_count, sizeof(uint32_t), cudaMemcpyDeviceToDevice, st);
+  if (e != cudaSuccess) return e;
+  if (tris.total) {
+    k_bin_batch<true><<<bin_grid, 256, 0, st>>>(tris, bb);
+    k_bin_big<true><<<big_grid, 256, 0, st>>>(0, bb.big, bb.big_cap, bb.big_count, nullptr, bb.brick_cursor,
+                                              bb.pair_list, bb.pair_cap, tris.scenes);
+    nl += 2;
+  }
+  const unsigned grid =
+      (unsigned)std::max(1, std::min<int>(sms * std::max(shape.bricks_ctas_per_sm, 1), (int)bricks.total));
+  if (mode == VCT_VOX_CONSERVATIVE) {
+    if (storage == VCT_STORAGE_RGBA8)
+      k_bricks_batch<VCT_VOX_CONSERVATIVE, VCT_STORAGE_RGBA8><<<grid, kThreads, 0, st>>>(bricks, bb);
+    else
+      k_bricks_batch<VCT_VOX_CONSERVATIVE, VCT_STORAGE_RGBA16F><<<grid, kThreads, 0, st>>>(bricks, bb);
+  } else {
+    if (storage == VCT_STORAGE_RGBA8)
+      k_bricks_batch<VCT_VOX_REF_RASTER2X, VCT_STORAGE_RGBA8><<<grid, kThreads, 0, st>>>(bricks, bb);
+    else
+      k_bricks_batch<VCT_VOX_REF_RASTER2X, VCT_STORAGE_RGBA16F><<<grid, kThreads, 0, st>>>(bricks, bb);
+  }
+  ++nl;
   if (launches) *launches += nl;
   return cudaGetLastError();
 }

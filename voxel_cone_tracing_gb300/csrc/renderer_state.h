@@ -130,6 +130,84 @@ struct MlpState {
   }
 };
 
+// The voxel maps of one grid: level 0 once (surface + texture) and one
+// mipmapped chain of levels 1..L-1 per map (surfaces per level + one
+// texture), as set_grid_resolution allocates them (renderer.cpp:178-188).
+struct MapStore {
+  cudaArray_t l0_arr = nullptr;
+  cudaMipmappedArray_t dir_arr[kMaxMaps] = {};
+  MapSet ms = {};
+
+  MapStore() = default;
+  MapStore(const MapStore&) = delete;
+  MapStore& operator=(const MapStore&) = delete;
+  ~MapStore() { release(); }
+
+  void release() {
+    if (ms.l0_tex) cudaDestroyTextureObject(ms.l0_tex);
+    if (ms.l0_surf) cudaDestroySurfaceObject(ms.l0_surf);
+    for (int d = 0; d < kMaxMaps; ++d) {
+      if (ms.tex[d]) cudaDestroyTextureObject(ms.tex[d]);
+      for (int l = 0; l < kMaxLevels; ++l)
+        if (ms.surf[d][l]) cudaDestroySurfaceObject(ms.surf[d][l]);
+      if (dir_arr[d]) cudaFreeMipmappedArray(dir_arr[d]);
+      dir_arr[d] = nullptr;
+    }
+    if (l0_arr) cudaFreeArray(l0_arr);
+    l0_arr = nullptr;
+    std::memset(&ms, 0, sizeof(ms));
+  }
+
+  vct_status alloc(uint32_t r, int mip_mode, int storage) {
+    release();
+    const int L = std::min(kMaxLevels, ilog2(r) + 1);
+    const int nmaps = mip_mode == VCT_MIP_ISO ? 1 : 6;
+    const cudaChannelFormatDesc desc = storage == VCT_STORAGE_RGBA16F
+                                           ? cudaCreateChannelDesc(16, 16, 16, 16, cudaChannelFormatKindFloat)
+                                           : cudaCreateChannelDesc(8, 8, 8, 8, cudaChannelFormatKindUnsigned);
+    VCT_CUDA(cudaMalloc3DArray(&l0_arr, &desc, make_cudaExtent(r, r, r), cudaArraySurfaceLoadStore));
+    cudaResourceDesc rd;
+    std::memset(&rd, 0, sizeof(rd));
+    rd.resType = cudaResourceTypeArray;
+    rd.res.array.array = l0_arr;
+    VCT_CUDA(cudaCreateSurfaceObject(&ms.l0_surf, &rd));
+    cudaTextureDesc td;
+    std::memset(&td, 0, sizeof(td));
+    td.addressMode[0] = td.addressMode[1] = td.addressMode[2] = cudaAddressModeBorder;
+    td.filterMode = cudaFilterModeLinear;
+    td.readMode = storage == VCT_STORAGE_RGBA16F ? cudaReadModeElementType : cudaReadModeNormalizedFloat;
+    td.normalizedCoords = 1;
+    td.mipmapFilterMode = cudaFilterModeLinear;
+    VCT_CUDA(cudaCreateTextureObject(&ms.l0_tex, &rd, &td, nullptr));
+    for (int d = 0; d < nmaps && L > 1; ++d) {
+      VCT_CUDA(cudaMallocMipmappedArray(&dir_arr[d], &desc, make_cudaExtent(r / 2, r / 2, r / 2), L - 1,
+                                        cudaArraySurfaceLoadStore));
+      for (int l = 1; l < L; ++l) {
+        cudaArray_t la;
+        VCT_CUDA(cudaGetMipmappedArrayLevel(&la, dir_arr[d], l - 1));
+        cudaResourceDesc lr;
+        std::memset(&lr, 0, sizeof(lr));
+        lr.resType = cudaResourceTypeArray;
+        lr.res.array.array = la;
+        VCT_CUDA(cudaCreateSurfaceObject(&ms.surf[d][l], &lr));
+      }
+      cudaResourceDesc mr;
+      std::memset(&mr, 0, sizeof(mr));
+      mr.resType = cudaResourceTypeMipmappedArray;
+      mr.res.mipmap.mipmap = dir_arr[d];
+      cudaTextureDesc mt = td;
+      mt.minMipmapLevelClamp = 0.0f;
+      mt.maxMipmapLevelClamp = (float)(L - 2);
+      VCT_CUDA(cudaCreateTextureObject(&ms.tex[d], &mr, &mt, nullptr));
+    }
+    ms.N = (int)r;
+    ms.L = L;
+    ms.nmaps = nmaps;
+    ms.storage = storage;
+    return VCT_OK;
+  }
+};
+
 struct vct_renderer {
   int W = 0, H = 0;
   vct_config cfg;
@@ -157,9 +235,8 @@ struct vct_renderer {
   cudaEvent_t ev[5] = {};
   cudaEvent_t ev_staged = nullptr;
   cudaEvent_t ev_done = nullptr;   // after the frame's status copy
-  cudaArray_t l0_arr = nullptr;
-  cudaMipmappedArray_t dir_arr[kMaxMaps] = {};
-  MapSet ms = {};
+  MapStore maps;
+  MapSet& ms = maps.ms;
   DevBuf<vct_material_data> d_materials;
   DevBuf<uint32_t> d_obj_material;
   DevBuf<DevInstance> d_inst;
@@ -197,73 +274,14 @@ struct vct_renderer {
     if (own_stream) cudaStreamDestroy(own_stream);
   }
 
-  void free_maps() {
-    if (ms.l0_tex) cudaDestroyTextureObject(ms.l0_tex);
-    if (ms.l0_surf) cudaDestroySurfaceObject(ms.l0_surf);
-    for (int d = 0; d < kMaxMaps; ++d) {
-      if (ms.tex[d]) cudaDestroyTextureObject(ms.tex[d]);
-      for (int l = 0; l < kMaxLevels; ++l)
-        if (ms.surf[d][l]) cudaDestroySurfaceObject(ms.surf[d][l]);
-      if (dir_arr[d]) cudaFreeMipmappedArray(dir_arr[d]);
-      dir_arr[d] = nullptr;
-    }
-    if (l0_arr) cudaFreeArray(l0_arr);
-    l0_arr = nullptr;
-    std::memset(&ms, 0, sizeof(ms));
-  }
-
-  cudaChannelFormatDesc texel_desc() const {
-    return cfg.storage == VCT_STORAGE_RGBA16F ? cudaCreateChannelDesc(16, 16, 16, 16, cudaChannelFormatKindFloat)
-                                              : cudaCreateChannelDesc(8, 8, 8, 8, cudaChannelFormatKindUnsigned);
-  }
+  void free_maps() { maps.release(); }
 
   // set_grid_resolution (renderer.cpp:178-188): six 3D textures of `levels`
   // mip levels.  Here: level 0 once + one chain (levels 1..L-1) per map.
   vct_status alloc_maps(uint32_t r) {
     if (stream) VCT_CUDA(cudaStreamSynchronize(stream));
-    free_maps();
-    const int L = std::min(kMaxLevels, ilog2(r) + 1);
-    const int nmaps = cfg.mip_mode == VCT_MIP_ISO ? 1 : 6;
-    const cudaChannelFormatDesc desc = texel_desc();
-    VCT_CUDA(cudaMalloc3DArray(&l0_arr, &desc, make_cudaExtent(r, r, r), cudaArraySurfaceLoadStore));
-    cudaResourceDesc rd;
-    std::memset(&rd, 0, sizeof(rd));
-    rd.resType = cudaResourceTypeArray;
-    rd.res.array.array = l0_arr;
-    VCT_CUDA(cudaCreateSurfaceObject(&ms.l0_surf, &rd));
-    cudaTextureDesc td;
-    std::memset(&td, 0, sizeof(td));
-    td.addressMode[0] = td.addressMode[1] = td.addressMode[2] = cudaAddressModeBorder;
-    td.filterMode = cudaFilterModeLinear;
-    td.readMode = cfg.storage == VCT_STORAGE_RGBA16F ? cudaReadModeElementType : cudaReadModeNormalizedFloat;
-    td.normalizedCoords = 1;
-    td.mipmapFilterMode = cudaFilterModeLinear;
-    VCT_CUDA(cudaCreateTextureObject(&ms.l0_tex, &rd, &td, nullptr));
-    for (int d = 0; d < nmaps && L > 1; ++d) {
-      VCT_CUDA(cudaMallocMipmappedArray(&dir_arr[d], &desc, make_cudaExtent(r / 2, r / 2, r / 2), L - 1,
-                                        cudaArraySurfaceLoadStore));
-      for (int l = 1; l < L; ++l) {
-        cudaArray_t la;
-        VCT_CUDA(cudaGetMipmappedArrayLevel(&la, dir_arr[d], l - 1));
-        cudaResourceDesc lr;
-        std::memset(&lr, 0, sizeof(lr));
-        lr.resType = cudaResourceTypeArray;
-        lr.res.array.array = la;
-        VCT_CUDA(cudaCreateSurfaceObject(&ms.surf[d][l], &lr));
-      }
-      cudaResourceDesc mr;
-      std::memset(&mr, 0, sizeof(mr));
-      mr.resType = cudaResourceTypeMipmappedArray;
-      mr.res.mipmap.mipmap = dir_arr[d];
-      cudaTextureDesc mt = td;
-      mt.minMipmapLevelClamp = 0.0f;
-      mt.maxMipmapLevelClamp = (float)(L - 2);
-      VCT_CUDA(cudaCreateTextureObject(&ms.tex[d], &mr, &mt, nullptr));
-    }
-    ms.N = (int)r;
-    ms.L = L;
-    ms.nmaps = nmaps;
-    ms.storage = cfg.storage;
+    VCT_CHECK(maps.alloc(r, cfg.mip_mode, cfg.storage));
+    const int L = ms.L;
     res = r;
     levels = L;
     const size_t nb = (size_t)(r / kBrick) * (r / kBrick) * (r / kBrick);

@@ -58,6 +58,8 @@ struct BinRec {
   float v[3][3];    // vertices in voxel units
   int blo[3], bhi[3];
   uint32_t t, vol;  // frame triangle id, candidate bricks
+  uint32_t scene;   // scene of a batch (0 for one renderer)
+  uint32_t pad;
 };
 
 // The voxel maps of a renderer: level 0 once, plus one chain per map.
@@ -112,6 +114,65 @@ struct TraceParams {
   const float4* diffuse_in;
 };
 
+// ---- batched rendering (api_batch.cu) --------------------------------------
+// One scene of a batch, device-resident.  Scenes own their voxel maps; the
+// per-frame work arrays are batch-wide, each scene using the slice that
+// starts at its base index.
+struct BatchScene {
+  SceneParams sp;
+  MapSet ms;
+  TraceParams tp;
+  int N;
+  int W, H;
+  uint32_t brick_base;  // first brick in the batch-wide brick arrays
+  uint32_t pad;
+  size_t px_base;       // first pixel in the batch-wide vis / G-buffer / frame arrays
+};
+
+// Work of one batched launch: the scene of global work item g is the s with
+// prefix[s] <= g < prefix[s + 1] (per-scene ranges padded so that a warp,
+// or a CTA, never straddles two scenes).
+struct BatchWork {
+  const BatchScene* scenes;
+  const CameraParams* cams;  // per scene (updated per frame)
+  int n;
+  const uint32_t* prefix;    // n + 1 entries
+  uint32_t total;            // prefix[n]
+  uint32_t* queue;           // dynamic scheduling counter (or null: static stride)
+};
+
+__device__ __forceinline__ int batch_scene_of(const BatchWork& w, uint32_t g) {
+  int lo = 0, hi = w.n - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (__ldg(w.prefix + mid) <= g) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+// Batch-wide work arrays.
+struct BatchBuffers {
+  uint32_t* brick_count;
+  uint32_t* brick_offset;
+  uint32_t* brick_cursor;
+  uint32_t* pair_list;
+  uint32_t pair_cap;
+  BinRec* big;
+  uint32_t big_cap;
+  uint32_t* big_count;
+  FrameStatus* status;
+  RasterBuffers rb;       // vis / gb_pos / gb_nrm point at pixel 0 of the batch
+  uchar4* frame;
+};
+
+// Tunable launch shapes of the batched kernels (chosen by the autotuner).
+struct BatchShape {
+  int bin_ctas_per_sm;
+  int bricks_ctas_per_sm;
+  int trace_ctas_per_sm;
+  int trace_dynamic;   // 1: tiles from an atomic queue; 0: static stride
+};
+
 // ---- learned diffuse term (k_mlp.cu) --------------------------------------
 constexpr int kMlpLevels = 16;
 constexpr int kMlpWeights = 5 * 64 * 64;  // W1..W4 64x64, W5 16x64 (padded to 64 rows)
@@ -161,6 +222,17 @@ cudaError_t launch_box_mip_rgba8(cudaSurfaceObject_t src, int sw, int sh, int sd
                                  int dh, int dd, cudaStream_t st);
 
 size_t big_record_bytes();
+
+// Batched stages (one launch per pass over all scenes of a batch).
+cudaError_t launch_voxelize_batch(const BatchWork& tris, const BatchWork& bricks, uint32_t total_bricks, int mode,
+                                  int storage, const BatchBuffers& bb, uint32_t* scan_tmp, const BatchShape& shape,
+                                  int sms, cudaStream_t st, int* launches);
+cudaError_t launch_mipmap_batch(const BatchWork& regions, const BatchWork* tail, int n_tail, int storage,
+                                cudaStream_t st, int* launches);
+cudaError_t launch_gbuffer_batch(const BatchWork& tris, const BatchWork& tiles, size_t total_px,
+                                 const BatchBuffers& bb, int sms, cudaStream_t st, int* launches);
+cudaError_t launch_trace_batch(const BatchWork& tiles, const BatchBuffers& bb, const BatchShape& shape, int sms,
+                               cudaStream_t st, int* launches);
 
 // Learned diffuse term.
 cudaError_t launch_mlp_init(float* prm, __nv_bfloat16* prm_bf, size_t n, float scale, uint64_t seed, cudaStream_t st);

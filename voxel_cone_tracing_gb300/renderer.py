@@ -39,7 +39,10 @@ EXPORTS = [
     "vct_activate_tex_3d", "vct_clear_tex_3d", "vct_mip_tex_3d", "vct_tex3d_upload", "vct_tex3d_download",
     "vct_mlp_desc_default", "vct_mlp_init", "vct_mlp_train", "vct_set_diffuse_mode", "vct_mlp_save",
     "vct_mlp_load", "vct_mlp_get_params", "vct_mlp_set_params", "vct_mlp_eval", "vct_mlp_gradients",
-    "vct_mlp_train_samples", "vct_voxelize_noalloc",
+    "vct_mlp_train_samples", "vct_voxelize_noalloc", "vct_batch_create", "vct_batch_destroy",
+    "vct_batch_set_camera", "vct_batch_render", "vct_batch_synchronize", "vct_batch_set_stream",
+    "vct_batch_read_frame", "vct_batch_read_voxels", "vct_batch_stage_times", "vct_batch_get_shape",
+    "vct_batch_set_shape", "vct_batch_autotune",
 ]
 DIFFUSE_CONES, DIFFUSE_MLP = 0, 1
 MLP_WEIGHTS = 5 * 64 * 64
@@ -125,6 +128,12 @@ def lib() -> C.CDLL:
             "vct_mlp_set_params": (I32, [P, P, P]), "vct_mlp_eval": (I32, [P, P, U32, P]),
             "vct_mlp_gradients": (I32, [P, P, U32, P, P, P]), "vct_mlp_train_samples": (I32, [P, P, U32, P, P]),
             "vct_voxelize_noalloc": (I32, [P, U32, P, U32, P, U32, F, I32, I32, P, P]),
+            "vct_batch_create": (I32, [P, U32, P, P]), "vct_batch_destroy": (None, [P]),
+            "vct_batch_set_camera": (I32, [P, U32, P, P]), "vct_batch_render": (I32, [P]),
+            "vct_batch_synchronize": (I32, [P]), "vct_batch_set_stream": (I32, [P, P]),
+            "vct_batch_read_frame": (I32, [P, U32, P]), "vct_batch_read_voxels": (I32, [P, U32, I32, I32, P]),
+            "vct_batch_stage_times": (I32, [P, P]), "vct_batch_get_shape": (I32, [P, P]),
+            "vct_batch_set_shape": (I32, [P, P]), "vct_batch_autotune": (I32, [P, I32, P, P, P]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
@@ -438,3 +447,123 @@ def queue_scene(r: Renderer, scene: "scenes.Scene", ids) -> None:
         r.queue_model(mid)
     for l in scene.lights:
         r.queue_point_light(l)
+
+
+# ---------------------------------------------------------------- batches --
+class BatchMesh(C.Structure):
+    _fields_ = [("verts", C.c_void_p), ("n_verts", C.c_uint32), ("indices", C.c_void_p), ("n_tris", C.c_uint32),
+                ("tri_material", C.c_void_p), ("model", C.c_float * 16)]
+
+
+class BatchScene(C.Structure):
+    _fields_ = [("width", C.c_int32), ("height", C.c_int32), ("grid_res", C.c_int32), ("cone_set", C.c_int32),
+                ("cube_size", C.c_float), ("meshes", C.c_void_p), ("n_meshes", C.c_uint32),
+                ("materials", C.c_void_p), ("n_materials", C.c_uint32), ("lights", C.c_void_p),
+                ("n_lights", C.c_uint32), ("view", C.c_float * 16), ("proj", C.c_float * 16)]
+
+
+class BatchConfig(C.Structure):
+    _fields_ = [("vox_mode", C.c_int32), ("use_graph", C.c_int32), ("reserved", C.c_int32 * 6)]
+
+
+class BatchShape(C.Structure):
+    _fields_ = [("bin_ctas_per_sm", C.c_int32), ("bricks_ctas_per_sm", C.c_int32),
+                ("trace_ctas_per_sm", C.c_int32), ("trace_dynamic", C.c_int32)]
+
+
+class Batch:
+    """Many independent scenes rendered per frame (vct_batch_*): each entry
+    of ``items`` is (scene, width, height, grid_res, cone_set); geometry,
+    materials, lights, camera and cube size come from the scene."""
+
+    def __init__(self, items, vox_mode: int = VOX_REF_RASTER2X, use_graph: bool = False):
+        keep = []
+        descs = (BatchScene * len(items))()
+        self.sizes = []
+        for d, (scene, w, h, grid, cones) in zip(descs, items):
+            meshes = (BatchMesh * max(len(scene.meshes), 1))()
+            for m, (mesh, model) in zip(meshes, zip(scene.meshes, scene.models)):
+                v = np.ascontiguousarray(mesh.verts, np.float32)
+                ix = np.ascontiguousarray(mesh.indices, np.uint32)
+                tm = np.ascontiguousarray(mesh.tri_material(), np.uint32)
+                keep += [v, ix, tm]
+                m.verts, m.n_verts = v.ctypes.data, v.shape[0]
+                m.indices, m.n_tris, m.tri_material = ix.ctypes.data, ix.shape[0], tm.ctypes.data
+                m.model[:] = [float(x) for x in np.asarray(model, np.float32).reshape(-1)]
+            mats = np.ascontiguousarray(scene.materials)
+            lights = np.ascontiguousarray(scene.lights)
+            keep += [meshes, mats, lights]
+            d.width, d.height, d.grid_res, d.cone_set = int(w), int(h), int(grid), int(cones)
+            d.cube_size = float(scene.cube_size)
+            d.meshes, d.n_meshes = C.addressof(meshes), len(scene.meshes)
+            d.materials, d.n_materials = mats.ctypes.data, mats.shape[0]
+            d.lights, d.n_lights = (lights.ctypes.data if lights.shape[0] else None), lights.shape[0]
+            d.view[:] = [float(x) for x in np.asarray(scene.view, np.float32).reshape(-1)]
+            d.proj[:] = [float(x) for x in np.asarray(scene.proj, np.float32).reshape(-1)]
+            self.sizes.append((int(w), int(h), int(grid)))
+        cfg = BatchConfig()
+        cfg.vox_mode, cfg.use_graph = int(vox_mode), int(bool(use_graph))
+        self._b = C.c_void_p()
+        _check(lib().vct_batch_create(descs, len(items), C.byref(cfg), C.byref(self._b)))
+
+    def close(self) -> None:
+        if getattr(self, "_b", None):
+            lib().vct_batch_destroy(self._b)
+            self._b = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def render(self) -> None:
+        _check(lib().vct_batch_render(self._b))
+
+    def synchronize(self) -> None:
+        _check(lib().vct_batch_synchronize(self._b))
+
+    def set_stream(self, stream_handle) -> None:
+        _check(lib().vct_batch_set_stream(self._b, C.c_void_p(stream_handle or 0)))
+
+    def set_camera(self, scene: int, view, proj) -> None:
+        v, p = _f16(view), _f16(proj)
+        _check(lib().vct_batch_set_camera(self._b, int(scene), v, p))
+
+    def read_frame(self, scene: int) -> np.ndarray:
+        w, h, _ = self.sizes[scene]
+        out = np.empty((h, w, 4), np.uint8)
+        _check(lib().vct_batch_read_frame(self._b, int(scene), out.ctypes.data))
+        return out
+
+    def read_voxels(self, scene: int, level: int, map_index: int = 0) -> np.ndarray:
+        s = self.sizes[scene][2] >> level
+        out = np.empty((s, s, s, 4), np.uint8)
+        _check(lib().vct_batch_read_voxels(self._b, int(scene), int(level), int(map_index), out.ctypes.data))
+        return out
+
+    def stage_times(self) -> dict:
+        t = StageTimes()
+        _check(lib().vct_batch_stage_times(self._b, C.byref(t)))
+        d = {k: float(getattr(t, k)) for k, _ in StageTimes._fields_}
+        d["kernel_launches"] = int(t.kernel_launches)
+        return d
+
+    @property
+    def shape(self) -> dict:
+        s = BatchShape()
+        _check(lib().vct_batch_get_shape(self._b, C.byref(s)))
+        return {k: int(getattr(s, k)) for k, _ in BatchShape._fields_}
+
+    @shape.setter
+    def shape(self, d: dict) -> None:
+        s = BatchShape()
+        for k, _ in BatchShape._fields_:
+            setattr(s, k, int(d[k]))
+        _check(lib().vct_batch_set_shape(self._b, C.byref(s)))
+
+    def autotune(self, frames: int = 3) -> dict:
+        s, before, after = BatchShape(), C.c_float(), C.c_float()
+        _check(lib().vct_batch_autotune(self._b, int(frames), C.byref(s), C.byref(before), C.byref(after)))
+        return {"shape": {k: int(getattr(s, k)) for k, _ in BatchShape._fields_},
+                "ms_before": float(before.value), "ms_after": float(after.value)}
