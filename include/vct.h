@@ -387,13 +387,16 @@ typedef struct {
 } vct_batch_config;
 
 /* Launch shapes of the batched kernels: persistent CTAs per SM of the
- * binning, brick and trace launches, and the trace's tile scheduling
- * (1 = atomic tile queue, 0 = static stride). */
+ * binning, brick and trace launches, the trace's tile scheduling (1 =
+ * atomic tile queue, 0 = static stride), and the trace's form: 0 = one
+ * persistent launch over all scenes, 1 = one launch of the one-scene trace
+ * kernel per scene, spread over parallel streams (graph branches). */
 typedef struct {
   int32_t bin_ctas_per_sm;
   int32_t bricks_ctas_per_sm;
   int32_t trace_ctas_per_sm;
   int32_t trace_dynamic;
+  int32_t trace_per_scene;
 } vct_batch_shape;
 
 typedef struct vct_batch vct_batch;

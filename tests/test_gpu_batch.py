@@ -59,10 +59,12 @@ def test_batch_rejects_bad_scenes(vct):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("per_scene", [0, 1], ids=["persistent_trace", "per_scene_trace"])
 @pytest.mark.parametrize("use_graph", [False, True], ids=["eager", "graph"])
-def test_batch_matches_renderer(vct, use_graph):
+def test_batch_matches_renderer(vct, use_graph, per_scene):
     items = _items()
     b = vct.Batch(items, use_graph=use_graph)
+    b.shape = dict(b.shape, trace_per_scene=per_scene)
     b.render()
     b.render()  # a second frame (a graph replay) gives the same result
     t = b.stage_times()
@@ -81,9 +83,11 @@ def test_batch_conservative_voxelizer(vct):
 
 
 @pytest.mark.gpu
-def test_batch_camera_update_under_graph(vct):
+@pytest.mark.parametrize("per_scene", [0, 1], ids=["persistent_trace", "per_scene_trace"])
+def test_batch_camera_update_under_graph(vct, per_scene):
     items = _items()[:4]
     b = vct.Batch(items, use_graph=True)
+    b.shape = dict(b.shape, trace_per_scene=per_scene)
     b.render()
     scene = items[2][0]
     view = scenes.look_at((0.1, 0.05, 0.45), (0.0, -0.1, -0.5))
@@ -102,7 +106,8 @@ def test_batch_autotune_keeps_results(vct):
     rep = b.autotune(frames=1)
     assert rep["shape"] == b.shape
     assert rep["ms_after"] <= rep["ms_before"] + 1e-6
-    assert rep["shape"]["trace_ctas_per_sm"] in (2, 3, 4) and rep["shape"]["trace_dynamic"] in (0, 1)
+    assert rep["shape"]["trace_ctas_per_sm"] in (2, 3) and rep["shape"]["trace_dynamic"] in (0, 1)
+    assert rep["shape"]["trace_per_scene"] in (0, 1)
     b.render()
     for i in range(len(items)):
         np.testing.assert_array_equal(b.read_frame(i), before[i])

@@ -59,7 +59,7 @@ struct vct_batch {
   vct_batch_config cfg;
   std::vector<std::unique_ptr<SceneRes>> scenes;
   int sms = 148;
-  BatchShape shape = {4, 4, 4, 1};
+  BatchShape shape = {8, 8, 3, 1, 1};
   // device descriptors
   DevBuf<BatchScene> d_scenes;
   HostBuf<CameraParams> h_cams;
@@ -82,6 +82,10 @@ struct vct_batch {
   HostBuf<FrameStatus> h_status;
   // execution
   cudaStream_t own_stream = nullptr, stream = nullptr;
+  static constexpr int kSide = 4;  // parallel streams of the per-scene trace
+  cudaStream_t side[kSide] = {};
+  cudaEvent_t fork_ev = nullptr, join_ev[kSide] = {};
+  std::vector<int> trace_order;    // scenes, largest frame first
   cudaEvent_t ev[5] = {};
   cudaGraphExec_t graph = nullptr;
   bool pending = false, have_frame = false;
@@ -92,6 +96,11 @@ struct vct_batch {
     drop_graph();
     for (auto& e : ev)
       if (e) cudaEventDestroy(e);
+    if (fork_ev) cudaEventDestroy(fork_ev);
+    for (int k = 0; k < kSide; ++k) {
+      if (join_ev[k]) cudaEventDestroy(join_ev[k]);
+      if (side[k]) cudaStreamDestroy(side[k]);
+    }
     if (own_stream) cudaStreamDestroy(own_stream);
   }
 
@@ -175,7 +184,9 @@ struct vct_batch {
                              stream));
     VCT_CUDA(cudaMemsetAsync(d_status.p, 0, sizeof(FrameStatus), stream));
     VCT_CUDA(record(0));
-    VCT_CUDA(launch_voxelize_batch(work(tris), work(bricks), bricks.total(), cfg.vox_mode, VCT_STORAGE_RGBA8, bb,
+    BatchWork wb = work(bricks);
+    wb.queue = queue.p + 1;  // the brick queue (queue[0] schedules the trace)
+    VCT_CUDA(launch_voxelize_batch(work(tris), wb, bricks.total(), cfg.vox_mode, VCT_STORAGE_RGBA8, bb,
                                    scan_tmp.p, shape, sms, stream, &launches));
     VCT_CUDA(record(1));
     const BatchWork tail[2] = {work(tail5), work(tail6)};
@@ -183,7 +194,24 @@ struct vct_batch {
     VCT_CUDA(record(2));
     VCT_CUDA(launch_gbuffer_batch(work(tris), work(tiles), total_px, bb, sms, stream, &launches));
     VCT_CUDA(record(3));
-    VCT_CUDA(launch_trace_batch(work(tiles, true), bb, shape, sms, stream, &launches));
+    if (shape.trace_per_scene) {
+      // Fork the side streams off the frame's stream, trace the scenes
+      // round-robin on them (largest first), join back.
+      VCT_CUDA(cudaEventRecord(fork_ev, stream));
+      for (int k = 0; k < kSide; ++k) VCT_CUDA(cudaStreamWaitEvent(side[k], fork_ev, 0));
+      for (size_t i = 0; i < trace_order.size(); ++i) {
+        const int s = trace_order[i];
+        const SceneRes& r = *scenes[s];
+        VCT_CUDA(launch_trace(r.sp, h_cams.p[s], r.maps.ms, r.tp, gb_pos.p + px_base[s], gb_nrm.p + px_base[s],
+                              frame.p + px_base[s], nullptr, side[i % kSide], &launches));
+      }
+      for (int k = 0; k < kSide; ++k) {
+        VCT_CUDA(cudaEventRecord(join_ev[k], side[k]));
+        VCT_CUDA(cudaStreamWaitEvent(stream, join_ev[k], 0));
+      }
+    } else {
+      VCT_CUDA(launch_trace_batch(work(tiles, true), bb, shape, sms, stream, &launches));
+    }
     VCT_CUDA(record(4));
     VCT_CUDA(cudaMemcpyAsync(h_status.p, d_status.p, sizeof(FrameStatus), cudaMemcpyDeviceToHost, stream));
     return VCT_OK;
@@ -357,6 +385,11 @@ vct_status build_batch(vct_batch* b, const vct_batch_scene* descs, uint32_t n) {
   VCT_CUDA(cudaStreamCreateWithFlags(&b->own_stream, cudaStreamNonBlocking));
   b->stream = b->own_stream;
   for (auto& e : b->ev) VCT_CUDA(cudaEventCreate(&e));
+  VCT_CUDA(cudaEventCreateWithFlags(&b->fork_ev, cudaEventDisableTiming));
+  for (int k = 0; k < vct_batch::kSide; ++k) {
+    VCT_CUDA(cudaStreamCreateWithFlags(&b->side[k], cudaStreamNonBlocking));
+    VCT_CUDA(cudaEventCreateWithFlags(&b->join_ev[k], cudaEventDisableTiming));
+  }
   std::vector<uint32_t> c_tris, c_bricks, c_regions, c_tail5, c_tail6, c_tiles;
   uint64_t total_tris = 0;
   for (uint32_t i = 0; i < n; ++i) {
@@ -399,6 +432,10 @@ vct_status build_batch(vct_batch* b, const vct_batch_scene* descs, uint32_t n) {
     px += (size_t)r.W * r.H;
   }
   b->total_px = px;
+  for (uint32_t i = 0; i < n; ++i) b->trace_order.push_back((int)i);
+  std::stable_sort(b->trace_order.begin(), b->trace_order.end(), [&](int a, int c) {
+    return (size_t)b->scenes[a]->W * b->scenes[a]->H > (size_t)b->scenes[c]->W * b->scenes[c]->H;
+  });
   VCT_CHECK(upload(b->d_scenes, hs.data(), hs.size()));
   VCT_CHECK(b->h_cams.ensure(n));
   VCT_CHECK(b->d_cams.ensure(n));
@@ -414,7 +451,7 @@ vct_status build_batch(vct_batch* b, const vct_batch_scene* descs, uint32_t n) {
   VCT_CHECK(b->grow_bin_big(1 << 12));
   VCT_CHECK(b->rbig_count.ensure(2));
   VCT_CHECK(b->grow_rbig(1 << 16));
-  VCT_CHECK(b->queue.ensure(1));
+  VCT_CHECK(b->queue.ensure(2));
   VCT_CHECK(b->vis.ensure(px));
   VCT_CHECK(b->gb_pos.ensure(px));
   VCT_CHECK(b->gb_nrm.ensure(px));
@@ -458,6 +495,9 @@ extern "C" vct_status vct_batch_set_camera(vct_batch* b, uint32_t scene, const f
   std::memcpy(b->scenes[scene]->view, view, 16 * sizeof(float));
   std::memcpy(b->scenes[scene]->proj, proj, 16 * sizeof(float));
   b->fill_camera(scene);
+  // The per-scene trace launches take the camera as a kernel parameter,
+  // which a captured graph holds by value: capture it again.
+  if (b->shape.trace_per_scene) b->drop_graph();
   return VCT_OK;
 }
 
@@ -544,6 +584,7 @@ extern "C" vct_status vct_batch_get_shape(vct_batch* b, vct_batch_shape* out) {
   out->bricks_ctas_per_sm = b->shape.bricks_ctas_per_sm;
   out->trace_ctas_per_sm = b->shape.trace_ctas_per_sm;
   out->trace_dynamic = b->shape.trace_dynamic;
+  out->trace_per_scene = b->shape.trace_per_scene;
   return VCT_OK;
 }
 
@@ -551,14 +592,15 @@ extern "C" vct_status vct_batch_set_shape(vct_batch* b, const vct_batch_shape* s
   clear_error();
   if (!b || !s) return set_error(VCT_ERR_INVALID_VALUE, "NULL argument");
   if (s->bin_ctas_per_sm < 1 || s->bin_ctas_per_sm > 32 || s->bricks_ctas_per_sm < 1 ||
-      s->bricks_ctas_per_sm > 32 || s->trace_ctas_per_sm < 1 || s->trace_ctas_per_sm > 4 ||
-      (s->trace_dynamic != 0 && s->trace_dynamic != 1))
+      s->bricks_ctas_per_sm > 32 || s->trace_ctas_per_sm < 1 || s->trace_ctas_per_sm > 3 ||
+      (s->trace_dynamic != 0 && s->trace_dynamic != 1) || (s->trace_per_scene != 0 && s->trace_per_scene != 1))
     return set_error(VCT_ERR_INVALID_VALUE, "launch shape out of range");
   VCT_CHECK(b->finish());
   b->shape.bin_ctas_per_sm = s->bin_ctas_per_sm;
   b->shape.bricks_ctas_per_sm = s->bricks_ctas_per_sm;
   b->shape.trace_ctas_per_sm = s->trace_ctas_per_sm;
   b->shape.trace_dynamic = s->trace_dynamic;
+  b->shape.trace_per_scene = s->trace_per_scene;
   b->drop_graph();  // launch shapes are baked into a captured graph
   return VCT_OK;
 }
@@ -598,9 +640,11 @@ extern "C" vct_status vct_batch_autotune(vct_batch* b, int32_t frames, vct_batch
   // others at their best values so far.
   const int bin_c[] = {2, 4, 8};
   const int brick_c[] = {2, 4, 8};
-  const int trace_c[] = {2, 3, 4};
+  const int trace_c[] = {2, 3};
   const int dyn_c[] = {0, 1};
-  auto try_field = [&](int BatchShape::*field, const int* cand, int nc) -> vct_status {
+  const int per_scene_c[] = {0, 1};
+  auto try_field = [&](int BatchShape::*field, const auto& cand) -> vct_status {
+    const int nc = (int)(sizeof(cand) / sizeof(cand[0]));
     for (int k = 0; k < nc; ++k) {
       if (cur.*field == cand[k]) continue;
       BatchShape s = cur;
@@ -616,10 +660,11 @@ extern "C" vct_status vct_batch_autotune(vct_batch* b, int32_t frames, vct_batch
     }
     return VCT_OK;
   };
-  VCT_CHECK(try_field(&BatchShape::trace_dynamic, dyn_c, 2));
-  VCT_CHECK(try_field(&BatchShape::trace_ctas_per_sm, trace_c, 3));
-  VCT_CHECK(try_field(&BatchShape::bricks_ctas_per_sm, brick_c, 3));
-  VCT_CHECK(try_field(&BatchShape::bin_ctas_per_sm, bin_c, 3));
+  VCT_CHECK(try_field(&BatchShape::trace_per_scene, per_scene_c));
+  VCT_CHECK(try_field(&BatchShape::trace_dynamic, dyn_c));
+  VCT_CHECK(try_field(&BatchShape::trace_ctas_per_sm, trace_c));
+  VCT_CHECK(try_field(&BatchShape::bricks_ctas_per_sm, brick_c));
+  VCT_CHECK(try_field(&BatchShape::bin_ctas_per_sm, bin_c));
   b->shape = cur;
   b->drop_graph();
   if (best) {
@@ -627,6 +672,7 @@ extern "C" vct_status vct_batch_autotune(vct_batch* b, int32_t frames, vct_batch
     best->bricks_ctas_per_sm = cur.bricks_ctas_per_sm;
     best->trace_ctas_per_sm = cur.trace_ctas_per_sm;
     best->trace_dynamic = cur.trace_dynamic;
+    best->trace_per_scene = cur.trace_per_scene;
   }
   if (ms_before) *ms_before = base;
   if (ms_after) *ms_after = cur_ms;

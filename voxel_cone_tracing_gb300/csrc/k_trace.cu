@@ -36,6 +36,12 @@ __device__ __forceinline__ float4 operator*(float4 a, float s) { return f4(a.x *
 // Resident 256-thread CTAs per SM the texture-unit variant is compiled for
 // (register budget 65536 / (256 * 4) = 64 per thread).
 constexpr int kTraceMinBlocks = VCT_TRACE_MIN_BLOCKS;
+#ifndef VCT_TRACE_BATCH_MIN_BLOCKS
+#define VCT_TRACE_BATCH_MIN_BLOCKS 3
+#endif
+// The batched trace keeps a scene's descriptor in shared memory and its
+// values in registers, so it is compiled for its own occupancy.
+constexpr int kTraceBatchMinBlocks = VCT_TRACE_BATCH_MIN_BLOCKS;
 
 constexpr float kTan22_5 = 0.55785173935f;      // TAN_22_5 (:164), kept verbatim
 constexpr float kMaxDistance = 1.73205080757f;  // MAX_DISTANCE (:166)
@@ -318,6 +324,28 @@ __global__ void __launch_bounds__(256, SAMPLER == VCT_SAMPLER_HW ? kTraceMinBloc
                                   blockIdx.x * 16 + (threadIdx.x & 15), blockIdx.y * 16 + (threadIdx.x >> 4));
 }
 
+// One pixel of a batch scene.  Called, not inlined, from the tile loop of
+// k_trace_batch: inlined into a loop, the shading's loop-invariant loads
+// (scene constants, texture handles) are hoisted out of the loop and held in
+// registers across all tiles, which spills the march loop (measured: 4 KB of
+// spill code against 0.2 KB for the one-scene kernel).
+#ifdef VCT_TRACE_BATCH_INLINE
+#define VCT_BATCH_PX_FN __forceinline__
+#else
+#define VCT_BATCH_PX_FN __noinline__
+#endif
+// The current scene of a k_trace_batch CTA, read by trace_batch_px at fixed
+// shared-memory addresses.
+__shared__ BatchScene s_batch_scene;
+__shared__ CameraParams s_batch_cam;
+
+template <bool ISO>
+__device__ VCT_BATCH_PX_FN void trace_batch_px(const float4* __restrict__ gb_pos, const float4* __restrict__ gb_nrm,
+                                            uchar4* __restrict__ frame, int px, int py) {
+  trace_px<VCT_SAMPLER_HW, ISO, VCT_STORAGE_RGBA8>(s_batch_scene.sp, s_batch_cam, s_batch_scene.ms,
+                                                   s_batch_scene.tp, gb_pos, gb_nrm, frame, nullptr, px, py);
+}
+
 // The 16x16 tiles of every scene of a batch in one persistent launch.  With
 // w.queue a CTA takes its next tile from an atomic counter (uneven scenes
 // balance across SMs); without, tiles are strided by the grid.  The CTA
@@ -325,11 +353,11 @@ __global__ void __launch_bounds__(256, SAMPLER == VCT_SAMPLER_HW ? kTraceMinBloc
 // shading code addresses them at fixed offsets (as kernel parameters are in
 // the one-scene kernel) instead of holding pointers in registers.
 template <bool ISO>
-__global__ void __launch_bounds__(256, kTraceMinBlocks) k_trace_batch(BatchWork w, BatchBuffers bb) {
+__global__ void __launch_bounds__(256, kTraceBatchMinBlocks) k_trace_batch(BatchWork w, BatchBuffers bb) {
   __shared__ uint32_t s_next;
   __shared__ int s_cur;
-  __shared__ BatchScene s_sc;
-  __shared__ CameraParams s_cam;
+  BatchScene& s_sc = s_batch_scene;
+  CameraParams& s_cam = s_batch_cam;
   static_assert(sizeof(BatchScene) % 4 == 0 && sizeof(CameraParams) % 4 == 0, "word copies");
   uint32_t g = blockIdx.x;
   if (threadIdx.x == 0) s_cur = -1;
@@ -353,10 +381,8 @@ __global__ void __launch_bounds__(256, kTraceMinBlocks) k_trace_batch(BatchWork 
       if (threadIdx.x == 0) s_cur = s;
     }
     const uint32_t lt = g - __ldg(w.prefix + s), tiles_x = (uint32_t)(s_sc.W + 15) / 16;
-    trace_px<VCT_SAMPLER_HW, ISO, VCT_STORAGE_RGBA8>(
-        s_sc.sp, s_cam, s_sc.ms, s_sc.tp, bb.rb.gb_pos + s_sc.px_base, bb.rb.gb_nrm + s_sc.px_base,
-        bb.frame + s_sc.px_base, nullptr, (int)(lt % tiles_x) * 16 + (threadIdx.x & 15),
-        (int)(lt / tiles_x) * 16 + (threadIdx.x >> 4));
+    trace_batch_px<ISO>(bb.rb.gb_pos + s_sc.px_base, bb.rb.gb_nrm + s_sc.px_base, bb.frame + s_sc.px_base,
+                        (int)(lt % tiles_x) * 16 + (threadIdx.x & 15), (int)(lt / tiles_x) * 16 + (threadIdx.x >> 4));
     if (w.queue) {
       __syncthreads();  // every thread has read s_next
       if (threadIdx.x == 0) s_next = atomicAdd(w.queue, 1u);
@@ -411,7 +437,7 @@ cudaError_t launch_trace_batch(const BatchWork& tiles, const BatchBuffers& bb, c
     cudaError_t e = cudaMemsetAsync(w.queue, 0, sizeof(uint32_t), st);
     if (e != cudaSuccess) return e;
   }
-  const int per_sm = std::min(std::max(shape.trace_ctas_per_sm, 1), kTraceMinBlocks);
+  const int per_sm = std::min(std::max(shape.trace_ctas_per_sm, 1), kTraceBatchMinBlocks);
   const unsigned grid = (unsigned)std::max(1, std::min<int>(sms * per_sm, (int)tiles.total));
   k_trace_batch<false><<<grid, 256, 0, st>>>(w, bb);
   if (launches) ++*launches;

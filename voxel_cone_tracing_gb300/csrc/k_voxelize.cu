@@ -683,19 +683,39 @@ __global__ void __launch_bounds__(kThreads) k_bricks(SceneParams sp, int N, cons
   brick_body<MODE, STORAGE>(sp, N, blockIdx.x, offset, list, cap, l0, counts, st, acc, setup, excl);
 }
 
-// Every scene's bricks in one persistent launch.
+// Every scene's bricks in one persistent launch; a CTA takes its next brick
+// from the atomic counter w.queue (brick costs range from an empty brick to
+// thousands of triangle samples).
 template <int MODE, int STORAGE>
 __global__ void __launch_bounds__(kThreads) k_bricks_batch(BatchWork w, BatchBuffers bb) {
   __shared__ AccT<STORAGE> acc;
   __shared__ SetupOf<MODE> setup[kWarps][32];
   __shared__ int excl[kWarps][33];
-  for (uint32_t g = blockIdx.x; g < w.total; g += gridDim.x) {
+  __shared__ uint32_t s_next;
+  if (threadIdx.x == 0) s_next = atomicAdd(w.queue, 1u);
+  __syncthreads();
+  uint32_t g = s_next;
+  while (g < w.total) {
     const int s = batch_scene_of(w, g);
     const BatchScene& S = w.scenes[s];
     brick_body<MODE, STORAGE>(S.sp, S.N, g - __ldg(w.prefix + s), bb.brick_offset + S.brick_base, bb.pair_list,
                               bb.pair_cap, S.ms.l0_surf, nullptr, bb.status, acc, setup, excl);
-    __syncthreads();  // the next brick clears the accumulators
+    __syncthreads();  // the next brick clears the accumulators; s_next has been read
+    if (threadIdx.x == 0) s_next = atomicAdd(w.queue, 1u);
+    __syncthreads();
+    g = s_next;
   }
+}
+
+// Persistent grid of a batched kernel: `per_sm` CTAs per SM, but never more
+// than fit on an SM at once (a CTA that waits for a slot would start its
+// share of the work only after a whole resident CTA has finished).
+template <class K>
+unsigned resident_grid(K kern, int threads, size_t smem, int sms, int per_sm, uint32_t items) {
+  int fit = 1;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fit, kern, threads, smem) != cudaSuccess || fit < 1) fit = 1;
+  const int n = sms * std::min(std::max(per_sm, 1), fit);
+  return (unsigned)std::max<uint32_t>(1u, std::min<uint32_t>((uint32_t)n, items));
 }
 
 // The same brick CTA writing RGBA8 level 0 into linear memory (x fastest)
@@ -871,8 +891,8 @@ cudaError_t launch_voxelize_batch(const BatchWork& tris, const BatchWork& bricks
   if (e != cudaSuccess) return e;
   e = cudaMemsetAsync(bb.big_count, 0, sizeof(uint32_t), st);
   if (e != cudaSuccess) return e;
-  const unsigned bin_grid =
-      (unsigned)std::max(1, std::min<int>(sms * std::max(shape.bin_ctas_per_sm, 1), (int)((tris.total + 255) / 256)));
+  const unsigned bin_grid = resident_grid(k_bin_batch<false>, 256, 0, sms, shape.bin_ctas_per_sm,
+                                          (tris.total + 255) / 256);
   const dim3 big_grid(128, kBigSplit);
   if (tris.total) {
     k_bin_batch<false><<<bin_grid, 256, 0, st>>>(tris, bb);
@@ -893,18 +913,18 @@ cudaError_t launch_voxelize_batch(const BatchWork& tris, const BatchWork& bricks
                                               bb.pair_list, bb.pair_cap, tris.scenes);
     nl += 2;
   }
-  const unsigned grid =
-      (unsigned)std::max(1, std::min<int>(sms * std::max(shape.bricks_ctas_per_sm, 1), (int)bricks.total));
+  e = cudaMemsetAsync(bricks.queue, 0, sizeof(uint32_t), st);
+  if (e != cudaSuccess) return e;
+  auto run = [&](auto kern) {
+    kern<<<resident_grid(kern, kThreads, 0, sms, shape.bricks_ctas_per_sm, bricks.total), kThreads, 0, st>>>(bricks,
+                                                                                                          bb);
+  };
   if (mode == VCT_VOX_CONSERVATIVE) {
-    if (storage == VCT_STORAGE_RGBA8)
-      k_bricks_batch<VCT_VOX_CONSERVATIVE, VCT_STORAGE_RGBA8><<<grid, kThreads, 0, st>>>(bricks, bb);
-    else
-      k_bricks_batch<VCT_VOX_CONSERVATIVE, VCT_STORAGE_RGBA16F><<<grid, kThreads, 0, st>>>(bricks, bb);
+    if (storage == VCT_STORAGE_RGBA8) run(k_bricks_batch<VCT_VOX_CONSERVATIVE, VCT_STORAGE_RGBA8>);
+    else run(k_bricks_batch<VCT_VOX_CONSERVATIVE, VCT_STORAGE_RGBA16F>);
   } else {
-    if (storage == VCT_STORAGE_RGBA8)
-      k_bricks_batch<VCT_VOX_REF_RASTER2X, VCT_STORAGE_RGBA8><<<grid, kThreads, 0, st>>>(bricks, bb);
-    else
-      k_bricks_batch<VCT_VOX_REF_RASTER2X, VCT_STORAGE_RGBA16F><<<grid, kThreads, 0, st>>>(bricks, bb);
+    if (storage == VCT_STORAGE_RGBA8) run(k_bricks_batch<VCT_VOX_REF_RASTER2X, VCT_STORAGE_RGBA8>);
+    else run(k_bricks_batch<VCT_VOX_REF_RASTER2X, VCT_STORAGE_RGBA16F>);
   }
   ++nl;
   if (launches) *launches += nl;

@@ -171,6 +171,7 @@ struct BatchShape {
   int bricks_ctas_per_sm;
   int trace_ctas_per_sm;
   int trace_dynamic;   // 1: tiles from an atomic queue; 0: static stride
+  int trace_per_scene; // 1: one launch of the one-scene trace kernel per scene
 };
 
 // ---- learned diffuse term (k_mlp.cu) --------------------------------------

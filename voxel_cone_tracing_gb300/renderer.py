@@ -468,7 +468,7 @@ class BatchConfig(C.Structure):
 
 class BatchShape(C.Structure):
     _fields_ = [("bin_ctas_per_sm", C.c_int32), ("bricks_ctas_per_sm", C.c_int32),
-                ("trace_ctas_per_sm", C.c_int32), ("trace_dynamic", C.c_int32)]
+                ("trace_ctas_per_sm", C.c_int32), ("trace_dynamic", C.c_int32), ("trace_per_scene", C.c_int32)]
 
 
 class Batch:

@@ -375,3 +375,43 @@ def scene_hdr(seed: int = 3000, freq: int = 158, n_spheres: int = 4, n_cuboids: 
     return Scene(meshes, models, np.array(mats, MATERIAL_DTYPE),
                  np.array([point_light((0.0, 0.38, 0.05), intensity=12.0)], LIGHT_DTYPE), view, proj,
                  ROOM_CUBE_SIZE, name=f"room+{n_spheres}icospheres{freq}+{n_cuboids}cuboids")
+
+
+BATCH_FRAMES = [(256, 256), (512, 384), (640, 480), (960, 540), (1280, 720), (1920, 1080)]
+BATCH_GRIDS = [32, 64, 128, 256]
+
+
+def batch_scenes(seed: int = 5000, n: int = 64, max_tris: int = 1_000_000, min_tris: int = 1_000) -> list:
+    """Seeded batch of `n` independent scenes of uneven size: triangle counts
+    log-uniform in [min_tris, max_tris] (the room plus one displaced geodesic
+    sphere of frequency round(sqrt((T - 10) / 20))), frames from 256^2 to
+    1920x1080, grids 32^3 to 256^3, 9 or 6 diffuse cones.  Scene i uses seed
+    `seed + i`.  Returns (scene, width, height, grid_res, cone_set) tuples,
+    cone_set 0 = the reference's 9 cones, 1 = 6 cones."""
+    out = []
+    sphere_cache = {}
+    for i in range(n):
+        rng = np.random.default_rng(seed + i)
+        target = math.exp(rng.uniform(math.log(min_tris), math.log(max_tris)))
+        freq = max(2, int(round(math.sqrt(max(target - 10.0, 40.0) / 20.0))))
+        w, h = BATCH_FRAMES[int(rng.integers(len(BATCH_FRAMES)))]
+        grid = BATCH_GRIDS[int(rng.integers(len(BATCH_GRIDS)))]
+        cones = int(rng.integers(2))
+        mats = [default_material()]
+        for _ in range(5):
+            mats.append(make_material(rng.uniform(0.2, 0.9, 3), roughness=rng.uniform(0.3, 1.0)))
+        room = box_room(list(range(1, 6)))
+        base = len(mats)
+        for _ in range(20):
+            mats.append(make_material(rng.uniform(0.0, 1.0, 3), roughness=rng.uniform(0.0, 1.0)))
+        if freq not in sphere_cache:
+            sphere_cache[freq] = geodesic_sphere(freq, seed + 100000 + freq, 0.05, material_base=base)
+        sphere = sphere_cache[freq]
+        model = trs(translate=rng.uniform([-0.2, -0.3, -0.25], [0.2, -0.1, 0.0]),
+                    scale=np.full(3, rng.uniform(0.12, 0.28)))
+        view, proj = _camera(w, h)
+        light = point_light(tuple(rng.uniform([-0.3, 0.3, -0.2], [0.3, 0.45, 0.2])))
+        s = Scene([room, sphere], [mat_identity(), model], np.array(mats, MATERIAL_DTYPE),
+                  np.array([light], LIGHT_DTYPE), view, proj, ROOM_CUBE_SIZE, name=f"batch{i}")
+        out.append((s, w, h, grid, cones))
+    return out
