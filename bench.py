@@ -252,6 +252,46 @@ def precision_leg(R, torch, steps, flush_mb=256):
     return out
 
 
+def injection_leg(R, torch, scene, steps, flush):
+    """Deferred light injection on the bench frame: the light moves every
+    frame, the geometry does not, so frames after the first skip
+    voxelization and light level 0 from the attribute grids."""
+    r = R.Renderer(WIDTH, HEIGHT, grid_res=GRID)
+    ids = R.load_scene(r, scene)
+    r.set_voxel_view_dir(7, 0.0)
+    r.set_light_injection(True)
+    stream = torch.cuda.Stream()
+    r.set_stream(stream.cuda_stream)
+    base = scene.lights[0]
+
+    def frame(k):
+        for mid in ids:
+            r.queue_model(mid)
+        light = base.copy()
+        light["position"] = base["position"] + (0.02 * (k % 5), 0.0, -0.01 * (k % 3))
+        r.queue_point_light(light)
+        r.render()
+
+    frame(0)
+    first = r.stage_times()
+    for k in range(3):
+        frame(k + 1)
+    stages = []
+    for k in range(steps):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        frame(k + 4)
+        r.synchronize()
+        stages.append(r.stage_times())
+    r.close()
+    mean = lambda key: statistics.mean(st[key] for st in stages)  # noqa: E731
+    return {"workload": "bench frame, light moved every frame, geometry fixed", "unit": UNIT,
+            "value": round(mean("voxelize") + mean("mipmap") + mean("trace"), 4),
+            "inject_ms": round(mean("voxelize"), 4), "voxelized_frames": sum(int(st["voxelized"]) for st in stages),
+            "first_frame_voxelize_ms": round(first["voxelize"], 4),
+            "stages_ms": {k: round(mean(k), 4) for k in ("voxelize", "mipmap", "gbuffer", "trace")}}
+
+
 def batch_leg(R, torch, steps):
     """Batched workload: 64 seeded scenes of uneven size (grids 32^3-256^3,
     990-865k triangles, frames 256^2-1920x1080, 9 or 6 diffuse cones), one
@@ -443,6 +483,7 @@ def run_ours(args):
     }
     if not args.no_mlp:
         line["mlp"] = mlp_leg(r, R, scene, ids, stream, flush, args.steps, stages)
+    line["injection"] = injection_leg(R, torch, scene, args.steps, flush)
     if not args.no_precision:
         line["precision"] = precision_leg(R, torch, args.steps)
     if not args.no_batch:

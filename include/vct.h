@@ -122,6 +122,8 @@ typedef struct {
   float trace;      /* cone-trace shading                                  */
   float total;      /* first to last event of the frame                    */
   uint32_t kernel_launches; /* engine kernels launched for the frame       */
+  uint32_t voxelized;       /* 1: the frame voxelized its geometry; 0: light
+                             * injection reused the attribute grids        */
 } vct_stage_times;
 
 /* --------------------------------------------------- error reporting --- */
@@ -324,6 +326,23 @@ vct_status vct_voxelize_noalloc(const vct_device_mesh* meshes, uint32_t n_meshes
                                 const vct_point_light* lights, uint32_t n_lights,
                                 float cube_size, int32_t grid_res, int32_t vox_mode,
                                 void* level0_rgba8, void* stream);
+
+/* ------------------------------------------- Deferred light injection --- */
+/* No reference counterpart: the reference shades every fragment while it
+ * voxelizes, so any light change re-voxelizes the scene (renderer.cpp
+ * :316-353 runs every frame).  With injection on, the voxelizer stores per
+ * voxel the mean albedo x transmittance and alpha, the mean normal and the
+ * mean emission x transmittance (three RGBA8 grids), and every frame lights
+ * the voxels at their centres from those grids (the per-light terms of
+ * voxelize.frag:208-227).  Frames whose queued models, matrices, cube size,
+ * grid and materials equal the previous frame's skip voxelization: a light
+ * change costs one injection pass.  The lighting is evaluated from voxel
+ * means at the voxel centre instead of per fragment, an approximation of
+ * the reference's shading.  RGBA8 storage only. */
+vct_status vct_set_light_injection(vct_renderer* r, int32_t enable);
+/* The three attribute grids (N^3 RGBA8 each, x fastest): albedo, normal
+ * (0.5 n + 0.5), emission (a = 255 where occupied). */
+vct_status vct_read_injection_grids(vct_renderer* r, void* albedo, void* normal, void* emission);
 
 /* ------------------------------------------------------- Texture3D ----- */
 

@@ -98,7 +98,8 @@ class Renderer {
   void queue_point_light(point_light_t& point_light) { status_ = vct_queue_point_light(r_, &point_light); }
   void render() { status_ = vct_render(r_); }
 
-  // Engine additions: synchronisation, read-back, status.
+  // Engine additions: deferred light injection, synchronisation, read-back, status.
+  void set_light_injection(bool enable) { status_ = vct_set_light_injection(r_, enable ? 1 : 0); }
   vct_status read_frame(void* rgba8) { return status_ = vct_read_frame(r_, rgba8, VCT_FRAME_RGBA8); }
   vct_status synchronize() { return status_ = vct_synchronize(r_); }
   vct_status last_status() const { return status_; }

@@ -75,6 +75,9 @@ def lib():
             getattr(L, f).restype = C.c_int64
             getattr(L, f).argtypes = [P, P, P, P]
         L.orc_mipmap.argtypes = [P, P, P]
+        L.orc_voxelize_attr.restype = C.c_int64
+        L.orc_voxelize_attr.argtypes = [P, P, P, P, P, P]
+        L.orc_inject.argtypes = [P, P, P, P, P, P]
         L.orc_voxelize_hdr.restype = C.c_int64
         L.orc_voxelize_hdr.argtypes = [P, P, P, P]
         L.orc_mip_level_f.argtypes = [C.c_int32, C.c_int32, P, C.c_int32, P]
@@ -187,6 +190,28 @@ def voxelize_hdr(scene, params: Params):
     sh, pc = _SceneHold(scene), params.c()
     rej = lib().orc_voxelize_hdr(sh.ptr, C.addressof(pc), _ptr(l0), _ptr(cnt))
     return l0, cnt, int(rej)
+
+
+def voxelize_attr(scene, params: Params):
+    """Light-injection attribute grids: -> dict(albedo, normal, emission:
+    uint8 (N,N,N,4) [z,y,x], counts, rejected)."""
+    n = params.grid_res
+    g = {k: np.zeros((n, n, n, 4), np.uint8) for k in ("albedo", "normal", "emission")}
+    cnt = np.zeros((n, n, n), np.uint32)
+    sh, pc = _SceneHold(scene), params.c()
+    rej = lib().orc_voxelize_attr(sh.ptr, C.addressof(pc), _ptr(g["albedo"]), _ptr(g["normal"]), _ptr(g["emission"]),
+                                  _ptr(cnt))
+    return dict(g, counts=cnt, rejected=int(rej))
+
+
+def inject(scene, params: Params, grids: dict) -> np.ndarray:
+    """Level 0 (N,N,N,4) uint8 lit from the attribute grids and the scene's lights."""
+    n = params.grid_res
+    out = np.zeros((n, n, n, 4), np.uint8)
+    sh, pc = _SceneHold(scene), params.c()
+    a, nm, e = (np.ascontiguousarray(grids[k], np.uint8) for k in ("albedo", "normal", "emission"))
+    lib().orc_inject(sh.ptr, C.addressof(pc), _ptr(a), _ptr(nm), _ptr(e), _ptr(out))
+    return out
 
 
 def mip_level_f(src: np.ndarray, mip_mode: int) -> np.ndarray:

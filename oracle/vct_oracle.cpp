@@ -161,6 +161,10 @@ static inline bool illum_transparent(int illum) { return illum == 4 || illum == 
 // orc_params.radiance_max for HDR storage.  Set by voxelize_impl before its
 // worker threads start (the oracle runs one call at a time).
 static double g_radiance_max = 1.0;
+// What a contribution carries: 0 the shaded colour; for light injection 1
+// albedo x transmittance + alpha, 2 the normal as 0.5 n + 0.5, 3 emission x
+// transmittance + 1 (occupancy).  Set before voxelize_impl's threads start.
+static int g_attr_mode = 0;
 
 // Per-fragment colour, voxelize.frag:208-239.  pos is in grid space
 // ([-1,1]^3 = world / cube_size), nrm the interpolated vertex normal.
@@ -184,6 +188,18 @@ static V4<R> voxel_fragment_color(const orc_scene* s, const orc_material& mat, V
   V3<R> trans(R(1), R(1), R(1));
   R alpha = R(1);
   if (illum_transparent(mat.illum)) { trans = mat_of<R>(mat, 2); alpha = R(mat.dissolve); }  // :231-237
+  if (g_attr_mode) {
+    const V3<R> t = illum_transparent(mat.illum) ? mat_of<R>(mat, 2) : V3<R>(R(1), R(1), R(1));
+    if (g_attr_mode == 1) {
+      const V3<R> a = mulv(mat_of<R>(mat, 0), t);
+      return V4<R>(clamp01(a.x), clamp01(a.y), clamp01(a.z), clamp01(alpha));
+    }
+    if (g_attr_mode == 2)
+      return V4<R>(clamp01(R(0.5) * nn.x + R(0.5)), clamp01(R(0.5) * nn.y + R(0.5)), clamp01(R(0.5) * nn.z + R(0.5)),
+                   R(0));
+    const V3<R> e = mulv(mat_of<R>(mat, 3), t);
+    return V4<R>(clamp01(e.x), clamp01(e.y), clamp01(e.z), R(1));
+  }
   V3<R> c = mulv(trans, color);
   const R hi = R(g_radiance_max);
   auto cl = [hi](R v) { return v < R(0) ? R(0) : (v > hi ? hi : v); };
@@ -1078,6 +1094,58 @@ int64_t orc_voxelize_f32(const orc_scene* s, const orc_params* p, uint8_t* level
 }
 
 void orc_mipmap(const orc_params* p, const uint8_t* level0, uint8_t* chains) { mipmap_impl(p, level0, chains); }
+
+int64_t orc_voxelize_attr(const orc_scene* s, const orc_params* p, uint8_t* albedo, uint8_t* normal,
+                          uint8_t* emission, uint32_t* counts) {
+  uint8_t* out[3] = {albedo, normal, emission};
+  int64_t rej = 0;
+  for (int m = 1; m <= 3; ++m) {
+    g_attr_mode = m;
+    rej = voxelize_impl<double>(s, p, out[m - 1], m == 1 ? counts : nullptr);
+  }
+  g_attr_mode = 0;
+  return rej;
+}
+
+// Deferred light injection (no reference counterpart), FP64: each occupied
+// voxel lit at its centre from its mean attributes with the per-light terms
+// of voxelize.frag:208-227; RGBA8 round to nearest.
+void orc_inject(const orc_scene* s, const orc_params* p, const uint8_t* albedo, const uint8_t* normal,
+                const uint8_t* emission, uint8_t* level0) {
+  const int N = p->grid_res;
+  const double k = 1.0 / 255.0, cube = (double)s->cube_size;
+  const int nl = std::min<int>((int)s->n_lights, 10);
+  parallel_for(std::max(1, p->threads), N, [&](int z) {
+    for (int y = 0; y < N; ++y)
+      for (int x = 0; x < N; ++x) {
+        const size_t i = 4 * (((size_t)z * N + y) * N + x);
+        uint8_t* o = level0 + i;
+        if (emission[i + 3] == 0) {
+          o[0] = o[1] = o[2] = o[3] = 0;
+          continue;
+        }
+        const V3<double> nn = normalize(V3<double>(normal[i] * k * 2.0 - 1.0, normal[i + 1] * k * 2.0 - 1.0,
+                                                   normal[i + 2] * k * 2.0 - 1.0));
+        const V3<double> pos((x + 0.5) * 2.0 / N - 1.0, (y + 0.5) * 2.0 / N - 1.0, (z + 0.5) * 2.0 / N - 1.0);
+        V3<double> lit;
+        for (int l = 0; l < nl; ++l) {
+          const orc_point_light& L = s->lights[l];
+          const V3<double> lp(L.position[0] / cube, L.position[1] / cube, L.position[2] / cube);
+          const V3<double> dl = lp - pos;
+          const double d = length(dl);
+          const double cs = fmaxr(dot(nn, normalize(dl)), 0.0);
+          lit = lit + V3<double>(L.color[0], L.color[1], L.color[2]) * (cs * (1.0 / (1.0 + d * d)) * L.intensity);
+        }
+        const V3<double> c = mulv(V3<double>(albedo[i] * k, albedo[i + 1] * k, albedo[i + 2] * k), lit) +
+                             V3<double>(emission[i] * k, emission[i + 1] * k, emission[i + 2] * k);
+        auto q = [](double v) { return (uint8_t)std::floor(clamp01(v) * 255.0 + 0.5); };
+        o[0] = q(c.x);
+        o[1] = q(c.y);
+        o[2] = q(c.z);
+        o[3] = albedo[i + 3];
+      }
+  });
+}
 
 int64_t orc_voxelize_hdr(const orc_scene* s, const orc_params* p, float* level0, uint32_t* counts) {
   return voxelize_impl<double>(s, p, nullptr, counts, level0);

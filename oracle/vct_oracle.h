@@ -113,6 +113,15 @@ int64_t orc_voxelize_f32(const orc_scene* s, const orc_params* p,
 int64_t orc_voxelize_hdr(const orc_scene* s, const orc_params* p,
                          float* level0, uint32_t* counts);
 
+/* Light injection (no reference counterpart): the attribute grids (N^3
+ * RGBA8 each: mean albedo x transmittance + alpha; mean normal as 0.5 n +
+ * 0.5; mean emission x transmittance + occupancy 255), with the coverage and
+ * averaging rule of orc_voxelize; then level 0 lit from them. */
+int64_t orc_voxelize_attr(const orc_scene* s, const orc_params* p, uint8_t* albedo,
+                          uint8_t* normal, uint8_t* emission, uint32_t* counts);
+void orc_inject(const orc_scene* s, const orc_params* p, const uint8_t* albedo,
+                const uint8_t* normal, const uint8_t* emission, uint8_t* level0);
+
 /* One mip level in FP64 from float texels: src holds src_maps (1 = the shared
  * level 0, or 6) maps of edge `n_src`; dst receives 6 maps (aniso) or 1 map
  * (iso) of edge n_src/2. */

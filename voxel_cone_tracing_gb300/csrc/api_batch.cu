@@ -574,6 +574,7 @@ extern "C" vct_status vct_batch_stage_times(vct_batch* b, vct_stage_times* out) 
   out->trace = t[3];
   VCT_CUDA(cudaEventElapsedTime(&out->total, b->ev[0], b->ev[4]));
   out->kernel_launches = (uint32_t)b->launches;
+  out->voxelized = 1u;
   return VCT_OK;
 }
 

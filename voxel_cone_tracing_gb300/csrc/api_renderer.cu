@@ -167,6 +167,7 @@ extern "C" vct_status vct_load_mesh(vct_renderer* r, const vct_vert_data* verts,
   m->obj_count = n_objs;
   for (uint32_t o = 0; o < n_objs; ++o) r->objs.push_back(objs[o]);
   r->objs_dirty = true;
+  ++r->scene_version;
   r->models.push_back(std::move(m));
   *out = r->models.size() - 1;
   return VCT_OK;
@@ -186,6 +187,7 @@ extern "C" vct_material_id vct_add_material(vct_renderer* r, const vct_material_
   }
   r->materials.push_back(*md);
   r->materials_dirty = true;
+  ++r->scene_version;
   return r->materials.size() - 1;
 }
 
@@ -195,6 +197,7 @@ extern "C" vct_status vct_upload_material_data(vct_renderer* r, const vct_materi
   if (id >= r->materials.size()) return set_error(VCT_ERR_INVALID_ID, "material %llu", (unsigned long long)id);
   r->materials[id] = *md;
   r->materials_dirty = true;
+  ++r->scene_version;
   return VCT_OK;
 }
 
@@ -206,6 +209,7 @@ extern "C" vct_status vct_set_model_material(vct_renderer* r, vct_material_id ma
   const Model& m = *r->models[model];
   for (uint32_t o = 0; o < m.obj_count; ++o) r->objs[m.obj_start + o].material_id = (uint32_t)mat;
   r->objs_dirty = true;
+  ++r->scene_version;
   return VCT_OK;
 }
 
@@ -354,6 +358,7 @@ extern "C" vct_status vct_get_stage_times(vct_renderer* r, vct_stage_times* out)
   out->trace = t[3];
   VCT_CUDA(cudaEventElapsedTime(&out->total, r->ev[0], r->ev[4]));
   out->kernel_launches = (uint32_t)r->launches;
+  out->voxelized = r->last_revoxelized ? 1u : 0u;
   return VCT_OK;
 }
 
@@ -379,6 +384,36 @@ extern "C" vct_status vct_frame_device_ptr(vct_renderer* r, void** out) {
   clear_error();
   if (!r || !out) return set_error(VCT_ERR_INVALID_VALUE, "NULL argument");
   *out = r->frame.p;
+  return VCT_OK;
+}
+
+extern "C" vct_status vct_set_light_injection(vct_renderer* r, int32_t enable) {
+  clear_error();
+  if (!r) return set_error(VCT_ERR_INVALID_VALUE, "NULL renderer");
+  if (enable && r->cfg.storage != VCT_STORAGE_RGBA8)
+    return set_error(VCT_ERR_UNSUPPORTED, "light injection needs RGBA8 storage");
+  VCT_CHECK(r->finish());
+  r->inject = enable != 0;
+  r->inj_valid = false;
+  return VCT_OK;
+}
+
+extern "C" vct_status vct_read_injection_grids(vct_renderer* r, void* albedo, void* normal, void* emission) {
+  clear_error();
+  if (!r || !albedo || !normal || !emission) return set_error(VCT_ERR_INVALID_VALUE, "NULL argument");
+  VCT_CHECK(r->finish());
+  if (!r->inj_arr[0]) return set_error(VCT_ERR_UNSUPPORTED, "no injection grids (injection off or no frame yet)");
+  void* dst[3] = {albedo, normal, emission};
+  for (int k = 0; k < 3; ++k) {
+    cudaMemcpy3DParms p;
+    std::memset(&p, 0, sizeof(p));
+    p.srcArray = r->inj_arr[k];
+    p.dstPtr = make_cudaPitchedPtr(dst[k], (size_t)r->res * 4, r->res, r->res);
+    p.extent = make_cudaExtent(r->res, r->res, r->res);
+    p.kind = cudaMemcpyDeviceToHost;
+    VCT_CUDA(cudaMemcpy3DAsync(&p, r->stream));
+  }
+  VCT_CUDA(cudaStreamSynchronize(r->stream));
   return VCT_OK;
 }
 

@@ -316,13 +316,15 @@ __device__ __forceinline__ float4 voxel_color(const SceneParams& sp, const vct_m
 // Per-brick sums of the contributions.  RGBA8: 16-bit fixed point per
 // contribution in u32 (exact for the 1/255 result).  RGBA16F: the colour
 // divided by radiance_max in 32-bit fixed point, summed in u64, so the sum
-// is exact, order-independent and far finer than half precision.
+// is exact, order-independent and far finer than half precision.  Attribute
+// grids (light injection): ten unorm channels in 16-bit fixed point.
 template <int STORAGE> struct AccT;
 template <> struct AccT<VCT_STORAGE_RGBA8> {
   uint32_t c[4][kBrickVox];
   uint32_t n[kBrickVox];
   __device__ __forceinline__ void clear(int i) { c[0][i] = 0; c[1][i] = 0; c[2][i] = 0; c[3][i] = 0; n[i] = 0; }
-  __device__ __forceinline__ void add(const SceneParams&, int v, float4 col) {
+  __device__ __forceinline__ void add(const SceneParams& sp, int v, const vct_material_data& m, V3 p, V3 nrm) {
+    const float4 col = voxel_color(sp, m, p, nrm);
     atomicAdd(&c[0][v], __float2uint_rn(col.x * kFix));
     atomicAdd(&c[1][v], __float2uint_rn(col.y * kFix));
     atomicAdd(&c[2][v], __float2uint_rn(col.z * kFix));
@@ -334,7 +336,8 @@ template <> struct AccT<VCT_STORAGE_RGBA16F> {
   unsigned long long c[4][kBrickVox];
   uint32_t n[kBrickVox];
   __device__ __forceinline__ void clear(int i) { c[0][i] = 0; c[1][i] = 0; c[2][i] = 0; c[3][i] = 0; n[i] = 0; }
-  __device__ __forceinline__ void add(const SceneParams& sp, int v, float4 col) {
+  __device__ __forceinline__ void add(const SceneParams& sp, int v, const vct_material_data& m, V3 p, V3 nrm) {
+    const float4 col = voxel_color(sp, m, p, nrm);
     const float k = 4294967296.0f / sp.radiance_max;
     atomicAdd(&c[0][v], __float2ull_rn(col.x * k));
     atomicAdd(&c[1][v], __float2ull_rn(col.y * k));
@@ -343,6 +346,49 @@ template <> struct AccT<VCT_STORAGE_RGBA16F> {
     atomicAdd(&n[v], 1u);
   }
 };
+// Light-injection attributes of one contribution (the factors of
+// voxelize.frag:228-239 that do not depend on the lights): colour =
+// t * (diffuse * lighting + emission), t = transmittance for transparent
+// materials, else 1.
+__device__ __forceinline__ void voxel_attrs(const vct_material_data& m, V3 nrm, float a[10]) {
+  const bool tr = m.illum == 4 || m.illum == 6 || m.illum == 7 || m.illum == 9;
+  const V3 t = tr ? v3(m.transmittance[0], m.transmittance[1], m.transmittance[2]) : v3(1.f, 1.f, 1.f);
+  const V3 nn = normalize(nrm);
+  a[0] = clamp01(m.diffuse[0] * t.x);
+  a[1] = clamp01(m.diffuse[1] * t.y);
+  a[2] = clamp01(m.diffuse[2] * t.z);
+  a[3] = tr ? clamp01(m.dissolve) : 1.0f;
+  a[4] = clamp01(0.5f * nn.x + 0.5f);
+  a[5] = clamp01(0.5f * nn.y + 0.5f);
+  a[6] = clamp01(0.5f * nn.z + 0.5f);
+  a[7] = clamp01(m.emission[0] * t.x);
+  a[8] = clamp01(m.emission[1] * t.y);
+  a[9] = clamp01(m.emission[2] * t.z);
+}
+template <> struct AccT<kStorageAttr> {
+  uint32_t c[10][kBrickVox];
+  uint32_t n[kBrickVox];
+  __device__ __forceinline__ void clear(int i) {
+#pragma unroll
+    for (int k = 0; k < 10; ++k) c[k][i] = 0;
+    n[i] = 0;
+  }
+  __device__ __forceinline__ void add(const SceneParams&, int v, const vct_material_data& m, V3, V3 nrm) {
+    float a[10];
+    voxel_attrs(m, nrm, a);
+#pragma unroll
+    for (int k = 0; k < 10; ++k) atomicAdd(&c[k][v], __float2uint_rn(a[k] * kFix));
+    atomicAdd(&n[v], 1u);
+  }
+};
+
+// Mean of n 16-bit fixed-point contributions summing to c, as unorm8
+// rounded to nearest (ties up).
+__device__ __forceinline__ unsigned char unorm8_mean(uint32_t c, uint32_t n) {
+  const unsigned long long v = ((unsigned long long)c * 510ull + (unsigned long long)n * 65535ull) /
+                               (2ull * n * 65535ull);
+  return (unsigned char)(v > 255ull ? 255ull : v);
+}
 typedef AccT<VCT_STORAGE_RGBA8> Acc;
 
 // -------------------------------------------------- reference raster mode --
@@ -447,7 +493,7 @@ __device__ __forceinline__ void item_ref(const SceneParams& sp, int N, const int
   const float l0 = __ll2float_rn(w0) / s.farea, l1 = __ll2float_rn(w1) / s.farea, l2 = __ll2float_rn(w2) / s.farea;
   const V3 p = s.gp[0] * l0 + s.gp[1] * l1 + s.gp[2] * l2;
   const V3 n = s.gn[0] * l0 + s.gn[1] * l1 + s.gn[2] * l2;
-  acc.add(sp, (lz * kBrick + ly) * kBrick + lx, voxel_color(sp, sp.materials[s.mat], p, n));
+  acc.add(sp, (lz * kBrick + ly) * kBrick + lx, sp.materials[s.mat], p, n);
 }
 
 // ---------------------------------------------------- conservative mode ----
@@ -575,7 +621,7 @@ __device__ __forceinline__ void item_sat(const SceneParams& sp, int N, const int
   const V3 p = s.gp[0] * w[0] + s.gp[1] * w[1] + s.gp[2] * w[2];
   const V3 n = s.gn[0] * w[0] + s.gn[1] * w[1] + s.gn[2] * w[2];
   const int lx = x - b3[0] * kBrick, ly = y - b3[1] * kBrick, lz = z - b3[2] * kBrick;
-  acc.add(sp, (lz * kBrick + ly) * kBrick + lx, voxel_color(sp, sp.materials[s.mat], p, n));
+  acc.add(sp, (lz * kBrick + ly) * kBrick + lx, sp.materials[s.mat], p, n);
 }
 
 // ------------------------------------------------------------ brick CTA ----
@@ -589,7 +635,7 @@ __device__ __forceinline__ void brick_body(const SceneParams& sp, int N, uint32_
                                            const uint32_t* __restrict__ offset, const uint32_t* __restrict__ list,
                                            uint32_t cap, cudaSurfaceObject_t l0, uint32_t* __restrict__ counts,
                                            FrameStatus* st, AccT<STORAGE>& acc, SetupOf<MODE> (&setup)[kWarps][32],
-                                           int (&excl)[kWarps][33]) {
+                                           int (&excl)[kWarps][33], const InjGrids& inj) {
   const int nb = N / kBrick;
   const int b3[3] = {(int)(brick % nb), (int)((brick / nb) % nb), (int)(brick / ((uint32_t)nb * nb))};
   const uint32_t beg = min(offset[brick], cap), end = min(offset[brick + 1], cap);
@@ -598,8 +644,15 @@ __device__ __forceinline__ void brick_body(const SceneParams& sp, int N, uint32_
     // without the accumulator or its barriers.
     for (int i = threadIdx.x; i < kBrickVox; i += kThreads) {
       const int x = b3[0] * kBrick + (i & 7), y = b3[1] * kBrick + ((i >> 3) & 7), z = b3[2] * kBrick + (i >> 6);
-      if (STORAGE == VCT_STORAGE_RGBA8) surf3Dwrite(make_uchar4(0, 0, 0, 0), l0, x * 4, y, z);
-      else surf3Dwrite(make_ushort4(0, 0, 0, 0), l0, x * 8, y, z);
+      if (STORAGE == kStorageAttr) {
+        surf3Dwrite(make_uchar4(0, 0, 0, 0), inj.albedo, x * 4, y, z);
+        surf3Dwrite(make_uchar4(0, 0, 0, 0), inj.normal, x * 4, y, z);
+        surf3Dwrite(make_uchar4(0, 0, 0, 0), inj.emission, x * 4, y, z);
+      } else if (STORAGE == VCT_STORAGE_RGBA8) {
+        surf3Dwrite(make_uchar4(0, 0, 0, 0), l0, x * 4, y, z);
+      } else {
+        surf3Dwrite(make_ushort4(0, 0, 0, 0), l0, x * 8, y, z);
+      }
       if (counts) counts[((size_t)z * N + y) * N + x] = 0u;
     }
     return;
@@ -645,7 +698,18 @@ __device__ __forceinline__ void brick_body(const SceneParams& sp, int N, uint32_
     const int lx = i & 7, ly = (i >> 3) & 7, lz = i >> 6;
     const int x = b3[0] * kBrick + lx, y = b3[1] * kBrick + ly, z = b3[2] * kBrick + lz;
     if (n > 65535u) atomicAdd(&st->count_saturated, 1u);
-    if (STORAGE == VCT_STORAGE_RGBA8) {
+    if constexpr (STORAGE == kStorageAttr) {
+      uchar4 a = make_uchar4(0, 0, 0, 0), nn = a, e = a;
+      if (n) {
+        a = make_uchar4(unorm8_mean(acc.c[0][i], n), unorm8_mean(acc.c[1][i], n), unorm8_mean(acc.c[2][i], n),
+                        unorm8_mean(acc.c[3][i], n));
+        nn = make_uchar4(unorm8_mean(acc.c[4][i], n), unorm8_mean(acc.c[5][i], n), unorm8_mean(acc.c[6][i], n), 0);
+        e = make_uchar4(unorm8_mean(acc.c[7][i], n), unorm8_mean(acc.c[8][i], n), unorm8_mean(acc.c[9][i], n), 255);
+      }
+      surf3Dwrite(a, inj.albedo, x * 4, y, z);
+      surf3Dwrite(nn, inj.normal, x * 4, y, z);
+      surf3Dwrite(e, inj.emission, x * 4, y, z);
+    } else if (STORAGE == VCT_STORAGE_RGBA8) {
       uchar4 o = make_uchar4(0, 0, 0, 0);
       if (n) {
         const unsigned long long den = 2ull * n * 65535ull;
@@ -676,11 +740,11 @@ template <int MODE, int STORAGE>
 __global__ void __launch_bounds__(kThreads) k_bricks(SceneParams sp, int N, const uint32_t* __restrict__ offset,
                                                      const uint32_t* __restrict__ list, uint32_t cap,
                                                      cudaSurfaceObject_t l0, uint32_t* __restrict__ counts,
-                                                     FrameStatus* st) {
+                                                     FrameStatus* st, InjGrids inj) {
   __shared__ AccT<STORAGE> acc;
   __shared__ SetupOf<MODE> setup[kWarps][32];
   __shared__ int excl[kWarps][33];
-  brick_body<MODE, STORAGE>(sp, N, blockIdx.x, offset, list, cap, l0, counts, st, acc, setup, excl);
+  brick_body<MODE, STORAGE>(sp, N, blockIdx.x, offset, list, cap, l0, counts, st, acc, setup, excl, inj);
 }
 
 // Every scene's bricks in one persistent launch; a CTA takes its next brick
@@ -699,7 +763,7 @@ __global__ void __launch_bounds__(kThreads) k_bricks_batch(BatchWork w, BatchBuf
     const int s = batch_scene_of(w, g);
     const BatchScene& S = w.scenes[s];
     brick_body<MODE, STORAGE>(S.sp, S.N, g - __ldg(w.prefix + s), bb.brick_offset + S.brick_base, bb.pair_list,
-                              bb.pair_cap, S.ms.l0_surf, nullptr, bb.status, acc, setup, excl);
+                              bb.pair_cap, S.ms.l0_surf, nullptr, bb.status, acc, setup, excl, InjGrids{});
     __syncthreads();  // the next brick clears the accumulators; s_next has been read
     if (threadIdx.x == 0) s_next = atomicAdd(w.queue, 1u);
     __syncthreads();
@@ -814,7 +878,7 @@ cudaError_t launch_voxelize_linear(const SceneParams& sp, int N, int mode, const
 }
 
 cudaError_t launch_voxelize(const SceneParams& sp, int N, int mode, int storage, const VoxBuffers& vb,
-                            cudaSurfaceObject_t l0, cudaStream_t st, int* launches) {
+                            cudaSurfaceObject_t l0, cudaStream_t st, int* launches, const InjGrids* inj) {
   int nl = 0;
   const int nb = N / kBrick;
   const size_t n_bricks = (size_t)nb * nb * nb;
@@ -858,20 +922,18 @@ cudaError_t launch_voxelize(const SceneParams& sp, int N, int mode, int storage,
   }
   ++nl;  // k_bricks
   const unsigned grid = (unsigned)n_bricks;
+  const InjGrids g = inj ? *inj : InjGrids{};
+  auto run = [&](auto kern) {
+    kern<<<grid, kThreads, 0, st>>>(sp, N, vb.brick_offset, vb.pair_list, vb.pair_cap, l0, vb.counts, vb.status, g);
+  };
   if (mode == VCT_VOX_CONSERVATIVE) {
-    if (storage == VCT_STORAGE_RGBA8)
-      k_bricks<VCT_VOX_CONSERVATIVE, VCT_STORAGE_RGBA8><<<grid, kThreads, 0, st>>>(
-          sp, N, vb.brick_offset, vb.pair_list, vb.pair_cap, l0, vb.counts, vb.status);
-    else
-      k_bricks<VCT_VOX_CONSERVATIVE, VCT_STORAGE_RGBA16F><<<grid, kThreads, 0, st>>>(
-          sp, N, vb.brick_offset, vb.pair_list, vb.pair_cap, l0, vb.counts, vb.status);
+    if (inj) run(k_bricks<VCT_VOX_CONSERVATIVE, kStorageAttr>);
+    else if (storage == VCT_STORAGE_RGBA8) run(k_bricks<VCT_VOX_CONSERVATIVE, VCT_STORAGE_RGBA8>);
+    else run(k_bricks<VCT_VOX_CONSERVATIVE, VCT_STORAGE_RGBA16F>);
   } else {
-    if (storage == VCT_STORAGE_RGBA8)
-      k_bricks<VCT_VOX_REF_RASTER2X, VCT_STORAGE_RGBA8><<<grid, kThreads, 0, st>>>(
-          sp, N, vb.brick_offset, vb.pair_list, vb.pair_cap, l0, vb.counts, vb.status);
-    else
-      k_bricks<VCT_VOX_REF_RASTER2X, VCT_STORAGE_RGBA16F><<<grid, kThreads, 0, st>>>(
-          sp, N, vb.brick_offset, vb.pair_list, vb.pair_cap, l0, vb.counts, vb.status);
+    if (inj) run(k_bricks<VCT_VOX_REF_RASTER2X, kStorageAttr>);
+    else if (storage == VCT_STORAGE_RGBA8) run(k_bricks<VCT_VOX_REF_RASTER2X, VCT_STORAGE_RGBA8>);
+    else run(k_bricks<VCT_VOX_REF_RASTER2X, VCT_STORAGE_RGBA16F>);
   }
   if (launches) *launches += nl;
   return cudaGetLastError();
@@ -928,6 +990,64 @@ cudaError_t launch_voxelize_batch(const BatchWork& tris, const BatchWork& bricks
   }
   ++nl;
   if (launches) *launches += nl;
+  return cudaGetLastError();
+}
+
+}  // namespace vct
+
+namespace vct {
+namespace {
+
+// Deferred light injection (no reference counterpart: the reference shades
+// every fragment while voxelizing, voxelize.frag:208-239).  Each occupied
+// voxel is lit at its centre (grid space (2x+1)/N - 1) with its mean normal
+// and the same per-light terms as voxelize.frag:208-227:
+//   colour = clamp(albedo * sum_i color_i * intensity_i * max(n.l_i, 0) /
+//                  (1 + d_i^2) + emission, 0, 1),  alpha = mean alpha,
+// stored as RGBA8 rounded to nearest.
+__global__ void __launch_bounds__(256) k_inject(SceneParams sp, int N, InjGrids g, cudaSurfaceObject_t l0) {
+  const size_t total = (size_t)N * N * N;
+  const float k = 1.0f / 255.0f, inv = 2.0f / (float)N;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
+    const int x = (int)(i % N), y = (int)((i / N) % N), z = (int)(i / ((size_t)N * N));
+    uchar4 e;
+    surf3Dread(&e, g.emission, x * 4, y, z);
+    if (e.w == 0) {
+      surf3Dwrite(make_uchar4(0, 0, 0, 0), l0, x * 4, y, z);
+      continue;
+    }
+    uchar4 a, nq;
+    surf3Dread(&a, g.albedo, x * 4, y, z);
+    surf3Dread(&nq, g.normal, x * 4, y, z);
+    const V3 nn = normalize(v3(nq.x * k * 2.0f - 1.0f, nq.y * k * 2.0f - 1.0f, nq.z * k * 2.0f - 1.0f));
+    const V3 pos = v3(((float)x + 0.5f) * inv - 1.0f, ((float)y + 0.5f) * inv - 1.0f, ((float)z + 0.5f) * inv - 1.0f);
+    V3 lit = v3(0.f, 0.f, 0.f);
+    const int nl = min(sp.n_lights, kMaxLights);
+    for (int l = 0; l < nl; ++l) {
+      const vct_point_light& L = sp.lights[l];
+      const V3 lp = v3(L.position[0] / sp.cube_size, L.position[1] / sp.cube_size, L.position[2] / sp.cube_size);
+      const V3 dl = lp - pos;
+      const float d = length(dl);
+      const float cs = fmaxf(dot(nn, normalize(dl)), 0.0f);
+      lit = lit + v3(L.color[0], L.color[1], L.color[2]) * (cs * (1.0f / (1.0f + d * d)) * L.intensity);
+    }
+    const V3 c = mulv(v3(a.x * k, a.y * k, a.z * k), lit) + v3(e.x * k, e.y * k, e.z * k);
+    auto q = [](float v) { return (unsigned char)__float2uint_rz(clamp01(v) * 255.0f + 0.5f); };
+    surf3Dwrite(make_uchar4(q(c.x), q(c.y), q(c.z), a.w), l0, x * 4, y, z);
+  }
+}
+
+}  // namespace
+
+cudaError_t launch_inject(const SceneParams& sp, int N, const InjGrids& g, cudaSurfaceObject_t l0, cudaStream_t st,
+                          int* launches) {
+  int dev = 0, sms = 148;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const size_t total = (size_t)N * N * N;
+  const unsigned grid = (unsigned)std::min<size_t>((total + 255) / 256, (size_t)sms * 16);
+  k_inject<<<grid, 256, 0, st>>>(sp, N, g, l0);
+  if (launches) ++*launches;
   return cudaGetLastError();
 }
 

@@ -217,6 +217,7 @@ struct vct_renderer {
   std::vector<std::unique_ptr<Model>> models;
   uint64_t next_shader = 0;
   bool materials_dirty = true, objs_dirty = true;
+  uint64_t scene_version = 0;  // bumped by every material / draw-object change
   // settings (renderer.h:173-186)
   float view[16], proj[16];
   float cube_size = 1.0f;
@@ -257,6 +258,13 @@ struct vct_renderer {
   bool frame_pending = false;
   bool have_frame = false;
   int launches = 0;  // engine kernels of the last encoded frame
+  // deferred light injection: attribute grids + the geometry they hold
+  bool inject = false;
+  cudaArray_t inj_arr[3] = {};
+  InjGrids inj_g = {};
+  std::vector<unsigned char> inj_key;
+  bool inj_valid = false;
+  bool last_revoxelized = true;
   // learned diffuse term
   int diffuse_mode = VCT_DIFFUSE_CONES;
   MlpState mlp;
@@ -274,12 +282,62 @@ struct vct_renderer {
     if (own_stream) cudaStreamDestroy(own_stream);
   }
 
-  void free_maps() { maps.release(); }
+  void free_maps() {
+    maps.release();
+    free_inj();
+  }
+
+  void free_inj() {
+    cudaSurfaceObject_t* s[3] = {&inj_g.albedo, &inj_g.normal, &inj_g.emission};
+    for (int k = 0; k < 3; ++k) {
+      if (*s[k]) cudaDestroySurfaceObject(*s[k]);
+      *s[k] = 0;
+      if (inj_arr[k]) cudaFreeArray(inj_arr[k]);
+      inj_arr[k] = nullptr;
+    }
+    inj_valid = false;
+  }
+
+  // The three RGBA8 attribute grids of light injection at the current grid.
+  vct_status alloc_inj() {
+    free_inj();
+    const cudaChannelFormatDesc desc = cudaCreateChannelDesc(8, 8, 8, 8, cudaChannelFormatKindUnsigned);
+    cudaSurfaceObject_t* s[3] = {&inj_g.albedo, &inj_g.normal, &inj_g.emission};
+    for (int k = 0; k < 3; ++k) {
+      VCT_CUDA(cudaMalloc3DArray(&inj_arr[k], &desc, make_cudaExtent(res, res, res), cudaArraySurfaceLoadStore));
+      cudaResourceDesc rd;
+      std::memset(&rd, 0, sizeof(rd));
+      rd.resType = cudaResourceTypeArray;
+      rd.res.array.array = inj_arr[k];
+      VCT_CUDA(cudaCreateSurfaceObject(s[k], &rd));
+    }
+    return VCT_OK;
+  }
+
+  // What the attribute grids depend on: queued models and their matrices,
+  // cube size, grid, coverage rule and the material / draw-object tables.
+  std::vector<unsigned char> voxel_key(const FrameInputs& fi) const {
+    std::vector<unsigned char> k;
+    auto put = [&k](const void* p, size_t n) {
+      const unsigned char* c = static_cast<const unsigned char*>(p);
+      k.insert(k.end(), c, c + n);
+    };
+    for (const Queued& q : fi.queue) {
+      put(&q.model, sizeof(q.model));
+      put(q.M, sizeof(q.M));
+    }
+    put(&fi.cube_size, sizeof(fi.cube_size));
+    put(&res, sizeof(res));
+    put(&cfg.vox_mode, sizeof(cfg.vox_mode));
+    put(&scene_version, sizeof(scene_version));
+    return k;
+  }
 
   // set_grid_resolution (renderer.cpp:178-188): six 3D textures of `levels`
   // mip levels.  Here: level 0 once + one chain (levels 1..L-1) per map.
   vct_status alloc_maps(uint32_t r) {
     if (stream) VCT_CUDA(cudaStreamSynchronize(stream));
+    free_inj();
     VCT_CHECK(maps.alloc(r, cfg.mip_mode, cfg.storage));
     const int L = ms.L;
     res = r;
@@ -450,7 +508,23 @@ struct vct_renderer {
     VCT_CUDA(cudaMemsetAsync(d_status.p, 0, sizeof(FrameStatus), stream));
     launches = 0;
     VCT_CUDA(cudaEventRecord(ev[0], stream));
-    VCT_CUDA(launch_voxelize(sp, (int)res, cfg.vox_mode, cfg.storage, vb, ms.l0_surf, stream, &launches));
+    if (inject) {
+      // Re-voxelize the attribute grids only when the geometry changed;
+      // light changes cost one injection pass.
+      std::vector<unsigned char> key = voxel_key(fi);
+      last_revoxelized = !inj_valid || key != inj_key;
+      if (last_revoxelized) {
+        if (!inj_arr[0]) VCT_CHECK(alloc_inj());
+        VCT_CUDA(launch_voxelize(sp, (int)res, cfg.vox_mode, cfg.storage, vb, ms.l0_surf, stream, &launches,
+                                 &inj_g));
+        inj_key.swap(key);
+        inj_valid = true;
+      }
+      VCT_CUDA(launch_inject(sp, (int)res, inj_g, ms.l0_surf, stream, &launches));
+    } else {
+      last_revoxelized = true;
+      VCT_CUDA(launch_voxelize(sp, (int)res, cfg.vox_mode, cfg.storage, vb, ms.l0_surf, stream, &launches));
+    }
     VCT_CUDA(cudaEventRecord(ev[1], stream));
     VCT_CUDA(launch_mipmap(ms, cfg.mip_mode, stream, &launches));
     VCT_CUDA(cudaEventRecord(ev[2], stream));
@@ -500,6 +574,7 @@ struct vct_renderer {
       }
       if (!redo) return VCT_OK;
       if (!have_last) return VCT_OK;
+      inj_valid = false;  // the attribute grids of the overflowed frame are incomplete
       VCT_CHECK(encode(last));
     }
     return set_error(VCT_ERR_CUDA, "frame work lists kept overflowing");

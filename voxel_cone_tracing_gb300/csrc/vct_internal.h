@@ -13,6 +13,16 @@ constexpr int kMaxLights = 10;   // MAX_POINT_LIGHTS, voxelize.frag:126
 constexpr int kMaxLevels = 7;    // create_tex_3d(res,res,res,7), renderer.cpp:186
 constexpr int kBrick = 8;        // voxelizer brick edge (voxels)
 constexpr int kMaxMaps = 6;
+// Internal storage mode of the voxelizer: per-voxel attribute grids for
+// deferred light injection instead of shaded level-0 radiance.
+constexpr int kStorageAttr = 2;
+
+// The attribute grids of light injection (RGBA8, N^3 each): mean albedo x
+// transmittance + mean alpha; mean normal as 0.5 n + 0.5; mean emission x
+// transmittance + occupancy flag (a = 1 where any triangle contributes).
+struct InjGrids {
+  cudaSurfaceObject_t albedo, normal, emission;
+};
 
 // One queued model instance of the frame (queue_model captures the model
 // matrix, renderer.cpp:209-218).
@@ -201,8 +211,13 @@ struct AdamStep {
 
 // ---- launchers (stream-ordered, no host synchronisation) ----------------
 // `launches` (may be null) is incremented by the number of kernels enqueued.
+// With `inj` the voxelizer writes the attribute grids instead of level 0.
 cudaError_t launch_voxelize(const SceneParams& sp, int N, int mode, int storage, const VoxBuffers& vb,
-                            cudaSurfaceObject_t l0, cudaStream_t st, int* launches);
+                            cudaSurfaceObject_t l0, cudaStream_t st, int* launches, const InjGrids* inj = nullptr);
+// Deferred light injection: level 0 (RGBA8) from the attribute grids and the
+// scene's lights.
+cudaError_t launch_inject(const SceneParams& sp, int N, const InjGrids& g, cudaSurfaceObject_t l0, cudaStream_t st,
+                          int* launches);
 // The voxelizer writing RGBA8 level 0 to linear memory (x fastest).
 cudaError_t launch_voxelize_linear(const SceneParams& sp, int N, int mode, const VoxBuffers& vb, uchar4* out,
                                    cudaStream_t st);

@@ -42,7 +42,7 @@ EXPORTS = [
     "vct_mlp_train_samples", "vct_voxelize_noalloc", "vct_batch_create", "vct_batch_destroy",
     "vct_batch_set_camera", "vct_batch_render", "vct_batch_synchronize", "vct_batch_set_stream",
     "vct_batch_read_frame", "vct_batch_read_voxels", "vct_batch_stage_times", "vct_batch_get_shape",
-    "vct_batch_set_shape", "vct_batch_autotune",
+    "vct_batch_set_shape", "vct_batch_autotune", "vct_set_light_injection", "vct_read_injection_grids",
 ]
 DIFFUSE_CONES, DIFFUSE_MLP = 0, 1
 MLP_WEIGHTS = 5 * 64 * 64
@@ -82,7 +82,7 @@ class Config(C.Structure):
 
 class StageTimes(C.Structure):
     _fields_ = [("voxelize", C.c_float), ("mipmap", C.c_float), ("gbuffer", C.c_float), ("trace", C.c_float),
-                ("total", C.c_float), ("kernel_launches", C.c_uint32)]
+                ("total", C.c_float), ("kernel_launches", C.c_uint32), ("voxelized", C.c_uint32)]
 
 
 class DrawObj(C.Structure):
@@ -134,6 +134,7 @@ def lib() -> C.CDLL:
             "vct_batch_read_frame": (I32, [P, U32, P]), "vct_batch_read_voxels": (I32, [P, U32, I32, I32, P]),
             "vct_batch_stage_times": (I32, [P, P]), "vct_batch_get_shape": (I32, [P, P]),
             "vct_batch_set_shape": (I32, [P, P]), "vct_batch_autotune": (I32, [P, I32, P, P, P]),
+            "vct_set_light_injection": (I32, [P, I32]), "vct_read_injection_grids": (I32, [P, P, P, P]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
@@ -274,6 +275,7 @@ class Renderer:
         _check(lib().vct_get_stage_times(self._r, C.byref(t)))
         d = {k: float(getattr(t, k)) for k, _ in StageTimes._fields_}
         d["kernel_launches"] = int(t.kernel_launches)
+        d["voxelized"] = bool(t.voxelized)
         return d
 
     def read_frame(self, fmt: int = FRAME_RGBA8, out: np.ndarray | None = None) -> np.ndarray:
@@ -359,6 +361,17 @@ class Renderer:
         _check(lib().vct_mlp_gradients(self._r, s.ctypes.data, s.shape[0], loss.ctypes.data, dw.ctypes.data,
                                        dt.ctypes.data))
         return float(loss[0]), dw, dt
+
+    def set_light_injection(self, enable: bool) -> None:
+        _check(lib().vct_set_light_injection(self._r, int(bool(enable))))
+
+    def read_injection_grids(self) -> dict:
+        """albedo / normal / emission grids, (N, N, N, 4) uint8 indexed [z, y, x]."""
+        n, _ = self.grid()
+        g = {k: np.empty((n, n, n, 4), np.uint8) for k in ("albedo", "normal", "emission")}
+        _check(lib().vct_read_injection_grids(self._r, g["albedo"].ctypes.data, g["normal"].ctypes.data,
+                                              g["emission"].ctypes.data))
+        return g
 
     def read_gbuffer(self) -> dict:
         h, w = self.height, self.width
@@ -547,6 +560,7 @@ class Batch:
         _check(lib().vct_batch_stage_times(self._b, C.byref(t)))
         d = {k: float(getattr(t, k)) for k, _ in StageTimes._fields_}
         d["kernel_launches"] = int(t.kernel_launches)
+        d["voxelized"] = bool(t.voxelized)
         return d
 
     @property
