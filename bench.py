@@ -292,15 +292,18 @@ def injection_leg(R, torch, scene, steps, flush):
             "stages_ms": {k: round(mean(k), 4) for k in ("voxelize", "mipmap", "gbuffer", "trace")}}
 
 
-def batch_leg(R, torch, steps):
+def batch_leg(R, torch, steps, rank=0, world=1, pg=None):
     """Batched workload: 64 seeded scenes of uneven size (grids 32^3-256^3,
     990-865k triangles, frames 256^2-1920x1080, 9 or 6 diffuse cones), one
     frame of all of them per step: every stage pass one persistent launch
     over all scenes, the frame captured once in a CUDA graph and replayed,
     launch shapes chosen by the autotuner.  Compared with the same 64 scenes
-    rendered one after another by 64 Renderers on one stream."""
-    from voxel_cone_tracing_gb300 import scenes
-    items = scenes.batch_scenes()
+    rendered one after another by 64 Renderers on one stream.  With N ranks
+    the scenes are split between them by cost (no data moves between
+    GPUs); times are the max over ranks."""
+    from voxel_cone_tracing_gb300 import replicas, scenes
+    all_items = scenes.batch_scenes()
+    items = replicas.my_scenes(all_items, rank, world)
     stream = torch.cuda.Stream()
     b = R.Batch(items, use_graph=True)
     b.set_stream(stream.cuda_stream)
@@ -349,10 +352,14 @@ def batch_leg(R, torch, steps):
     for r, _, _ in rs:
         r.close()
     mean = lambda k: statistics.mean(st[k] for st in stages)  # noqa: E731
+    dev_ms = replicas.job_time(statistics.mean(dev), pg, "cuda" if pg else None)
+    seq_ms = replicas.job_time(statistics.mean(seq_wall), pg, "cuda" if pg else None)
+    wall_ms = replicas.job_time(statistics.mean(wall), pg, "cuda" if pg else None)
+    items = all_items
     return {"workload": f"{len(items)} scenes, {sum(it[0].n_tris for it in items)} triangles, "
                         f"{sum(it[1] * it[2] for it in items) / 1e6:.1f} Mpx per frame, grids 32^3-256^3, "
                         "6-9 diffuse cones", "unit": "ms/batch frame",
-            "value": round(statistics.mean(dev), 3), "wall_ms": round(statistics.mean(wall), 3),
+            "value": round(dev_ms, 3), "wall_ms": round(wall_ms, 3), "ranks": world,
             "stages_ms": {k: round(mean(k), 3) for k in ("voxelize", "mipmap", "gbuffer", "trace")},
             "kernel_launches_per_frame": launches, "autotune": tune,
             "sequential_renderers": {"device_ms": round(statistics.mean(seq_dev), 3),
@@ -360,7 +367,7 @@ def batch_leg(R, torch, steps):
                                                    for k in ("voxelize", "mipmap", "gbuffer", "trace")},
                                      "wall_ms": round(statistics.mean(seq_wall), 3),
                                      "kernel_launches_per_frame": seq_launches},
-            "speedup_wall": round(statistics.mean(seq_wall) / statistics.mean(wall), 3)}
+            "speedup_wall": round(seq_ms / wall_ms, 3)}
 
 
 def run_ours(args):
@@ -487,7 +494,7 @@ def run_ours(args):
     if not args.no_precision:
         line["precision"] = precision_leg(R, torch, args.steps)
     if not args.no_batch:
-        line["batch"] = batch_leg(R, torch, max(args.steps, 3))
+        line["batch"] = batch_leg(R, torch, max(args.steps, 3), rank, world, pg)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
         v, ms = cpu_frame_ms(scene, threads, CPU_ROW_STRIDE)
