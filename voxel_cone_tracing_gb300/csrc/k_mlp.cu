@@ -554,7 +554,12 @@ cudaError_t launch_mlp_infer(const MlpParams& p, const SceneParams& sp, const fl
   const size_t smem = sizeof(InferSmem);
   cudaError_t e = cudaFuncSetAttribute(k_mlp_infer, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  k_mlp_infer<<<sm_count() * 2, 256, smem, st>>>(p, sp, gb_pos, gb_nrm, n_px, out);
+  // Persistent: every CTA slot the SMs can hold (the gathers of the hash
+  // encoding need the warps to hide their latency).
+  int per_sm = 1;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_mlp_infer, 256, smem) != cudaSuccess || per_sm < 1)
+    per_sm = 1;
+  k_mlp_infer<<<sm_count() * per_sm, 256, smem, st>>>(p, sp, gb_pos, gb_nrm, n_px, out);
   return cudaGetLastError();
 }
 
