@@ -20,6 +20,8 @@
 
 #include <algorithm>
 
+#include <cuda.h>
+
 #include "vct_internal.h"
 
 namespace vct {
@@ -164,27 +166,14 @@ __device__ __forceinline__ void aniso6_rgba16f(const uint2* ch, uint2* out) {
 
 // One pass: source level `src_level` (0 = the shared level 0) -> levels
 // src_level+1 .. src_level+K of NMAPS maps, one CTA per B^3 source region.
+// Levels src_level+1 .. src_level+K of the B^3 source region at (ox, oy, oz)
+// held in shared memory at `src` ([map][z][y][x]); intermediate levels go to
+// `lvl` (NMAPS * (B/2)^3, (B/4)^3, ...) and every level to its surfaces.
 template <int NMAPS, bool FROM_L0, int K, int STORAGE>
-__device__ __forceinline__ void mip_region(const MapSet& ms, int src_level, uint32_t region, unsigned char* smem_raw) {
+__device__ __forceinline__ void mip_reduce(const MapSet& ms, int src_level, int ox, int oy, int oz,
+                                           const typename Texel<STORAGE>::T* src, typename Texel<STORAGE>::T* lvl) {
   typedef typename Texel<STORAGE>::T T;
   constexpr int B = 1 << K;
-  constexpr int B3 = B * B * B;
-  constexpr int NSRC = FROM_L0 ? 1 : NMAPS;
-  T* src = reinterpret_cast<T*>(smem_raw);
-  T* lvl = src + NSRC * B3;  // level buffers follow, NMAPS * (B/2)^3, (B/4)^3, ...
-  const int S = ms.N >> src_level;
-  const int nbx = S / B;
-  const int bx = region % nbx, by = (region / nbx) % nbx, bz = region / (nbx * nbx);
-  const int ox = bx * B, oy = by * B, oz = bz * B;
-  for (int i = threadIdx.x; i < NSRC * B3; i += kThreads) {
-    const int m = i / B3, r = i % B3;
-    const int x = r % B, y = (r / B) % B, z = r / (B * B);
-    const cudaSurfaceObject_t s = FROM_L0 ? ms.l0_surf : ms.surf[m][src_level];
-    T v;
-    surf3Dread(&v, s, (ox + x) * Texel<STORAGE>::kBytes, oy + y, oz + z);
-    src[i] = v;
-  }
-  __syncthreads();
   const T* cur = src;
   int cur_b = B;
   bool cur_shared = FROM_L0;
@@ -235,6 +224,125 @@ __device__ __forceinline__ void mip_region(const MapSet& ms, int src_level, uint
     cur_b = b;
     cur_shared = false;
     out += NMAPS * b3;
+  }
+}
+
+template <int NMAPS, bool FROM_L0, int K, int STORAGE>
+__device__ __forceinline__ void mip_region(const MapSet& ms, int src_level, uint32_t region, unsigned char* smem_raw) {
+  typedef typename Texel<STORAGE>::T T;
+  constexpr int B = 1 << K;
+  constexpr int B3 = B * B * B;
+  constexpr int NSRC = FROM_L0 ? 1 : NMAPS;
+  T* src = reinterpret_cast<T*>(smem_raw);
+  T* lvl = src + NSRC * B3;  // level buffers follow, NMAPS * (B/2)^3, (B/4)^3, ...
+  const int S = ms.N >> src_level;
+  const int nbx = S / B;
+  const int bx = region % nbx, by = (region / nbx) % nbx, bz = region / (nbx * nbx);
+  const int ox = bx * B, oy = by * B, oz = bz * B;
+  for (int i = threadIdx.x; i < NSRC * B3; i += kThreads) {
+    const int m = i / B3, r = i % B3;
+    const int x = r % B, y = (r / B) % B, z = r / (B * B);
+    const cudaSurfaceObject_t s = FROM_L0 ? ms.l0_surf : ms.surf[m][src_level];
+    T v;
+    surf3Dread(&v, s, (ox + x) * Texel<STORAGE>::kBytes, oy + y, oz + z);
+    src[i] = v;
+  }
+  __syncthreads();
+  mip_reduce<NMAPS, FROM_L0, K, STORAGE>(ms, src_level, ox, oy, oz, src, lvl);
+}
+
+// ---- TMA-staged first pass --------------------------------------------------
+// Level 0 in linear memory is read through a 3D tensor map, one 16^3 box per
+// region, by cp.async.bulk.tensor into shared memory, completing on an
+// mbarrier.  A persistent CTA double-buffers: while it reduces region i it
+// has the copy of region i+1 in flight.  Every wait is bounded; a wait that
+// gives up sets FrameStatus::async_timeout (the host reports an error),
+// waits (bounded) for the copy it still has in flight and leaves.
+constexpr int kTmaBox = 16;
+constexpr uint32_t kWaitLimit = 1u << 24;  // polls (seconds of spinning; a copy takes microseconds)
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+// Arrive (expecting `bytes` of copy traffic) and issue the 3D box load.
+__device__ __forceinline__ void tma_load_box(const CUtensorMap* map, void* dst, uint64_t* bar, uint32_t bytes, int x,
+                                             int y, int z) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];"
+      ::"r"(smem_u32(dst)), "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
+      : "memory");
+}
+
+// Waits for phase `parity` of the barrier; false if it gave up.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+  for (uint32_t it = 0; it < kWaitLimit; ++it) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(done)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+
+template <int NMAPS, int STORAGE>
+__global__ void __launch_bounds__(kThreads) k_mip_tma(const __grid_constant__ CUtensorMap map, MapSet ms,
+                                                      FrameStatus* status) {
+  typedef typename Texel<STORAGE>::T T;
+  constexpr int B3 = kTmaBox * kTmaBox * kTmaBox;
+  constexpr uint32_t kBytes = B3 * sizeof(T);
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  __shared__ __align__(8) uint64_t bar[2];
+  // Copy destinations 128-byte aligned (the launch adds 128 bytes of slack).
+  unsigned char* base = smem_raw + ((128u - (smem_u32(smem_raw) & 127u)) & 127u);
+  T* stage[2] = {reinterpret_cast<T*>(base), reinterpret_cast<T*>(base + kBytes)};
+  T* lvl = reinterpret_cast<T*>(base + 2 * kBytes);
+  const int nbx = ms.N / kTmaBox;
+  const uint32_t total = (uint32_t)nbx * nbx * nbx;
+  auto coords = [nbx](uint32_t r, int& x, int& y, int& z) {
+    x = (int)(r % nbx) * kTmaBox;
+    y = (int)((r / nbx) % nbx) * kTmaBox;
+    z = (int)(r / ((uint32_t)nbx * nbx)) * kTmaBox;
+  };
+  if (threadIdx.x == 0) {
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  uint32_t r = blockIdx.x;
+  if (threadIdx.x == 0 && r < total) {
+    int x, y, z;
+    coords(r, x, y, z);
+    tma_load_box(&map, stage[0], &bar[0], kBytes, x, y, z);
+  }
+  for (uint32_t it = 0; r < total; r += gridDim.x, ++it) {
+    const int s = (int)(it & 1);
+    const uint32_t next = r + gridDim.x;
+    if (threadIdx.x == 0 && next < total) {  // stage s^1 was released by the barrier ending iteration it-1
+      int x, y, z;
+      coords(next, x, y, z);
+      tma_load_box(&map, stage[s ^ 1], &bar[s ^ 1], kBytes, x, y, z);
+    }
+    const bool ok = mbar_wait(&bar[s], (it >> 1) & 1);
+    if (__syncthreads_or(!ok)) {
+      if (threadIdx.x == 0) {
+        atomicOr(&status->async_timeout, 1u);
+        if (next < total) mbar_wait(&bar[s ^ 1], ((it + 1) >> 1) & 1);  // the copy still in flight
+      }
+      __syncthreads();
+      return;
+    }
+    int ox, oy, oz;
+    coords(r, ox, oy, oz);
+    mip_reduce<NMAPS, true, 4, STORAGE>(ms, 0, ox, oy, oz, stage[s], lvl);
+    __syncthreads();  // every thread is done with stage s and the level buffers
   }
 }
 
@@ -341,10 +449,32 @@ cudaError_t run_pass_k(const MapSet& ms, int src_level, int K, cudaStream_t st) 
 }
 
 template <int NMAPS, int STORAGE>
-cudaError_t run_all(const MapSet& ms, cudaStream_t st, int* launches) {
+cudaError_t run_tma(const MapSet& ms, const CUtensorMap* map, FrameStatus* status, cudaStream_t st) {
+  typedef typename Texel<STORAGE>::T T;
+  constexpr int B = kTmaBox;
+  size_t smem = 128 + 2 * (size_t)B * B * B * sizeof(T);
+  for (int l = 1; l <= 4; ++l) smem += (size_t)NMAPS * (B >> l) * (B >> l) * (B >> l) * sizeof(T);
+  auto kern = k_mip_tma<NMAPS, STORAGE>;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  int dev = 0, sms = 148, per_sm = 1;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kThreads, smem) != cudaSuccess || per_sm < 1)
+    per_sm = 1;
+  const int nbx = ms.N / B;
+  const int regions = nbx * nbx * nbx;
+  kern<<<(unsigned)std::max(1, std::min(regions, sms * per_sm)), kThreads, smem, st>>>(*map, ms, status);
+  return cudaGetLastError();
+}
+
+template <int NMAPS, int STORAGE>
+cudaError_t run_all(const MapSet& ms, cudaStream_t st, int* launches, const CUtensorMap* map, FrameStatus* status) {
   const int K1 = ms.L - 1 < 4 ? ms.L - 1 : 4;
   if (K1 < 1) return cudaSuccess;
-  cudaError_t e = run_pass_k<NMAPS, true, STORAGE>(ms, 0, K1, st);
+  // The TMA-staged first pass needs four levels below a 16^3 box.
+  cudaError_t e = (map && status && K1 == 4 && ms.N % kTmaBox == 0) ? run_tma<NMAPS, STORAGE>(ms, map, status, st)
+                                                                     : run_pass_k<NMAPS, true, STORAGE>(ms, 0, K1, st);
   if (e != cudaSuccess) return e;
   if (launches) ++*launches;
   int done = K1;
@@ -387,13 +517,15 @@ __global__ void k_box_mip_rgba8(cudaSurfaceObject_t src, int sw, int sh, int sd,
 
 }  // namespace
 
-cudaError_t launch_mipmap(const MapSet& ms, int mip_mode, cudaStream_t st, int* launches) {
+cudaError_t launch_mipmap(const MapSet& ms, int mip_mode, cudaStream_t st, int* launches, const void* tmap,
+                          FrameStatus* status) {
+  const CUtensorMap* map = static_cast<const CUtensorMap*>(tmap);
   if (mip_mode == VCT_MIP_ISO) {
-    return ms.storage == VCT_STORAGE_RGBA8 ? run_all<1, VCT_STORAGE_RGBA8>(ms, st, launches)
-                                           : run_all<1, VCT_STORAGE_RGBA16F>(ms, st, launches);
+    return ms.storage == VCT_STORAGE_RGBA8 ? run_all<1, VCT_STORAGE_RGBA8>(ms, st, launches, map, status)
+                                           : run_all<1, VCT_STORAGE_RGBA16F>(ms, st, launches, map, status);
   }
-  return ms.storage == VCT_STORAGE_RGBA8 ? run_all<6, VCT_STORAGE_RGBA8>(ms, st, launches)
-                                         : run_all<6, VCT_STORAGE_RGBA16F>(ms, st, launches);
+  return ms.storage == VCT_STORAGE_RGBA8 ? run_all<6, VCT_STORAGE_RGBA8>(ms, st, launches, map, status)
+                                         : run_all<6, VCT_STORAGE_RGBA16F>(ms, st, launches, map, status);
 }
 
 cudaError_t launch_mipmap_batch(const BatchWork& regions, const BatchWork* tail, int n_tail, int storage,

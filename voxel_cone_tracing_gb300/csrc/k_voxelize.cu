@@ -635,7 +635,7 @@ __device__ __forceinline__ void brick_body(const SceneParams& sp, int N, uint32_
                                            const uint32_t* __restrict__ offset, const uint32_t* __restrict__ list,
                                            uint32_t cap, cudaSurfaceObject_t l0, uint32_t* __restrict__ counts,
                                            FrameStatus* st, AccT<STORAGE>& acc, SetupOf<MODE> (&setup)[kWarps][32],
-                                           int (&excl)[kWarps][33], const InjGrids& inj) {
+                                           int (&excl)[kWarps][33], const InjGrids& inj, void* l0_lin) {
   const int nb = N / kBrick;
   const int b3[3] = {(int)(brick % nb), (int)((brick / nb) % nb), (int)(brick / ((uint32_t)nb * nb))};
   const uint32_t beg = min(offset[brick], cap), end = min(offset[brick + 1], cap);
@@ -650,8 +650,10 @@ __device__ __forceinline__ void brick_body(const SceneParams& sp, int N, uint32_
         surf3Dwrite(make_uchar4(0, 0, 0, 0), inj.emission, x * 4, y, z);
       } else if (STORAGE == VCT_STORAGE_RGBA8) {
         surf3Dwrite(make_uchar4(0, 0, 0, 0), l0, x * 4, y, z);
+        if (l0_lin) static_cast<uchar4*>(l0_lin)[((size_t)z * N + y) * N + x] = make_uchar4(0, 0, 0, 0);
       } else {
         surf3Dwrite(make_ushort4(0, 0, 0, 0), l0, x * 8, y, z);
+        if (l0_lin) static_cast<ushort4*>(l0_lin)[((size_t)z * N + y) * N + x] = make_ushort4(0, 0, 0, 0);
       }
       if (counts) counts[((size_t)z * N + y) * N + x] = 0u;
     }
@@ -721,6 +723,7 @@ __device__ __forceinline__ void brick_body(const SceneParams& sp, int N, uint32_
         o = make_uchar4(q[0], q[1], q[2], q[3]);
       }
       surf3Dwrite(o, l0, x * 4, y, z);
+      if (l0_lin) static_cast<uchar4*>(l0_lin)[((size_t)z * N + y) * N + x] = o;
     } else {
       ushort4 o = make_ushort4(0, 0, 0, 0);
       if (n) {
@@ -731,6 +734,7 @@ __device__ __forceinline__ void brick_body(const SceneParams& sp, int N, uint32_
                          __half_as_ushort(__float2half_rn((float)acc.c[3][i] * inv)));
       }
       surf3Dwrite(o, l0, x * 8, y, z);
+      if (l0_lin) static_cast<ushort4*>(l0_lin)[((size_t)z * N + y) * N + x] = o;
     }
     if (counts) counts[((size_t)z * N + y) * N + x] = n;
   }
@@ -740,11 +744,11 @@ template <int MODE, int STORAGE>
 __global__ void __launch_bounds__(kThreads) k_bricks(SceneParams sp, int N, const uint32_t* __restrict__ offset,
                                                      const uint32_t* __restrict__ list, uint32_t cap,
                                                      cudaSurfaceObject_t l0, uint32_t* __restrict__ counts,
-                                                     FrameStatus* st, InjGrids inj) {
+                                                     FrameStatus* st, InjGrids inj, void* l0_lin) {
   __shared__ AccT<STORAGE> acc;
   __shared__ SetupOf<MODE> setup[kWarps][32];
   __shared__ int excl[kWarps][33];
-  brick_body<MODE, STORAGE>(sp, N, blockIdx.x, offset, list, cap, l0, counts, st, acc, setup, excl, inj);
+  brick_body<MODE, STORAGE>(sp, N, blockIdx.x, offset, list, cap, l0, counts, st, acc, setup, excl, inj, l0_lin);
 }
 
 // Every scene's bricks in one persistent launch; a CTA takes its next brick
@@ -763,7 +767,7 @@ __global__ void __launch_bounds__(kThreads) k_bricks_batch(BatchWork w, BatchBuf
     const int s = batch_scene_of(w, g);
     const BatchScene& S = w.scenes[s];
     brick_body<MODE, STORAGE>(S.sp, S.N, g - __ldg(w.prefix + s), bb.brick_offset + S.brick_base, bb.pair_list,
-                              bb.pair_cap, S.ms.l0_surf, nullptr, bb.status, acc, setup, excl, InjGrids{});
+                              bb.pair_cap, S.ms.l0_surf, nullptr, bb.status, acc, setup, excl, InjGrids{}, nullptr);
     __syncthreads();  // the next brick clears the accumulators; s_next has been read
     if (threadIdx.x == 0) s_next = atomicAdd(w.queue, 1u);
     __syncthreads();
@@ -924,7 +928,8 @@ cudaError_t launch_voxelize(const SceneParams& sp, int N, int mode, int storage,
   const unsigned grid = (unsigned)n_bricks;
   const InjGrids g = inj ? *inj : InjGrids{};
   auto run = [&](auto kern) {
-    kern<<<grid, kThreads, 0, st>>>(sp, N, vb.brick_offset, vb.pair_list, vb.pair_cap, l0, vb.counts, vb.status, g);
+    kern<<<grid, kThreads, 0, st>>>(sp, N, vb.brick_offset, vb.pair_list, vb.pair_cap, l0, vb.counts, vb.status, g,
+                                    inj ? nullptr : vb.level0_lin);
   };
   if (mode == VCT_VOX_CONSERVATIVE) {
     if (inj) run(k_bricks<VCT_VOX_CONSERVATIVE, kStorageAttr>);
@@ -1005,7 +1010,8 @@ namespace {
 //   colour = clamp(albedo * sum_i color_i * intensity_i * max(n.l_i, 0) /
 //                  (1 + d_i^2) + emission, 0, 1),  alpha = mean alpha,
 // stored as RGBA8 rounded to nearest.
-__global__ void __launch_bounds__(256) k_inject(SceneParams sp, int N, InjGrids g, cudaSurfaceObject_t l0) {
+__global__ void __launch_bounds__(256) k_inject(SceneParams sp, int N, InjGrids g, cudaSurfaceObject_t l0,
+                                                uchar4* __restrict__ l0_lin) {
   const size_t total = (size_t)N * N * N;
   const float k = 1.0f / 255.0f, inv = 2.0f / (float)N;
   for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
@@ -1014,6 +1020,7 @@ __global__ void __launch_bounds__(256) k_inject(SceneParams sp, int N, InjGrids 
     surf3Dread(&e, g.emission, x * 4, y, z);
     if (e.w == 0) {
       surf3Dwrite(make_uchar4(0, 0, 0, 0), l0, x * 4, y, z);
+      if (l0_lin) l0_lin[i] = make_uchar4(0, 0, 0, 0);
       continue;
     }
     uchar4 a, nq;
@@ -1033,20 +1040,22 @@ __global__ void __launch_bounds__(256) k_inject(SceneParams sp, int N, InjGrids 
     }
     const V3 c = mulv(v3(a.x * k, a.y * k, a.z * k), lit) + v3(e.x * k, e.y * k, e.z * k);
     auto q = [](float v) { return (unsigned char)__float2uint_rz(clamp01(v) * 255.0f + 0.5f); };
-    surf3Dwrite(make_uchar4(q(c.x), q(c.y), q(c.z), a.w), l0, x * 4, y, z);
+    const uchar4 o = make_uchar4(q(c.x), q(c.y), q(c.z), a.w);
+    surf3Dwrite(o, l0, x * 4, y, z);
+    if (l0_lin) l0_lin[i] = o;
   }
 }
 
 }  // namespace
 
-cudaError_t launch_inject(const SceneParams& sp, int N, const InjGrids& g, cudaSurfaceObject_t l0, cudaStream_t st,
-                          int* launches) {
+cudaError_t launch_inject(const SceneParams& sp, int N, const InjGrids& g, cudaSurfaceObject_t l0, uchar4* l0_lin,
+                          cudaStream_t st, int* launches) {
   int dev = 0, sms = 148;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   const size_t total = (size_t)N * N * N;
   const unsigned grid = (unsigned)std::min<size_t>((total + 255) / 256, (size_t)sms * 16);
-  k_inject<<<grid, 256, 0, st>>>(sp, N, g, l0);
+  k_inject<<<grid, 256, 0, st>>>(sp, N, g, l0, l0_lin);
   if (launches) ++*launches;
   return cudaGetLastError();
 }

@@ -2,6 +2,8 @@
 // translation units of the C ABI; not a public header).
 #pragma once
 
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_fp16.h>
 
 #include <algorithm>
@@ -78,6 +80,31 @@ struct Queued {
   uint64_t model;
   float M[16];
 };
+
+// A 3D tensor map (TMA descriptor) over a dense N^3 array of `elem_bytes`
+// texels, boxes of 16^3, for the MipBuilder's bulk-tensor copies.  The
+// driver's encoder is reached through the runtime's entry-point query, so
+// the library does not link libcuda.
+inline vct_status encode_box_map(CUtensorMap* map, void* base, uint32_t N, uint32_t elem_bytes) {
+  static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
+  if (!encode) {
+    void* fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    VCT_CUDA(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q));
+    if (q != cudaDriverEntryPointSuccess || !fn)
+      return set_error(VCT_ERR_UNSUPPORTED, "cuTensorMapEncodeTiled is not available");
+    encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+  }
+  const cuuint64_t dims[3] = {N, N, N};
+  const cuuint64_t strides[2] = {(cuuint64_t)N * elem_bytes, (cuuint64_t)N * N * elem_bytes};  // bytes, dims 1..2
+  const cuuint32_t box[3] = {16, 16, 16};
+  const cuuint32_t estr[3] = {1, 1, 1};
+  const CUresult r = encode(map, elem_bytes == 8 ? CU_TENSOR_MAP_DATA_TYPE_INT64 : CU_TENSOR_MAP_DATA_TYPE_UINT32, 3,
+                            base, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                            CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return set_error(VCT_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
+  return VCT_OK;
+}
 
 // Everything a frame reads, captured by vct_render so that a frame can be
 // re-encoded after its work buffers were grown.
@@ -238,6 +265,9 @@ struct vct_renderer {
   cudaEvent_t ev_done = nullptr;   // after the frame's status copy
   MapStore maps;
   MapSet& ms = maps.ms;
+  DevBuf<unsigned char> l0_lin;  // level 0 also in linear memory (the MipBuilder's TMA source)
+  CUtensorMap l0_map;
+  bool have_l0_map = false;
   DevBuf<vct_material_data> d_materials;
   DevBuf<uint32_t> d_obj_material;
   DevBuf<DevInstance> d_inst;
@@ -340,6 +370,13 @@ struct vct_renderer {
     free_inj();
     VCT_CHECK(maps.alloc(r, cfg.mip_mode, cfg.storage));
     const int L = ms.L;
+    const uint32_t tb = cfg.storage == VCT_STORAGE_RGBA16F ? 8u : 4u;
+    have_l0_map = false;
+    if (r >= 16) {
+      VCT_CHECK(l0_lin.ensure((size_t)r * r * r * tb));
+      VCT_CHECK(encode_box_map(&l0_map, l0_lin.p, r, tb));
+      have_l0_map = true;
+    }
     res = r;
     levels = L;
     const size_t nb = (size_t)(r / kBrick) * (r / kBrick) * (r / kBrick);
@@ -493,6 +530,7 @@ struct vct_renderer {
     vb.big = bin_big.p;
     vb.big_cap = bin_big_cap;
     vb.big_count = bin_big_count.p;
+    vb.level0_lin = have_l0_map ? (void*)l0_lin.p : nullptr;
 
     RasterBuffers rb;
     rb.vis = vis.p;
@@ -520,13 +558,14 @@ struct vct_renderer {
         inj_key.swap(key);
         inj_valid = true;
       }
-      VCT_CUDA(launch_inject(sp, (int)res, inj_g, ms.l0_surf, stream, &launches));
+      VCT_CUDA(launch_inject(sp, (int)res, inj_g, ms.l0_surf, have_l0_map ? (uchar4*)l0_lin.p : nullptr, stream,
+                             &launches));
     } else {
       last_revoxelized = true;
       VCT_CUDA(launch_voxelize(sp, (int)res, cfg.vox_mode, cfg.storage, vb, ms.l0_surf, stream, &launches));
     }
     VCT_CUDA(cudaEventRecord(ev[1], stream));
-    VCT_CUDA(launch_mipmap(ms, cfg.mip_mode, stream, &launches));
+    VCT_CUDA(launch_mipmap(ms, cfg.mip_mode, stream, &launches, have_l0_map ? &l0_map : nullptr, d_status.p));
     VCT_CUDA(cudaEventRecord(ev[2], stream));
     VCT_CUDA(launch_gbuffer(sp, cp, rb, stream, &launches));
     VCT_CUDA(cudaEventRecord(ev[3], stream));
@@ -559,6 +598,7 @@ struct vct_renderer {
       VCT_CUDA(cudaStreamSynchronize(stream));
       frame_pending = false;
       const FrameStatus s = *h_status.p;
+      if (s.async_timeout) return set_error(VCT_ERR_CUDA, "a bulk copy of the MipBuilder did not complete");
       bool redo = false;
       if (s.pair_total > pair_list.n) {
         VCT_CHECK(pair_list.ensure((size_t)s.pair_total + s.pair_total / 4 + 4096));

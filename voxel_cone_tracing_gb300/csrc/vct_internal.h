@@ -60,7 +60,8 @@ struct FrameStatus {
   uint32_t rejected_tris;   // non-finite / out-of-range triangles
   uint32_t count_saturated; // voxels with > 65535 contributions
   uint32_t bigtri_total;    // large-triangle binning records needed
-  uint32_t pad[2];
+  uint32_t async_timeout;   // a bounded wait for a bulk copy gave up (never expected)
+  uint32_t pad;
 };
 
 // A triangle with many candidate bricks, binned by k_bin_big.
@@ -93,6 +94,7 @@ struct VoxBuffers {
   BinRec* big;             // large-triangle records (nullptr: bin them in-warp)
   uint32_t big_cap;
   uint32_t* big_count;
+  void* level0_lin;        // level 0 also in linear memory (x fastest), or null
 };
 
 struct RasterBuffers {
@@ -216,12 +218,15 @@ cudaError_t launch_voxelize(const SceneParams& sp, int N, int mode, int storage,
                             cudaSurfaceObject_t l0, cudaStream_t st, int* launches, const InjGrids* inj = nullptr);
 // Deferred light injection: level 0 (RGBA8) from the attribute grids and the
 // scene's lights.
-cudaError_t launch_inject(const SceneParams& sp, int N, const InjGrids& g, cudaSurfaceObject_t l0, cudaStream_t st,
-                          int* launches);
+cudaError_t launch_inject(const SceneParams& sp, int N, const InjGrids& g, cudaSurfaceObject_t l0, uchar4* l0_lin,
+                          cudaStream_t st, int* launches);
 // The voxelizer writing RGBA8 level 0 to linear memory (x fastest).
 cudaError_t launch_voxelize_linear(const SceneParams& sp, int N, int mode, const VoxBuffers& vb, uchar4* out,
                                    cudaStream_t st);
-cudaError_t launch_mipmap(const MapSet& ms, int mip_mode, cudaStream_t st, int* launches);
+// `tmap` (a CUtensorMap over the linear level 0, or null): the first pass
+// stages level 0 through TMA bulk-tensor copies; `status` receives timeouts.
+cudaError_t launch_mipmap(const MapSet& ms, int mip_mode, cudaStream_t st, int* launches, const void* tmap = nullptr,
+                          FrameStatus* status = nullptr);
 cudaError_t launch_gbuffer(const SceneParams& sp, const CameraParams& cp, const RasterBuffers& rb,
                            cudaStream_t st, int* launches);
 cudaError_t launch_trace(const SceneParams& sp, const CameraParams& cp, const MapSet& ms, const TraceParams& tp,
