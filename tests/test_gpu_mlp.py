@@ -67,6 +67,23 @@ def test_forward_matches_oracle(net, oracle):
     assert np.abs(got - ref).max() <= 0.03 * scale, (np.abs(got - ref).max(), scale)
 
 
+def test_forward_tcgen05_matches_oracle_and_warp_tiles(net, oracle):
+    """The forward on tcgen05 / TMEM (128-row tiles, several tiles and a
+    ragged last one) against the oracle and the mma.sync warp tiles: same
+    BF16 operands, FP32 accumulation in a different order."""
+    r, t, w = net
+    rows = _rows(np.random.default_rng(2), 3 * 128 + 37)
+    r.mlp_set_tensor_kernels(True)
+    tc = r.mlp_eval(rows)
+    r.mlp_set_tensor_kernels(False)
+    ws = r.mlp_eval(rows)
+    ref = oracle.mlp_forward(_cfg(oracle), t, w, rows[:, 0:3], rows[:, 3:6], rows[:, 6:9])
+    scale = np.abs(ref).max()
+    print(f"tcgen05 vs oracle {np.abs(tc - ref).max() / scale:.2e}, vs warp tiles {np.abs(tc - ws).max() / scale:.2e}")
+    assert np.abs(tc - ref).max() <= 0.03 * scale
+    assert np.abs(tc - ws).max() <= 0.01 * scale
+
+
 @pytest.mark.parametrize("n, tol", [(2, 0.03), (96, 0.12)])
 def test_gradients_match_oracle(net, oracle, n, tol):
     """Per-sample gradients agree to BF16 precision (~1%); summed over many
@@ -152,6 +169,12 @@ def test_learned_diffuse_replaces_cones(vct):
     rep = r.mlp_train(vct.mlp_desc(n_max=256, seed=1, steps=600, batch=1 << 16, n_samples=1 << 20))
     r.set_diffuse_mode(vct.DIFFUSE_MLP)
     learned = frame()
+    r.mlp_set_tensor_kernels(True)
+    learned_tc = frame()
+    r.mlp_set_tensor_kernels(False)
+    q_kernels = psnr(np.clip(learned_tc, 0, 1), np.clip(learned, 0, 1))
+    print(f"learned frame, tcgen05 vs warp-tile inference: PSNR {q_kernels:.1f} dB")
+    assert q_kernels >= 50.0
     q_learned = psnr(np.clip(learned, 0, 1), np.clip(cones, 0, 1))
     q_untrained = psnr(np.clip(untrained, 0, 1), np.clip(cones, 0, 1))
     print(f"diffuse-only PSNR: learned {q_learned:.1f} dB, untrained {q_untrained:.1f} dB, report {rep}")

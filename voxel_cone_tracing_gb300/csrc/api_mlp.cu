@@ -272,9 +272,15 @@ extern "C" vct_status vct_mlp_eval(vct_renderer* r, const float* samples, uint32
   VCT_CHECK(in.ensure((size_t)n * 12));
   VCT_CHECK(out.ensure((size_t)n * 3));
   VCT_CUDA(cudaMemcpyAsync(in.p, samples, (size_t)n * 12 * sizeof(float), cudaMemcpyHostToDevice, r->stream));
-  VCT_CUDA(launch_mlp_eval(r->mlp.params(), in.p, (int)n, out.p, r->stream));
+  DevBuf<FrameStatus> st;
+  VCT_CHECK(st.ensure(1));
+  VCT_CUDA(cudaMemsetAsync(st.p, 0, sizeof(FrameStatus), r->stream));
+  VCT_CUDA(launch_mlp_eval(r->mlp.params(), in.p, (int)n, out.p, r->stream, r->mlp.tc, st.p));
   VCT_CUDA(cudaMemcpyAsync(rgb_out, out.p, (size_t)n * 3 * sizeof(float), cudaMemcpyDeviceToHost, r->stream));
+  FrameStatus hs;
+  VCT_CUDA(cudaMemcpyAsync(&hs, st.p, sizeof(FrameStatus), cudaMemcpyDeviceToHost, r->stream));
   VCT_CUDA(cudaStreamSynchronize(r->stream));
+  if (hs.async_timeout) return set_error(VCT_ERR_CUDA, "a tensor-core group did not complete");
   return VCT_OK;
 }
 
@@ -385,5 +391,13 @@ extern "C" vct_status vct_mlp_load(vct_renderer* r, const char* path) {
   m.adam_t = h.adam_t;
   VCT_CHECK(refresh_bf16(r));
   m.trained = true;
+  return VCT_OK;
+}
+
+extern "C" vct_status vct_mlp_set_tensor_kernels(vct_renderer* r, int32_t use_tcgen05) {
+  clear_error();
+  if (!r) return set_error(VCT_ERR_INVALID_VALUE, "NULL renderer");
+  VCT_CHECK(r->finish());
+  r->mlp.tc = use_tcgen05 != 0;
   return VCT_OK;
 }

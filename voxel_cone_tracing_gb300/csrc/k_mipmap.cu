@@ -22,6 +22,7 @@
 
 #include <cuda.h>
 
+#include "vct_async.cuh"
 #include "vct_internal.h"
 
 namespace vct {
@@ -259,38 +260,6 @@ __device__ __forceinline__ void mip_region(const MapSet& ms, int src_level, uint
 // gives up sets FrameStatus::async_timeout (the host reports an error),
 // waits (bounded) for the copy it still has in flight and leaves.
 constexpr int kTmaBox = 16;
-constexpr uint32_t kWaitLimit = 1u << 24;  // polls (seconds of spinning; a copy takes microseconds)
-
-__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
-
-__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
-}
-
-// Arrive (expecting `bytes` of copy traffic) and issue the 3D box load.
-__device__ __forceinline__ void tma_load_box(const CUtensorMap* map, void* dst, uint64_t* bar, uint32_t bytes, int x,
-                                             int y, int z) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
-  asm volatile(
-      "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];"
-      ::"r"(smem_u32(dst)), "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
-      : "memory");
-}
-
-// Waits for phase `parity` of the barrier; false if it gave up.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
-  for (uint32_t it = 0; it < kWaitLimit; ++it) {
-    uint32_t done;
-    asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
-        : "=r"(done)
-        : "r"(smem_u32(bar)), "r"(parity)
-        : "memory");
-    if (done) return true;
-  }
-  return false;
-}
-
 template <int NMAPS, int STORAGE>
 __global__ void __launch_bounds__(kThreads) k_mip_tma(const __grid_constant__ CUtensorMap map, MapSet ms,
                                                       FrameStatus* status) {
@@ -313,14 +282,14 @@ __global__ void __launch_bounds__(kThreads) k_mip_tma(const __grid_constant__ CU
   if (threadIdx.x == 0) {
     mbar_init(&bar[0], 1);
     mbar_init(&bar[1], 1);
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    mbar_init_fence();
   }
   __syncthreads();
   uint32_t r = blockIdx.x;
   if (threadIdx.x == 0 && r < total) {
     int x, y, z;
     coords(r, x, y, z);
-    tma_load_box(&map, stage[0], &bar[0], kBytes, x, y, z);
+    tma_load_box3(&map, stage[0], &bar[0], kBytes, x, y, z);
   }
   for (uint32_t it = 0; r < total; r += gridDim.x, ++it) {
     const int s = (int)(it & 1);
@@ -328,7 +297,7 @@ __global__ void __launch_bounds__(kThreads) k_mip_tma(const __grid_constant__ CU
     if (threadIdx.x == 0 && next < total) {  // stage s^1 was released by the barrier ending iteration it-1
       int x, y, z;
       coords(next, x, y, z);
-      tma_load_box(&map, stage[s ^ 1], &bar[s ^ 1], kBytes, x, y, z);
+      tma_load_box3(&map, stage[s ^ 1], &bar[s ^ 1], kBytes, x, y, z);
     }
     const bool ok = mbar_wait(&bar[s], (it >> 1) & 1);
     if (__syncthreads_or(!ok)) {

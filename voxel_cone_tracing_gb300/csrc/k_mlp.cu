@@ -21,6 +21,10 @@
 // table gradient (float2 atomics).  Adam runs as a separate elementwise pass.
 #include <cuda_bf16.h>
 
+#include <algorithm>
+#include <cstring>
+
+#include "vct_async.cuh"
 #include "vct_internal.h"
 #include "vct_math.cuh"
 
@@ -514,6 +518,178 @@ __global__ void __launch_bounds__(256) k_mlp_eval(MlpParams p, const float* __re
   }
 }
 
+// ---- forward on the 5th-generation tensor cores ----------------------------
+// A CTA takes tiles of 128 rows.  The activation tile (128 x 64 BF16) and
+// the weights live in shared memory in the canonical K-major layout of
+// tcgen05.mma without swizzle (8-row x 16-byte core matrices: element
+// (r, k) at (r/8)*512 + (k/8)*64 + (r%8)*8 + k%8); one thread issues the four
+// K=16 steps of a layer into a TMEM accumulator (128 lanes = rows, 64 FP32
+// columns) and commits them to an mbarrier; then every warp reads its rows
+// back with tcgen05.ld (warp w: TMEM lanes 32*(w%4)..+31, columns
+// 32*(w/4)..+31), applies ReLU, packs to BF16 and writes the tile of the next
+// layer.  The inputs are the same as the warp-tile kernels' (hash encoding,
+// normal, albedo, 1).
+constexpr int kTcRows = 128;
+constexpr int kTcThreads = 256;
+constexpr uint32_t kTcCols = 64;  // TMEM columns allocated per CTA
+constexpr uint32_t kCoreLbo = 128, kCoreSbo = 1024;
+
+__device__ __forceinline__ int umma_elem(int r, int k) { return (r >> 3) * 512 + (k >> 3) * 64 + (r & 7) * 8 + (k & 7); }
+
+struct TcSmem {
+  unsigned short w[4][64 * 64];   // W1..W4 (rows = outputs), canonical layout
+  unsigned short w5[16 * 64];     // W5 (16 output rows, 3 used)
+  unsigned short a[kTcRows * 64]; // activations of the current layer
+  uint64_t bar;
+  uint32_t tmem;
+};
+
+__device__ __forceinline__ uint4 pack8(const float* x) {
+  return make_uint4(pack_bf16(x[0], x[1]), pack_bf16(x[2], x[3]), pack_bf16(x[4], x[5]), pack_bf16(x[6], x[7]));
+}
+
+template <bool FROM_GBUF>
+__global__ void __launch_bounds__(kTcThreads, 4)
+    k_mlp_fwd_tc(MlpParams p, SceneParams sp, const float4* __restrict__ gb_pos, const float4* __restrict__ gb_nrm,
+                 const float* __restrict__ samples, int n, float4* __restrict__ out4, float* __restrict__ out3,
+                 FrameStatus* status) {
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  TcSmem& S = *reinterpret_cast<TcSmem*>(smem_raw + ((128u - (smem_u32(smem_raw) & 127u)) & 127u));
+  const int tid = threadIdx.x, warp = tid >> 5, row = tid & (kTcRows - 1), half = tid >> 7;
+  const unsigned short* g = reinterpret_cast<const unsigned short*>(p.w_bf);
+  for (int i = tid; i < 4 * 64 * 64; i += kTcThreads) {
+    const int l = i >> 12, o = (i >> 6) & 63, k = i & 63;
+    S.w[l][umma_elem(o, k)] = g[i];
+  }
+  for (int i = tid; i < 16 * 64; i += kTcThreads) S.w5[umma_elem(i >> 6, i & 63)] = g[4 * 4096 + i];
+  if (tid == 0) {
+    mbar_init(&S.bar, 1);
+    mbar_init_fence();
+  }
+  __syncwarp();
+  if (warp == 0) tc_alloc(&S.tmem, kTcCols);
+  fence_async_smem();
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = S.tmem;
+  const uint32_t lane_addr = tmem + ((uint32_t)((warp & 3) * 32) << 16);
+  const float inv_cube = 1.0f / sp.cube_size;
+  uint32_t phase = 0;
+  bool ok = true;
+  const int tiles = (n + kTcRows - 1) / kTcRows;
+  for (int tile = blockIdx.x; tile < tiles && ok; tile += gridDim.x) {
+    const int r = tile * kTcRows + row;
+    V3 pos = v3(0.f, 0.f, 0.f), nrm = pos, alb = pos;
+    bool valid = false;
+    if (FROM_GBUF) {
+      if (r < n) {
+        const float4 a = gb_pos[r], c = gb_nrm[r];
+        if (__float_as_uint(c.w) != 0xffffffffu) {
+          valid = true;
+          pos = v3(a.x * inv_cube, a.y * inv_cube, a.z * inv_cube) * 0.5f + v3(0.5f, 0.5f, 0.5f);
+          nrm = v3(c.x, c.y, c.z);
+          const vct_material_data& m = sp.materials[__float_as_uint(a.w)];
+          alb = v3(m.diffuse[0], m.diffuse[1], m.diffuse[2]);
+        }
+      }
+    } else if (r < n) {
+      const float* q = samples + (size_t)r * 12;
+      valid = true;
+      pos = v3(q[0], q[1], q[2]);
+      nrm = v3(q[3], q[4], q[5]);
+      alb = v3(q[6], q[7], q[8]);
+    }
+    // Inputs: half 0 the hash levels 0..7 (k 0..15), half 1 levels 8..15
+    // (k 16..31) and normal, albedo, 1, zeros (k 32..63).
+    float x[16];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      const float2 f = valid ? level_features(p, 8 * half + j, pos) : make_float2(0.f, 0.f);
+      x[2 * j] = f.x;
+      x[2 * j + 1] = f.y;
+    }
+    uint4* arow = reinterpret_cast<uint4*>(S.a);
+    arow[umma_elem(row, 16 * half) / 8] = pack8(x);
+    arow[umma_elem(row, 16 * half + 8) / 8] = pack8(x + 8);
+    if (half) {
+      const V3 nn = normalize(nrm);
+      float e[32];
+#pragma unroll
+      for (int i = 0; i < 32; ++i) e[i] = 0.f;
+      if (valid) {
+        e[0] = nn.x; e[1] = nn.y; e[2] = nn.z;
+        e[3] = alb.x; e[4] = alb.y; e[5] = alb.z;
+        e[6] = 1.0f;
+      }
+#pragma unroll
+      for (int c = 0; c < 4; ++c) arow[umma_elem(row, 32 + 8 * c) / 8] = pack8(e + 8 * c);
+    }
+    fence_async_smem();
+    tc_fence_before();
+    __syncthreads();
+    for (int layer = 0; layer < 5 && ok; ++layer) {
+      const int N = layer < 4 ? 64 : 16;
+      if (tid == 0) {
+        tc_fence_after();
+        const unsigned short* W = layer < 4 ? S.w[layer] : S.w5;
+#pragma unroll
+        for (int kk = 0; kk < 4; ++kk)
+          tc_mma_bf16(tmem, tc_smem_desc(S.a + 128 * kk, kCoreLbo, kCoreSbo),
+                      tc_smem_desc(W + 128 * kk, kCoreLbo, kCoreSbo), tc_idesc_bf16(kTcRows, N), kk > 0 ? 1u : 0u);
+        tc_commit(&S.bar);
+      }
+      const bool done = mbar_wait(&S.bar, phase & 1);
+      ++phase;
+      if (__syncthreads_or(!done)) {
+        ok = false;
+        break;
+      }
+      tc_fence_after();
+      if (layer < 4) {
+        float v[16], w[16];
+        tc_ld16(lane_addr + 32 * half, v);
+        tc_ld16(lane_addr + 32 * half + 16, w);
+        tc_wait_ld();
+#pragma unroll
+        for (int i = 0; i < 16; ++i) {
+          v[i] = fmaxf(v[i], 0.f);
+          w[i] = fmaxf(w[i], 0.f);
+        }
+        arow[umma_elem(row, 32 * half) / 8] = pack8(v);
+        arow[umma_elem(row, 32 * half + 8) / 8] = pack8(v + 8);
+        arow[umma_elem(row, 32 * half + 16) / 8] = pack8(w);
+        arow[umma_elem(row, 32 * half + 24) / 8] = pack8(w + 8);
+        fence_async_smem();
+      } else if (half == 0) {
+        float v[16];
+        tc_ld16(lane_addr, v);
+        tc_wait_ld();
+        if (r < n) {
+          if (FROM_GBUF) out4[r] = make_float4(v[0], v[1], v[2], 0.f);
+          else {
+            out3[3 * r] = v[0];
+            out3[3 * r + 1] = v[1];
+            out3[3 * r + 2] = v[2];
+          }
+        }
+      }
+      tc_fence_before();
+      __syncthreads();
+    }
+  }
+  __syncthreads();
+  if (!ok && tid == 0) {
+    atomicOr(&status->async_timeout, 1u);
+    mbar_wait(&S.bar, phase & 1);  // the group still in flight, if any
+  }
+  __syncthreads();
+  if (warp == 0) {
+    tc_fence_after();
+    tc_dealloc(tmem, kTcCols);
+  }
+}
+
 int sm_count() {
   int dev = 0, sms = 148;
   cudaGetDevice(&dev);
@@ -549,8 +725,32 @@ cudaError_t launch_adam(float* prm, float* grad, float* m, float* v, __nv_bfloat
   return cudaGetLastError();
 }
 
+namespace {
+
+template <bool FROM_GBUF>
+cudaError_t run_fwd_tc(const MlpParams& p, const SceneParams& sp, const float4* gb_pos, const float4* gb_nrm,
+                       const float* samples, int n, float4* out4, float* out3, cudaStream_t st, FrameStatus* status) {
+  if (n <= 0) return cudaSuccess;
+  const size_t smem = sizeof(TcSmem) + 128;
+  auto kern = k_mlp_fwd_tc<FROM_GBUF>;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  int per_sm = 1;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kTcThreads, smem) != cudaSuccess || per_sm < 1)
+    per_sm = 1;
+  // Each resident CTA holds kTcCols of the SM's 512 TMEM columns.
+  per_sm = std::min(per_sm, (int)(512 / kTcCols));
+  const int tiles = (n + kTcRows - 1) / kTcRows;
+  kern<<<std::max(1, std::min(tiles, sm_count() * per_sm)), kTcThreads, smem, st>>>(p, sp, gb_pos, gb_nrm, samples, n,
+                                                                                  out4, out3, status);
+  return cudaGetLastError();
+}
+
+}  // namespace
+
 cudaError_t launch_mlp_infer(const MlpParams& p, const SceneParams& sp, const float4* gb_pos, const float4* gb_nrm,
-                             int n_px, float4* out, cudaStream_t st) {
+                             int n_px, float4* out, cudaStream_t st, bool tc, FrameStatus* status) {
+  if (tc) return run_fwd_tc<true>(p, sp, gb_pos, gb_nrm, nullptr, n_px, out, nullptr, st, status);
   const size_t smem = sizeof(InferSmem);
   cudaError_t e = cudaFuncSetAttribute(k_mlp_infer, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
@@ -563,7 +763,14 @@ cudaError_t launch_mlp_infer(const MlpParams& p, const SceneParams& sp, const fl
   return cudaGetLastError();
 }
 
-cudaError_t launch_mlp_eval(const MlpParams& p, const float* samples, int n, float* out, cudaStream_t st) {
+cudaError_t launch_mlp_eval(const MlpParams& p, const float* samples, int n, float* out, cudaStream_t st, bool tc,
+                            FrameStatus* status) {
+  if (tc) {
+    SceneParams sp;
+    std::memset(&sp, 0, sizeof(sp));
+    sp.cube_size = 1.0f;
+    return run_fwd_tc<false>(p, sp, nullptr, nullptr, samples, n, nullptr, out, st, status);
+  }
   const size_t smem = sizeof(InferSmem);
   cudaError_t e = cudaFuncSetAttribute(k_mlp_eval, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;

@@ -127,6 +127,7 @@ using namespace vct::detail;
 struct MlpState {
   bool ready = false;  // parameters allocated and initialised
   bool trained = false;
+  bool tc = false;     // forward on tcgen05 / TMEM (else mma.sync warp tiles)
   int32_t levels = 16, log2_table = 19, n_min = 16, n_max = 512;
   int adam_t = 0;
   DevBuf<float> table, table_grad, table_m, table_v;  // levels * T * 2
@@ -574,7 +575,7 @@ struct vct_renderer {
     if (diffuse_mode == VCT_DIFFUSE_MLP && mlp.trained && tp.enable_diffuse && tp.view_voxel_dir >= 7) {
       // The learned term replaces the nine diffuse cones (its time counts as trace time).
       VCT_CHECK(diffuse_px.ensure((size_t)W * H));
-      VCT_CUDA(launch_mlp_infer(mlp.params(), sp, gb_pos.p, gb_nrm.p, W * H, diffuse_px.p, stream));
+      VCT_CUDA(launch_mlp_infer(mlp.params(), sp, gb_pos.p, gb_nrm.p, W * H, diffuse_px.p, stream, mlp.tc, d_status.p));
       ++launches;
       tp.diffuse_in = diffuse_px.p;
     }
@@ -598,7 +599,7 @@ struct vct_renderer {
       VCT_CUDA(cudaStreamSynchronize(stream));
       frame_pending = false;
       const FrameStatus s = *h_status.p;
-      if (s.async_timeout) return set_error(VCT_ERR_CUDA, "a bulk copy of the MipBuilder did not complete");
+      if (s.async_timeout) return set_error(VCT_ERR_CUDA, "an asynchronous copy or tensor-core group did not complete");
       bool redo = false;
       if (s.pair_total > pair_list.n) {
         VCT_CHECK(pair_list.ensure((size_t)s.pair_total + s.pair_total / 4 + 4096));

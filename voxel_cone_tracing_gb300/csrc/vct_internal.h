@@ -260,9 +260,12 @@ cudaError_t launch_mlp_init(float* prm, __nv_bfloat16* prm_bf, size_t n, float s
 cudaError_t launch_mlp_train(const MlpParams& p, const MlpBatch& b, float* loss, cudaStream_t st);
 cudaError_t launch_adam(float* prm, float* grad, float* m, float* v, __nv_bfloat16* prm_bf, size_t n,
                         const AdamStep& a, cudaStream_t st);
+// Inference / evaluation of the network: on the 5th-generation tensor cores
+// (tcgen05.mma, TMEM accumulators) when `tc`, else in mma.sync warp tiles.
 cudaError_t launch_mlp_infer(const MlpParams& p, const SceneParams& sp, const float4* gb_pos, const float4* gb_nrm,
-                             int n_px, float4* out, cudaStream_t st);
-cudaError_t launch_mlp_eval(const MlpParams& p, const float* samples, int n, float* out, cudaStream_t st);
+                             int n_px, float4* out, cudaStream_t st, bool tc, FrameStatus* status);
+cudaError_t launch_mlp_eval(const MlpParams& p, const float* samples, int n, float* out, cudaStream_t st, bool tc,
+                            FrameStatus* status);
 // Training data: world-space area of every queued triangle; surface samples
 // drawn from the area CDF (rows of 12 floats, see MlpBatch); their
 // cone-traced diffuse targets (trace_diffuse with the texture-unit sampler).

@@ -43,6 +43,7 @@ EXPORTS = [
     "vct_batch_set_camera", "vct_batch_render", "vct_batch_synchronize", "vct_batch_set_stream",
     "vct_batch_read_frame", "vct_batch_read_voxels", "vct_batch_stage_times", "vct_batch_get_shape",
     "vct_batch_set_shape", "vct_batch_autotune", "vct_set_light_injection", "vct_read_injection_grids",
+    "vct_mlp_set_tensor_kernels",
 ]
 DIFFUSE_CONES, DIFFUSE_MLP = 0, 1
 MLP_WEIGHTS = 5 * 64 * 64
@@ -135,6 +136,7 @@ def lib() -> C.CDLL:
             "vct_batch_stage_times": (I32, [P, P]), "vct_batch_get_shape": (I32, [P, P]),
             "vct_batch_set_shape": (I32, [P, P]), "vct_batch_autotune": (I32, [P, I32, P, P, P]),
             "vct_set_light_injection": (I32, [P, I32]), "vct_read_injection_grids": (I32, [P, P, P, P]),
+            "vct_mlp_set_tensor_kernels": (I32, [P, I32]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
@@ -361,6 +363,9 @@ class Renderer:
         _check(lib().vct_mlp_gradients(self._r, s.ctypes.data, s.shape[0], loss.ctypes.data, dw.ctypes.data,
                                        dt.ctypes.data))
         return float(loss[0]), dw, dt
+
+    def mlp_set_tensor_kernels(self, use_tcgen05: bool) -> None:
+        _check(lib().vct_mlp_set_tensor_kernels(self._r, int(bool(use_tcgen05))))
 
     def set_light_injection(self, enable: bool) -> None:
         _check(lib().vct_set_light_injection(self._r, int(bool(enable))))
