@@ -110,6 +110,33 @@ class Renderer {
   vct_status status_ = VCT_OK;
 };
 
+// Many independent scenes per frame (vct_batch_*; no reference counterpart).
+class Batch {
+ public:
+  Batch(const vct_batch_scene* scenes, uint32_t n, const vct_batch_config* cfg = nullptr) {
+    status_ = vct_batch_create(scenes, n, cfg, &b_);
+  }
+  ~Batch() { vct_batch_destroy(b_); }
+  Batch(const Batch&) = delete;
+  Batch& operator=(const Batch&) = delete;
+
+  void set_camera(uint32_t scene, mat4& lookat, mat4& projection) {
+    status_ = vct_batch_set_camera(b_, scene, lookat.m, projection.m);
+  }
+  void render() { status_ = vct_batch_render(b_); }
+  vct_status synchronize() { return status_ = vct_batch_synchronize(b_); }
+  vct_status read_frame(uint32_t scene, void* rgba8) { return status_ = vct_batch_read_frame(b_, scene, rgba8); }
+  vct_status autotune(int frames, vct_batch_shape* best = nullptr) {
+    return status_ = vct_batch_autotune(b_, frames, best, nullptr, nullptr);
+  }
+  vct_status last_status() const { return status_; }
+  vct_batch* handle() { return b_; }
+
+ private:
+  vct_batch* b_ = nullptr;
+  vct_status status_ = VCT_OK;
+};
+
 // Texture3D, texture_3d.h:6-10.
 inline uint32_t create_tex_3d(int width, int height, int depth, int levels) {
   return vct_create_tex_3d(width, height, depth, levels);
