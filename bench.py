@@ -46,7 +46,7 @@ NUM_SMS = 152
 # tests/test_scenes.py::test_bench_frame_work).
 TRACE_FETCHES_PER_PIXEL = 778.9
 INSTANCE_RECORD_BYTES = 144   # one per queued model (DevInstance)
-STATUS_BYTES = 32             # per-frame status read back with the frame
+STATUS_BYTES = 48             # per-frame status read back with the frame
 
 
 def _peaks():

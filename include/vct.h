@@ -124,6 +124,8 @@ typedef struct {
   uint32_t kernel_launches; /* engine kernels launched for the frame       */
   uint32_t voxelized;       /* 1: the frame voxelized its geometry; 0: light
                              * injection reused the attribute grids        */
+  uint32_t split_bricks;    /* dense bricks (> 1024 triangle pairs) whose
+                             * pairs were spread over several CTAs         */
 } vct_stage_times;
 
 /* --------------------------------------------------- error reporting --- */

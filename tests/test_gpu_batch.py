@@ -129,3 +129,18 @@ def test_batch_work_lists_grow(vct):
     b.render()
     for i, item in enumerate(items):
         _check_scene(vct, b, i, item)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("vox_mode", [0, 1], ids=["ref_raster2x", "conservative"])
+def test_batch_dense_bricks(vct, vox_mode):
+    """Dense spheres in coarse grids (the batch's brick pairs split across
+    CTAs) render what a Renderer renders."""
+    items = [(scenes.scene_sphere(seed=31, freq=60, width=64, height=48), 64, 48, 16, CONES[9]),
+             (scenes.scene_sphere(seed=32, freq=40, width=48, height=48), 48, 48, 32, CONES[6]),
+             _items()[0]]
+    b = vct.Batch(items, vox_mode=vox_mode)
+    b.render()
+    assert b.stage_times()["split_bricks"] > 0
+    for i, item in enumerate(items):
+        _check_scene(vct, b, i, item, vox_mode=vox_mode)

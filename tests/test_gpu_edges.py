@@ -130,3 +130,37 @@ def test_camera_outside_the_grid(vct, oracle):
     assert outside.any() and shaded_beyond.any()
     assert (f[outside] == (38, 64, 64, 255)).all()
     assert (f[shaded_beyond] != (38, 64, 64, 255)).any(axis=-1).all()
+
+
+@pytest.mark.parametrize("mode", [0, 1], ids=["ref_raster2x", "conservative"])
+def test_dense_bricks_split_across_ctas(vct, oracle, mode):
+    """72,000 triangles in a 16^3 grid: the bricks around the sphere hold
+    thousands of (triangle, brick) pairs each, so their pairs are spread over
+    several CTAs (chunks of 1024 pairs) and summed in global memory."""
+    s = scenes.scene_sphere(seed=77, freq=60, width=48, height=32)
+    r, _ = _parity(vct, oracle, s, 48, 32, 16, mode=mode)
+    assert r.stage_times()["split_bricks"] > 0
+
+
+def test_dense_brick_plan_overflow(vct, oracle):
+    """4,000 planes at random depths in the two lowest brick layers of a
+    128^3 grid, each over 9 x 16 bricks: 288 dense bricks of ~2,000 pairs,
+    more than the 256 accumulator slots of a new renderer.  The bricks that
+    did not get a slot run whole on one CTA (still exact), the slots grow,
+    and the next frame splits every dense brick."""
+    rng = np.random.default_rng(9)
+    z = rng.uniform(-0.995, -0.755, 4000)
+    # x in [-1.2, 0.12] (brick columns 0..8), y over the whole grid
+    tris = [[(-1.2, -1.2, zi), (0.12, -1.2, zi), (-1.2, 60.0, zi)] for zi in z]
+    s = tri_scene(tris)
+    n = 128
+    p = oracle.Params(grid_res=n, width=8, height=8)
+    l0, cnt, _ = oracle.voxelize(s, p)
+    r = vct.Renderer(8, 8, grid_res=n, keep_counts=1)
+    ids = vct.load_scene(r, s)
+    for _ in range(2):
+        vct.queue_scene(r, s, ids)
+        r.render()
+        np.testing.assert_array_equal(r.read_voxel_counts(), cnt)
+        assert np.abs(r.read_voxels(0).astype(int) - l0.astype(int)).max(initial=0) <= 1
+        assert r.stage_times()["split_bricks"] == 288

@@ -136,3 +136,19 @@ def test_half_storage_ldr_matches_rgba8(vct, oracle):
     q = psnr(np.clip(a, 0, 1), np.clip(b, 0, 1))
     print(f"RGBA8 vs RGBA16F frame PSNR {q:.1f} dB")
     assert q >= 40.0
+
+
+def test_hdr_dense_bricks(vct, oracle):
+    """Half-precision level 0 of bricks whose pairs are split across CTAs
+    (72,000 triangles in a 16^3 grid): the 64-bit fixed-point sums of the
+    chunks add exactly, so the tolerance stays 1 half ulp."""
+    s = scenes.scene_sphere(seed=78, freq=60, width=W, height=H)
+    r = vct.Renderer(W, H, grid_res=16, keep_counts=1, storage=vct.STORAGE_RGBA16F, radiance_max=RMAX)
+    ids = vct.load_scene(r, s)
+    vct.queue_scene(r, s, ids)
+    r.render()
+    assert r.stage_times()["split_bricks"] > 0
+    ref, cnt_ref, _ = oracle.voxelize_hdr(s, oracle.Params(grid_res=16, radiance_max=RMAX))
+    np.testing.assert_array_equal(r.read_voxel_counts(), cnt_ref)
+    d = np.abs(r.read_voxels(0).astype(np.float64) - ref)
+    assert (d <= _half_ulp(ref)).all()

@@ -122,3 +122,20 @@ def test_gpu_injection_frame_close_to_direct(vct, small):
     q = psnr(fd / 255.0, fi / 255.0)
     print(f"injected vs direct frame: PSNR {q:.1f} dB")
     assert q >= 40.0
+
+
+@pytest.mark.gpu
+def test_gpu_injection_dense_bricks(vct, oracle):
+    """Attribute grids of bricks whose pairs are split across CTAs (72,000
+    triangles in a 16^3 grid)."""
+    s = scenes.scene_sphere(seed=79, freq=60, width=W, height=H)
+    r = vct.Renderer(W, H, grid_res=16, keep_counts=1)
+    ids = vct.load_scene(r, s)
+    r.set_light_injection(True)
+    _frame(vct, r, s, ids, s.lights)
+    assert r.stage_times()["split_bricks"] > 0
+    ref = oracle.voxelize_attr(s, oracle.Params(grid_res=16))
+    np.testing.assert_array_equal(r.read_voxel_counts(), ref["counts"])
+    g = r.read_injection_grids()
+    for k in ("albedo", "normal", "emission"):
+        assert np.abs(g[k].astype(int) - ref[k].astype(int)).max() <= 1, k

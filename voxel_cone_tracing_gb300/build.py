@@ -21,8 +21,10 @@ DEMO_SRC = os.path.join(HERE, "demo", "vct_demo.cpp")
 DEMO = os.path.join(HERE, "vct_demo")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=off", "-I", CSRC]
-# Extra nvcc flags (e.g. -DVCT_TRACE_MIN_BLOCKS=3 for tuning sweeps).
+# Extra nvcc flags (e.g. -DVCT_TRACE_MIN_BLOCKS=3 for tuning sweeps); the
+# library is rebuilt when they differ from the ones it was built with.
 EXTRA = os.environ.get("VCT_NVCC_FLAGS", "").split()
+STAMP = LIB + ".flags"
 
 
 def nvcc() -> str:
@@ -43,6 +45,12 @@ def _deps() -> list:
 
 def up_to_date() -> bool:
     if not os.path.exists(LIB):
+        return False
+    try:
+        with open(STAMP) as f:
+            if f.read() != " ".join(EXTRA):
+                return False
+    except OSError:
         return False
     t = os.path.getmtime(LIB)
     return all(os.path.getmtime(d) <= t for d in _deps())
@@ -92,6 +100,8 @@ def build(force: bool = False, verbose: bool = False) -> str:
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stderr}")
     os.replace(tmp, LIB)
+    with open(STAMP, "w") as f:
+        f.write(" ".join(EXTRA))
     build_demo(force=True)
     return LIB
 

@@ -72,6 +72,7 @@ struct vct_batch {
   DevBuf<uint32_t> brick_count, brick_offset, brick_cursor, pair_list, scan_tmp, bin_big_count, queue;
   DevBuf<BinRec> bin_big;
   uint32_t bin_big_cap = 0;
+  HeavyStore heavy;
   DevBuf<unsigned char> rbig;
   DevBuf<uint32_t> rbig_count, rbig_offset;
   uint32_t rbig_cap = 0;
@@ -131,6 +132,7 @@ struct vct_batch {
     bb.rb.gb_nrm = gb_nrm.p;
     bb.rb.status = d_status.p;
     bb.frame = frame.p;
+    bb.heavy = kHeavySplit ? heavy.view() : HeavyBricks{};
     return bb;
   }
 
@@ -252,6 +254,7 @@ struct vct_batch {
       VCT_CUDA(cudaStreamSynchronize(stream));
       pending = false;
       const FrameStatus s = *h_status.p;
+      VCT_CHECK(heavy.grow(s, brick_count.n));  // exact either way: no redo
       bool redo = false;
       if (s.pair_total > pair_list.n) {
         VCT_CHECK(pair_list.ensure((size_t)s.pair_total + s.pair_total / 4 + 4096));
@@ -445,6 +448,7 @@ vct_status build_batch(vct_batch* b, const vct_batch_scene* descs, uint32_t n) {
   VCT_CHECK(b->brick_count.ensure(nbk));
   VCT_CHECK(b->brick_offset.ensure(nbk + 1));
   VCT_CHECK(b->brick_cursor.ensure(nbk));
+  VCT_CHECK(b->heavy.reserve(nbk, 1024, 65536));
   VCT_CHECK(b->scan_tmp.ensure(scan_tmp_words(nbk)));
   VCT_CHECK(b->pair_list.ensure((size_t)std::min<uint64_t>(0xffffff00ull, 4ull * total_tris + 65536ull)));
   VCT_CHECK(b->bin_big_count.ensure(1));
@@ -575,6 +579,7 @@ extern "C" vct_status vct_batch_stage_times(vct_batch* b, vct_stage_times* out) 
   VCT_CUDA(cudaEventElapsedTime(&out->total, b->ev[0], b->ev[4]));
   out->kernel_launches = (uint32_t)b->launches;
   out->voxelized = 1u;
+  out->split_bricks = b->h_status.p->heavy_total;
   return VCT_OK;
 }
 

@@ -359,6 +359,7 @@ extern "C" vct_status vct_get_stage_times(vct_renderer* r, vct_stage_times* out)
   VCT_CUDA(cudaEventElapsedTime(&out->total, r->ev[0], r->ev[4]));
   out->kernel_launches = (uint32_t)r->launches;
   out->voxelized = r->last_revoxelized ? 1u : 0u;
+  out->split_bricks = r->h_status.p->heavy_total;
   return VCT_OK;
 }
 

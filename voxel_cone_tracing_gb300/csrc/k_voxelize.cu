@@ -27,6 +27,7 @@
 #include <cuda_fp16.h>
 
 #include <algorithm>
+#include <cstring>
 #include <climits>
 #include <type_traits>
 
@@ -319,10 +320,30 @@ __device__ __forceinline__ float4 voxel_color(const SceneParams& sp, const vct_m
 // is exact, order-independent and far finer than half precision.  Attribute
 // grids (light injection): ten unorm channels in 16-bit fixed point.
 template <int STORAGE> struct AccT;
+// A value of the global accumulator copy, read past L1 and zeroed.
+template <class T>
+__device__ __forceinline__ T take_cg(T& g) {
+  const T v = __ldcg(&g);
+  g = 0;
+  return v;
+}
+// atomic_add_to: voxel i of these sums added into a global copy (the
+// accumulator slot of a split brick); take_from: voxel i of the global copy
+// read from L2 into these sums and zeroed there.
 template <> struct AccT<VCT_STORAGE_RGBA8> {
   uint32_t c[4][kBrickVox];
   uint32_t n[kBrickVox];
   __device__ __forceinline__ void clear(int i) { c[0][i] = 0; c[1][i] = 0; c[2][i] = 0; c[3][i] = 0; n[i] = 0; }
+  __device__ __forceinline__ void take_from(AccT& g, int i) {
+    for (int k = 0; k < 4; ++k) c[k][i] = take_cg(g.c[k][i]);
+    n[i] = take_cg(g.n[i]);
+  }
+  __device__ __forceinline__ void atomic_add_to(AccT& g, int i) const {
+    if (!n[i]) return;
+    for (int k = 0; k < 4; ++k)
+      if (c[k][i]) atomicAdd(&g.c[k][i], c[k][i]);
+    atomicAdd(&g.n[i], n[i]);
+  }
   __device__ __forceinline__ void add(const SceneParams& sp, int v, const vct_material_data& m, V3 p, V3 nrm) {
     const float4 col = voxel_color(sp, m, p, nrm);
     atomicAdd(&c[0][v], __float2uint_rn(col.x * kFix));
@@ -336,6 +357,16 @@ template <> struct AccT<VCT_STORAGE_RGBA16F> {
   unsigned long long c[4][kBrickVox];
   uint32_t n[kBrickVox];
   __device__ __forceinline__ void clear(int i) { c[0][i] = 0; c[1][i] = 0; c[2][i] = 0; c[3][i] = 0; n[i] = 0; }
+  __device__ __forceinline__ void take_from(AccT& g, int i) {
+    for (int k = 0; k < 4; ++k) c[k][i] = take_cg(g.c[k][i]);
+    n[i] = take_cg(g.n[i]);
+  }
+  __device__ __forceinline__ void atomic_add_to(AccT& g, int i) const {
+    if (!n[i]) return;
+    for (int k = 0; k < 4; ++k)
+      if (c[k][i]) atomicAdd(&g.c[k][i], c[k][i]);
+    atomicAdd(&g.n[i], n[i]);
+  }
   __device__ __forceinline__ void add(const SceneParams& sp, int v, const vct_material_data& m, V3 p, V3 nrm) {
     const float4 col = voxel_color(sp, m, p, nrm);
     const float k = 4294967296.0f / sp.radiance_max;
@@ -372,6 +403,16 @@ template <> struct AccT<kStorageAttr> {
 #pragma unroll
     for (int k = 0; k < 10; ++k) c[k][i] = 0;
     n[i] = 0;
+  }
+  __device__ __forceinline__ void take_from(AccT& g, int i) {
+    for (int k = 0; k < 10; ++k) c[k][i] = take_cg(g.c[k][i]);
+    n[i] = take_cg(g.n[i]);
+  }
+  __device__ __forceinline__ void atomic_add_to(AccT& g, int i) const {
+    if (!n[i]) return;
+    for (int k = 0; k < 10; ++k)
+      if (c[k][i]) atomicAdd(&g.c[k][i], c[k][i]);
+    atomicAdd(&g.n[i], n[i]);
   }
   __device__ __forceinline__ void add(const SceneParams&, int v, const vct_material_data& m, V3, V3 nrm) {
     float a[10];
@@ -628,37 +669,13 @@ __device__ __forceinline__ void item_sat(const SceneParams& sp, int N, const int
 template <int MODE>
 using SetupOf = typename std::conditional<MODE == VCT_VOX_CONSERVATIVE, SetupSat, SetupRef>::type;
 
-// One brick, all threads of the CTA (the shared-memory arrays come from the
-// caller, so that a persistent CTA reuses them brick after brick).
+// Accumulates the (triangle, brick) pairs list[beg, end) of the brick at b3
+// into acc (all threads of the CTA; cleared first, barrier at the end).
 template <int MODE, int STORAGE>
-__device__ __forceinline__ void brick_body(const SceneParams& sp, int N, uint32_t brick,
-                                           const uint32_t* __restrict__ offset, const uint32_t* __restrict__ list,
-                                           uint32_t cap, cudaSurfaceObject_t l0, uint32_t* __restrict__ counts,
-                                           FrameStatus* st, AccT<STORAGE>& acc, SetupOf<MODE> (&setup)[kWarps][32],
-                                           int (&excl)[kWarps][33], const InjGrids& inj, void* l0_lin) {
-  const int nb = N / kBrick;
-  const int b3[3] = {(int)(brick % nb), (int)((brick / nb) % nb), (int)(brick / ((uint32_t)nb * nb))};
-  const uint32_t beg = min(offset[brick], cap), end = min(offset[brick + 1], cap);
-  if (beg == end) {
-    // No triangle touches this brick (most of the grid): store cleared texels
-    // without the accumulator or its barriers.
-    for (int i = threadIdx.x; i < kBrickVox; i += kThreads) {
-      const int x = b3[0] * kBrick + (i & 7), y = b3[1] * kBrick + ((i >> 3) & 7), z = b3[2] * kBrick + (i >> 6);
-      if (STORAGE == kStorageAttr) {
-        surf3Dwrite(make_uchar4(0, 0, 0, 0), inj.albedo, x * 4, y, z);
-        surf3Dwrite(make_uchar4(0, 0, 0, 0), inj.normal, x * 4, y, z);
-        surf3Dwrite(make_uchar4(0, 0, 0, 0), inj.emission, x * 4, y, z);
-      } else if (STORAGE == VCT_STORAGE_RGBA8) {
-        surf3Dwrite(make_uchar4(0, 0, 0, 0), l0, x * 4, y, z);
-        if (l0_lin) static_cast<uchar4*>(l0_lin)[((size_t)z * N + y) * N + x] = make_uchar4(0, 0, 0, 0);
-      } else {
-        surf3Dwrite(make_ushort4(0, 0, 0, 0), l0, x * 8, y, z);
-        if (l0_lin) static_cast<ushort4*>(l0_lin)[((size_t)z * N + y) * N + x] = make_ushort4(0, 0, 0, 0);
-      }
-      if (counts) counts[((size_t)z * N + y) * N + x] = 0u;
-    }
-    return;
-  }
+__device__ __forceinline__ void brick_accumulate(const SceneParams& sp, int N, const int b3[3],
+                                                 const uint32_t* __restrict__ list, uint32_t beg, uint32_t end,
+                                                 AccT<STORAGE>& acc, SetupOf<MODE> (&setup)[kWarps][32],
+                                                 int (&excl)[kWarps][33]) {
   for (int i = threadIdx.x; i < kBrickVox; i += kThreads) acc.clear(i);
   __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -694,7 +711,15 @@ __device__ __forceinline__ void brick_body(const SceneParams& sp, int N, uint32_
     __syncwarp();
   }
   __syncthreads();
-  // Order-independent mean, round to nearest (ties up); empty voxels = 0.
+}
+
+// Writes the brick at b3 from its sums: order-independent mean, round to
+// nearest (ties up); empty voxels = 0.  `acc` may be in shared or global
+// memory.
+template <int STORAGE>
+__device__ __forceinline__ void brick_finalize(const SceneParams& sp, int N, const int b3[3], const AccT<STORAGE>& acc,
+                                               cudaSurfaceObject_t l0, uint32_t* __restrict__ counts,
+                                               FrameStatus* st, const InjGrids& inj, void* l0_lin) {
   for (int i = threadIdx.x; i < kBrickVox; i += kThreads) {
     const uint32_t n = acc.n[i];
     const int lx = i & 7, ly = (i >> 3) & 7, lz = i >> 6;
@@ -711,17 +736,10 @@ __device__ __forceinline__ void brick_body(const SceneParams& sp, int N, uint32_
       surf3Dwrite(a, inj.albedo, x * 4, y, z);
       surf3Dwrite(nn, inj.normal, x * 4, y, z);
       surf3Dwrite(e, inj.emission, x * 4, y, z);
-    } else if (STORAGE == VCT_STORAGE_RGBA8) {
+    } else if constexpr (STORAGE == VCT_STORAGE_RGBA8) {
       uchar4 o = make_uchar4(0, 0, 0, 0);
-      if (n) {
-        const unsigned long long den = 2ull * n * 65535ull;
-        unsigned char q[4];
-        for (int ch = 0; ch < 4; ++ch) {
-          unsigned long long v = ((unsigned long long)acc.c[ch][i] * 510ull + (unsigned long long)n * 65535ull) / den;
-          q[ch] = (unsigned char)(v > 255ull ? 255ull : v);
-        }
-        o = make_uchar4(q[0], q[1], q[2], q[3]);
-      }
+      if (n) o = make_uchar4(unorm8_mean(acc.c[0][i], n), unorm8_mean(acc.c[1][i], n), unorm8_mean(acc.c[2][i], n),
+                             unorm8_mean(acc.c[3][i], n));
       surf3Dwrite(o, l0, x * 4, y, z);
       if (l0_lin) static_cast<uchar4*>(l0_lin)[((size_t)z * N + y) * N + x] = o;
     } else {
@@ -740,38 +758,154 @@ __device__ __forceinline__ void brick_body(const SceneParams& sp, int N, uint32_
   }
 }
 
+__device__ __forceinline__ void brick_coords(int N, uint32_t brick, int b3[3]) {
+  const int nb = N / kBrick;
+  b3[0] = (int)(brick % nb);
+  b3[1] = (int)((brick / nb) % nb);
+  b3[2] = (int)(brick / ((uint32_t)nb * nb));
+}
+
+// One unit of brick work, all threads of the CTA (the shared-memory arrays
+// come from the caller, so that a persistent CTA reuses them unit after
+// unit): the whole brick, or -- for a dense brick with an accumulator slot
+// (hb->slot[slot_index] >= 0) -- its chunk `chunk` of kHeavyChunk pairs.
+// A chunk adds its sums into the slot; the CTA that completes the brick's
+// last chunk takes the sums back (zeroing the slot and its counter for the
+// next frame) and writes the brick.  `item`: the unit is an extra chunk
+// (>= 1) of a split brick.  Every kernel calls this from one place only,
+// so that its code exists once per kernel (instruction-cache footprint).
+template <int MODE, int STORAGE>
+__device__ __forceinline__ void brick_unit(const SceneParams& sp, int N, uint32_t brick,
+                                           const uint32_t* __restrict__ offset, const uint32_t* __restrict__ list,
+                                           uint32_t cap, cudaSurfaceObject_t l0, uint32_t* __restrict__ counts,
+                                           FrameStatus* st, AccT<STORAGE>& acc, SetupOf<MODE> (&setup)[kWarps][32],
+                                           int (&excl)[kWarps][33], const InjGrids& inj, void* l0_lin,
+                                           const HeavyBricks* hb, uint32_t slot_index, uint32_t chunk, bool item) {
+  __shared__ uint32_t s_last;
+  int b3[3];
+  brick_coords(N, brick, b3);
+  const uint32_t beg0 = min(offset[brick], cap), end = min(offset[brick + 1], cap);
+  if (beg0 == end) {
+    // No triangle touches this brick (most of the grid): store cleared texels
+    // without the accumulator or its barriers.
+    for (int i = threadIdx.x; i < kBrickVox; i += kThreads) {
+      const int x = b3[0] * kBrick + (i & 7), y = b3[1] * kBrick + ((i >> 3) & 7), z = b3[2] * kBrick + (i >> 6);
+      if (STORAGE == kStorageAttr) {
+        surf3Dwrite(make_uchar4(0, 0, 0, 0), inj.albedo, x * 4, y, z);
+        surf3Dwrite(make_uchar4(0, 0, 0, 0), inj.normal, x * 4, y, z);
+        surf3Dwrite(make_uchar4(0, 0, 0, 0), inj.emission, x * 4, y, z);
+      } else if (STORAGE == VCT_STORAGE_RGBA8) {
+        surf3Dwrite(make_uchar4(0, 0, 0, 0), l0, x * 4, y, z);
+        if (l0_lin) static_cast<uchar4*>(l0_lin)[((size_t)z * N + y) * N + x] = make_uchar4(0, 0, 0, 0);
+      } else {
+        surf3Dwrite(make_ushort4(0, 0, 0, 0), l0, x * 8, y, z);
+        if (l0_lin) static_cast<ushort4*>(l0_lin)[((size_t)z * N + y) * N + x] = make_ushort4(0, 0, 0, 0);
+      }
+      if (counts) counts[((size_t)z * N + y) * N + x] = 0u;
+    }
+    return;
+  }
+  // Only a dense brick looks up its slot.
+  const int slot = (hb && hb->slot && (item || end - beg0 > kHeavyChunk)) ? hb->slot[slot_index] : -1;
+  uint32_t beg = beg0, stop = end;
+  if (slot >= 0) {
+    beg = min(beg0 + chunk * kHeavyChunk, end);
+    stop = min(beg + kHeavyChunk, end);
+  }
+  brick_accumulate<MODE, STORAGE>(sp, N, b3, list, beg, stop, acc, setup, excl);
+  if (slot >= 0) {
+    AccT<STORAGE>& g = static_cast<AccT<STORAGE>*>(hb->acc)[slot];
+    for (int i = threadIdx.x; i < kBrickVox; i += kThreads) acc.atomic_add_to(g, i);
+    __threadfence();  // this CTA's sums are in L2 before its chunk counts as done
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      const uint32_t nch = (end - beg0 + kHeavyChunk - 1) / kHeavyChunk;
+      s_last = atomicAdd(&hb->done[slot], 1u) == nch - 1 ? 1u : 0u;
+    }
+    __syncthreads();
+    if (!s_last) return;
+    __threadfence();
+    for (int i = threadIdx.x; i < kBrickVox; i += kThreads) acc.take_from(g, i);
+    if (threadIdx.x == 0) hb->done[slot] = 0;
+    __syncthreads();
+  }
+  brick_finalize<STORAGE>(sp, N, b3, acc, l0, counts, st, inj, l0_lin);
+}
+
+// One CTA per brick, after `n_extra` CTAs that run the extra chunks of
+// split bricks from the launch-wide item queue (first in the grid, so that
+// the dense bricks' chunks start with the first bricks, not in the tail).
 template <int MODE, int STORAGE>
 __global__ void __launch_bounds__(kThreads) k_bricks(SceneParams sp, int N, const uint32_t* __restrict__ offset,
                                                      const uint32_t* __restrict__ list, uint32_t cap,
                                                      cudaSurfaceObject_t l0, uint32_t* __restrict__ counts,
-                                                     FrameStatus* st, InjGrids inj, void* l0_lin) {
+                                                     FrameStatus* st, InjGrids inj, void* l0_lin, HeavyBricks hb,
+                                                     uint32_t n_extra) {
   __shared__ AccT<STORAGE> acc;
   __shared__ SetupOf<MODE> setup[kWarps][32];
   __shared__ int excl[kWarps][33];
-  brick_body<MODE, STORAGE>(sp, N, blockIdx.x, offset, list, cap, l0, counts, st, acc, setup, excl, inj, l0_lin);
+  __shared__ uint32_t s_next;
+  const bool extra = blockIdx.x < n_extra;
+  const uint32_t n_items = extra ? min(hb.counters[1], hb.item_cap) : 0u;
+  if (extra && blockIdx.x == 0 && threadIdx.x < 2) (&st->heavy_total)[threadIdx.x] = hb.counters[threadIdx.x];
+  for (bool first = true;; first = false) {
+    uint32_t brick, chunk = 0;
+    if (!extra) {
+      if (!first) return;
+      brick = blockIdx.x - n_extra;
+    } else {
+      if (threadIdx.x == 0) s_next = atomicAdd(&hb.counters[2], 1u);
+      __syncthreads();
+      const uint32_t it = s_next;
+      __syncthreads();  // s_next read by every thread before the next write
+      if (it >= n_items) return;
+      const uint2 w = hb.items[it];
+      if (w.x == 0xffffffffu) continue;  // CTA-uniform
+      brick = w.x;
+      chunk = w.y;
+    }
+    brick_unit<MODE, STORAGE>(sp, N, brick, offset, list, cap, l0, counts, st, acc, setup, excl, inj, l0_lin, &hb,
+                              brick, chunk, extra);
+    __syncthreads();  // done with acc
+  }
 }
 
-// Every scene's bricks in one persistent launch; a CTA takes its next brick
+// Every scene's bricks in one persistent launch; a CTA takes its next unit
 // from the atomic counter w.queue (brick costs range from an empty brick to
-// thousands of triangle samples).
+// thousands of triangle samples).  The queue hands out the extra chunks of
+// the split bricks first (global brick indices), then the bricks.
 template <int MODE, int STORAGE>
 __global__ void __launch_bounds__(kThreads) k_bricks_batch(BatchWork w, BatchBuffers bb) {
   __shared__ AccT<STORAGE> acc;
   __shared__ SetupOf<MODE> setup[kWarps][32];
   __shared__ int excl[kWarps][33];
   __shared__ uint32_t s_next;
-  if (threadIdx.x == 0) s_next = atomicAdd(w.queue, 1u);
-  __syncthreads();
-  uint32_t g = s_next;
-  while (g < w.total) {
-    const int s = batch_scene_of(w, g);
-    const BatchScene& S = w.scenes[s];
-    brick_body<MODE, STORAGE>(S.sp, S.N, g - __ldg(w.prefix + s), bb.brick_offset + S.brick_base, bb.pair_list,
-                              bb.pair_cap, S.ms.l0_surf, nullptr, bb.status, acc, setup, excl, InjGrids{}, nullptr);
-    __syncthreads();  // the next brick clears the accumulators; s_next has been read
+  const HeavyBricks& hb = bb.heavy;
+  const uint32_t n_items = hb.slot ? min(hb.counters[1], hb.item_cap) : 0u;
+  const uint32_t total = n_items + w.total;
+  if (hb.slot && blockIdx.x == 0 && threadIdx.x < 2) (&bb.status->heavy_total)[threadIdx.x] = hb.counters[threadIdx.x];
+  for (;;) {
     if (threadIdx.x == 0) s_next = atomicAdd(w.queue, 1u);
     __syncthreads();
-    g = s_next;
+    const uint32_t q = s_next;
+    __syncthreads();  // s_next read by every thread before the next write
+    if (q >= total) return;
+    uint32_t g, chunk = 0;
+    const bool item = q < n_items;
+    if (item) {
+      const uint2 it = hb.items[q];
+      if (it.x == 0xffffffffu) continue;  // CTA-uniform
+      g = it.x;
+      chunk = it.y;
+    } else {
+      g = q - n_items;
+    }
+    const int s = batch_scene_of(w, g);
+    const BatchScene& S = w.scenes[s];
+    brick_unit<MODE, STORAGE>(S.sp, S.N, g - __ldg(w.prefix + s), bb.brick_offset + S.brick_base, bb.pair_list,
+                              bb.pair_cap, S.ms.l0_surf, nullptr, bb.status, acc, setup, excl, InjGrids{}, nullptr,
+                              &hb, g, chunk, item);
+    __syncthreads();  // done with acc
   }
 }
 
@@ -881,11 +1015,46 @@ cudaError_t launch_voxelize_linear(const SceneParams& sp, int N, int mode, const
   return cudaGetLastError();
 }
 
+// Calls f(mode tag, storage tag) for the brick kernel a frame uses.
+template <class F>
+void dispatch_bricks(int mode, int storage, bool attr, F&& f) {
+  using RAS = std::integral_constant<int, VCT_VOX_REF_RASTER2X>;
+  using SAT = std::integral_constant<int, VCT_VOX_CONSERVATIVE>;
+  using R8 = std::integral_constant<int, VCT_STORAGE_RGBA8>;
+  using F16 = std::integral_constant<int, VCT_STORAGE_RGBA16F>;
+  using ATR = std::integral_constant<int, kStorageAttr>;
+  if (mode == VCT_VOX_CONSERVATIVE) {
+    if (attr) f(SAT(), ATR());
+    else if (storage == VCT_STORAGE_RGBA8) f(SAT(), R8());
+    else f(SAT(), F16());
+  } else {
+    if (attr) f(RAS(), ATR());
+    else if (storage == VCT_STORAGE_RGBA8) f(RAS(), R8());
+    else f(RAS(), F16());
+  }
+}
+
+// CTAs of a kernel resident on one SM (cached per kernel).
+template <class K>
+int resident_per_sm(K kern) {
+  int f = 1;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&f, kern, kThreads, 0) != cudaSuccess || f < 1) f = 1;
+  return f;
+}
+
 cudaError_t launch_voxelize(const SceneParams& sp, int N, int mode, int storage, const VoxBuffers& vb,
                             cudaSurfaceObject_t l0, cudaStream_t st, int* launches, const InjGrids* inj) {
   int nl = 0;
   const int nb = N / kBrick;
   const size_t n_bricks = (size_t)nb * nb * nb;
+  int dev = 0, sms = 148;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  int fit = 1;
+  dispatch_bricks(mode, storage, inj != nullptr, [&](auto mode_tag, auto storage_tag) {
+    static const int f = resident_per_sm(k_bricks<decltype(mode_tag)::value, decltype(storage_tag)::value>);
+    fit = f;
+  });
   cudaError_t e = cudaMemsetAsync(vb.brick_count, 0, n_bricks * sizeof(uint32_t), st);
   if (e != cudaSuccess) return e;
   const unsigned tri_blocks = (sp.total_tris + 255) / 256;
@@ -904,11 +1073,16 @@ cudaError_t launch_voxelize(const SceneParams& sp, int N, int mode, int storage,
       ++nl;
     }
   }
-  e = launch_exclusive_scan(vb.brick_count, vb.brick_offset, vb.brick_cursor, n_bricks, vb.scan_tmp, st, &nl);
-  if (e != cudaSuccess) return e;
-  // pair_total <- offset[n_bricks]; bigtri_total <- records needed
-  e = cudaMemcpyAsync(&vb.status->pair_total, vb.brick_offset + n_bricks, sizeof(uint32_t),
-                      cudaMemcpyDeviceToDevice, st);
+  // Offsets, pair_total <- offset[n_bricks], and the dense-brick plan
+  // against the brick CTAs resident at once.
+  const HeavyBricks& hb = vb.heavy;
+  ScanFuse fuse;
+  std::memset(&fuse, 0, sizeof(fuse));
+  fuse.hb = hb;
+  fuse.cap = vb.pair_cap;
+  fuse.slots = (uint32_t)(sms * fit);
+  fuse.total_copy = &vb.status->pair_total;
+  e = launch_exclusive_scan(vb.brick_count, vb.brick_offset, vb.brick_cursor, n_bricks, vb.scan_tmp, st, &nl, &fuse);
   if (e != cudaSuccess) return e;
   if (vb.big) {
     e = cudaMemcpyAsync(&vb.status->bigtri_total, vb.big_count, sizeof(uint32_t), cudaMemcpyDeviceToDevice, st);
@@ -924,24 +1098,24 @@ cudaError_t launch_voxelize(const SceneParams& sp, int N, int mode, int storage,
       ++nl;
     }
   }
-  ++nl;  // k_bricks
-  const unsigned grid = (unsigned)n_bricks;
   const InjGrids g = inj ? *inj : InjGrids{};
-  auto run = [&](auto kern) {
-    kern<<<grid, kThreads, 0, st>>>(sp, N, vb.brick_offset, vb.pair_list, vb.pair_cap, l0, vb.counts, vb.status, g,
-                                    inj ? nullptr : vb.level0_lin);
-  };
-  if (mode == VCT_VOX_CONSERVATIVE) {
-    if (inj) run(k_bricks<VCT_VOX_CONSERVATIVE, kStorageAttr>);
-    else if (storage == VCT_STORAGE_RGBA8) run(k_bricks<VCT_VOX_CONSERVATIVE, VCT_STORAGE_RGBA8>);
-    else run(k_bricks<VCT_VOX_CONSERVATIVE, VCT_STORAGE_RGBA16F>);
-  } else {
-    if (inj) run(k_bricks<VCT_VOX_REF_RASTER2X, kStorageAttr>);
-    else if (storage == VCT_STORAGE_RGBA8) run(k_bricks<VCT_VOX_REF_RASTER2X, VCT_STORAGE_RGBA8>);
-    else run(k_bricks<VCT_VOX_REF_RASTER2X, VCT_STORAGE_RGBA16F>);
-  }
+  void* lin = inj ? nullptr : vb.level0_lin;
+  // Before the bricks: two CTAs per SM that run the extra chunks.
+  const uint32_t n_extra = hb.slot ? std::min<uint32_t>(hb.item_cap, (uint32_t)(sms * std::min(fit, 2))) : 0u;
+  dispatch_bricks(mode, storage, inj != nullptr, [&](auto mode_tag, auto storage_tag) {
+    k_bricks<decltype(mode_tag)::value, decltype(storage_tag)::value>
+        <<<(unsigned)(n_extra + n_bricks), kThreads, 0, st>>>(sp, N, vb.brick_offset, vb.pair_list, vb.pair_cap, l0,
+                                                               vb.counts, vb.status, g, lin, hb, n_extra);
+  });
+  ++nl;
   if (launches) *launches += nl;
   return cudaGetLastError();
+}
+
+size_t heavy_slot_bytes(int storage) {
+  return storage == kStorageAttr          ? sizeof(AccT<kStorageAttr>)
+         : storage == VCT_STORAGE_RGBA16F ? sizeof(AccT<VCT_STORAGE_RGBA16F>)
+                                          : sizeof(AccT<VCT_STORAGE_RGBA8>);
 }
 
 }  // namespace vct
@@ -954,6 +1128,13 @@ cudaError_t launch_voxelize_batch(const BatchWork& tris, const BatchWork& bricks
                                   int storage, const BatchBuffers& bb, uint32_t* scan_tmp, const BatchShape& shape,
                                   int sms, cudaStream_t st, int* launches) {
   int nl = 0;
+  const HeavyBricks& hb = bb.heavy;
+  // The persistent brick grid (bricks + at most item_cap extra chunks).
+  unsigned grid = 1;
+  dispatch_bricks(mode, storage, false, [&](auto mode_tag, auto storage_tag) {
+    grid = resident_grid(k_bricks_batch<decltype(mode_tag)::value, decltype(storage_tag)::value>, kThreads, 0, sms,
+                         shape.bricks_ctas_per_sm, bricks.total + (hb.slot ? hb.item_cap : 0u));
+  });
   cudaError_t e = cudaMemsetAsync(bb.brick_count, 0, (size_t)total_bricks * sizeof(uint32_t), st);
   if (e != cudaSuccess) return e;
   e = cudaMemsetAsync(bb.big_count, 0, sizeof(uint32_t), st);
@@ -967,10 +1148,15 @@ cudaError_t launch_voxelize_batch(const BatchWork& tris, const BatchWork& bricks
                                                0, tris.scenes);
     nl += 2;
   }
-  e = launch_exclusive_scan(bb.brick_count, bb.brick_offset, bb.brick_cursor, total_bricks, scan_tmp, st, &nl);
-  if (e != cudaSuccess) return e;
-  e = cudaMemcpyAsync(&bb.status->pair_total, bb.brick_offset + total_bricks, sizeof(uint32_t),
-                      cudaMemcpyDeviceToDevice, st);
+  // Offsets, pair_total, and the dense-brick plan against the persistent
+  // grid's CTAs.
+  ScanFuse fuse;
+  std::memset(&fuse, 0, sizeof(fuse));
+  fuse.hb = hb;
+  fuse.cap = bb.pair_cap;
+  fuse.slots = grid;
+  fuse.total_copy = &bb.status->pair_total;
+  e = launch_exclusive_scan(bb.brick_count, bb.brick_offset, bb.brick_cursor, total_bricks, scan_tmp, st, &nl, &fuse);
   if (e != cudaSuccess) return e;
   e = cudaMemcpyAsync(&bb.status->bigtri_total, bb.big_count, sizeof(uint32_t), cudaMemcpyDeviceToDevice, st);
   if (e != cudaSuccess) return e;
@@ -982,17 +1168,9 @@ cudaError_t launch_voxelize_batch(const BatchWork& tris, const BatchWork& bricks
   }
   e = cudaMemsetAsync(bricks.queue, 0, sizeof(uint32_t), st);
   if (e != cudaSuccess) return e;
-  auto run = [&](auto kern) {
-    kern<<<resident_grid(kern, kThreads, 0, sms, shape.bricks_ctas_per_sm, bricks.total), kThreads, 0, st>>>(bricks,
-                                                                                                          bb);
-  };
-  if (mode == VCT_VOX_CONSERVATIVE) {
-    if (storage == VCT_STORAGE_RGBA8) run(k_bricks_batch<VCT_VOX_CONSERVATIVE, VCT_STORAGE_RGBA8>);
-    else run(k_bricks_batch<VCT_VOX_CONSERVATIVE, VCT_STORAGE_RGBA16F>);
-  } else {
-    if (storage == VCT_STORAGE_RGBA8) run(k_bricks_batch<VCT_VOX_REF_RASTER2X, VCT_STORAGE_RGBA8>);
-    else run(k_bricks_batch<VCT_VOX_REF_RASTER2X, VCT_STORAGE_RGBA16F>);
-  }
+  dispatch_bricks(mode, storage, false, [&](auto mode_tag, auto storage_tag) {
+    k_bricks_batch<decltype(mode_tag)::value, decltype(storage_tag)::value><<<grid, kThreads, 0, st>>>(bricks, bb);
+  });
   ++nl;
   if (launches) *launches += nl;
   return cudaGetLastError();

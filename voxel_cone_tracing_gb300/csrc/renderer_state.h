@@ -158,6 +158,61 @@ struct MlpState {
   }
 };
 
+// Buffers of the dense-brick split (HeavyBricks): a slot index per brick,
+// accumulator slots sized for the largest accumulator type, and the extra
+// chunk items.  A frame whose plan overflowed them is still exact (the
+// bricks that did not fit ran whole); grow() enlarges them for the next.
+struct HeavyStore {
+  DevBuf<int32_t> slot;
+  DevBuf<uint32_t> brick, done, counters;
+  DevBuf<unsigned char> acc;
+  DevBuf<uint2> items;
+  uint32_t slot_cap = 0, item_cap = 0;
+
+  static size_t slot_bytes() {
+    return std::max({heavy_slot_bytes(VCT_STORAGE_RGBA8), heavy_slot_bytes(VCT_STORAGE_RGBA16F),
+                     heavy_slot_bytes(kStorageAttr)});
+  }
+  vct_status reserve(size_t n_bricks, uint32_t slots, uint32_t n_items) {
+    VCT_CHECK(slot.ensure(n_bricks));
+    VCT_CHECK(counters.ensure(3));
+    if (slots > slot_cap) {
+      // Called between frames (no kernel in flight): the slots and their
+      // counters start at zero and every frame leaves them so.
+      VCT_CHECK(brick.ensure(slots));
+      VCT_CHECK(done.ensure(slots));
+      VCT_CHECK(acc.ensure((size_t)slots * slot_bytes()));
+      VCT_CUDA(cudaMemset(done.p, 0, (size_t)slots * sizeof(uint32_t)));
+      VCT_CUDA(cudaMemset(acc.p, 0, (size_t)slots * slot_bytes()));
+      VCT_CUDA(cudaDeviceSynchronize());
+      slot_cap = slots;
+    }
+    if (n_items > item_cap) {
+      VCT_CHECK(items.ensure(n_items));
+      item_cap = n_items;
+    }
+    return VCT_OK;
+  }
+  // After a frame: room for its split with a margin.
+  vct_status grow(const FrameStatus& s, size_t n_bricks) {
+    if (s.heavy_total <= slot_cap && s.extra_total <= item_cap) return VCT_OK;
+    return reserve(n_bricks, std::max(slot_cap, s.heavy_total + s.heavy_total / 4 + 64),
+                   std::max(item_cap, s.extra_total + s.extra_total / 4 + 1024));
+  }
+  HeavyBricks view() const {
+    HeavyBricks h;
+    h.slot = slot.p;
+    h.brick = brick.p;
+    h.done = done.p;
+    h.acc = acc.p;
+    h.items = items.p;
+    h.counters = counters.p;
+    h.slot_cap = slot_cap;
+    h.item_cap = item_cap;
+    return h;
+  }
+};
+
 // The voxel maps of one grid: level 0 once (surface + texture) and one
 // mipmapped chain of levels 1..L-1 per map (surfaces per level + one
 // texture), as set_grid_resolution allocates them (renderer.cpp:178-188).
@@ -277,6 +332,7 @@ struct vct_renderer {
   DevBuf<BinRec> bin_big;           // large-triangle binning records
   DevBuf<uint32_t> bin_big_count;
   uint32_t bin_big_cap = 0;
+  HeavyStore heavy;                 // dense bricks split across CTAs
   DevBuf<FrameStatus> d_status;
   HostBuf<FrameStatus> h_status;
   DevBuf<unsigned long long> vis;
@@ -385,6 +441,7 @@ struct vct_renderer {
     VCT_CHECK(brick_offset.ensure(nb + 1));
     VCT_CHECK(brick_cursor.ensure(nb));
     VCT_CHECK(scan_tmp.ensure(scan_tmp_words(nb)));
+    VCT_CHECK(heavy.reserve(nb, 256, 16384));
     if (cfg.keep_counts) VCT_CHECK(counts.ensure((size_t)r * r * r));
     have_frame = false;
     return VCT_OK;
@@ -532,6 +589,7 @@ struct vct_renderer {
     vb.big_cap = bin_big_cap;
     vb.big_count = bin_big_count.p;
     vb.level0_lin = have_l0_map ? (void*)l0_lin.p : nullptr;
+    vb.heavy = kHeavySplit ? heavy.view() : HeavyBricks{};
 
     RasterBuffers rb;
     rb.vis = vis.p;
@@ -600,6 +658,7 @@ struct vct_renderer {
       frame_pending = false;
       const FrameStatus s = *h_status.p;
       if (s.async_timeout) return set_error(VCT_ERR_CUDA, "an asynchronous copy or tensor-core group did not complete");
+      VCT_CHECK(heavy.grow(s, brick_count.n));  // exact either way: no redo
       bool redo = false;
       if (s.pair_total > pair_list.n) {
         VCT_CHECK(pair_list.ensure((size_t)s.pair_total + s.pair_total / 4 + 4096));

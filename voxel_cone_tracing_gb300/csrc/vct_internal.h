@@ -61,7 +61,32 @@ struct FrameStatus {
   uint32_t count_saturated; // voxels with > 65535 contributions
   uint32_t bigtri_total;    // large-triangle binning records needed
   uint32_t async_timeout;   // a bounded wait for a bulk copy gave up (never expected)
-  uint32_t pad;
+  uint32_t heavy_total;     // dense bricks split across CTAs (accumulator slots needed)
+  uint32_t extra_total;     // extra chunk work items of the split bricks
+  uint32_t pad[3];
+};
+
+// Dense bricks: a brick with more than kHeavyChunk (triangle, brick) pairs
+// is split into chunks of kHeavyChunk pairs processed by different CTAs of
+// the same launch.  Every chunk adds its sums atomically into the brick's
+// global accumulator slot (integer sums: exact and order-free); the CTA that
+// finishes the last chunk (a per-slot counter) writes the brick's texels and
+// zeroes the slot and its counter again, so slots are zero between frames.
+// A brick that gets no slot (the lists are full) is processed whole by one
+// CTA, which is also exact.
+constexpr uint32_t kHeavyChunk = 1024;
+#ifndef VCT_HEAVY_SPLIT
+#define VCT_HEAVY_SPLIT 1  // build with -DVCT_HEAVY_SPLIT=0 to time whole-brick CTAs only
+#endif
+constexpr bool kHeavySplit = VCT_HEAVY_SPLIT != 0;
+struct HeavyBricks {
+  int32_t* slot;       // per brick: accumulator slot, -1 = one CTA takes the whole brick
+  uint32_t* brick;     // per slot: its brick (0xffffffff = unused)
+  uint32_t* done;      // per slot: chunks finished in this frame
+  void* acc;           // per slot: the brick's sums (the voxelizer's accumulator type)
+  uint2* items;        // (brick, chunk >= 1), (0xffffffff, 0) = unused
+  uint32_t* counters;  // [0] slots taken, [1] items taken, [2] next item to run
+  uint32_t slot_cap, item_cap;
 };
 
 // A triangle with many candidate bricks, binned by k_bin_big.
@@ -95,6 +120,7 @@ struct VoxBuffers {
   uint32_t big_cap;
   uint32_t* big_count;
   void* level0_lin;        // level 0 also in linear memory (x fastest), or null
+  HeavyBricks heavy;       // dense-brick splitting (heavy.slot null: off)
 };
 
 struct RasterBuffers {
@@ -175,6 +201,7 @@ struct BatchBuffers {
   FrameStatus* status;
   RasterBuffers rb;       // vis / gb_pos / gb_nrm point at pixel 0 of the batch
   uchar4* frame;
+  HeavyBricks heavy;      // over the batch-wide (global) brick indices
 };
 
 // Tunable launch shapes of the batched kernels (chosen by the autotuner).
@@ -235,14 +262,51 @@ cudaError_t launch_trace(const SceneParams& sp, const CameraParams& cp, const Ma
 // Exclusive scan of n u32 values into out[0..n] (out[n] = total); tmp must
 // hold scan_tmp_words(n) words.
 size_t scan_tmp_words(size_t n);
+// Work fused into the exclusive scan of the brick counts (no launches of
+// its own): the dense-brick plan, one brick per thread of the add-back
+// kernel, and a copy of the total.
+struct ScanFuse {
+  HeavyBricks hb;        // hb.slot null: no plan
+  uint32_t cap;          // pair-list capacity (offsets beyond it are clamped)
+  uint32_t slots;        // CTAs of the brick launch resident at once
+  uint32_t* total_copy;  // also receives the total (or null)
+};
 cudaError_t launch_exclusive_scan(const uint32_t* in, uint32_t* out, uint32_t* copy_out, size_t n, uint32_t* tmp,
-                                  cudaStream_t st, int* launches = nullptr);
+                                  cudaStream_t st, int* launches = nullptr, const ScanFuse* fuse = nullptr);
+
+// The split plan of brick b with pairs [beg, end) of `pairs` in all: the
+// brick is dense when it has more than kHeavyChunk pairs and more than the
+// launch's pairs per resident CTA (a lighter brick cannot hold up the
+// launch's end).  A dense brick gets an accumulator slot and one work item
+// per extra chunk of kHeavyChunk pairs; every brick's slot is written (-1:
+// not split).  A brick whose slot or items do not fit is left whole.
+// counters[0..1] count the dense bricks and their extra chunks (all of
+// them, also those that did not fit).
+__device__ __forceinline__ void heavy_plan_brick(uint32_t b, uint32_t beg, uint32_t end, uint32_t pairs,
+                                                 uint32_t slots, const HeavyBricks& hb) {
+  const unsigned long long fair = ((unsigned long long)pairs + slots - 1) / (slots ? slots : 1u);
+  const uint32_t dense = fair > kHeavyChunk ? (fair > 0xffffffffull ? 0xffffffffu : (uint32_t)fair) : kHeavyChunk;
+  int32_t slot = -1;
+  if (end - beg > dense) {
+    const uint32_t nch = (end - beg + kHeavyChunk - 1) / kHeavyChunk;
+    const uint32_t s = atomicAdd(&hb.counters[0], 1u);
+    const uint32_t e = atomicAdd(&hb.counters[1], nch - 1);
+    const bool ok = s < hb.slot_cap && e + (nch - 1) <= hb.item_cap;
+    if (s < hb.slot_cap) hb.brick[s] = ok ? b : 0xffffffffu;
+    for (uint32_t j = 1; j < nch; ++j)
+      if (e + j - 1 < hb.item_cap) hb.items[e + j - 1] = ok ? make_uint2(b, j) : make_uint2(0xffffffffu, 0u);
+    if (ok) slot = (int32_t)s;
+  }
+  hb.slot[b] = slot;
+}
 // Texture3D helpers.
 cudaError_t launch_fill_rgba8(cudaSurfaceObject_t s, int w, int h, int d, uchar4 v, cudaStream_t st);
 cudaError_t launch_box_mip_rgba8(cudaSurfaceObject_t src, int sw, int sh, int sd, cudaSurfaceObject_t dst, int dw,
                                  int dh, int dd, cudaStream_t st);
 
 size_t big_record_bytes();
+// Bytes of one dense-brick accumulator slot for a storage mode.
+size_t heavy_slot_bytes(int storage);
 
 // Batched stages (one launch per pass over all scenes of a batch).
 cudaError_t launch_voxelize_batch(const BatchWork& tris, const BatchWork& bricks, uint32_t total_bricks, int mode,

@@ -83,7 +83,8 @@ class Config(C.Structure):
 
 class StageTimes(C.Structure):
     _fields_ = [("voxelize", C.c_float), ("mipmap", C.c_float), ("gbuffer", C.c_float), ("trace", C.c_float),
-                ("total", C.c_float), ("kernel_launches", C.c_uint32), ("voxelized", C.c_uint32)]
+                ("total", C.c_float), ("kernel_launches", C.c_uint32), ("voxelized", C.c_uint32),
+                ("split_bricks", C.c_uint32)]
 
 
 class DrawObj(C.Structure):
@@ -278,6 +279,7 @@ class Renderer:
         d = {k: float(getattr(t, k)) for k, _ in StageTimes._fields_}
         d["kernel_launches"] = int(t.kernel_launches)
         d["voxelized"] = bool(t.voxelized)
+        d["split_bricks"] = int(t.split_bricks)
         return d
 
     def read_frame(self, fmt: int = FRAME_RGBA8, out: np.ndarray | None = None) -> np.ndarray:
@@ -566,6 +568,7 @@ class Batch:
         d = {k: float(getattr(t, k)) for k, _ in StageTimes._fields_}
         d["kernel_launches"] = int(t.kernel_launches)
         d["voxelized"] = bool(t.voxelized)
+        d["split_bricks"] = int(t.split_bricks)
         return d
 
     @property
