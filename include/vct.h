@@ -96,7 +96,7 @@ enum { VCT_FRAME_RGBA8 = 0, VCT_FRAME_RGBA32F = 1 };
 
 /* Engine settings the reference hard-codes (7 mip levels, renderer.cpp:186;
  * 6-direction mips, mipmap.comp; 9 diffuse cones, voxel_cone_tracing.frag
- * :168-196) plus the engine's own choices. */
+ * :140-168) plus the engine's own choices. */
 typedef struct {
   int32_t grid_res;     /* initial set_grid_resolution (reference: 128)    */
   int32_t vox_mode;     /* VCT_VOX_*: coverage rule of the voxelizer        */
@@ -106,7 +106,7 @@ typedef struct {
   int32_t cone_set;     /* VCT_CONES_*                                      */
   int32_t keep_counts;  /* keep per-voxel contribution counts (debug)       */
   int32_t keep_float_frame; /* also write the unclamped RGBA32F frame       */
-  float radiance_max;   /* upper clamp of voxel radiance (voxelize.frag:239
+  float radiance_max;   /* upper clamp of voxel radiance (voxelize.frag:153
                          * clamps to 1).  0 or 1: the reference's clamp;
                          * > 1 (HDR, e.g. 16) needs VCT_STORAGE_RGBA16F      */
   int32_t reserved[7];
@@ -238,7 +238,7 @@ vct_status vct_get_grid(vct_renderer* r, int32_t* res, int32_t* levels);
 /* No reference counterpart: an engine extension.  A small network (hash
  * encoding of the surface position + normal + albedo -> 4 x 64 ReLU MLP ->
  * RGB, BF16 tensor cores, FP32 accumulation) trained on the GPU to predict
- * trace_diffuse (voxel_cone_tracing.frag:168-196), the average of the nine
+ * trace_diffuse (voxel_cone_tracing.frag:140-168), the average of the nine
  * diffuse cones; with VCT_DIFFUSE_MLP a frame evaluates it instead of
  * tracing those cones.  The cone tracer stays the default and the judge. */
 enum { VCT_DIFFUSE_CONES = 0, VCT_DIFFUSE_MLP = 1 };
@@ -340,7 +340,7 @@ vct_status vct_voxelize_noalloc(const vct_device_mesh* meshes, uint32_t n_meshes
  * voxel the mean albedo x transmittance and alpha, the mean normal and the
  * mean emission x transmittance (three RGBA8 grids), and every frame lights
  * the voxels at their centres from those grids (the per-light terms of
- * voxelize.frag:208-227).  Frames whose queued models, matrices, cube size,
+ * voxelize.frag:128-143).  Frames whose queued models, matrices, cube size,
  * grid and materials equal the previous frame's skip voxelization: a light
  * change costs one injection pass.  The lighting is evaluated from voxel
  * means at the voxel centre instead of per fragment, an approximation of

@@ -157,7 +157,7 @@ template <class R> static inline V3<R> mat_of(const orc_material& m, int which) 
 static inline bool illum_transparent(int illum) { return illum == 4 || illum == 6 || illum == 7 || illum == 9; }
 
 // --------------------------------------------------------- voxelize.frag --
-// Upper clamp of the voxel colour: 1 in the reference (voxelize.frag:239);
+// Upper clamp of the voxel colour: 1 in the reference (voxelize.frag:153);
 // orc_params.radiance_max for HDR storage.  Set by voxelize_impl before its
 // worker threads start (the oracle runs one call at a time).
 static double g_radiance_max = 1.0;
@@ -166,12 +166,12 @@ static double g_radiance_max = 1.0;
 // transmittance + 1 (occupancy).  Set before voxelize_impl's threads start.
 static int g_attr_mode = 0;
 
-// Per-fragment colour, voxelize.frag:208-239.  pos is in grid space
+// Per-fragment colour, voxelize.frag:124-153.  pos is in grid space
 // ([-1,1]^3 = world / cube_size), nrm the interpolated vertex normal.
 template <class R>
 static V4<R> voxel_fragment_color(const orc_scene* s, const orc_material& mat, V3<R> pos, V3<R> nrm) {
   V3<R> color;
-  int nl = std::min<int>((int)s->n_lights, 10);  // MAX_POINT_LIGHTS, voxelize.frag:126,214
+  int nl = std::min<int>((int)s->n_lights, 10);  // MAX_POINT_LIGHTS, voxelize.frag:40,128
   R cube = R(s->cube_size);
   V3<R> nn = normalize(nrm);
   for (int i = 0; i < nl; ++i) {
@@ -179,15 +179,15 @@ static V4<R> voxel_fragment_color(const orc_scene* s, const orc_material& mat, V
     V3<R> lp(R(L.position[0]) / cube, R(L.position[1]) / cube, R(L.position[2]) / cube);
     V3<R> dir = normalize(lp - pos);
     R d = length(lp - pos);
-    R a = R(1) / (R(1) + R(0) * d + R(1) * d * d);  // attenuate(1,0,1,d), :142-145
+    R a = R(1) / (R(1) + R(0) * d + R(1) * d * d);  // attenuate(1,0,1,d), voxelize.frag:56-59,134
     R cs = fmaxr(dot(nn, dir), R(0));
     V3<R> lc(R(L.color[0]), R(L.color[1]), R(L.color[2]));
     color = color + lc * (cs * a * R(L.intensity));
   }
-  color = mulv(mat_of<R>(mat, 0), color) + mat_of<R>(mat, 3);  // :228-229
+  color = mulv(mat_of<R>(mat, 0), color) + mat_of<R>(mat, 3);  // voxelize.frag:142-143
   V3<R> trans(R(1), R(1), R(1));
   R alpha = R(1);
-  if (illum_transparent(mat.illum)) { trans = mat_of<R>(mat, 2); alpha = R(mat.dissolve); }  // :231-237
+  if (illum_transparent(mat.illum)) { trans = mat_of<R>(mat, 2); alpha = R(mat.dissolve); }  // voxelize.frag:145-151
   if (g_attr_mode) {
     const V3<R> t = illum_transparent(mat.illum) ? mat_of<R>(mat, 2) : V3<R>(R(1), R(1), R(1));
     if (g_attr_mode == 1) {
@@ -203,7 +203,7 @@ static V4<R> voxel_fragment_color(const orc_scene* s, const orc_material& mat, V
   V3<R> c = mulv(trans, color);
   const R hi = R(g_radiance_max);
   auto cl = [hi](R v) { return v < R(0) ? R(0) : (v > hi ? hi : v); };
-  return V4<R>(cl(c.x), cl(c.y), cl(c.z), clamp01(alpha));  // :239
+  return V4<R>(cl(c.x), cl(c.y), cl(c.z), clamp01(alpha));  // voxelize.frag:153
 }
 
 // One voxel contribution: voxel index + clamped colour.
@@ -226,7 +226,7 @@ static inline bool top_left(i64 ax, i64 ay, i64 bx, i64 by) {
 }
 static inline bool edge_in(i64 e, bool tl) { return e > 0 || (e == 0 && tl); }
 
-// Dominant axis of voxelize.geom:58-82: 2 -> project to (x,y), 0 -> (y,z),
+// Dominant axis of voxelize.geom:27-51: 2 -> project to (x,y), 0 -> (y,z),
 // 1 -> (x,z).  Strict comparisons: ties fall through to the y projection.
 static inline int dominant_axis(const float v[3][3]) {
   float e1[3], e2[3];
@@ -247,7 +247,7 @@ static inline bool coord_ok(float v) { return std::fabs(v) <= 64.0f; }  // also 
 // dominant projection.  A sample (i, j) sits at window (i + 0.5, j + 0.5);
 // vertices are snapped to 1/256 of a sample pixel; the sample's depth is the
 // FP32 barycentric interpolation of the vertex depths and its voxel is
-// int(N * (0.5*c + 0.5)) (truncation, voxelize.frag:242-243).
+// int(N * (0.5*c + 0.5)) (truncation, voxelize.frag:156-157).
 template <class R>
 static bool raster_tri_ref(const orc_scene* s, int N, const TriVerts& tv, const float* nrm_obj[3],
                            const orc_material& mat, std::vector<Contrib<R>>& out) {
@@ -701,8 +701,8 @@ static std::atomic<uint64_t> g_stats[kStatN];
 static bool g_stats_on = false;
 static thread_local int t_cone_class = 0;
 
-// trace_cone, voxel_cone_tracing.frag:116-147 (face_indices :99-106,
-// sample_voxel :108-114).
+// trace_cone, voxel_cone_tracing.frag:88-119 (face_indices :71-78,
+// sample_voxel :80-86).
 template <class R>
 static ConeOut<R> trace_cone(const Maps& m, V3<R> origin, V3<R> dir, R aperture, R max_dist) {
   dir = normalize(dir);
@@ -736,17 +736,17 @@ static ConeOut<R> trace_cone(const Maps& m, V3<R> origin, V3<R> dir, R aperture,
   return {acc, steps};
 }
 
-// tangent, voxel_cone_tracing.frag:154-162.
+// tangent, voxel_cone_tracing.frag:126-134.
 template <class R> static V3<R> tangent(V3<R> n) {
   V3<R> t1 = cross(n, V3<R>(0, 0, 1)), t2 = cross(n, V3<R>(0, 1, 0));
   return length(t1) > length(t2) ? normalize(t1) : normalize(t2);
 }
 template <class R> static inline V3<R> mixv(V3<R> a, V3<R> b, R t) { return a * (R(1) - t) + b * t; }
 
-static const double kTan22_5 = 0.55785173935;   // TAN_22_5, :164 (kept verbatim)
-static const double kMaxDistance = 1.73205080757;  // MAX_DISTANCE, :166
+static const double kTan22_5 = 0.55785173935;   // TAN_22_5, :136 (kept verbatim)
+static const double kMaxDistance = 1.73205080757;  // MAX_DISTANCE, :138
 
-// trace_diffuse, voxel_cone_tracing.frag:168-196 (9 cones, equal weights).
+// trace_diffuse, voxel_cone_tracing.frag:140-168 (9 cones, equal weights).
 // cone_set SIX60 (no reference counterpart): the normal plus 5 cones 60
 // degrees off it, evenly spaced in azimuth in the same tangent frame, each
 // of aperture 2*tan(30 deg), equal weights.
@@ -788,14 +788,14 @@ template <class R> static V3<R> refract(V3<R> I, V3<R> N, R eta) {
 }
 template <class R> static V3<R> reflect(V3<R> I, V3<R> N) { return I - N * (R(2) * dot(N, I)); }
 
-template <class R> static R specular_aperture(const orc_material& mat) {  // :248-255
+template <class R> static R specular_aperture(const orc_material& mat) {  // voxel_cone_tracing.frag:220-227
   R r = std::sqrt(R(2) / (R(mat.shininess) + R(2)));
   R a = R(std::tan(R(1.57079) * r));
   const R lo = R(0.0174533), hi = R(3.14159265);
   return a < lo ? lo : (a > hi ? hi : a);
 }
 
-// direct_light, voxel_cone_tracing.frag:203-246.
+// direct_light, voxel_cone_tracing.frag:175-218.
 template <class R>
 static V3<R> direct_light(const orc_scene* s, const Maps& m, int enable_shadow, const orc_material& mat,
                           V3<R> pos, V3<R> nrm, V3<R> view_dir) {
@@ -832,7 +832,7 @@ static V3<R> direct_light(const orc_scene* s, const Maps& m, int enable_shadow, 
   return result + V3<R>(clamp01(e.x), clamp01(e.y), clamp01(e.z));
 }
 
-// main, voxel_cone_tracing.frag:274-303, for one visible surface point.
+// main, voxel_cone_tracing.frag:246-275, for one visible surface point.
 template <class R>
 static V4<R> shade_pixel(const orc_scene* s, const orc_params* p, const Maps& m, V3<R> world, V3<R> nrm,
                          uint32_t mat_id, bool* written) {
@@ -1109,7 +1109,7 @@ int64_t orc_voxelize_attr(const orc_scene* s, const orc_params* p, uint8_t* albe
 
 // Deferred light injection (no reference counterpart), FP64: each occupied
 // voxel lit at its centre from its mean attributes with the per-light terms
-// of voxelize.frag:208-227; RGBA8 round to nearest.
+// of voxelize.frag:128-143; RGBA8 round to nearest.
 void orc_inject(const orc_scene* s, const orc_params* p, const uint8_t* albedo, const uint8_t* normal,
                 const uint8_t* emission, uint8_t* level0) {
   const int N = p->grid_res;

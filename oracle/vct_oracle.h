@@ -35,8 +35,8 @@ typedef struct {
 } orc_point_light;
 
 /* material_data_t, renderer.h:94-120 (packed, 128 bytes, std140 layout of
- * the GLSL `material` block in voxelize.frag:96-117 and
- * voxel_cone_tracing.frag:31-52). */
+ * the GLSL `material` block in voxelize.frag:10-31 and
+ * voxel_cone_tracing.frag:3-24). */
 typedef struct {
   float ambient[4];
   float diffuse[4];
@@ -170,7 +170,7 @@ void orc_texture_lod(const orc_params* p, const uint8_t* level0,
                      const uint8_t* chains, int32_t map, const double* u,
                      double lod, double* rgba);
 
-/* One cone march, trace_cone() of voxel_cone_tracing.frag:116-147. */
+/* One cone march, trace_cone() of voxel_cone_tracing.frag:88-119. */
 void orc_trace_cone(const orc_params* p, const uint8_t* level0,
                     const uint8_t* chains, const double* origin,
                     const double* dir, double aperture, double max_dist,

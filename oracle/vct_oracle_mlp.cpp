@@ -2,7 +2,7 @@
 // diffuse term: multiresolution hash encoding of the surface position +
 // normal + albedo -> 4 x 64 ReLU MLP -> RGB, its MSE loss and its exact FP64
 // gradients.  The reference has no learned component (the MLP stands in for
-// trace_diffuse, voxel_cone_tracing.frag:168-196); this file pins the CUDA
+// trace_diffuse, voxel_cone_tracing.frag:140-168); this file pins the CUDA
 // training kernels' forward and backward passes.
 //
 // Encoding (per level l of 16): resolution N_l = floor(N_min * b^l),

@@ -68,7 +68,7 @@ def _frame(vct, scene, setup=None, **cfg):
 
 
 def test_rendering_phases_are_additive(vct, oracle, scene):
-    """final = specular + diffuse + direct (voxel_cone_tracing.frag:297-300,
+    """final = specular + diffuse + direct (voxel_cone_tracing.frag:265-272,
     no transparent materials here), each phase switched by
     set_rendering_phases (renderer.cpp:368-371)."""
     parts = {}

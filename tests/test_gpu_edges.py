@@ -81,7 +81,7 @@ def test_pathological_triangles(vct, oracle, mode):
 
 
 def test_light_limit_and_materials(vct, oracle):
-    """11 queued lights (the shader reads 10, voxelize.frag:126), transparent
+    """11 queued lights (the shader reads 10, voxelize.frag:40,128), transparent
     (illum 4: refraction cone, dissolve), emissive and very glossy
     materials, instanced models, the six-cone set and isotropic mips."""
     base = scenes.scene_small(seed=31, width=72, height=48)
@@ -112,7 +112,7 @@ def test_ragged_frames_and_small_grids(vct, oracle, w, h, n):
 
 
 def test_camera_outside_the_grid(vct, oracle):
-    """within_cube (voxel_cone_tracing.frag:278-279) tests the texture-space
+    """within_cube (voxel_cone_tracing.frag:61-64, 250) tests the texture-space
     position u = 0.5 p + 0.5 against |u| < 1, i.e. grid-space p in (-3, 1):
     fragments with some p >= 1 or p <= -3 keep the clear colour, fragments
     with p in (-3, -1] are shaded although they lie outside the voxel grid."""

@@ -149,7 +149,7 @@ def test_empty_queue_gives_clear_colour(vct):
 
 def test_voxel_debug_view(vct, oracle, small_scene):
     """view_voxel_dir < 7 shows textureLod(map, pos, lod) (voxel_cone_tracing
-    .frag:281-285); the reference's constructor default is map 0, lod 0."""
+    .frag:253-257); the reference's constructor default is map 0, lod 0."""
     r = _render(vct, small_scene, sampler=1)
     r.set_voxel_view_dir(3, 1.5)
     ids = list(range(len(small_scene.meshes)))

@@ -96,7 +96,7 @@ def _steps_to(n, aperture, max_dist):
 
 def test_cone_through_empty_space(oracle):
     """Empty grid: the cone accumulates nothing and marches until max_dist
-    with steps max(diam/2, 1/N) (voxel_cone_tracing.frag:116-147)."""
+    with steps max(diam/2, 1/N) (voxel_cone_tracing.frag:88-119)."""
     n = 32
     p = oracle.Params(grid_res=n)
     l0 = np.zeros((n, n, n, 4), np.uint8)
@@ -139,7 +139,7 @@ def test_axis_aligned_slab_ref(oracle):
 
 
 def test_degenerate_dominant_axis_dropped_ref(oracle):
-    """|n| = (1,0,1): both strict tests of voxelize.geom:71-75 fail, the y
+    """|n| = (1,0,1): both strict tests of voxelize.geom:40-47 fail, the y
     projection is chosen and the triangle projects to a line -> no samples.
     The conservative mode still voxelizes it."""
     n = 16
@@ -153,7 +153,7 @@ def test_degenerate_dominant_axis_dropped_ref(oracle):
 
 def test_truncation_quirk_low_face(oracle):
     """int(N*(0.5c+0.5)) truncates toward 0: depth a quarter voxel below the
-    grid still lands in slab 0 (voxelize.frag:243); depth exactly +1 maps to
+    grid still lands in slab 0 (voxelize.frag:157); depth exactly +1 maps to
     index N and is dropped."""
     n = 16
     s = tri_scene(quad_z(-1.0 - 0.25 * 2 / n))
@@ -177,7 +177,7 @@ def test_running_average_is_mean(oracle):
 
 def test_light_attenuation_value(oracle):
     """One light straight above a floor quad: colour = diffuse * cos *
-    1/(1+d^2) (voxelize.frag:214-229) at the sample points."""
+    1/(1+d^2) (voxelize.frag:128-139) at the sample points."""
     n = 8
     k = 3
     z = (k + 0.5) * 2 / n - 1

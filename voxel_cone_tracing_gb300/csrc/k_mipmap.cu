@@ -7,7 +7,7 @@
 // and produces up to four levels of all six directional maps from it (the
 // intermediate levels never leave shared memory except for their own store).
 // Level 0 is stored once and shared by the six maps, as in the reference
-// (all six textures receive identical level-0 data, voxelize.frag:245-246).
+// (all six textures receive identical level-0 data, voxelize.frag:159-160).
 // A second, tiny pass builds the remaining levels (5, 6) from level 4.
 //
 // RGBA8 texels are evaluated exactly: with texels k/255 the stored value of

@@ -1,6 +1,6 @@
 // k_mlp.cu -- the learned diffuse term: a multiresolution hash encoding of
 // the surface position plus normal and albedo, fed to a 4 x 64 ReLU MLP that
-// predicts trace_diffuse (voxel_cone_tracing.frag:168-196) -- the average of
+// predicts trace_diffuse (voxel_cone_tracing.frag:140-168) -- the average of
 // the nine diffuse cones -- so that a frame can skip those cones.
 //
 // Network (the CPU oracle, oracle/vct_oracle_mlp.cpp, restates it in FP64):

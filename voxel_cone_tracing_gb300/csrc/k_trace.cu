@@ -1,5 +1,5 @@
 // k_trace.cu -- the ConeTracer: replaces the per-fragment cone marching of
-// voxel_cone_tracing.frag (main :274-303) over the G-buffer.
+// voxel_cone_tracing.frag (main :246-275) over the G-buffer.
 //
 // One thread shades one visible pixel; a 16x16 CTA covers a 16x16 pixel tile
 // (each warp a 16x2 strip) so that neighbouring lanes march neighbouring,
@@ -9,7 +9,7 @@
 // CLAMP_TO_BORDER(0) over levels 0..L-1 (texture_3d.cpp:10-15).  Level 0 is
 // one texture shared by the six maps (as in the reference, where all six
 // maps hold identical level-0 data), so for lambda < 1 the three per-axis
-// lookups of sample_voxel (:108-114) need one level-0 fetch:
+// lookups of sample_voxel (:80-86) need one level-0 fetch:
 //   sum_k a_k [(1-f) T0 + f T1_k] = (1-f) T0 sum_k a_k + f sum_k a_k T1_k.
 // Two samplers:
 //   VCT_SAMPLER_HW    -- the texture unit filters (trilinear within a level,
@@ -43,8 +43,8 @@ constexpr int kTraceMinBlocks = VCT_TRACE_MIN_BLOCKS;
 // values in registers, so it is compiled for its own occupancy.
 constexpr int kTraceBatchMinBlocks = VCT_TRACE_BATCH_MIN_BLOCKS;
 
-constexpr float kTan22_5 = 0.55785173935f;      // TAN_22_5 (:164), kept verbatim
-constexpr float kMaxDistance = 1.73205080757f;  // MAX_DISTANCE (:166)
+constexpr float kTan22_5 = 0.55785173935f;      // TAN_22_5 (:136), kept verbatim
+constexpr float kMaxDistance = 1.73205080757f;  // MAX_DISTANCE (:138)
 
 // ---------------------------------------------------------------- samplers --
 template <int STORAGE>
@@ -135,7 +135,7 @@ __device__ __forceinline__ float4 sample_voxel(const MapSet& m, V3 u, int ix, in
 }
 
 // ------------------------------------------------------------ cone march ----
-// trace_cone, voxel_cone_tracing.frag:116-147.
+// trace_cone, voxel_cone_tracing.frag:88-119.
 template <int SAMPLER, bool ISO, int STORAGE>
 __device__ float4 trace_cone(const MapSet& m, V3 origin, V3 dir, float aperture, float max_dist) {
   dir = normalize(dir);
@@ -159,14 +159,14 @@ __device__ float4 trace_cone(const MapSet& m, V3 origin, V3 dir, float aperture,
   return acc;
 }
 
-// tangent, :154-162.
+// tangent, :126-134.
 __device__ __forceinline__ V3 tangent(V3 n) {
   const V3 t1 = cross(n, v3(0.f, 0.f, 1.f)), t2 = cross(n, v3(0.f, 1.f, 0.f));
   return length(t1) > length(t2) ? normalize(t1) : normalize(t2);
 }
 __device__ __forceinline__ V3 mixv(V3 a, V3 b, float t) { return a * (1.0f - t) + b * t; }
 
-// trace_diffuse, :168-196 (9 equal-weight cones); cone set SIX60 (no
+// trace_diffuse, :140-168 (9 equal-weight cones); cone set SIX60 (no
 // reference counterpart): the normal plus 5 cones 60 degrees off it in the
 // same tangent frame, aperture 2 tan(30 deg), equal weights.
 template <int SAMPLER, bool ISO, int STORAGE>
@@ -189,7 +189,7 @@ __device__ V3 trace_diffuse(const MapSet& m, int cone_set, V3 origin, V3 n) {
   }
   const V3 c1 = (o1 + o2) * 0.5f, c2 = (o1 - o2) * 0.5f;
   acc = trace_cone<SAMPLER, ISO, STORAGE>(m, origin, n, kTan22_5, kMaxDistance);
-  // Side cones o1, -o1, o2, -o2, c1, -c1, c2, -c2 (:184-193), selected
+  // Side cones o1, -o1, o2, -o2, c1, -c1, c2, -c2 (:156-165), selected
   // arithmetically so that no local-memory array is needed.
 #pragma unroll 1
   for (int k = 0; k < 8; ++k) {
@@ -210,7 +210,7 @@ __device__ __forceinline__ V3 reflect(V3 I, V3 N) { return I - N * (2.0f * dot(N
 
 __device__ __forceinline__ V3 mat3v(const float* f) { return v3(f[0], f[1], f[2]); }
 
-// direct_light, :203-246.
+// direct_light, :175-218.
 template <int SAMPLER, bool ISO, int STORAGE>
 __device__ V3 direct_light(const SceneParams& sp, const MapSet& m, int enable_shadow, const vct_material_data& mat,
                            V3 pos, V3 nrm, V3 view_dir) {
@@ -243,7 +243,7 @@ __device__ V3 direct_light(const SceneParams& sp, const MapSet& m, int enable_sh
   return result + v3(clamp01(mat.emission[0]), clamp01(mat.emission[1]), clamp01(mat.emission[2]));
 }
 
-__device__ __forceinline__ float specular_aperture(float shininess) {  // :248-255
+__device__ __forceinline__ float specular_aperture(float shininess) {  // :220-227
   const float r = sqrtf(2.0f / (shininess + 2.0f));
   const float a = tanf(1.57079f * r);
   return fminf(fmaxf(a, 0.0174533f), 3.14159265f);
@@ -253,7 +253,7 @@ __device__ __forceinline__ unsigned char unorm8(float v) {
   return (unsigned char)__float2uint_rz(clamp01(v) * 255.0f + 0.5f);
 }
 
-// Shades pixel (px, py) of one frame (main, voxel_cone_tracing.frag:274-303).
+// Shades pixel (px, py) of one frame (main, voxel_cone_tracing.frag:246-275).
 template <int SAMPLER, bool ISO, int STORAGE>
 __device__ __forceinline__ void trace_px(const SceneParams& sp, const CameraParams& cp, const MapSet& m,
                                          const TraceParams& tp, const float4* __restrict__ gb_pos,
@@ -269,10 +269,10 @@ __device__ __forceinline__ void trace_px(const SceneParams& sp, const CameraPara
     const vct_material_data& mat = sp.materials[__float_as_uint(g0.w)];
     const V3 pos = v3(world.x / sp.cube_size, world.y / sp.cube_size, world.z / sp.cube_size) * 0.5f +
                    v3(0.5f, 0.5f, 0.5f);
-    // within_cube(pos, 0) (:278-279): a fragment outside returns without
+    // within_cube(pos, 0) (:61-64, 250): a fragment outside returns without
     // writing; the pixel keeps the clear colour.
     if (fabsf(pos.x) < 1.0f && fabsf(pos.y) < 1.0f && fabsf(pos.z) < 1.0f) {
-      if (tp.view_voxel_dir < 7) {  // voxel debug view, :281-285
+      if (tp.view_voxel_dir < 7) {  // voxel debug view, :253-257
         if (tp.view_voxel_dir >= 0 && tp.view_voxel_dir <= 5) {
           const float lod = fmaxf(tp.view_voxel_lod, 0.0f);
           const V3 one = v3(1.f, 0.f, 0.f);

@@ -9,18 +9,18 @@
 //   4. k_bricks: one CTA per brick.  Warps take 32 triangles at a time, set
 //      them up in shared memory, expand (triangle, sample|voxel) work items
 //      across lanes, decide coverage with the exact rule of the selected mode,
-//      shade in FP32 (voxelize.frag:208-239) and add fixed-point colour sums
+//      shade in FP32 (voxelize.frag:124-153) and add fixed-point colour sums
 //      and counts into shared-memory accumulators.  The CTA then writes its
 //      whole brick of level 0 (empty voxels = 0, which is the clear) as RGBA8
 //      or RGBA16F through a surface -- level 0 is written exactly once.
 //
 // Coverage rules (the CPU oracle implements the same ones):
 //   REF_RASTER2X -- the reference's method: dominant-axis projection
-//     (voxelize.geom:58-82) rasterised on the 2N x 2N viewport
+//     (voxelize.geom:27-51) rasterised on the 2N x 2N viewport
 //     (renderer.cpp:339-340): vertices snapped to 1/256 sample pixel,
 //     integer edge functions, top-left fill rule; sample depth = FP32
 //     barycentric interpolation, voxel = int(N*(0.5*c+0.5)) (voxelize.frag
-//     :242-243, truncation).
+//     :156-157, truncation).
 //   CONSERVATIVE -- exact separating-axis triangle/box test on vertices
 //     snapped to 1/256 voxel (int64, the plane test in int128), colour at
 //     the triangle point closest to the voxel centre.
@@ -286,7 +286,7 @@ __global__ void __launch_bounds__(256) k_bin_big(int N, const BinRec* __restrict
 }
 
 // ------------------------------------------------------------- shading -----
-// voxelize.frag:208-239 in FP32.
+// voxelize.frag:124-153 in FP32.
 __device__ __forceinline__ float4 voxel_color(const SceneParams& sp, const vct_material_data& m, V3 pos, V3 nrm) {
   V3 color = v3(0.f, 0.f, 0.f);
   const V3 nn = normalize(nrm);
@@ -307,7 +307,7 @@ __device__ __forceinline__ float4 voxel_color(const SceneParams& sp, const vct_m
     color = mulv(color, v3(m.transmittance[0], m.transmittance[1], m.transmittance[2]));
     alpha = m.dissolve;
   }
-  // clamp(vec4, 0, 1) (:239); with HDR storage the colour clamps to
+  // clamp(vec4, 0, 1) (voxelize.frag:153); with HDR storage the colour clamps to
   // [0, radiance_max] instead (radiance_max = 1 is the reference).
   const float hi = sp.radiance_max;
   return make_float4(fminf(fmaxf(color.x, 0.0f), hi), fminf(fmaxf(color.y, 0.0f), hi),
@@ -378,7 +378,7 @@ template <> struct AccT<VCT_STORAGE_RGBA16F> {
   }
 };
 // Light-injection attributes of one contribution (the factors of
-// voxelize.frag:228-239 that do not depend on the lights): colour =
+// voxelize.frag:141-153 that do not depend on the lights): colour =
 // t * (diffuse * lighting + emission), t = transmittance for transparent
 // materials, else 1.
 __device__ __forceinline__ void voxel_attrs(const vct_material_data& m, V3 nrm, float a[10]) {
@@ -449,7 +449,7 @@ __device__ int setup_ref(const SceneParams& sp, int N, uint32_t t, const int b3[
   TriLoad tl;
   load_tri<true>(sp, t, tl);
   if (!tl.ok) return 0;
-  // Dominant axis, voxelize.geom:58-82 (FP32, fixed order).
+  // Dominant axis, voxelize.geom:27-51 (FP32, fixed order).
   float e1[3], e2[3];
   for (int i = 0; i < 3; ++i) { e1[i] = rsub(tl.g[1][i], tl.g[0][i]); e2[i] = rsub(tl.g[2][i], tl.g[0][i]); }
   const float px = fabsf(rsub(rmul(e1[1], e2[2]), rmul(e2[1], e1[2])));
@@ -1182,9 +1182,9 @@ namespace vct {
 namespace {
 
 // Deferred light injection (no reference counterpart: the reference shades
-// every fragment while voxelizing, voxelize.frag:208-239).  Each occupied
+// every fragment while voxelizing, voxelize.frag:124-153).  Each occupied
 // voxel is lit at its centre (grid space (2x+1)/N - 1) with its mean normal
-// and the same per-light terms as voxelize.frag:208-227:
+// and the same per-light terms as voxelize.frag:128-143:
 //   colour = clamp(albedo * sum_i color_i * intensity_i * max(n.l_i, 0) /
 //                  (1 + d_i^2) + emission, 0, 1),  alpha = mean alpha,
 // stored as RGBA8 rounded to nearest.

@@ -9,7 +9,7 @@
 
 namespace vct {
 
-constexpr int kMaxLights = 10;   // MAX_POINT_LIGHTS, voxelize.frag:126
+constexpr int kMaxLights = 10;   // MAX_POINT_LIGHTS, voxelize.frag:40,128
 constexpr int kMaxLevels = 7;    // create_tex_3d(res,res,res,7), renderer.cpp:186
 constexpr int kBrick = 8;        // voxelizer brick edge (voxels)
 constexpr int kMaxMaps = 6;

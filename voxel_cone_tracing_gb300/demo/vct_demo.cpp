@@ -204,7 +204,7 @@ bool write_ppm(const std::string& path, const std::vector<uint8_t>& rgba, int w,
 
 int main(int argc, char** argv) {
   std::string assets, out = "vct_frame";
-  int frames = 1, width = 800, height = 600, grid = 128;  // main.cpp:18-19; renderer.cpp:146
+  int frames = 1, width = 800, height = 600, grid = 128;  // main.cpp:28-29; renderer.cpp:146
   float rot_step = 0.05f;
   for (int i = 1; i < argc; ++i) {
     const std::string a = argv[i];

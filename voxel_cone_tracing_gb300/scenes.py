@@ -55,7 +55,7 @@ def default_material() -> np.ndarray:
 def make_material(albedo, roughness=1.0, specular=None, emission=(0, 0, 0), illum=2,
                   dissolve=1.0, ior=1.5, transmittance=(1, 1, 1)) -> np.ndarray:
     """A material_data_t.  roughness r maps to the reference's shininess by
-    inverting voxel_cone_tracing.frag:248 (r = sqrt(2 / (shininess + 2)))."""
+    inverting voxel_cone_tracing.frag:220 (r = sqrt(2 / (shininess + 2)))."""
     m = np.zeros((), MATERIAL_DTYPE)
     r = float(np.clip(roughness, 0.05, 1.0))
     m["ambient"][:3] = albedo
