@@ -75,6 +75,10 @@ def lib():
             getattr(L, f).restype = C.c_int64
             getattr(L, f).argtypes = [P, P, P, P]
         L.orc_mipmap.argtypes = [P, P, P]
+        L.orc_voxelize_cas.restype = C.c_int64
+        L.orc_voxelize_cas.argtypes = [P, P, C.c_int32, C.c_uint64, P]
+        L.orc_cas_avg.restype = C.c_uint32
+        L.orc_cas_avg.argtypes = [P, C.c_int32]
         L.orc_voxelize_attr.restype = C.c_int64
         L.orc_voxelize_attr.argtypes = [P, P, P, P, P, P]
         L.orc_inject.argtypes = [P, P, P, P, P, P]
@@ -179,6 +183,27 @@ def voxelize(scene, params: Params, fp32: bool = False):
     f = lib().orc_voxelize_f32 if fp32 else lib().orc_voxelize
     rej = f(sh.ptr, C.addressof(pc), _ptr(l0), _ptr(cnt))
     return l0, cnt, int(rej)
+
+
+ORDER_DRAW, ORDER_REVERSE, ORDER_SHUFFLED = 0, 1, 2
+
+
+def voxelize_cas(scene, params: Params, order: int = ORDER_DRAW, seed: int = 0):
+    """Informational: level 0 as the reference's running average
+    (imageAtomicRGBA8Avg, voxelize.frag:62-119) leaves it for one arrival
+    order of the contributions -> uint8 (N,N,N,4) [z,y,x], low bits = count."""
+    n = params.grid_res
+    l0 = np.zeros((n, n, n, 4), np.uint8)
+    sh, pc = _SceneHold(scene), params.c()
+    lib().orc_voxelize_cas(sh.ptr, C.addressof(pc), int(order), int(seed), _ptr(l0))
+    return l0
+
+
+def cas_avg(rgba) -> int:
+    """The running average of a sequence of RGBA contributions arriving at a
+    cleared voxel; returns the stored 32-bit word (R in the low byte)."""
+    a = np.ascontiguousarray(np.asarray(rgba, np.float32).reshape(-1, 4))
+    return int(lib().orc_cas_avg(a.ctypes.data, a.shape[0]))
 
 
 def voxelize_hdr(scene, params: Params):

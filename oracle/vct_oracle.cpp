@@ -461,9 +461,11 @@ static inline void tri_verts(const orc_scene* s, const orc_instance& in, uint32_
 // stored RGBA8 with round-to-nearest.  Contributions are generated in
 // triangle chunks and summed per voxel in global triangle order, so the
 // result does not depend on the thread count.
+// Every contribution of the frame, in triangle chunks of consecutive queued
+// triangles: lists[0], lists[1], ... concatenated are in draw order
+// (triangles in queue order, each triangle's samples in scan order).
 template <class R>
-static int64_t voxelize_impl(const orc_scene* s, const orc_params* p, uint8_t* level0, uint32_t* counts,
-                             float* level0f = nullptr) {
+static int64_t gather_contribs(const orc_scene* s, const orc_params* p, std::vector<std::vector<Contrib<R>>>& lists) {
   const int N = p->grid_res;
   g_radiance_max = p->radiance_max > 0.0f ? (double)p->radiance_max : 1.0;
   std::vector<TriRef> tris;
@@ -474,7 +476,7 @@ static int64_t voxelize_impl(const orc_scene* s, const orc_params* p, uint8_t* l
   }
   const int nthreads = std::max(1, p->threads);
   const int chunks = std::max(1, std::min<int>(nthreads * 4, (int)std::max<size_t>(1, tris.size() / 64)));
-  std::vector<std::vector<Contrib<R>>> lists(chunks);
+  lists.assign(chunks, {});
   std::vector<int64_t> rejected(chunks, 0);
   parallel_for(nthreads, chunks, [&](int ch) {
     size_t b = tris.size() * ch / chunks, e = tris.size() * (ch + 1) / chunks;
@@ -490,6 +492,19 @@ static int64_t voxelize_impl(const orc_scene* s, const orc_params* p, uint8_t* l
       if (!ok) rejected[ch]++;
     }
   });
+  int64_t rej = 0;
+  for (int64_t r : rejected) rej += r;
+  return rej;
+}
+
+template <class R>
+static int64_t voxelize_impl(const orc_scene* s, const orc_params* p, uint8_t* level0, uint32_t* counts,
+                             float* level0f = nullptr) {
+  const int N = p->grid_res;
+  const int nthreads = std::max(1, p->threads);
+  std::vector<std::vector<Contrib<R>>> lists;
+  const int64_t rej = gather_contribs<R>(s, p, lists);
+  const int chunks = (int)lists.size();
   const size_t nvox = (size_t)N * N * N;
   const int parts = nthreads;
   parallel_for(nthreads, parts, [&](int part) {
@@ -518,8 +533,70 @@ static int64_t voxelize_impl(const orc_scene* s, const orc_params* p, uint8_t* l
       }
     }
   });
-  int64_t rej = 0;
-  for (int64_t r : rejected) rej += r;
+  return rej;
+}
+
+// ---- the reference's running average (informational) ----------------------
+// imageAtomicRGBA8Avg and its helpers, voxelize.frag:62-119, for one
+// contribution arriving at a voxel that holds `cur` (0 = cleared).  With one
+// writer at a time the compare-and-swap loop runs its body once: the stored
+// RGBA8 (the low bit of each byte masked off) times the 4-bit count n in those
+// low bits, plus the new value (x 255), divided by n + 1, rounded to an even
+// integer (round(x / 2) * 2; GLSL leaves the direction of a .5 tie to the
+// implementation, here away from zero), each channel truncated to uint and
+// masked to 8 bits (so 256 wraps to 0), and n + 1 stored back in the low bits
+// (16 wraps to 0, restarting the average).  FP32 throughout, as in GLSL.
+static inline uint32_t cas_pack(const float v[4]) {
+  return ((uint32_t)v[3] & 0xFFu) << 24 | ((uint32_t)v[2] & 0xFFu) << 16 | ((uint32_t)v[1] & 0xFFu) << 8 |
+         ((uint32_t)v[0] & 0xFFu);
+}
+static inline uint32_t cas_enc(uint32_t m, uint32_t n) {
+  return (m & 0xFEFEFEFEu) | (n & 1u) | (n & 2u) << 7 | (n & 4u) << 14 | (n & 8u) << 21;
+}
+static inline uint32_t cas_dec(uint32_t m) {
+  return (m & 1u) | (m & 0x100u) >> 7 | (m & 0x10000u) >> 14 | (m & 0x1000000u) >> 21;
+}
+static uint32_t cas_step(uint32_t cur, const float c[4]) {
+  float val[4];
+  for (int q = 0; q < 4; ++q) val[q] = c[q] * 255.0f;
+  if (cur == 0) return cas_enc(cas_pack(val), 1u);  // the first compare-and-swap (expected 0) succeeds
+  const uint32_t m = cur & 0xFEFEFEFEu;
+  const uint32_t n = cas_dec(cur);
+  float r[4];
+  for (int q = 0; q < 4; ++q) {
+    float x = (float)((m >> (8 * q)) & 0xFFu);
+    x = x * (float)n + val[q];
+    x = x / (float)(n + 1);
+    r[q] = std::round(x / 2.0f) * 2.0f;
+  }
+  return cas_enc(cas_pack(r), n + 1);
+}
+
+// Level 0 as the reference's running average leaves it after the frame's
+// contributions arrive one at a time in a fixed order: 0 = draw order,
+// 1 = reverse draw order, 2 = a permutation drawn from `seed` (Fisher-Yates
+// over a 64-bit linear congruential generator).  The stored bytes keep the
+// count bits in their low bits, as the reference's maps do.
+static int64_t voxelize_cas_impl(const orc_scene* s, const orc_params* p, int order, uint64_t seed,
+                                 uint8_t* level0) {
+  const int N = p->grid_res;
+  std::vector<std::vector<Contrib<float>>> lists;
+  const int64_t rej = gather_contribs<float>(s, p, lists);
+  std::vector<const Contrib<float>*> seq;
+  for (const auto& l : lists)
+    for (const auto& c : l) seq.push_back(&c);
+  if (order == 1) std::reverse(seq.begin(), seq.end());
+  if (order == 2) {
+    uint64_t x = seed * 2862933555777941757ull + 3037000493ull;
+    for (size_t i = seq.size(); i > 1; --i) {
+      x = x * 6364136223846793005ull + 1442695040888963407ull;
+      std::swap(seq[i - 1], seq[(size_t)((x >> 33) % i)]);
+    }
+  }
+  std::vector<uint32_t> state((size_t)N * N * N, 0u);
+  for (const Contrib<float>* c : seq) state[c->voxel] = cas_step(state[c->voxel], c->c);
+  for (size_t v = 0; v < state.size(); ++v)
+    for (int q = 0; q < 4; ++q) level0[4 * v + q] = (uint8_t)(state[v] >> (8 * q));
   return rej;
 }
 
@@ -1094,6 +1171,16 @@ int64_t orc_voxelize_f32(const orc_scene* s, const orc_params* p, uint8_t* level
 }
 
 void orc_mipmap(const orc_params* p, const uint8_t* level0, uint8_t* chains) { mipmap_impl(p, level0, chains); }
+
+int64_t orc_voxelize_cas(const orc_scene* s, const orc_params* p, int32_t order, uint64_t seed, uint8_t* level0) {
+  return voxelize_cas_impl(s, p, order, seed, level0);
+}
+
+uint32_t orc_cas_avg(const float* rgba, int32_t n) {
+  uint32_t cur = 0;
+  for (int32_t i = 0; i < n; ++i) cur = cas_step(cur, rgba + 4 * i);
+  return cur;
+}
 
 int64_t orc_voxelize_attr(const orc_scene* s, const orc_params* p, uint8_t* albedo, uint8_t* normal,
                           uint8_t* emission, uint32_t* counts) {

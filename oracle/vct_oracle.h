@@ -104,6 +104,17 @@ uint64_t orc_chain_texels(int32_t N, int32_t L);
 int64_t orc_voxelize(const orc_scene* s, const orc_params* p,
                      uint8_t* level0, uint32_t* counts);
 
+/* Informational: level 0 as the reference's running average
+ * (imageAtomicRGBA8Avg, voxelize.frag:62-119) leaves it when the frame's
+ * contributions (FP32 shading) arrive one at a time in a fixed order: 0 =
+ * draw order, 1 = reverse, 2 = a permutation drawn from `seed`.  Bytes keep
+ * the 4-bit count in their low bits, as the reference's maps do. */
+int64_t orc_voxelize_cas(const orc_scene* s, const orc_params* p, int32_t order, uint64_t seed,
+                         uint8_t* level0);
+/* The same running average of n RGBA contributions (rgba: n x 4 floats in
+ * [0, 1]) arriving in order at a cleared voxel; returns the stored word. */
+uint32_t orc_cas_avg(const float* rgba, int32_t n);
+
 /* Voxelize with FP32 shading (the timed CPU restatement).  counts may be 0. */
 int64_t orc_voxelize_f32(const orc_scene* s, const orc_params* p,
                          uint8_t* level0, uint32_t* counts);

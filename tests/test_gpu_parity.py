@@ -116,6 +116,38 @@ def test_trace_radiance(vct, oracle, small_scene, sampler, mip_mode):
         assert q >= 40.0
 
 
+PHASES = {"direct": (1, 0, 0, 1), "diffuse": (0, 1, 0, 1), "specular": (0, 0, 1, 1), "final": (1, 1, 1, 1)}
+
+
+@pytest.mark.parametrize("sampler", [1, 0], ids=["exact", "hw"])
+@pytest.mark.parametrize("phase", list(PHASES))
+def test_trace_radiance_per_output(vct, oracle, small_scene, sampler, phase):
+    """Each output of voxel_cone_tracing.frag:265-272 on its own (switched by
+    set_rendering_phases, renderer.cpp:368-371): the oracle's FP64 trace of
+    the same phase from the GPU's maps and G-buffer vs the GPU's radiance."""
+    direct, diffuse, specular, shadow = PHASES[phase]
+    r = vct.Renderer(W, H, grid_res=N, keep_float_frame=1, sampler=sampler)
+    ids = vct.load_scene(r, small_scene)
+    r.set_voxel_view_dir(7, 0.0)
+    r.set_rendering_phases(direct, diffuse, specular, shadow)
+    vct.queue_scene(r, small_scene, ids)
+    r.render()
+    n, levels = r.grid()
+    p = oracle.Params(grid_res=n, width=W, height=H, enable_direct=bool(direct), enable_diffuse=bool(diffuse),
+                      enable_specular=bool(specular), enable_shadow=bool(shadow))
+    ref = oracle.trace(small_scene, p, r.read_voxels(0), _gpu_chains(r, n, levels, 6), _gb64(r.read_gbuffer()))
+    got = r.read_frame(vct.FRAME_RGBA32F)
+    d = np.abs(got - ref)[..., :3]
+    q = psnr(np.clip(got[..., :3], 0, 1), np.clip(ref[..., :3], 0, 1))
+    print(f"{phase:8s} sampler={sampler}: max|d| {d.max():.3e}, mean|d| {d.mean():.3e}, PSNR {q:.1f} dB, "
+          f"peak {ref[..., :3].max():.3f}")
+    assert ref[..., :3].max() > 0.05  # the phase contributes
+    if sampler == 1:
+        assert q >= 60.0
+    else:
+        assert q >= 40.0
+
+
 def test_frame_end_to_end_vs_oracle(vct, oracle, small_scene):
     r = _render(vct, small_scene, sampler=1)
     ref = oracle.render(small_scene, oracle.Params(grid_res=N, width=W, height=H))
