@@ -489,12 +489,12 @@ def run_ours(args):
         "clocks": clk.summary(),
     }
     if not args.no_mlp:
-        line["mlp"] = mlp_leg(r, R, scene, ids, stream, flush, args.steps, stages)
-    line["injection"] = injection_leg(R, torch, scene, args.steps, flush)
+        line["mlp"] = mlp_leg(r, R, scene, ids, stream, flush, min(args.steps, 20), stages)
+    line["injection"] = injection_leg(R, torch, scene, min(args.steps, 20), flush)
     if not args.no_precision:
-        line["precision"] = precision_leg(R, torch, args.steps)
+        line["precision"] = precision_leg(R, torch, min(args.steps, 20))
     if not args.no_batch:
-        line["batch"] = batch_leg(R, torch, max(args.steps, 3), rank, world, pg)
+        line["batch"] = batch_leg(R, torch, min(max(args.steps, 3), 10), rank, world, pg)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
         v, ms = cpu_frame_ms(scene, threads, CPU_ROW_STRIDE)
@@ -513,7 +513,7 @@ def run_ours(args):
 def main():
     ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
