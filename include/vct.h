@@ -109,7 +109,11 @@ typedef struct {
   float radiance_max;   /* upper clamp of voxel radiance (voxelize.frag:153
                          * clamps to 1).  0 or 1: the reference's clamp;
                          * > 1 (HDR, e.g. 16) needs VCT_STORAGE_RGBA16F      */
-  int32_t reserved[7];
+  int32_t shadow_from_maps; /* 0 (default): shadow cones of the texture-unit
+                         * sampler read packed alpha-only copies of the six
+                         * maps' chains (two fetches per step instead of
+                         * three, identical values); 1: the six maps       */
+  int32_t reserved[6];
 } vct_config;
 
 typedef struct vct_renderer vct_renderer;

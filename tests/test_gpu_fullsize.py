@@ -97,3 +97,12 @@ def test_fullsize_frames_repeat_bit_exactly(vct, bench_scene, frame_hw):
     r.render()
     np.testing.assert_array_equal(r.read_frame(), a)
     np.testing.assert_array_equal(r.read_voxels(0), l0)
+
+
+def test_fullsize_shadow_alpha_chains_bit_exact(vct, bench_scene, frame_hw):
+    """Shadow cones read packed alpha-only copies of the six chains by
+    default; the frame (RGBA32F, so every bit of the radiance) equals the
+    one whose shadow cones read the six maps."""
+    r = frame_hw[0]
+    other = _render(vct, bench_scene, shadow_from_maps=1)[0]
+    np.testing.assert_array_equal(r.read_frame(vct.FRAME_RGBA32F), other.read_frame(vct.FRAME_RGBA32F))

@@ -206,3 +206,17 @@ def test_error_paths(vct, small_scene):
         r.upload_material_data(scenes.default_material(), 99)
     r.set_grid_resolution(32)
     assert r.grid() == (32, 6)
+
+
+@pytest.mark.parametrize("cfg", [dict(), dict(vox_mode=1), dict(cone_set=1)], ids=["default", "sat", "six_cones"])
+def test_shadow_alpha_chains_bit_exact(vct, small_scene, cfg):
+    """Packed alpha-only chains for shadow cones (default) against shadow
+    cones over the six maps: identical radiance, bit for bit; with the six
+    maps' chains also identical (the alpha copies only add textures)."""
+    a = _render(vct, small_scene, **cfg)
+    b = _render(vct, small_scene, shadow_from_maps=1, **cfg)
+    np.testing.assert_array_equal(a.read_frame(vct.FRAME_RGBA32F), b.read_frame(vct.FRAME_RGBA32F))
+    n, levels = a.grid()
+    for lvl in range(1, levels):
+        for m in range(6):
+            np.testing.assert_array_equal(a.read_voxels(lvl, m), b.read_voxels(lvl, m))

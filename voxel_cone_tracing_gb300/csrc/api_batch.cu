@@ -405,8 +405,8 @@ vct_status build_batch(vct_batch* b, const vct_batch_scene* descs, uint32_t n) {
     const uint32_t rg = (uint32_t)(r.N / 16);
     c_regions.push_back(rg * rg * rg);
     const uint32_t s5 = r.L > 5 ? (uint32_t)(r.N >> 5) : 0u, s6 = r.L > 6 ? (uint32_t)(r.N >> 6) : 0u;
-    c_tail5.push_back(6u * s5 * s5 * s5);
-    c_tail6.push_back(6u * s6 * s6 * s6);
+    c_tail5.push_back(s5 * s5 * s5);  // texels; a thread computes all six maps
+    c_tail6.push_back(s6 * s6 * s6);
     c_tiles.push_back((uint32_t)((r.W + 15) / 16) * (uint32_t)((r.H + 15) / 16));
     total_tris += r.n_tris;
   }

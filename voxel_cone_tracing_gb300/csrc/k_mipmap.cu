@@ -165,6 +165,15 @@ __device__ __forceinline__ void aniso6_rgba16f(const uint2* ch, uint2* out) {
   }
 }
 
+// Texel (x, y, z) of level `level` of the alpha-only chains from the six
+// maps' RGBA8 texels v[0], v[stride], ..., v[5 * stride].
+__device__ __forceinline__ void write_alpha(const MapSet& ms, int level, int x, int y, int z, const uint32_t* v,
+                                            int stride) {
+  surf3Dwrite(make_uchar4(v[0] >> 24, v[stride] >> 24, v[2 * stride] >> 24, v[3 * stride] >> 24),
+              ms.alpha_surf[0][level], x * 4, y, z);
+  surf3Dwrite(make_uchar2(v[4 * stride] >> 24, v[5 * stride] >> 24), ms.alpha_surf[1][level], x * 2, y, z);
+}
+
 // One pass: source level `src_level` (0 = the shared level 0) -> levels
 // src_level+1 .. src_level+K of NMAPS maps, one CTA per B^3 source region.
 // Levels src_level+1 .. src_level+K of the B^3 source region at (ox, oy, oz)
@@ -199,6 +208,8 @@ __device__ __forceinline__ void mip_reduce(const MapSet& ms, int src_level, int 
           out[d * b3 + r] = v6[d];
           surf3Dwrite(v6[d], ms.surf[d][dl], ((ox >> 1) + x) * Texel<STORAGE>::kBytes, (oy >> 1) + y, (oz >> 1) + z);
         }
+        if constexpr (STORAGE == VCT_STORAGE_RGBA8)
+          if (ms.alpha_tex[0]) write_alpha(ms, dl, (ox >> 1) + x, (oy >> 1) + y, (oz >> 1) + z, v6, 1);
       }
       __syncthreads();
       cur = out;
@@ -221,6 +232,16 @@ __device__ __forceinline__ void mip_reduce(const MapSet& ms, int src_level, int 
       surf3Dwrite(v, ms.surf[d][dl], ((ox >> l) + x) * Texel<STORAGE>::kBytes, (oy >> l) + y, (oz >> l) + z);
     }
     __syncthreads();
+    if constexpr (NMAPS == 6 && STORAGE == VCT_STORAGE_RGBA8) {
+      if (ms.alpha_tex[0]) {
+        // The alpha copies of this level, from the six maps in shared memory
+        // (read only; the next level writes past them).
+        for (int r = threadIdx.x; r < b3; r += kThreads) {
+          const int x = r % b, y = (r / b) % b, z = r / (b * b);
+          write_alpha(ms, src_level + l, (ox >> l) + x, (oy >> l) + y, (oz >> l) + z, out + r, b3);
+        }
+      }
+    }
     cur = out;
     cur_b = b;
     cur_shared = false;
@@ -336,26 +357,29 @@ __global__ void __launch_bounds__(kThreads) k_mip_batch(BatchWork w) {
 }
 
 // Level `level` (>= 2) of every scene of a batch from its level - 1, one
-// thread per destination texel of every map (the small last levels).
+// thread per destination texel, all maps (the small last levels).
 template <int NMAPS, int STORAGE>
 __global__ void __launch_bounds__(kThreads) k_mip_level_batch(BatchWork w, int level) {
   typedef typename Texel<STORAGE>::T T;
   for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < w.total; g += gridDim.x * blockDim.x) {
     const int s = batch_scene_of(w, g);
     const MapSet& ms = w.scenes[s].ms;
-    const uint32_t i = g - __ldg(w.prefix + s);
+    const uint32_t r = g - __ldg(w.prefix + s);
     const int n = ms.N >> level;
-    const uint32_t n3 = (uint32_t)n * n * n;
-    const int d = (int)(i / n3);
-    const uint32_t r = i % n3;
     const int x = (int)(r % n), y = (int)((r / n) % n), z = (int)(r / ((uint32_t)n * n));
-    T ch[8];
+    T v[NMAPS];
 #pragma unroll
-    for (int k = 0; k < 8; ++k)
-      surf3Dread(&ch[k], ms.surf[d][level - 1], (2 * x + c_off[k][0]) * Texel<STORAGE>::kBytes, 2 * y + c_off[k][1],
-                 2 * z + c_off[k][2]);
-    const T v = reduce<STORAGE>(ch, d, NMAPS == 1);
-    surf3Dwrite(v, ms.surf[d][level], x * Texel<STORAGE>::kBytes, y, z);
+    for (int d = 0; d < NMAPS; ++d) {
+      T ch[8];
+#pragma unroll
+      for (int k = 0; k < 8; ++k)
+        surf3Dread(&ch[k], ms.surf[d][level - 1], (2 * x + c_off[k][0]) * Texel<STORAGE>::kBytes,
+                   2 * y + c_off[k][1], 2 * z + c_off[k][2]);
+      v[d] = reduce<STORAGE>(ch, d, NMAPS == 1);
+      surf3Dwrite(v[d], ms.surf[d][level], x * Texel<STORAGE>::kBytes, y, z);
+    }
+    if constexpr (NMAPS == 6 && STORAGE == VCT_STORAGE_RGBA8)
+      if (ms.alpha_tex[0]) write_alpha(ms, level, x, y, z, v, 1);
   }
 }
 

@@ -279,7 +279,7 @@ __device__ __forceinline__ void back64(const uint32_t (&dh)[4][4], const uint32_
 }
 
 __global__ void __launch_bounds__(256, 1) k_mlp_train(MlpParams p, MlpBatch b, float* __restrict__ loss_out) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
+  extern __shared__ __align__(128) unsigned char smem_raw[];
   TrainSmem& S = *reinterpret_cast<TrainSmem*>(smem_raw);
   load_weights(p.w_bf, S.w, &S.wt);
   for (int i = threadIdx.x; i < 4 * 64 * kDWS; i += blockDim.x) (&S.dw[0][0])[i] = 0.f;
@@ -431,7 +431,7 @@ struct InferSmem {
 __global__ void __launch_bounds__(256) k_mlp_infer(MlpParams p, SceneParams sp, const float4* __restrict__ gb_pos,
                                                    const float4* __restrict__ gb_nrm, int n_px,
                                                    float4* __restrict__ out) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
+  extern __shared__ __align__(128) unsigned char smem_raw[];
   InferSmem& S = *reinterpret_cast<InferSmem*>(smem_raw);
   load_weights(p.w_bf, S.w, nullptr);
   __syncthreads();
@@ -481,7 +481,7 @@ __global__ void __launch_bounds__(256) k_mlp_infer(MlpParams p, SceneParams sp, 
 // (pos, normal, albedo, ignored target).
 __global__ void __launch_bounds__(256) k_mlp_eval(MlpParams p, const float* __restrict__ samples, int n,
                                                   float* __restrict__ out) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
+  extern __shared__ __align__(128) unsigned char smem_raw[];
   InferSmem& S = *reinterpret_cast<InferSmem*>(smem_raw);
   load_weights(p.w_bf, S.w, nullptr);
   __syncthreads();

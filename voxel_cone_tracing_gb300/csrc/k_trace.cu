@@ -29,6 +29,14 @@ namespace {
 __device__ __forceinline__ float4 f4(float x, float y, float z, float w) { return make_float4(x, y, z, w); }
 __device__ __forceinline__ float4 operator+(float4 a, float4 b) { return f4(a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w); }
 __device__ __forceinline__ float4 operator*(float4 a, float s) { return f4(a.x * s, a.y * s, a.z * s, a.w * s); }
+// a * s and a * s + c with one rounding each, spelled out so that the alpha
+// channel is computed identically by the RGBA and the alpha-only paths.
+__device__ __forceinline__ float4 mul4(float4 a, float s) {
+  return f4(__fmul_rn(a.x, s), __fmul_rn(a.y, s), __fmul_rn(a.z, s), __fmul_rn(a.w, s));
+}
+__device__ __forceinline__ float4 fma4(float4 a, float s, float4 c) {
+  return f4(__fmaf_rn(a.x, s, c.x), __fmaf_rn(a.y, s, c.y), __fmaf_rn(a.z, s, c.z), __fmaf_rn(a.w, s, c.w));
+}
 
 #ifndef VCT_TRACE_MIN_BLOCKS
 #define VCT_TRACE_MIN_BLOCKS 4
@@ -105,9 +113,27 @@ __device__ float4 texture_lod_exact(const MapSet& m, int map, V3 u, float lod) {
 // (every wall pixel) have one or two such weights.
 __device__ __forceinline__ float4 aniso_fetch(const MapSet& m, V3 u, int ix, int iy, int iz, V3 ad, float l) {
   float4 r = f4(0.f, 0.f, 0.f, 0.f);
-  if (ad.x != 0.0f) r = tex3DLod<float4>(m.tex[ix], u.x, u.y, u.z, l) * ad.x;
-  if (ad.y != 0.0f) r = r + tex3DLod<float4>(m.tex[iy], u.x, u.y, u.z, l) * ad.y;
-  if (ad.z != 0.0f) r = r + tex3DLod<float4>(m.tex[iz], u.x, u.y, u.z, l) * ad.z;
+  if (ad.x != 0.0f) r = mul4(tex3DLod<float4>(m.tex[ix], u.x, u.y, u.z, l), ad.x);
+  if (ad.y != 0.0f) r = fma4(tex3DLod<float4>(m.tex[iy], u.x, u.y, u.z, l), ad.y, r);
+  if (ad.z != 0.0f) r = fma4(tex3DLod<float4>(m.tex[iz], u.x, u.y, u.z, l), ad.z, r);
+  return r;
+}
+
+// The alpha channel of aniso_fetch from the alpha-only chains: one fetch
+// covers the x and y maps (a-x, a+x, a-y, a+y), one the z maps (a-z, a+z).
+// The texture unit filters every channel with the same weights, so each
+// term equals the alpha of the corresponding map's fetch bit for bit.
+__device__ __forceinline__ float aniso_alpha(const MapSet& m, V3 u, int ix, int iy, int iz, V3 ad, float l) {
+  float r = 0.0f;
+  if (ad.x != 0.0f || ad.y != 0.0f) {
+    const float4 a = tex3DLod<float4>(m.alpha_tex[0], u.x, u.y, u.z, l);
+    if (ad.x != 0.0f) r = __fmul_rn(ix == 0 ? a.x : a.y, ad.x);
+    if (ad.y != 0.0f) r = __fmaf_rn(iy == 2 ? a.z : a.w, ad.y, r);
+  }
+  if (ad.z != 0.0f) {
+    const float2 b = tex3DLod<float2>(m.alpha_tex[1], u.x, u.y, u.z, l);
+    r = __fmaf_rn(iz == 4 ? b.x : b.y, ad.z, r);
+  }
   return r;
 }
 
@@ -123,15 +149,29 @@ __device__ __forceinline__ float4 sample_voxel(const MapSet& m, V3 u, int ix, in
   const float wsum = ad.x + ad.y + ad.z;
   if (lod < 1.0f) {
     const float4 t0 = tex3D<float4>(m.l0_tex, u.x, u.y, u.z);
-    if (!(lod > 0.0f)) return t0 * wsum;
+    if (!(lod > 0.0f)) return mul4(t0, wsum);
     float4 t1;
     if (ISO) t1 = tex3DLod<float4>(m.tex[0], u.x, u.y, u.z, 0.0f) * wsum;
     else t1 = aniso_fetch(m, u, ix, iy, iz, ad, 0.0f);
-    return t0 * ((1.0f - lod) * wsum) + t1 * lod;
+    return fma4(t1, lod, mul4(t0, __fmul_rn(1.0f - lod, wsum)));
   }
   const float l = lod - 1.0f;
   if (ISO) return tex3DLod<float4>(m.tex[0], u.x, u.y, u.z, l) * wsum;
   return aniso_fetch(m, u, ix, iy, iz, ad, l);
+}
+
+// The alpha of sample_voxel (texture unit, anisotropic RGBA8 maps) from the
+// alpha-only chains, with the same arithmetic as the alpha channel there.
+__device__ __forceinline__ float sample_alpha(const MapSet& m, V3 u, int ix, int iy, int iz, V3 ad, float lod) {
+  if (!u_sane(u)) return 0.0f;
+  const float wsum = ad.x + ad.y + ad.z;
+  if (lod < 1.0f) {
+    const float t0 = tex3D<float4>(m.l0_tex, u.x, u.y, u.z).w;
+    if (!(lod > 0.0f)) return __fmul_rn(t0, wsum);
+    const float t1 = aniso_alpha(m, u, ix, iy, iz, ad, 0.0f);
+    return __fmaf_rn(t1, lod, __fmul_rn(t0, __fmul_rn(1.0f - lod, wsum)));
+  }
+  return aniso_alpha(m, u, ix, iy, iz, ad, lod - 1.0f);
 }
 
 // ------------------------------------------------------------ cone march ----
@@ -150,13 +190,37 @@ __device__ float4 trace_cone(const MapSet& m, V3 origin, V3 dir, float aperture,
   while (acc.w < 1.0f && dist < max_dist) {
     const float mip = fmaxf(log2f(diam * cube_res), 0.0f);
     const float4 s = sample_voxel<SAMPLER, ISO, STORAGE>(m, sp, ix, iy, iz, ad, mip);
-    acc = acc + s * (1.0f - acc.w);
+    acc = fma4(s, 1.0f - acc.w, acc);
     const float step = fmaxf(diam * 0.5f, voxel_size);
     dist += step;
     diam = dist * aperture;
     sp = dir * dist + origin;
   }
   return acc;
+}
+
+// trace_cone(...).a (trace_shadow, :121-124) with the texture unit over the
+// alpha-only chains: the same march and the same alpha arithmetic, two
+// texture fetches per step instead of three.
+__device__ float trace_alpha(const MapSet& m, V3 origin, V3 dir, float aperture, float max_dist) {
+  dir = normalize(dir);
+  const int ix = dir.x < 0.0f ? 0 : 1, iy = dir.y < 0.0f ? 2 : 3, iz = dir.z < 0.0f ? 4 : 5;
+  const V3 ad = vabs(dir);
+  const float cube_res = (float)m.N;
+  const float voxel_size = 1.0f / cube_res;
+  float a = 0.0f;
+  float dist = 3.0f * voxel_size;
+  float diam = dist * aperture;
+  V3 sp = dir * dist + origin;
+  while (a < 1.0f && dist < max_dist) {
+    const float mip = fmaxf(log2f(diam * cube_res), 0.0f);
+    a = __fmaf_rn(sample_alpha(m, sp, ix, iy, iz, ad, mip), 1.0f - a, a);
+    const float step = fmaxf(diam * 0.5f, voxel_size);
+    dist += step;
+    diam = dist * aperture;
+    sp = dir * dist + origin;
+  }
+  return a;
 }
 
 // tangent, :126-134.
@@ -226,7 +290,14 @@ __device__ V3 direct_light(const SceneParams& sp, const MapSet& m, int enable_sh
     const float cs = fmaxf(dot(nrm, ld), 0.0f);
     const V3 lc = v3(L.color[0], L.color[1], L.color[2]) * ((1.0f / (1.0f + d * d)) * cs * L.intensity);
     float shadow = 1.0f;
-    if (enable_shadow) shadow = fmaxf(0.0f, 1.0f - trace_cone<SAMPLER, ISO, STORAGE>(m, pos, ld, 0.1f, d).w);
+    if (enable_shadow) {
+      float occ;
+      if constexpr (SAMPLER == VCT_SAMPLER_HW && !ISO && STORAGE == VCT_STORAGE_RGBA8)
+        occ = m.alpha_tex[0] ? trace_alpha(m, pos, ld, 0.1f, d) : trace_cone<SAMPLER, ISO, STORAGE>(m, pos, ld, 0.1f, d).w;
+      else
+        occ = trace_cone<SAMPLER, ISO, STORAGE>(m, pos, ld, 0.1f, d).w;
+      shadow = fmaxf(0.0f, 1.0f - occ);
+    }
     const float lambert = fmaxf(dot(ld, nrm), 0.0f);
     float refract_angle = 0.0f;
     if (mat.dissolve <= 0.1f) {

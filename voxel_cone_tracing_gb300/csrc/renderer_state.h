@@ -219,6 +219,7 @@ struct HeavyStore {
 struct MapStore {
   cudaArray_t l0_arr = nullptr;
   cudaMipmappedArray_t dir_arr[kMaxMaps] = {};
+  cudaMipmappedArray_t alpha_arr[2] = {};
   MapSet ms = {};
 
   MapStore() = default;
@@ -236,12 +237,45 @@ struct MapStore {
       if (dir_arr[d]) cudaFreeMipmappedArray(dir_arr[d]);
       dir_arr[d] = nullptr;
     }
+    for (int k = 0; k < 2; ++k) {
+      if (ms.alpha_tex[k]) cudaDestroyTextureObject(ms.alpha_tex[k]);
+      for (int l = 0; l < kMaxLevels; ++l)
+        if (ms.alpha_surf[k][l]) cudaDestroySurfaceObject(ms.alpha_surf[k][l]);
+      if (alpha_arr[k]) cudaFreeMipmappedArray(alpha_arr[k]);
+      alpha_arr[k] = nullptr;
+    }
     if (l0_arr) cudaFreeArray(l0_arr);
     l0_arr = nullptr;
     std::memset(&ms, 0, sizeof(ms));
   }
 
-  vct_status alloc(uint32_t r, int mip_mode, int storage) {
+  // A mipmapped array of levels 1..L-1 (base r/2) with a surface per level
+  // and one filtered texture over all of them.
+  static vct_status chain(uint32_t r, int L, const cudaChannelFormatDesc& desc, const cudaTextureDesc& td,
+                          cudaMipmappedArray_t* arr, cudaSurfaceObject_t* surf, cudaTextureObject_t* tex) {
+    VCT_CUDA(cudaMallocMipmappedArray(arr, &desc, make_cudaExtent(r / 2, r / 2, r / 2), L - 1,
+                                      cudaArraySurfaceLoadStore));
+    for (int l = 1; l < L; ++l) {
+      cudaArray_t la;
+      VCT_CUDA(cudaGetMipmappedArrayLevel(&la, *arr, l - 1));
+      cudaResourceDesc lr;
+      std::memset(&lr, 0, sizeof(lr));
+      lr.resType = cudaResourceTypeArray;
+      lr.res.array.array = la;
+      VCT_CUDA(cudaCreateSurfaceObject(&surf[l], &lr));
+    }
+    cudaResourceDesc mr;
+    std::memset(&mr, 0, sizeof(mr));
+    mr.resType = cudaResourceTypeMipmappedArray;
+    mr.res.mipmap.mipmap = *arr;
+    cudaTextureDesc mt = td;
+    mt.minMipmapLevelClamp = 0.0f;
+    mt.maxMipmapLevelClamp = (float)(L - 2);
+    VCT_CUDA(cudaCreateTextureObject(tex, &mr, &mt, nullptr));
+    return VCT_OK;
+  }
+
+  vct_status alloc(uint32_t r, int mip_mode, int storage, bool alpha_chains = true) {
     release();
     const int L = std::min(kMaxLevels, ilog2(r) + 1);
     const int nmaps = mip_mode == VCT_MIP_ISO ? 1 : 6;
@@ -262,26 +296,12 @@ struct MapStore {
     td.normalizedCoords = 1;
     td.mipmapFilterMode = cudaFilterModeLinear;
     VCT_CUDA(cudaCreateTextureObject(&ms.l0_tex, &rd, &td, nullptr));
-    for (int d = 0; d < nmaps && L > 1; ++d) {
-      VCT_CUDA(cudaMallocMipmappedArray(&dir_arr[d], &desc, make_cudaExtent(r / 2, r / 2, r / 2), L - 1,
-                                        cudaArraySurfaceLoadStore));
-      for (int l = 1; l < L; ++l) {
-        cudaArray_t la;
-        VCT_CUDA(cudaGetMipmappedArrayLevel(&la, dir_arr[d], l - 1));
-        cudaResourceDesc lr;
-        std::memset(&lr, 0, sizeof(lr));
-        lr.resType = cudaResourceTypeArray;
-        lr.res.array.array = la;
-        VCT_CUDA(cudaCreateSurfaceObject(&ms.surf[d][l], &lr));
-      }
-      cudaResourceDesc mr;
-      std::memset(&mr, 0, sizeof(mr));
-      mr.resType = cudaResourceTypeMipmappedArray;
-      mr.res.mipmap.mipmap = dir_arr[d];
-      cudaTextureDesc mt = td;
-      mt.minMipmapLevelClamp = 0.0f;
-      mt.maxMipmapLevelClamp = (float)(L - 2);
-      VCT_CUDA(cudaCreateTextureObject(&ms.tex[d], &mr, &mt, nullptr));
+    for (int d = 0; d < nmaps && L > 1; ++d) VCT_CHECK(chain(r, L, desc, td, &dir_arr[d], ms.surf[d], &ms.tex[d]));
+    if (alpha_chains && nmaps == 6 && storage == VCT_STORAGE_RGBA8 && L > 1) {
+      const cudaChannelFormatDesc d4 = cudaCreateChannelDesc(8, 8, 8, 8, cudaChannelFormatKindUnsigned);
+      const cudaChannelFormatDesc d2 = cudaCreateChannelDesc(8, 8, 0, 0, cudaChannelFormatKindUnsigned);
+      VCT_CHECK(chain(r, L, d4, td, &alpha_arr[0], ms.alpha_surf[0], &ms.alpha_tex[0]));
+      VCT_CHECK(chain(r, L, d2, td, &alpha_arr[1], ms.alpha_surf[1], &ms.alpha_tex[1]));
     }
     ms.N = (int)r;
     ms.L = L;
@@ -425,7 +445,7 @@ struct vct_renderer {
   vct_status alloc_maps(uint32_t r) {
     if (stream) VCT_CUDA(cudaStreamSynchronize(stream));
     free_inj();
-    VCT_CHECK(maps.alloc(r, cfg.mip_mode, cfg.storage));
+    VCT_CHECK(maps.alloc(r, cfg.mip_mode, cfg.storage, cfg.shadow_from_maps == 0 && cfg.sampler == VCT_SAMPLER_HW));
     const int L = ms.L;
     const uint32_t tb = cfg.storage == VCT_STORAGE_RGBA16F ? 8u : 4u;
     have_l0_map = false;

@@ -105,6 +105,11 @@ struct MapSet {
   cudaTextureObject_t l0_tex;                    // linear, normalized coords, border 0
   cudaSurfaceObject_t surf[kMaxMaps][kMaxLevels];  // level l >= 1 of map d
   cudaTextureObject_t tex[kMaxMaps];             // mipmapped chain (base = level 1)
+  // Alpha-only copies of the six chains for shadow cones (anisotropic RGBA8;
+  // 0 when absent): levels 1..L-1 of (a-x, a+x, a-y, a+y) as RGBA8 in
+  // alpha_tex[0] and of (a-z, a+z) as RG8 in alpha_tex[1].
+  cudaSurfaceObject_t alpha_surf[2][kMaxLevels];
+  cudaTextureObject_t alpha_tex[2];
 };
 
 struct VoxBuffers {
