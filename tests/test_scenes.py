@@ -69,4 +69,6 @@ def test_bench_frame_work(oracle):
     lt1 = sum(v["lod_lt1"] for v in st.values()) / px
     assert sum(bands) == sum(v["steps"] for v in st.values())
     assert st["diffuse"]["cones"] == 9 * px
-    assert 3 * steps + lt1 == pytest.approx(bench.TRACE_FETCHES_PER_PIXEL, rel=0.02)
+    assert 3 * steps + lt1 == pytest.approx(bench.TRACE_FETCHES_PER_PIXEL_REF, rel=0.02)
+    shadow = st["shadow"]["steps"] / px
+    assert 3 * steps + lt1 - shadow == pytest.approx(bench.TRACE_FETCHES_PER_PIXEL, rel=0.02)
