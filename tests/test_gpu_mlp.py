@@ -175,9 +175,8 @@ def test_learned_diffuse_replaces_cones(vct):
     r.mlp_set_tensor_kernels(True)
     learned_tc = frame()
     r.mlp_set_tensor_kernels(False)
-    q_kernels = psnr(np.clip(learned_tc, 0, 1), np.clip(learned, 0, 1))
-    print(f"learned frame, tcgen05 vs warp-tile inference: PSNR {q_kernels:.1f} dB")
-    assert q_kernels >= 50.0
+    # same encoding, same BF16 products, FP32 accumulation in the same order
+    np.testing.assert_array_equal(learned_tc, learned)
     q_learned = psnr(np.clip(learned, 0, 1), np.clip(cones, 0, 1))
     q_untrained = psnr(np.clip(untrained, 0, 1), np.clip(cones, 0, 1))
     print(f"diffuse-only PSNR: learned {q_learned:.1f} dB, untrained {q_untrained:.1f} dB, report {rep}")

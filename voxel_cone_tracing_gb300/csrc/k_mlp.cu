@@ -164,6 +164,45 @@ __device__ void build_inputs(const MlpParams& p, unsigned short* E, Get get) {
   __syncwarp();
 }
 
+// The first layer's A fragments built directly in registers (no input tile
+// in shared memory): lane (g, t) holds rows g and g + 8 of columns
+// 16 kk + 2t, +1 (a[kk][0], a[kk][1]) and 16 kk + 8 + 2t, +1 (a[kk][2],
+// a[kk][3]), i.e. hash levels t and t + 4 (kk 0), 8 + t and 12 + t (kk 1),
+// inputs x[2t], x[2t + 1] (kk 2) and zeros.  The values and their bf16
+// packing are those of build_inputs + load_a.
+template <class Get>
+__device__ __forceinline__ void build_a(const MlpParams& p, uint32_t (&a)[4][4], Get get) {
+  const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+#pragma unroll
+  for (int h = 0; h < 2; ++h) {
+    V3 pos, nrm, alb;
+    bool valid;
+    get(g + 8 * h, pos, nrm, alb, valid);
+    const int lv[4] = {t, t + 4, 8 + t, 12 + t};
+    uint32_t f[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const float2 v = valid ? level_features(p, lv[q], pos) : make_float2(0.f, 0.f);
+      f[q] = pack_bf16(v.x, v.y);
+    }
+    a[0][h] = f[0];
+    a[0][2 + h] = f[1];
+    a[1][h] = f[2];
+    a[1][2 + h] = f[3];
+    float x0 = 0.f, x1 = 0.f;
+    if (valid) {
+      const V3 n = normalize(nrm);
+      // x = (n.x, n.y, n.z, alb.x, alb.y, alb.z, 1, 0, 0, ...)
+      x0 = t == 0 ? n.x : (t == 1 ? n.z : (t == 2 ? alb.y : 1.0f));
+      x1 = t == 0 ? n.y : (t == 1 ? alb.x : (t == 2 ? alb.z : 0.0f));
+    }
+    a[2][h] = pack_bf16(x0, x1);
+    a[2][2 + h] = pack_bf16(0.f, 0.f);
+    a[3][h] = pack_bf16(0.f, 0.f);
+    a[3][2 + h] = pack_bf16(0.f, 0.f);
+  }
+}
+
 __device__ __forceinline__ void load_a(const unsigned short* E, uint32_t (&a)[4][4]) {
   const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
   const uint32_t* E32 = reinterpret_cast<const uint32_t*>(E);
@@ -428,20 +467,20 @@ struct InferSmem {
   unsigned short E[8][16 * kWS];
 };
 
-__global__ void __launch_bounds__(256) k_mlp_infer(MlpParams p, SceneParams sp, const float4* __restrict__ gb_pos,
+__global__ void __launch_bounds__(256, 4) k_mlp_infer(MlpParams p, SceneParams sp, const float4* __restrict__ gb_pos,
                                                    const float4* __restrict__ gb_nrm, int n_px,
                                                    float4* __restrict__ out) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
-  InferSmem& S = *reinterpret_cast<InferSmem*>(smem_raw);
-  load_weights(p.w_bf, S.w, nullptr);
+  SmemW& W = *reinterpret_cast<SmemW*>(smem_raw);
+  load_weights(p.w_bf, W, nullptr);
   __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
   const int nwarps = blockDim.x >> 5;
-  unsigned short* E = S.E[warp];
   const float inv_cube = 1.0f / sp.cube_size;
   for (int tile = blockIdx.x * nwarps + warp; tile * 16 < n_px; tile += gridDim.x * nwarps) {
     const int row0 = tile * 16;
-    build_inputs(p, E, [&](int row, V3& pos, V3& nrm, V3& alb, bool& valid) {
+    uint32_t x[4][4], h[4][4];
+    build_a(p, x, [&](int row, V3& pos, V3& nrm, V3& alb, bool& valid) {
       const int px = row0 + row;
       valid = false;
       pos = nrm = alb = v3(0.f, 0.f, 0.f);
@@ -456,15 +495,13 @@ __global__ void __launch_bounds__(256) k_mlp_infer(MlpParams p, SceneParams sp, 
         }
       }
     });
-    uint32_t x[4][4], h[4][4];
     float acc[8][4];
-    load_a(E, x);
-    layer64(x, S.w.w[0], acc); d_to_a(acc, h, true);
-    layer64(h, S.w.w[1], acc); d_to_a(acc, x, true);
-    layer64(x, S.w.w[2], acc); d_to_a(acc, h, true);
-    layer64(h, S.w.w[3], acc); d_to_a(acc, x, true);
+    layer64(x, W.w[0], acc); d_to_a(acc, h, true);
+    layer64(h, W.w[1], acc); d_to_a(acc, x, true);
+    layer64(x, W.w[2], acc); d_to_a(acc, h, true);
+    layer64(h, W.w[3], acc); d_to_a(acc, x, true);
     float y[2][4];
-    layer_out(x, S.w.w5, y);
+    layer_out(x, W.w5, y);
     // lanes t = 0 hold cols 0,1; t = 1 holds col 2 -> gather per row
     const float c2_lo = __shfl_sync(0xffffffffu, y[0][0], (lane & ~3) | 1);
     const float c2_hi = __shfl_sync(0xffffffffu, y[0][2], (lane & ~3) | 1);
@@ -751,7 +788,7 @@ cudaError_t run_fwd_tc(const MlpParams& p, const SceneParams& sp, const float4* 
 cudaError_t launch_mlp_infer(const MlpParams& p, const SceneParams& sp, const float4* gb_pos, const float4* gb_nrm,
                              int n_px, float4* out, cudaStream_t st, bool tc, FrameStatus* status) {
   if (tc) return run_fwd_tc<true>(p, sp, gb_pos, gb_nrm, nullptr, n_px, out, nullptr, st, status);
-  const size_t smem = sizeof(InferSmem);
+  const size_t smem = sizeof(SmemW);
   cudaError_t e = cudaFuncSetAttribute(k_mlp_infer, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   // Persistent: every CTA slot the SMs can hold (the gathers of the hash
