@@ -113,7 +113,11 @@ typedef struct {
                          * sampler read packed alpha-only copies of the six
                          * maps' chains (two fetches per step instead of
                          * three, identical values); 1: the six maps       */
-  int32_t reserved[6];
+  int32_t full_march;   /* 1: cones march their full length also outside the
+                         * grid, as the reference's loop does; 0 (default):
+                         * a cone stops once every further sample can only
+                         * read border texels (identical results)          */
+  int32_t reserved[5];
 } vct_config;
 
 typedef struct vct_renderer vct_renderer;

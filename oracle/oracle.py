@@ -313,18 +313,21 @@ def trace(scene, params: Params, level0, chains, gb: dict, row_stride: int = 1, 
 
 
 def trace_stats(scene, params: Params, level0, chains, gb: dict, row_stride: int = 1) -> dict:
-    """Instrumented FP64 trace: cones, march steps and lod<1 steps per cone
-    class over the traced rows (the algorithmic texture work of the trace)."""
+    """Instrumented FP64 trace: cones, march steps, lod<1 steps and steps
+    beyond the grid (taken by the reference's loop, skipped by the engine's
+    exact early exit) per cone class over the traced rows (the algorithmic
+    texture work of the trace)."""
     w, h = params.width, params.height
     out = np.zeros((h, w, 4), np.float32)
-    st = np.zeros(20, np.uint64)
+    st = np.zeros(24, np.uint64)
     sh, pc = _SceneHold(scene), params.c()
     args = [np.ascontiguousarray(level0, np.uint8), np.ascontiguousarray(chains, np.uint8),
             np.ascontiguousarray(gb["tri_id"], np.uint32), np.ascontiguousarray(gb["pos"], np.float64),
             np.ascontiguousarray(gb["nrm"], np.float64), np.ascontiguousarray(gb["mat"], np.uint32)]
     lib().orc_trace_stats(sh.ptr, C.addressof(pc), *[_ptr(a) for a in args], int(row_stride), _ptr(out), _ptr(st))
     names = ["diffuse", "specular", "shadow", "refraction"]
-    res = {n: dict(cones=int(st[i]), steps=int(st[4 + i]), lod_lt1=int(st[8 + i])) for i, n in enumerate(names)}
+    res = {n: dict(cones=int(st[i]), steps=int(st[4 + i]), lod_lt1=int(st[8 + i]), beyond=int(st[20 + i]))
+           for i, n in enumerate(names)}
     res["lod_bands"] = [int(v) for v in st[12:20]]  # all classes: lod in [k, k+1), last = lod >= 7
     return res
 

@@ -772,8 +772,10 @@ template <class R> struct ConeOut { V4<R> c; int steps; };
 // specular, 2 shadow, 3 refraction) the cones traced, the march steps and
 // the steps whose lod is < 1 (those read level 0 plus level 1); then, over
 // all classes, the steps whose lod lies in [k, k+1) for k = 0..6 (k = 7:
-// lod >= 7).
-enum { kStatCones = 0, kStatSteps = 4, kStatLodLt1 = 8, kStatLodBand = 12, kStatN = 20 };
+// lod >= 7); then per class the steps taken once the cone has moved more
+// than 3/4 of the coarsest texel outside [0,1] along an axis it travels
+// away on (they read border texels only; the engine does not take them).
+enum { kStatCones = 0, kStatSteps = 4, kStatLodLt1 = 8, kStatLodBand = 12, kStatBeyond = 20, kStatN = 24 };
 static std::atomic<uint64_t> g_stats[kStatN];
 static bool g_stats_on = false;
 static thread_local int t_cone_class = 0;
@@ -791,8 +793,11 @@ static ConeOut<R> trace_cone(const Maps& m, V3<R> origin, V3<R> dir, R aperture,
   R dist = R(3) * voxel_size;
   R diam = dist * aperture;
   V3<R> sp = dir * dist + origin;
-  int steps = 0, lod_lt1 = 0;
+  int steps = 0, lod_lt1 = 0, beyond = 0;
+  const R margin = R(0.75) * R(1 << (m.L - 1)) / cube_res;
+  auto outside = [&](R p, bool up) { return up ? p > R(1) + margin : p < -margin; };
   while (acc.a < R(1) && dist < max_dist) {
+    if (outside(sp.x, ix == 1) || outside(sp.y, iy == 3) || outside(sp.z, iz == 5)) ++beyond;
     R mip = fmaxr(R(std::log2(diam * cube_res)), R(0));
     V4<R> smp = texture_lod<R>(m, ix, sp, mip) * ad.x + texture_lod<R>(m, iy, sp, mip) * ad.y +
                 texture_lod<R>(m, iz, sp, mip) * ad.z;
@@ -809,6 +814,7 @@ static ConeOut<R> trace_cone(const Maps& m, V3<R> origin, V3<R> dir, R aperture,
     g_stats[kStatCones + t_cone_class] += 1;
     g_stats[kStatSteps + t_cone_class] += (uint64_t)steps;
     g_stats[kStatLodLt1 + t_cone_class] += (uint64_t)lod_lt1;
+    g_stats[kStatBeyond + t_cone_class] += (uint64_t)beyond;
   }
   return {acc, steps};
 }

@@ -106,3 +106,11 @@ def test_fullsize_shadow_alpha_chains_bit_exact(vct, bench_scene, frame_hw):
     r = frame_hw[0]
     other = _render(vct, bench_scene, shadow_from_maps=1)[0]
     np.testing.assert_array_equal(r.read_frame(vct.FRAME_RGBA32F), other.read_frame(vct.FRAME_RGBA32F))
+
+
+def test_fullsize_cone_exit_bit_exact(vct, bench_scene, frame_hw):
+    """The exact early exit of cones leaving the grid (default) against
+    full-length marches: identical RGBA32F frames at the bench size."""
+    r = frame_hw[0]
+    other = _render(vct, bench_scene, full_march=1, shadow_from_maps=1)[0]
+    np.testing.assert_array_equal(r.read_frame(vct.FRAME_RGBA32F), other.read_frame(vct.FRAME_RGBA32F))

@@ -220,3 +220,14 @@ def test_shadow_alpha_chains_bit_exact(vct, small_scene, cfg):
     for lvl in range(1, levels):
         for m in range(6):
             np.testing.assert_array_equal(a.read_voxels(lvl, m), b.read_voxels(lvl, m))
+
+
+@pytest.mark.parametrize("cfg", [dict(), dict(sampler=1), dict(mip_mode=1), dict(cone_set=1)],
+                         ids=["hw", "exact", "iso", "six_cones"])
+def test_cone_exit_outside_grid_bit_exact(vct, small_scene, cfg):
+    """Cones stop once every further sample can only read border texels
+    (default) or march their full length as the reference's loop does
+    (full_march=1): identical radiance, bit for bit."""
+    a = _render(vct, small_scene, **cfg)
+    b = _render(vct, small_scene, full_march=1, **cfg)
+    np.testing.assert_array_equal(a.read_frame(vct.FRAME_RGBA32F), b.read_frame(vct.FRAME_RGBA32F))

@@ -71,4 +71,6 @@ def test_bench_frame_work(oracle):
     assert st["diffuse"]["cones"] == 9 * px
     assert 3 * steps + lt1 == pytest.approx(bench.TRACE_FETCHES_PER_PIXEL_REF, rel=0.02)
     shadow = st["shadow"]["steps"] / px
-    assert 3 * steps + lt1 - shadow == pytest.approx(bench.TRACE_FETCHES_PER_PIXEL, rel=0.02)
+    beyond = sum(v["beyond"] for v in st.values()) / px
+    assert st["shadow"]["beyond"] == 0  # shadow cones end at the light, inside the grid
+    assert 3 * steps + lt1 - shadow - 3 * beyond == pytest.approx(bench.TRACE_FETCHES_PER_PIXEL, rel=0.02)

@@ -91,7 +91,7 @@ static vct_status check_config(const vct_config& c) {
     return set_error(VCT_ERR_INVALID_VALUE, "radiance_max %g > 1 needs RGBA16F storage", c.radiance_max);
   if (c.vox_mode < 0 || c.vox_mode > 1 || c.mip_mode < 0 || c.mip_mode > 1 || c.storage < 0 || c.storage > 1 ||
       c.sampler < 0 || c.sampler > 1 || c.cone_set < 0 || c.cone_set > 1 || c.shadow_from_maps < 0 ||
-      c.shadow_from_maps > 1)
+      c.shadow_from_maps > 1 || c.full_march < 0 || c.full_march > 1)
     return set_error(VCT_ERR_INVALID_VALUE, "config field out of range");
   return VCT_OK;
 }

@@ -175,6 +175,29 @@ __device__ __forceinline__ float sample_alpha(const MapSet& m, V3 u, int ix, int
 }
 
 // ------------------------------------------------------------ cone march ----
+// Exact early exit: a sample whose position lies more than `margin` outside
+// [0,1] along an axis reads only border texels (0) at every level -- a
+// filtered fetch at level l reads texels within one texel (2^l / N) of the
+// position, and the coarsest level is L-1 -- so with margin = 3/4 of the
+// coarsest texel (MapSet::exit_margin, set by the host), a cone moving away
+// from the volume along that axis adds exact zeros for the rest of its march
+// and can stop.  Diffuse cones that
+// pass the room's walls (their alpha stays below 1 at the coarse levels)
+// otherwise march on to sqrt(3) outside the grid.
+// The test uses the map indices of the cone (ix = 1 when dir.x >= 0, ...):
+// an axis with dir component 0 keeps its position, so a position beyond
+// the margin on either side stays beyond it and exiting is exact there too.
+struct ExitTest {
+  float lo, hi;  // gone when p < lo moving down an axis, or p > hi moving up
+  __device__ __forceinline__ explicit ExitTest(const MapSet& m) {
+    lo = -m.exit_margin;
+    hi = 1.0f + m.exit_margin;
+  }
+  __device__ __forceinline__ bool gone(V3 p, int ix, int iy, int iz) const {
+    return (ix == 1 ? p.x > hi : p.x < lo) || (iy == 3 ? p.y > hi : p.y < lo) || (iz == 5 ? p.z > hi : p.z < lo);
+  }
+};
+
 // trace_cone, voxel_cone_tracing.frag:88-119.
 template <int SAMPLER, bool ISO, int STORAGE>
 __device__ float4 trace_cone(const MapSet& m, V3 origin, V3 dir, float aperture, float max_dist) {
@@ -187,7 +210,9 @@ __device__ float4 trace_cone(const MapSet& m, V3 origin, V3 dir, float aperture,
   float dist = 3.0f * voxel_size;
   float diam = dist * aperture;
   V3 sp = dir * dist + origin;
+  const ExitTest exit(m);
   while (acc.w < 1.0f && dist < max_dist) {
+    if (exit.gone(sp, ix, iy, iz)) break;
     const float mip = fmaxf(log2f(diam * cube_res), 0.0f);
     const float4 s = sample_voxel<SAMPLER, ISO, STORAGE>(m, sp, ix, iy, iz, ad, mip);
     acc = fma4(s, 1.0f - acc.w, acc);
@@ -212,7 +237,9 @@ __device__ float trace_alpha(const MapSet& m, V3 origin, V3 dir, float aperture,
   float dist = 3.0f * voxel_size;
   float diam = dist * aperture;
   V3 sp = dir * dist + origin;
+  const ExitTest exit(m);
   while (a < 1.0f && dist < max_dist) {
+    if (exit.gone(sp, ix, iy, iz)) break;
     const float mip = fmaxf(log2f(diam * cube_res), 0.0f);
     a = __fmaf_rn(sample_alpha(m, sp, ix, iy, iz, ad, mip), 1.0f - a, a);
     const float step = fmaxf(diam * 0.5f, voxel_size);

@@ -10,6 +10,7 @@
 #include <cfloat>
 #include <cmath>
 #include <cstring>
+#include <limits>
 #include <memory>
 #include <vector>
 
@@ -307,7 +308,13 @@ struct MapStore {
     ms.L = L;
     ms.nmaps = nmaps;
     ms.storage = storage;
+    set_full_march(false);
     return VCT_OK;
+  }
+
+  // Cones stop 3/4 of the coarsest texel outside the grid (exact), or never.
+  void set_full_march(bool full) {
+    ms.exit_margin = full ? std::numeric_limits<float>::infinity() : 0.75f * (float)(1 << (ms.L - 1)) / (float)ms.N;
   }
 };
 
@@ -446,6 +453,7 @@ struct vct_renderer {
     if (stream) VCT_CUDA(cudaStreamSynchronize(stream));
     free_inj();
     VCT_CHECK(maps.alloc(r, cfg.mip_mode, cfg.storage, cfg.shadow_from_maps == 0 && cfg.sampler == VCT_SAMPLER_HW));
+    maps.set_full_march(cfg.full_march != 0);
     const int L = ms.L;
     const uint32_t tb = cfg.storage == VCT_STORAGE_RGBA16F ? 8u : 4u;
     have_l0_map = false;

@@ -110,6 +110,9 @@ struct MapSet {
   // alpha_tex[0] and of (a-z, a+z) as RG8 in alpha_tex[1].
   cudaSurfaceObject_t alpha_surf[2][kMaxLevels];
   cudaTextureObject_t alpha_tex[2];
+  // A cone moving away from the grid stops once its sample position is more
+  // than this far outside [0,1] along that axis (+inf: never).
+  float exit_margin;
 };
 
 struct VoxBuffers {
