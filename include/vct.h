@@ -258,7 +258,9 @@ typedef struct {
   uint32_t n_samples;   /* training samples drawn from the scene (2^24)   */
   uint32_t batch;       /* samples per optimiser step (2^18)              */
   uint32_t steps;       /* Adam steps (1000)                              */
-  float lr;             /* Adam learning rate (1e-2)                      */
+  float lr;             /* Adam learning rate (1e-2); constant over the first
+                         * half of the steps, then decaying geometrically to
+                         * lr / 10 at the last step                       */
   uint64_t seed;
   uint32_t reserved[8];
 } vct_mlp_desc;

@@ -118,9 +118,9 @@ def test_training_reduces_loss(vct):
     spread = float(np.std(held_out[:, 9:12]))
     print(f"smooth fit: rmse {rmse:.4f}, target std {spread:.4f}, report {rep}")
     # Training is not bit-reproducible (the table gradients are accumulated
-    # with float atomics in arrival order): held-out RMSE 0.017-0.039 over
-    # repeated runs of this case.
-    assert rmse < 0.3 * spread
+    # with float atomics in arrival order); with the learning-rate decay the
+    # held-out RMSE of this case stays within 0.014-0.018 over repeated runs.
+    assert rmse < 0.2 * spread
 
 
 def test_checkpoint_roundtrip(vct, tmp_path):

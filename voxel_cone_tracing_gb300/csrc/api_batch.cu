@@ -64,7 +64,7 @@ struct vct_batch {
   DevBuf<BatchScene> d_scenes;
   HostBuf<CameraParams> h_cams;
   DevBuf<CameraParams> d_cams;
-  Prefix tris, bricks, regions, tail5, tail6, tiles;
+  Prefix tris, bricks, regions, tail5, tail6, tiles, occw;
   std::vector<uint32_t> brick_base;
   std::vector<size_t> px_base;
   size_t total_px = 0;
@@ -193,6 +193,7 @@ struct vct_batch {
     VCT_CUDA(record(1));
     const BatchWork tail[2] = {work(tail5), work(tail6)};
     VCT_CUDA(launch_mipmap_batch(work(regions), tail, 2, VCT_STORAGE_RGBA8, stream, &launches));
+    VCT_CUDA(launch_occupancy_batch(work(occw), stream, &launches));
     VCT_CUDA(record(2));
     VCT_CUDA(launch_gbuffer_batch(work(tris), work(tiles), total_px, bb, sms, stream, &launches));
     VCT_CUDA(record(3));
@@ -393,7 +394,7 @@ vct_status build_batch(vct_batch* b, const vct_batch_scene* descs, uint32_t n) {
     VCT_CUDA(cudaStreamCreateWithFlags(&b->side[k], cudaStreamNonBlocking));
     VCT_CUDA(cudaEventCreateWithFlags(&b->join_ev[k], cudaEventDisableTiming));
   }
-  std::vector<uint32_t> c_tris, c_bricks, c_regions, c_tail5, c_tail6, c_tiles;
+  std::vector<uint32_t> c_tris, c_bricks, c_regions, c_tail5, c_tail6, c_tiles, c_occw;
   uint64_t total_tris = 0;
   for (uint32_t i = 0; i < n; ++i) {
     b->scenes.emplace_back(new SceneRes());
@@ -408,6 +409,7 @@ vct_status build_batch(vct_batch* b, const vct_batch_scene* descs, uint32_t n) {
     c_tail5.push_back(s5 * s5 * s5);  // texels; a thread computes all six maps
     c_tail6.push_back(s6 * s6 * s6);
     c_tiles.push_back((uint32_t)((r.W + 15) / 16) * (uint32_t)((r.H + 15) / 16));
+    c_occw.push_back(occupancy_words(r.maps.ms));
     total_tris += r.n_tris;
   }
   VCT_CHECK(make_prefix(b->tris, c_tris));
@@ -415,6 +417,7 @@ vct_status build_batch(vct_batch* b, const vct_batch_scene* descs, uint32_t n) {
   VCT_CHECK(make_prefix(b->regions, c_regions));
   VCT_CHECK(make_prefix(b->tail5, c_tail5));
   VCT_CHECK(make_prefix(b->tail6, c_tail6));
+  VCT_CHECK(make_prefix(b->occw, c_occw));
   VCT_CHECK(make_prefix(b->tiles, c_tiles));
   // scene descriptors
   std::vector<BatchScene> hs(n);

@@ -110,7 +110,10 @@ vct_status train_loop(vct_renderer* r, const vct_mlp_desc& d, vct_mlp_report* re
     b.first = (int)(((uint64_t)s * batch) % m.n_samples);
     b.n = (int)batch;
     VCT_CUDA(launch_mlp_train(p, b, m.loss.p + s, r->stream));
-    VCT_CHECK(adam_step(r, d.lr));
+    // Constant for the first half of the steps, then decaying geometrically
+    // to a tenth (the optimiser settles instead of ending on a noisy step).
+    const double t = steps > 1 ? std::max(0.0, ((double)s - 0.5 * steps) / (0.5 * steps)) : 0.0;
+    VCT_CHECK(adam_step(r, (float)(d.lr * std::pow(0.1, t))));
   }
   VCT_CUDA(cudaEventRecord(e1, r->stream));
   VCT_CUDA(cudaEventSynchronize(e1));

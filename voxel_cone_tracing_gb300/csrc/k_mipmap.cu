@@ -179,18 +179,64 @@ __device__ __forceinline__ void write_alpha(const MapSet& ms, int level, int x, 
 // Levels src_level+1 .. src_level+K of the B^3 source region at (ox, oy, oz)
 // held in shared memory at `src` ([map][z][y][x]); intermediate levels go to
 // `lvl` (NMAPS * (B/2)^3, (B/4)^3, ...) and every level to its surfaces.
+__device__ __forceinline__ bool nonzero(uint32_t v) { return v != 0u; }
+__device__ __forceinline__ bool nonzero(uint2 v) { return (v.x | v.y) != 0u; }
+
+// Occupancy of cell (x, y, z) (index r) of level l of the region at
+// (ox, oy, oz): into the region's shared copy and to global memory -- level 1
+// of 16^3 regions straight into the packed bits (a warp holds four rows of
+// eight cells, each row one byte of its x-aligned word), other levels as
+// bytes.  Called by every thread of a warp together for level 1.
+template <int B>
+__device__ __forceinline__ void occ_store(const MapSet& ms, int l, int ox, int oy, int oz, int x, int y, int z,
+                                          int r, bool any, uint8_t* box) {
+  box[r] = any ? 1 : 0;
+  const int s = ms.N >> l;
+  if (B == 16 && l == 1) {
+    const uint32_t bits = __ballot_sync(0xffffffffu, any);
+    if ((threadIdx.x & 7) == 0) {
+      unsigned char* row = reinterpret_cast<unsigned char*>(
+          ms.occ_pack[1] + ((size_t)((oz >> 1) + z) * s + (oy >> 1) + y) * ms.occ_wpr[1]);
+      row[((ox >> 1) + x) >> 3] = (unsigned char)(bits >> (threadIdx.x & 31));
+    }
+  } else {
+    ms.occ_raw[l][((size_t)((oz >> l) + z) * s + (oy >> l) + y) * s + (ox >> l) + x] = any ? 1 : 0;
+  }
+}
+
 template <int NMAPS, bool FROM_L0, int K, int STORAGE>
 __device__ __forceinline__ void mip_reduce(const MapSet& ms, int src_level, int ox, int oy, int oz,
                                            const typename Texel<STORAGE>::T* src, typename Texel<STORAGE>::T* lvl) {
   typedef typename Texel<STORAGE>::T T;
   constexpr int B = 1 << K;
+  // Occupancy of the region's cells at levels 1..K (first pass only): a cell
+  // is 1 when its block of level 0 holds a non-zero texel.
+  __shared__ uint8_t occ_box[(B / 2) * (B / 2) * (B / 2) + (B / 4) * (B / 4) * (B / 4) + 16];
   const T* cur = src;
   int cur_b = B;
   bool cur_shared = FROM_L0;
   T* out = lvl;
+  int occ_prev = 0, occ_off = 0;
 #pragma unroll 1
   for (int l = 1; l <= K; ++l) {
     const int b = B >> l, b3 = b * b * b, cb3 = cur_b * cur_b * cur_b;
+    if (FROM_L0 && ms.skip_empty && !(NMAPS == 6 && l == 1)) {
+      const int cb = b * 2;
+      for (int r = threadIdx.x; r < b3; r += kThreads) {
+        const int x = r % b, y = (r / b) % b, z = r / (b * b);
+        bool any = false;
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+          const int ci = ((2 * z + c_off[k][2]) * cb + (2 * y + c_off[k][1])) * cb + (2 * x + c_off[k][0]);
+          any |= l == 1 ? nonzero(src[ci]) : occ_box[occ_prev + ci] != 0;
+        }
+        occ_store<B>(ms, l, ox, oy, oz, x, y, z, r, any, occ_box + occ_off);
+      }
+    }
+    if (FROM_L0 && ms.skip_empty) {
+      occ_prev = occ_off;
+      occ_off += b3;
+    }
     if (FROM_L0 && NMAPS == 6 && l == 1) {
       // The six maps of level 1 read the same children: one thread per
       // destination texel evaluates all six directions.
@@ -202,6 +248,12 @@ __device__ __forceinline__ void mip_reduce(const MapSet& ms, int src_level, int 
           ch[k] = cur[((2 * z + c_off[k][2]) * cur_b + (2 * y + c_off[k][1])) * cur_b + (2 * x + c_off[k][0])];
         if constexpr (STORAGE == VCT_STORAGE_RGBA8) aniso6_rgba8(ch, v6);
         else aniso6_rgba16f(ch, v6);
+        if (ms.skip_empty) {
+          bool any = false;
+#pragma unroll
+          for (int k = 0; k < 8; ++k) any |= nonzero(ch[k]);
+          occ_store<B>(ms, 1, ox, oy, oz, x, y, z, r, any, occ_box);
+        }
         const int dl = src_level + 1;
 #pragma unroll
         for (int d = 0; d < 6; ++d) {
@@ -482,6 +534,104 @@ cudaError_t run_all(const MapSet& ms, cudaStream_t st, int* launches, const CUte
   return cudaSuccess;
 }
 
+// ---- empty-space occupancy -------------------------------------------------
+// Two passes over one 32-bit word per thread, every level of a map set in
+// one launch each: (1) pack the raw occupancy of cells x0..x0+31 of a row
+// into bits (occ_pack[c]; levels above the first pass's OR their block of
+// level-occ_k bytes), (2) dilate by one cell along x, y and z (occ[c]).
+
+// Raw occupancy of cell (x, y, z) of level c (inside the grid).
+__device__ __forceinline__ bool occ_raw_cell(const MapSet& ms, int c, int x, int y, int z) {
+  if (c <= ms.occ_k) {
+    const int s = ms.N >> c;
+    return ms.occ_raw[c][((size_t)z * s + y) * s + x] != 0;
+  }
+  const int k = ms.occ_k, f = 1 << (c - k), sk = ms.N >> k;
+  for (int dz = 0; dz < f; ++dz)
+    for (int dy = 0; dy < f; ++dy)
+      for (int dx = 0; dx < f; ++dx)
+        if (ms.occ_raw[k][((size_t)(z * f + dz) * sk + (y * f + dy)) * sk + x * f + dx]) return true;
+  return false;
+}
+
+__device__ void occ_pack_word(const MapSet& ms, int c, uint32_t w) {
+  if (c == 1 && ms.occ_k == 4) return;  // written packed by the first pass (16^3 regions)
+  const int s = ms.N >> c, wpr = ms.occ_wpr[c];
+  const int xw = (int)(w % wpr), y = (int)((w / wpr) % s), z = (int)(w / ((uint32_t)wpr * s));
+  const int x0 = xw * 32;
+  uint32_t bits = 0;
+  if (c <= ms.occ_k && s >= 32) {
+    const uint32_t* r = reinterpret_cast<const uint32_t*>(ms.occ_raw[c] + ((size_t)z * s + y) * s + x0);
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      const uint32_t v = __ldg(r + j);
+#pragma unroll
+      for (int q = 0; q < 4; ++q) bits |= (((v >> (8 * q)) & 0xffu) ? 1u : 0u) << (4 * j + q);
+    }
+  } else {
+    for (int i = 0; i < 32 && x0 + i < s; ++i)
+      if (occ_raw_cell(ms, c, x0 + i, y, z)) bits |= 1u << i;
+  }
+  ms.occ_pack[c][w] = bits;
+}
+
+__device__ void occ_dilate_word(const MapSet& ms, int c, uint32_t w) {
+  const int s = ms.N >> c, wpr = ms.occ_wpr[c];
+  const int xw = (int)(w % wpr), y = (int)((w / wpr) % s), z = (int)(w / ((uint32_t)wpr * s));
+  uint32_t acc = 0;
+  for (int dz = -1; dz <= 1; ++dz) {
+    if ((unsigned)(z + dz) >= (unsigned)s) continue;
+    for (int dy = -1; dy <= 1; ++dy) {
+      if ((unsigned)(y + dy) >= (unsigned)s) continue;
+      const uint32_t* row = ms.occ_pack[c] + ((size_t)(z + dz) * s + (y + dy)) * wpr;
+      const uint32_t cur = row[xw];
+      const uint32_t lo = xw > 0 ? row[xw - 1] : 0u, hi = xw + 1 < wpr ? row[xw + 1] : 0u;
+      // bit i: cells x0+i-1 (from the word below for i = 0), x0+i, x0+i+1
+      acc |= cur | (cur << 1) | (lo >> 31) | (cur >> 1) | (hi << 31);
+    }
+  }
+  if (s - xw * 32 < 32) acc &= (1u << (s - xw * 32)) - 1u;
+  ms.occ[c][w] = acc;
+}
+
+// Words of levels 1..L-1 of one map set, and the level of flat word g.
+__host__ __device__ inline uint32_t occ_words(const MapSet& ms) {
+  uint32_t t = 0;
+  for (int c = 1; c < ms.L; ++c) t += (uint32_t)(ms.N >> c) * (uint32_t)(ms.N >> c) * (uint32_t)ms.occ_wpr[c];
+  return t;
+}
+__device__ __forceinline__ int occ_level(const MapSet& ms, uint32_t& g) {
+  for (int c = 1; c < ms.L; ++c) {
+    const uint32_t n = (uint32_t)(ms.N >> c) * (uint32_t)(ms.N >> c) * (uint32_t)ms.occ_wpr[c];
+    if (g < n) return c;
+    g -= n;
+  }
+  return 0;
+}
+
+template <bool DILATE>
+__global__ void __launch_bounds__(256) k_occupancy(MapSet ms, uint32_t total) {
+  for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < total; g += gridDim.x * blockDim.x) {
+    uint32_t w = g;
+    const int c = occ_level(ms, w);
+    if (DILATE) occ_dilate_word(ms, c, w);
+    else occ_pack_word(ms, c, w);
+  }
+}
+
+template <bool DILATE>
+__global__ void __launch_bounds__(256) k_occupancy_batch(BatchWork bw) {
+  for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < bw.total; g += gridDim.x * blockDim.x) {
+    const int s = batch_scene_of(bw, g);
+    const MapSet& ms = bw.scenes[s].ms;
+    if (!ms.skip_empty) continue;
+    uint32_t w = g - __ldg(bw.prefix + s);
+    const int c = occ_level(ms, w);
+    if (DILATE) occ_dilate_word(ms, c, w);
+    else occ_pack_word(ms, c, w);
+  }
+}
+
 // ---- Texture3D helpers (create/clear/mip of standalone RGBA8 textures) ----
 __global__ void k_fill_rgba8(cudaSurfaceObject_t s, int w, int h, int d, uchar4 v) {
   const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -513,13 +663,31 @@ __global__ void k_box_mip_rgba8(cudaSurfaceObject_t src, int sw, int sh, int sd,
 cudaError_t launch_mipmap(const MapSet& ms, int mip_mode, cudaStream_t st, int* launches, const void* tmap,
                           FrameStatus* status) {
   const CUtensorMap* map = static_cast<const CUtensorMap*>(tmap);
+  cudaError_t e;
   if (mip_mode == VCT_MIP_ISO) {
-    return ms.storage == VCT_STORAGE_RGBA8 ? run_all<1, VCT_STORAGE_RGBA8>(ms, st, launches, map, status)
-                                           : run_all<1, VCT_STORAGE_RGBA16F>(ms, st, launches, map, status);
+    e = ms.storage == VCT_STORAGE_RGBA8 ? run_all<1, VCT_STORAGE_RGBA8>(ms, st, launches, map, status)
+                                        : run_all<1, VCT_STORAGE_RGBA16F>(ms, st, launches, map, status);
+  } else {
+    e = ms.storage == VCT_STORAGE_RGBA8 ? run_all<6, VCT_STORAGE_RGBA8>(ms, st, launches, map, status)
+                                        : run_all<6, VCT_STORAGE_RGBA16F>(ms, st, launches, map, status);
   }
-  return ms.storage == VCT_STORAGE_RGBA8 ? run_all<6, VCT_STORAGE_RGBA8>(ms, st, launches, map, status)
-                                         : run_all<6, VCT_STORAGE_RGBA16F>(ms, st, launches, map, status);
+  if (e != cudaSuccess || !ms.skip_empty || ms.L < 2) return e;
+  const uint32_t total = occ_words(ms);
+  k_occupancy<false><<<(total + 255) / 256, 256, 0, st>>>(ms, total);
+  k_occupancy<true><<<(total + 255) / 256, 256, 0, st>>>(ms, total);
+  if (launches) *launches += 2;
+  return cudaGetLastError();
 }
+
+cudaError_t launch_occupancy_batch(const BatchWork& words, cudaStream_t st, int* launches) {
+  if (!words.total) return cudaSuccess;
+  k_occupancy_batch<false><<<(words.total + 255) / 256, 256, 0, st>>>(words);
+  k_occupancy_batch<true><<<(words.total + 255) / 256, 256, 0, st>>>(words);
+  if (launches) *launches += 2;
+  return cudaGetLastError();
+}
+
+uint32_t occupancy_words(const MapSet& ms) { return ms.skip_empty && ms.L > 1 ? occ_words(ms) : 0u; }
 
 cudaError_t launch_mipmap_batch(const BatchWork& regions, const BatchWork* tail, int n_tail, int storage,
                                 cudaStream_t st, int* launches) {

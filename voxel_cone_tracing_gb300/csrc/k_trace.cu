@@ -198,6 +198,33 @@ struct ExitTest {
   }
 };
 
+// Exact empty-space skip: true when every texel the sample at u with this
+// lod reads is 0 (MapSet::occ).  Its coarser quadrilinear level is c
+// (level 1 when lod < 1, where level 0 and level 1 are read); along each
+// axis the texels read at level c lie within cells floor(u * (N >> c)) +/- 1
+// (the finer level's texels lie inside them), which the dilated occupancy
+// bit of that cell covers; positions the texture path returns 0 for (not
+// finite or huge) and cells two or more outside the grid are empty too.
+__device__ __forceinline__ bool sample_empty(const MapSet& m, V3 u, float lod) {
+  // (A position that is not finite or is huge converts to an out-of-range
+  // or clamped cell; the texture path returns 0 for it either way.)
+  const int c = lod < 1.0f ? 1 : min((int)lod + 1, m.L - 1);
+  const int s = m.N >> c;
+  const float fs = (float)s;
+  int kx = __float2int_rd(u.x * fs), ky = __float2int_rd(u.y * fs), kz = __float2int_rd(u.z * fs);
+  if (min(kx, min(ky, kz)) < -1 || max(kx, max(ky, kz)) > s) return true;
+  kx = min(max(kx, 0), s - 1);
+  ky = min(max(ky, 0), s - 1);
+  kz = min(max(kz, 0), s - 1);
+  const uint32_t w = __ldg(m.occ[c] + ((size_t)kz * s + ky) * m.occ_wpr[c] + (kx >> 5));
+  return ((w >> (kx & 31)) & 1u) == 0u;
+}
+
+#ifndef VCT_SKIP_EMPTY_RGBA
+#define VCT_SKIP_EMPTY_RGBA 1
+#endif
+constexpr bool kSkipEmptyRGBA = VCT_SKIP_EMPTY_RGBA != 0;  // also in the RGBA cones (else shadow cones only)
+
 // trace_cone, voxel_cone_tracing.frag:88-119.
 template <int SAMPLER, bool ISO, int STORAGE>
 __device__ float4 trace_cone(const MapSet& m, V3 origin, V3 dir, float aperture, float max_dist) {
@@ -214,8 +241,10 @@ __device__ float4 trace_cone(const MapSet& m, V3 origin, V3 dir, float aperture,
   while (acc.w < 1.0f && dist < max_dist) {
     if (exit.gone(sp, ix, iy, iz)) break;
     const float mip = fmaxf(log2f(diam * cube_res), 0.0f);
-    const float4 s = sample_voxel<SAMPLER, ISO, STORAGE>(m, sp, ix, iy, iz, ad, mip);
-    acc = fma4(s, 1.0f - acc.w, acc);
+    if (!(kSkipEmptyRGBA && m.skip_empty && sample_empty(m, sp, mip))) {  // an empty sample adds exact zeros
+      const float4 s = sample_voxel<SAMPLER, ISO, STORAGE>(m, sp, ix, iy, iz, ad, mip);
+      acc = fma4(s, 1.0f - acc.w, acc);
+    }
     const float step = fmaxf(diam * 0.5f, voxel_size);
     dist += step;
     diam = dist * aperture;
@@ -241,7 +270,7 @@ __device__ float trace_alpha(const MapSet& m, V3 origin, V3 dir, float aperture,
   while (a < 1.0f && dist < max_dist) {
     if (exit.gone(sp, ix, iy, iz)) break;
     const float mip = fmaxf(log2f(diam * cube_res), 0.0f);
-    a = __fmaf_rn(sample_alpha(m, sp, ix, iy, iz, ad, mip), 1.0f - a, a);
+    if (!(m.skip_empty && sample_empty(m, sp, mip))) a = __fmaf_rn(sample_alpha(m, sp, ix, iy, iz, ad, mip), 1.0f - a, a);
     const float step = fmaxf(diam * 0.5f, voxel_size);
     dist += step;
     diam = dist * aperture;

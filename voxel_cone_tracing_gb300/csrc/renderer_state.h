@@ -221,6 +221,7 @@ struct MapStore {
   cudaArray_t l0_arr = nullptr;
   cudaMipmappedArray_t dir_arr[kMaxMaps] = {};
   cudaMipmappedArray_t alpha_arr[2] = {};
+  void* occ_mem = nullptr;  // occupancy grids of empty-space skipping
   MapSet ms = {};
 
   MapStore() = default;
@@ -247,6 +248,8 @@ struct MapStore {
     }
     if (l0_arr) cudaFreeArray(l0_arr);
     l0_arr = nullptr;
+    if (occ_mem) cudaFree(occ_mem);
+    occ_mem = nullptr;
     std::memset(&ms, 0, sizeof(ms));
   }
 
@@ -308,12 +311,42 @@ struct MapStore {
     ms.L = L;
     ms.nmaps = nmaps;
     ms.storage = storage;
+    if (L > 1) {
+      // occupancy: raw bytes for the first pass's levels, dilated bits for all
+      ms.occ_k = std::min(L - 1, 4);
+      size_t bytes = 0;
+      for (int c = 1; c <= ms.occ_k; ++c) bytes += (size_t)(r >> c) * (r >> c) * (r >> c);
+      bytes = (bytes + 255) & ~(size_t)255;
+      const size_t raw_bytes = bytes;
+      for (int c = 1; c < L; ++c) {
+        const size_t s = r >> c;
+        ms.occ_wpr[c] = (int)((s + 31) / 32);
+        bytes += 2 * s * s * (size_t)ms.occ_wpr[c] * 4;  // packed + dilated
+      }
+      VCT_CUDA(cudaMalloc(&occ_mem, bytes));
+      unsigned char* base = static_cast<unsigned char*>(occ_mem);
+      size_t o = 0;
+      for (int c = 1; c <= ms.occ_k; ++c) {
+        ms.occ_raw[c] = base + o;
+        o += (size_t)(r >> c) * (r >> c) * (r >> c);
+      }
+      o = raw_bytes;
+      for (int c = 1; c < L; ++c) {
+        const size_t s = r >> c;
+        ms.occ[c] = reinterpret_cast<uint32_t*>(base + o);
+        o += s * s * (size_t)ms.occ_wpr[c] * 4;
+        ms.occ_pack[c] = reinterpret_cast<uint32_t*>(base + o);
+        o += s * s * (size_t)ms.occ_wpr[c] * 4;
+      }
+    }
     set_full_march(false);
     return VCT_OK;
   }
 
-  // Cones stop 3/4 of the coarsest texel outside the grid (exact), or never.
+  // Cones stop 3/4 of the coarsest texel outside the grid and skip samples
+  // in empty space (both exact), or march and sample every step.
   void set_full_march(bool full) {
+    ms.skip_empty = (!full && occ_mem) ? 1 : 0;
     ms.exit_margin = full ? std::numeric_limits<float>::infinity() : 0.75f * (float)(1 << (ms.L - 1)) / (float)ms.N;
   }
 };

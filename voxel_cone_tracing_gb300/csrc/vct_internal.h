@@ -113,6 +113,20 @@ struct MapSet {
   // A cone moving away from the grid stops once its sample position is more
   // than this far outside [0,1] along that axis (+inf: never).
   float exit_margin;
+  // Empty-space skipping (skip_empty != 0).  occ_raw[c], c = 1..K (K = the
+  // levels of the MipBuilder's first pass): one byte per level-c cell, 1 when
+  // its block of 2^c level-0 voxels holds a non-zero texel (written by that
+  // pass).  occ[c], c = 1..L-1: that occupancy dilated by one cell (3x3x3 OR),
+  // one bit per cell, packed along x in occ_wpr[c] words per row.  A sample
+  // whose coarser quadrilinear level is c reads only texels of the cells
+  // floor(u * (N >> c)) +/- 1 along each axis (and the finer level's texels
+  // lie inside those), so an unset bit means every texel it reads is 0.
+  int skip_empty;
+  int occ_k;
+  uint8_t* occ_raw[kMaxLevels];
+  uint32_t* occ_pack[kMaxLevels];  // undilated occupancy bits (same layout as occ)
+  uint32_t* occ[kMaxLevels];
+  int occ_wpr[kMaxLevels];
 };
 
 struct VoxBuffers {
@@ -320,6 +334,10 @@ size_t heavy_slot_bytes(int storage);
 cudaError_t launch_voxelize_batch(const BatchWork& tris, const BatchWork& bricks, uint32_t total_bricks, int mode,
                                   int storage, const BatchBuffers& bb, uint32_t* scan_tmp, const BatchShape& shape,
                                   int sms, cudaStream_t st, int* launches);
+// Dilated occupancy words of a map set (0 without empty-space skipping) and
+// their batch pass (one work item per word of every scene).
+uint32_t occupancy_words(const MapSet& ms);
+cudaError_t launch_occupancy_batch(const BatchWork& words, cudaStream_t st, int* launches);
 cudaError_t launch_mipmap_batch(const BatchWork& regions, const BatchWork* tail, int n_tail, int storage,
                                 cudaStream_t st, int* launches);
 cudaError_t launch_gbuffer_batch(const BatchWork& tris, const BatchWork& tiles, size_t total_px,
