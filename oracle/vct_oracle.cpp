@@ -774,9 +774,98 @@ template <class R> struct ConeOut { V4<R> c; int steps; };
 // all classes, the steps whose lod lies in [k, k+1) for k = 0..6 (k = 7:
 // lod >= 7); then per class the steps taken once the cone has moved more
 // than 3/4 of the coarsest texel outside [0,1] along an axis it travels
-// away on (they read border texels only; the engine does not take them).
-enum { kStatCones = 0, kStatSteps = 4, kStatLodLt1 = 8, kStatLodBand = 12, kStatBeyond = 20, kStatN = 24 };
+// away on (they read border texels only; the engine does not take them);
+// then per class the other steps whose texels are all 0 by the engine's
+// occupancy rule (below), and how many of those have lod < 1.
+enum {
+  kStatCones = 0, kStatSteps = 4, kStatLodLt1 = 8, kStatLodBand = 12, kStatBeyond = 20, kStatEmpty = 24,
+  kStatEmptyLt1 = 28, kStatN = 32
+};
 static std::atomic<uint64_t> g_stats[kStatN];
+// The engine's empty-space rule (csrc/k_trace.cu sample_empty): per level c
+// >= 1, cell occupancy (its block of level 0 holds a non-zero texel) ORed
+// over the 2x2x2 cells k..k+1; a sample with lod is empty, for c = (lod < 1
+// ? 1 : min(floor(lod) + 1, L - 1)) and k = floor(u * (N >> c) - 0.5), when
+// no coordinate lies within 1/64 of a texel boundary and either k lies two
+// or more texels outside the grid or the ORed occupancy of k is 0.  Shadow
+// cones use the coarser rule of sample_empty3: occupancy ORed over the 3x3x3
+// cells around k = floor(u * (N >> c)), empty when that is 0 or k lies two
+// or more cells outside the grid.
+static std::vector<std::vector<uint8_t>> g_dilated, g_dilated3;
+static void build_dilated(const uint8_t* level0, int N, int L) {
+  std::vector<std::vector<uint8_t>> raw(1, std::vector<uint8_t>((size_t)N * N * N));
+  for (size_t v = 0; v < (size_t)N * N * N; ++v)
+    raw[0][v] = (level0[4 * v] | level0[4 * v + 1] | level0[4 * v + 2] | level0[4 * v + 3]) != 0;
+  g_dilated.assign(L, {});
+  g_dilated3.assign(L, {});
+  for (int c = 1; c < L; ++c) {
+    const int s = N >> c, p = 2 * s;
+    std::vector<uint8_t> o((size_t)s * s * s, 0);
+    for (int z = 0; z < s; ++z)
+      for (int y = 0; y < s; ++y)
+        for (int x = 0; x < s; ++x) {
+          uint8_t a = 0;
+          for (int k = 0; k < 8; ++k)
+            a |= raw[c - 1][((size_t)(2 * z + (k >> 2)) * p + 2 * y + ((k >> 1) & 1)) * p + 2 * x + (k & 1)];
+          o[((size_t)z * s + y) * s + x] = a;
+        }
+    raw.push_back(o);
+    std::vector<uint8_t> d((size_t)s * s * s, 0);
+    for (int z = 0; z < s; ++z)
+      for (int y = 0; y < s; ++y)
+        for (int x = 0; x < s; ++x) {
+          uint8_t a = 0;
+          for (int dz = 0; dz <= 1; ++dz)
+            for (int dy = 0; dy <= 1; ++dy)
+              for (int dx = 0; dx <= 1; ++dx) {
+                const int X = x + dx, Y = y + dy, Z = z + dz;
+                if (X >= 0 && Y >= 0 && Z >= 0 && X < s && Y < s && Z < s) a |= o[((size_t)Z * s + Y) * s + X];
+              }
+          d[((size_t)z * s + y) * s + x] = a;
+        }
+    g_dilated[c] = std::move(d);
+    std::vector<uint8_t> d3((size_t)s * s * s, 0);
+    for (int z = 0; z < s; ++z)
+      for (int y = 0; y < s; ++y)
+        for (int x = 0; x < s; ++x) {
+          uint8_t a = 0;
+          for (int dz = -1; dz <= 1; ++dz)
+            for (int dy = -1; dy <= 1; ++dy)
+              for (int dx = -1; dx <= 1; ++dx) {
+                const int X = x + dx, Y = y + dy, Z = z + dz;
+                if (X >= 0 && Y >= 0 && Z >= 0 && X < s && Y < s && Z < s) a |= o[((size_t)Z * s + Y) * s + X];
+              }
+          d3[((size_t)z * s + y) * s + x] = a;
+        }
+    g_dilated3[c] = std::move(d3);
+  }
+}
+template <class R> static bool sample_empty3_rule(int N, int L, V3<R> u, R lod) {
+  const int c = lod < R(1) ? 1 : std::min((int)lod + 1, L - 1);
+  const int s = N >> c;
+  int k[3] = {(int)std::floor(u.x * R(s)), (int)std::floor(u.y * R(s)), (int)std::floor(u.z * R(s))};
+  for (int a = 0; a < 3; ++a) {
+    if (k[a] < -1 || k[a] > s) return true;
+    k[a] = std::min(std::max(k[a], 0), s - 1);
+  }
+  return g_dilated3[c][((size_t)k[2] * s + k[1]) * s + k[0]] == 0;
+}
+template <class R> static bool sample_empty_rule(int N, int L, V3<R> u, R lod) {
+  const int c = lod < R(1) ? 1 : std::min((int)lod + 1, L - 1);
+  const int s = N >> c;
+  const R t[3] = {u.x * R(s) - R(0.5), u.y * R(s) - R(0.5), u.z * R(s) - R(0.5)};
+  int k[3];
+  bool out = false;
+  for (int a = 0; a < 3; ++a) {
+    const R b = std::floor(t[a]), f = t[a] - b;
+    if (f < R(1) / R(64) || f > R(1) - R(1) / R(64)) return false;
+    k[a] = (int)b;
+    if (k[a] < -1 || k[a] > s - 1) out = true;
+  }
+  if (out) return true;
+  for (int a = 0; a < 3; ++a) k[a] = std::max(k[a], 0);
+  return g_dilated[c][((size_t)k[2] * s + k[1]) * s + k[0]] == 0;
+}
 static bool g_stats_on = false;
 static thread_local int t_cone_class = 0;
 
@@ -793,12 +882,19 @@ static ConeOut<R> trace_cone(const Maps& m, V3<R> origin, V3<R> dir, R aperture,
   R dist = R(3) * voxel_size;
   R diam = dist * aperture;
   V3<R> sp = dir * dist + origin;
-  int steps = 0, lod_lt1 = 0, beyond = 0;
+  int steps = 0, lod_lt1 = 0, beyond = 0, empty = 0, empty_lt1 = 0;
   const R margin = R(0.75) * R(1 << (m.L - 1)) / cube_res;
   auto outside = [&](R p, bool up) { return up ? p > R(1) + margin : p < -margin; };
+  bool gone = false;
   while (acc.a < R(1) && dist < max_dist) {
-    if (outside(sp.x, ix == 1) || outside(sp.y, iy == 3) || outside(sp.z, iz == 5)) ++beyond;
+    gone = gone || outside(sp.x, ix == 1) || outside(sp.y, iy == 3) || outside(sp.z, iz == 5);
+    if (gone) ++beyond;
     R mip = fmaxr(R(std::log2(diam * cube_res)), R(0));
+    if (g_stats_on && !gone && !g_dilated.empty() &&
+        (t_cone_class == 2 ? sample_empty3_rule<R>(m.N, m.L, sp, mip) : sample_empty_rule<R>(m.N, m.L, sp, mip))) {
+      ++empty;
+      if (mip < R(1)) ++empty_lt1;
+    }
     V4<R> smp = texture_lod<R>(m, ix, sp, mip) * ad.x + texture_lod<R>(m, iy, sp, mip) * ad.y +
                 texture_lod<R>(m, iz, sp, mip) * ad.z;
     acc = acc + smp * (R(1) - acc.a);
@@ -815,6 +911,8 @@ static ConeOut<R> trace_cone(const Maps& m, V3<R> origin, V3<R> dir, R aperture,
     g_stats[kStatSteps + t_cone_class] += (uint64_t)steps;
     g_stats[kStatLodLt1 + t_cone_class] += (uint64_t)lod_lt1;
     g_stats[kStatBeyond + t_cone_class] += (uint64_t)beyond;
+    g_stats[kStatEmpty + t_cone_class] += (uint64_t)empty;
+    g_stats[kStatEmptyLt1 + t_cone_class] += (uint64_t)empty_lt1;
   }
   return {acc, steps};
 }
@@ -1290,9 +1388,12 @@ void orc_trace_stats(const orc_scene* s, const orc_params* p, const uint8_t* lev
                      const uint32_t* tri_id, const double* pos, const double* nrm, const uint32_t* mat,
                      int32_t row_stride, float* out, uint64_t* stats) {
   for (auto& g : g_stats) g = 0;
+  build_dilated(level0, p->grid_res, p->levels);
   g_stats_on = true;
   trace_impl<double>(s, p, level0, chains, tri_id, pos, nrm, mat, row_stride, out);
   g_stats_on = false;
+  g_dilated.clear();
+  g_dilated3.clear();
   for (int i = 0; i < kStatN; ++i) stats[i] = g_stats[i].load();
 }
 

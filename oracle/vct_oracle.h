@@ -171,8 +171,10 @@ void orc_trace_f32(const orc_scene* s, const orc_params* p,
  * refraction); [12..19] steps of all classes with lod in [k, k+1), k = 0..6,
  * and lod >= 7; [20..23] per class the steps taken more than 3/4 of the
  * coarsest texel outside [0,1] along an axis the cone moves away on (border
- * texels only).  stats holds 24 entries.  Not thread-safe against
- * concurrent orc_trace_stats. */
+ * texels only); [24..27] per class the other steps whose texels are all 0
+ * by the engine's occupancy rule, [28..31] those of them with lod < 1.
+ * stats holds 32 entries.  Not thread-safe against concurrent
+ * orc_trace_stats. */
 void orc_trace_stats(const orc_scene* s, const orc_params* p, const uint8_t* level0,
                      const uint8_t* chains, const uint32_t* tri_id, const double* pos,
                      const double* nrm, const uint32_t* mat, int32_t row_stride,

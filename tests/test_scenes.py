@@ -70,7 +70,7 @@ def test_bench_frame_work(oracle):
     assert sum(bands) == sum(v["steps"] for v in st.values())
     assert st["diffuse"]["cones"] == 9 * px
     assert 3 * steps + lt1 == pytest.approx(bench.TRACE_FETCHES_PER_PIXEL_REF, rel=0.02)
-    shadow = st["shadow"]["steps"] / px
-    beyond = sum(v["beyond"] for v in st.values()) / px
     assert st["shadow"]["beyond"] == 0  # shadow cones end at the light, inside the grid
-    assert 3 * steps + lt1 - shadow - 3 * beyond == pytest.approx(bench.TRACE_FETCHES_PER_PIXEL, rel=0.02)
+    engine = sum((2 if k == "shadow" else 3) * (v["steps"] - v["beyond"] - v["empty"]) + v["lod_lt1"] - v["empty_lt1"]
+                 for k, v in st.items()) / px
+    assert engine == pytest.approx(bench.TRACE_FETCHES_PER_PIXEL, rel=0.02)

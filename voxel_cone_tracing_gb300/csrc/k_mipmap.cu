@@ -538,7 +538,8 @@ cudaError_t run_all(const MapSet& ms, cudaStream_t st, int* launches, const CUte
 // Two passes over one 32-bit word per thread, every level of a map set in
 // one launch each: (1) pack the raw occupancy of cells x0..x0+31 of a row
 // into bits (occ_pack[c]; levels above the first pass's OR their block of
-// level-occ_k bytes), (2) dilate by one cell along x, y and z (occ[c]).
+// level-occ_k bytes), (2) OR each cell with its +1 neighbours along x, y
+// and z (occ[c]: the 2x2x2 block a trilinear lookup reads).
 
 // Raw occupancy of cell (x, y, z) of level c (inside the grid).
 __device__ __forceinline__ bool occ_raw_cell(const MapSet& ms, int c, int x, int y, int z) {
@@ -575,10 +576,14 @@ __device__ void occ_pack_word(const MapSet& ms, int c, uint32_t w) {
   ms.occ_pack[c][w] = bits;
 }
 
+// Bit i of word (x0 / 32) of row (y, z) of occ[c]: the OR over the 2x2x2
+// cells x0+i .. x0+i+1, y .. y+1, z .. z+1 (the texels of one trilinear
+// lookup whose lower texel is that cell); of occ3[c]: the OR over the
+// 3x3x3 cells around it.
 __device__ void occ_dilate_word(const MapSet& ms, int c, uint32_t w) {
   const int s = ms.N >> c, wpr = ms.occ_wpr[c];
   const int xw = (int)(w % wpr), y = (int)((w / wpr) % s), z = (int)(w / ((uint32_t)wpr * s));
-  uint32_t acc = 0;
+  uint32_t box = 0, dil = 0;
   for (int dz = -1; dz <= 1; ++dz) {
     if ((unsigned)(z + dz) >= (unsigned)s) continue;
     for (int dy = -1; dy <= 1; ++dy) {
@@ -586,12 +591,17 @@ __device__ void occ_dilate_word(const MapSet& ms, int c, uint32_t w) {
       const uint32_t* row = ms.occ_pack[c] + ((size_t)(z + dz) * s + (y + dy)) * wpr;
       const uint32_t cur = row[xw];
       const uint32_t lo = xw > 0 ? row[xw - 1] : 0u, hi = xw + 1 < wpr ? row[xw + 1] : 0u;
-      // bit i: cells x0+i-1 (from the word below for i = 0), x0+i, x0+i+1
-      acc |= cur | (cur << 1) | (lo >> 31) | (cur >> 1) | (hi << 31);
+      const uint32_t up = cur | (cur >> 1) | (hi << 31);  // cells x0+i, x0+i+1
+      dil |= up | (cur << 1) | (lo >> 31);                // and x0+i-1
+      if (dz >= 0 && dy >= 0) box |= up;
     }
   }
-  if (s - xw * 32 < 32) acc &= (1u << (s - xw * 32)) - 1u;
-  ms.occ[c][w] = acc;
+  if (s - xw * 32 < 32) {
+    box &= (1u << (s - xw * 32)) - 1u;
+    dil &= (1u << (s - xw * 32)) - 1u;
+  }
+  ms.occ[c][w] = box;
+  ms.occ3[c][w] = dil;
 }
 
 // Words of levels 1..L-1 of one map set, and the level of flat word g.

@@ -199,15 +199,36 @@ struct ExitTest {
 };
 
 // Exact empty-space skip: true when every texel the sample at u with this
-// lod reads is 0 (MapSet::occ).  Its coarser quadrilinear level is c
-// (level 1 when lod < 1, where level 0 and level 1 are read); along each
-// axis the texels read at level c lie within cells floor(u * (N >> c)) +/- 1
-// (the finer level's texels lie inside them), which the dilated occupancy
-// bit of that cell covers; positions the texture path returns 0 for (not
-// finite or huge) and cells two or more outside the grid are empty too.
+// lod reads is 0 (MapSet::occ).  Its coarser quadrilinear level is c (level
+// 1 when lod < 1, where level 0 and level 1 are read); there the lookup reads
+// texels k .. k+1 along each axis, k = floor(u * (N >> c) - 0.5), and the
+// finer level's texels lie inside them, so the occ bit of k decides.  Within
+// 1/64 texel of a texel boundary the texture unit's fixed-point coordinate
+// could pick the neighbouring pair: such samples are fetched.  A pair two or
+// more texels outside the grid reads border texels only.  (A position that is
+// not finite or is huge ends up outside or fetched; the texture path returns
+// 0 for it either way.)
 __device__ __forceinline__ bool sample_empty(const MapSet& m, V3 u, float lod) {
-  // (A position that is not finite or is huge converts to an out-of-range
-  // or clamped cell; the texture path returns 0 for it either way.)
+  const int c = lod < 1.0f ? 1 : min((int)lod + 1, m.L - 1);
+  const int s = m.N >> c;
+  const float fs = (float)s;
+  const float tx = u.x * fs - 0.5f, ty = u.y * fs - 0.5f, tz = u.z * fs - 0.5f;
+  const float bx = floorf(tx), by = floorf(ty), bz = floorf(tz);
+  const float fx = tx - bx, fy = ty - by, fz = tz - bz;
+  constexpr float kEps = 1.0f / 64.0f;
+  if (fminf(fx, fminf(fy, fz)) < kEps || fmaxf(fx, fmaxf(fy, fz)) > 1.0f - kEps) return false;
+  if (fminf(bx, fminf(by, bz)) < -1.0f || fmaxf(bx, fmaxf(by, bz)) > (float)(s - 1)) return true;
+  const int kx = max((int)bx, 0), ky = max((int)by, 0), kz = max((int)bz, 0);
+  const uint32_t w = __ldg(m.occ[c] + ((size_t)kz * s + ky) * m.occ_wpr[c] + (kx >> 5));
+  return ((w >> (kx & 31)) & 1u) == 0u;
+}
+
+// The coarser test (MapSet::occ3): the texels the sample reads at level c
+// lie within one cell of floor(u * (N >> c)) along each axis, under any
+// rounding of the texture unit's coordinate; cells two or more outside the
+// grid hold border texels only.  Cheaper than sample_empty (no boundary
+// test); it finds nearly all the empty steps of the narrow shadow cones.
+__device__ __forceinline__ bool sample_empty3(const MapSet& m, V3 u, float lod) {
   const int c = lod < 1.0f ? 1 : min((int)lod + 1, m.L - 1);
   const int s = m.N >> c;
   const float fs = (float)s;
@@ -216,7 +237,7 @@ __device__ __forceinline__ bool sample_empty(const MapSet& m, V3 u, float lod) {
   kx = min(max(kx, 0), s - 1);
   ky = min(max(ky, 0), s - 1);
   kz = min(max(kz, 0), s - 1);
-  const uint32_t w = __ldg(m.occ[c] + ((size_t)kz * s + ky) * m.occ_wpr[c] + (kx >> 5));
+  const uint32_t w = __ldg(m.occ3[c] + ((size_t)kz * s + ky) * m.occ_wpr[c] + (kx >> 5));
   return ((w >> (kx & 31)) & 1u) == 0u;
 }
 
@@ -270,7 +291,7 @@ __device__ float trace_alpha(const MapSet& m, V3 origin, V3 dir, float aperture,
   while (a < 1.0f && dist < max_dist) {
     if (exit.gone(sp, ix, iy, iz)) break;
     const float mip = fmaxf(log2f(diam * cube_res), 0.0f);
-    if (!(m.skip_empty && sample_empty(m, sp, mip))) a = __fmaf_rn(sample_alpha(m, sp, ix, iy, iz, ad, mip), 1.0f - a, a);
+    if (!(m.skip_empty && sample_empty3(m, sp, mip))) a = __fmaf_rn(sample_alpha(m, sp, ix, iy, iz, ad, mip), 1.0f - a, a);
     const float step = fmaxf(diam * 0.5f, voxel_size);
     dist += step;
     diam = dist * aperture;

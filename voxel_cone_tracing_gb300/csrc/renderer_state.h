@@ -321,7 +321,7 @@ struct MapStore {
       for (int c = 1; c < L; ++c) {
         const size_t s = r >> c;
         ms.occ_wpr[c] = (int)((s + 31) / 32);
-        bytes += 2 * s * s * (size_t)ms.occ_wpr[c] * 4;  // packed + dilated
+        bytes += 3 * s * s * (size_t)ms.occ_wpr[c] * 4;  // packed + box + dilated
       }
       VCT_CUDA(cudaMalloc(&occ_mem, bytes));
       unsigned char* base = static_cast<unsigned char*>(occ_mem);
@@ -336,6 +336,8 @@ struct MapStore {
         ms.occ[c] = reinterpret_cast<uint32_t*>(base + o);
         o += s * s * (size_t)ms.occ_wpr[c] * 4;
         ms.occ_pack[c] = reinterpret_cast<uint32_t*>(base + o);
+        o += s * s * (size_t)ms.occ_wpr[c] * 4;
+        ms.occ3[c] = reinterpret_cast<uint32_t*>(base + o);
         o += s * s * (size_t)ms.occ_wpr[c] * 4;
       }
     }

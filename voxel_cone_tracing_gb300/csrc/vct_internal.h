@@ -113,19 +113,22 @@ struct MapSet {
   // A cone moving away from the grid stops once its sample position is more
   // than this far outside [0,1] along that axis (+inf: never).
   float exit_margin;
-  // Empty-space skipping (skip_empty != 0).  occ_raw[c], c = 1..K (K = the
-  // levels of the MipBuilder's first pass): one byte per level-c cell, 1 when
-  // its block of 2^c level-0 voxels holds a non-zero texel (written by that
-  // pass).  occ[c], c = 1..L-1: that occupancy dilated by one cell (3x3x3 OR),
-  // one bit per cell, packed along x in occ_wpr[c] words per row.  A sample
-  // whose coarser quadrilinear level is c reads only texels of the cells
-  // floor(u * (N >> c)) +/- 1 along each axis (and the finer level's texels
-  // lie inside those), so an unset bit means every texel it reads is 0.
+  // Empty-space skipping (skip_empty != 0).  occ_raw[c], c = 2..K (K = the
+  // levels of the MipBuilder's first pass; level 1 goes straight to
+  // occ_pack): one byte per level-c cell, 1 when its block of 2^c level-0
+  // voxels holds a non-zero texel.  occ_pack[c]: those bits packed along x
+  // in occ_wpr[c] words per row; occ[c], c = 1..L-1: bit k = OR over the
+  // 2x2x2 cells k..k+1 -- the texels a trilinear lookup at level c reads when
+  // its lower texel is k (the finer level's texels lie inside them), so an
+  // unset bit means the sample reads only zeros; occ3[c]: the OR over the
+  // 3x3x3 cells around k (a cheaper, coarser test: the texels read lie within
+  // one cell of floor(u * (N >> c))).
   int skip_empty;
   int occ_k;
   uint8_t* occ_raw[kMaxLevels];
   uint32_t* occ_pack[kMaxLevels];  // undilated occupancy bits (same layout as occ)
   uint32_t* occ[kMaxLevels];
+  uint32_t* occ3[kMaxLevels];
   int occ_wpr[kMaxLevels];
 };
 
