@@ -44,11 +44,11 @@ NUM_SMS = 152
 # pixel (3 fetches each, +1 level-0 fetch for the 25.2 steps with lod < 1)
 # by the reference's sample rule; here the 58.0 shadow steps take 2 fetches
 # (alpha-only chains), the 24.6 steps beyond the grid are not taken (exact
-# early exit) and 89.8 more steps find only empty cells (exact empty-space
+# early exit) and 86 more steps find only empty cells (exact empty-space
 # skip: no fetch); counted by the instrumented oracle (oracle.trace_stats;
 # checked by tests/test_scenes.py::test_bench_frame_work).
 TRACE_FETCHES_PER_PIXEL_REF = 778.9
-TRACE_FETCHES_PER_PIXEL = 406.4
+TRACE_FETCHES_PER_PIXEL = 417.3
 INSTANCE_RECORD_BYTES = 144   # one per queued model (DevInstance)
 STATUS_BYTES = 48             # per-frame status read back with the frame
 

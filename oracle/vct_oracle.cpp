@@ -785,12 +785,11 @@ static std::atomic<uint64_t> g_stats[kStatN];
 // The engine's empty-space rule (csrc/k_trace.cu sample_empty): per level c
 // >= 1, cell occupancy (its block of level 0 holds a non-zero texel) ORed
 // over the 2x2x2 cells k..k+1; a sample with lod is empty, for c = (lod < 1
-// ? 1 : min(floor(lod) + 1, L - 1)) and k = floor(u * (N >> c) - 0.5), when
-// no coordinate lies within 1/64 of a texel boundary and either k lies two
-// or more texels outside the grid or the ORed occupancy of k is 0.  Shadow
-// cones use the coarser rule of sample_empty3: occupancy ORed over the 3x3x3
-// cells around k = floor(u * (N >> c)), empty when that is 0 or k lies two
-// or more cells outside the grid.
+// ? 1 : min(floor(lod) + 1, L - 1)) and k = floor(u * (N >> c) - 0.5)
+// clamped into the grid, when no coordinate lies within 1/64 of a texel
+// boundary and the ORed occupancy of k is 0.  Shadow cones use the coarser
+// rule of sample_empty3: occupancy ORed over the 3x3x3 cells around k =
+// floor(u * (N >> c)) clamped into the grid, empty when that is 0.
 static std::vector<std::vector<uint8_t>> g_dilated, g_dilated3;
 static void build_dilated(const uint8_t* level0, int N, int L) {
   std::vector<std::vector<uint8_t>> raw(1, std::vector<uint8_t>((size_t)N * N * N));
@@ -844,10 +843,7 @@ template <class R> static bool sample_empty3_rule(int N, int L, V3<R> u, R lod) 
   const int c = lod < R(1) ? 1 : std::min((int)lod + 1, L - 1);
   const int s = N >> c;
   int k[3] = {(int)std::floor(u.x * R(s)), (int)std::floor(u.y * R(s)), (int)std::floor(u.z * R(s))};
-  for (int a = 0; a < 3; ++a) {
-    if (k[a] < -1 || k[a] > s) return true;
-    k[a] = std::min(std::max(k[a], 0), s - 1);
-  }
+  for (int a = 0; a < 3; ++a) k[a] = std::min(std::max(k[a], 0), s - 1);
   return g_dilated3[c][((size_t)k[2] * s + k[1]) * s + k[0]] == 0;
 }
 template <class R> static bool sample_empty_rule(int N, int L, V3<R> u, R lod) {
@@ -855,15 +851,11 @@ template <class R> static bool sample_empty_rule(int N, int L, V3<R> u, R lod) {
   const int s = N >> c;
   const R t[3] = {u.x * R(s) - R(0.5), u.y * R(s) - R(0.5), u.z * R(s) - R(0.5)};
   int k[3];
-  bool out = false;
   for (int a = 0; a < 3; ++a) {
     const R b = std::floor(t[a]), f = t[a] - b;
     if (f < R(1) / R(64) || f > R(1) - R(1) / R(64)) return false;
-    k[a] = (int)b;
-    if (k[a] < -1 || k[a] > s - 1) out = true;
+    k[a] = std::min(std::max((int)b, 0), s - 1);
   }
-  if (out) return true;
-  for (int a = 0; a < 3; ++a) k[a] = std::max(k[a], 0);
   return g_dilated[c][((size_t)k[2] * s + k[1]) * s + k[0]] == 0;
 }
 static bool g_stats_on = false;

@@ -204,12 +204,13 @@ struct ExitTest {
 // texels k .. k+1 along each axis, k = floor(u * (N >> c) - 0.5), and the
 // finer level's texels lie inside them, so the occ bit of k decides.  Within
 // 1/64 texel of a texel boundary the texture unit's fixed-point coordinate
-// could pick the neighbouring pair: such samples are fetched.  A pair two or
-// more texels outside the grid reads border texels only.  (A position that is
-// not finite or is huge ends up outside or fetched; the texture path returns
-// 0 for it either way.)
+// could pick the neighbouring pair: such samples are fetched.  A pair outside
+// the grid is tested at the nearest cell inside it (conservative: border
+// texels are 0, and cones leaving the grid stop by ExitTest).  (A position
+// that is not finite or is huge ends up clamped or fetched; the texture path
+// returns 0 for it either way.)
 __device__ __forceinline__ bool sample_empty(const MapSet& m, V3 u, float lod) {
-  const int c = lod < 1.0f ? 1 : min((int)lod + 1, m.L - 1);
+  const int c = min((int)lod + 1, m.L - 1);  // lod >= 0
   const int s = m.N >> c;
   const float fs = (float)s;
   const float tx = u.x * fs - 0.5f, ty = u.y * fs - 0.5f, tz = u.z * fs - 0.5f;
@@ -217,27 +218,24 @@ __device__ __forceinline__ bool sample_empty(const MapSet& m, V3 u, float lod) {
   const float fx = tx - bx, fy = ty - by, fz = tz - bz;
   constexpr float kEps = 1.0f / 64.0f;
   if (fminf(fx, fminf(fy, fz)) < kEps || fmaxf(fx, fmaxf(fy, fz)) > 1.0f - kEps) return false;
-  if (fminf(bx, fminf(by, bz)) < -1.0f || fmaxf(bx, fmaxf(by, bz)) > (float)(s - 1)) return true;
-  const int kx = max((int)bx, 0), ky = max((int)by, 0), kz = max((int)bz, 0);
-  const uint32_t w = __ldg(m.occ[c] + ((size_t)kz * s + ky) * m.occ_wpr[c] + (kx >> 5));
+  const int kx = min(max((int)bx, 0), s - 1), ky = min(max((int)by, 0), s - 1), kz = min(max((int)bz, 0), s - 1);
+  const uint32_t w = __ldg(m.occ[c] + ((uint32_t)kz * s + ky) * m.occ_wpr[c] + (kx >> 5));
   return ((w >> (kx & 31)) & 1u) == 0u;
 }
 
 // The coarser test (MapSet::occ3): the texels the sample reads at level c
 // lie within one cell of floor(u * (N >> c)) along each axis, under any
-// rounding of the texture unit's coordinate; cells two or more outside the
-// grid hold border texels only.  Cheaper than sample_empty (no boundary
-// test); it finds nearly all the empty steps of the narrow shadow cones.
+// rounding of the texture unit's coordinate (positions outside the grid are
+// tested at the nearest cell inside, conservatively).  Cheaper than
+// sample_empty (no boundary test); it finds nearly all the empty steps of
+// the narrow shadow cones.
 __device__ __forceinline__ bool sample_empty3(const MapSet& m, V3 u, float lod) {
-  const int c = lod < 1.0f ? 1 : min((int)lod + 1, m.L - 1);
+  const int c = min((int)lod + 1, m.L - 1);  // lod >= 0
   const int s = m.N >> c;
   const float fs = (float)s;
-  int kx = __float2int_rd(u.x * fs), ky = __float2int_rd(u.y * fs), kz = __float2int_rd(u.z * fs);
-  if (min(kx, min(ky, kz)) < -1 || max(kx, max(ky, kz)) > s) return true;
-  kx = min(max(kx, 0), s - 1);
-  ky = min(max(ky, 0), s - 1);
-  kz = min(max(kz, 0), s - 1);
-  const uint32_t w = __ldg(m.occ3[c] + ((size_t)kz * s + ky) * m.occ_wpr[c] + (kx >> 5));
+  const int kx = min(max(__float2int_rd(u.x * fs), 0), s - 1), ky = min(max(__float2int_rd(u.y * fs), 0), s - 1),
+            kz = min(max(__float2int_rd(u.z * fs), 0), s - 1);
+  const uint32_t w = __ldg(m.occ3[c] + ((uint32_t)kz * s + ky) * m.occ_wpr[c] + (kx >> 5));
   return ((w >> (kx & 31)) & 1u) == 0u;
 }
 
