@@ -175,28 +175,27 @@ __device__ __forceinline__ float sample_alpha(const MapSet& m, V3 u, int ix, int
 }
 
 // ------------------------------------------------------------ cone march ----
-// Exact early exit: a sample whose position lies more than `margin` outside
-// [0,1] along an axis reads only border texels (0) at every level -- a
-// filtered fetch at level l reads texels within one texel (2^l / N) of the
-// position, and the coarsest level is L-1 -- so with margin = 3/4 of the
-// coarsest texel (MapSet::exit_margin, set by the host), a cone moving away
-// from the volume along that axis adds exact zeros for the rest of its march
-// and can stop.  Diffuse cones that
-// pass the room's walls (their alpha stays below 1 at the coarse levels)
-// otherwise march on to sqrt(3) outside the grid.
-// The test uses the map indices of the cone (ix = 1 when dir.x >= 0, ...):
-// an axis with dir component 0 keeps its position, so a position beyond
-// the margin on either side stays beyond it and exiting is exact there too.
-struct ExitTest {
-  float lo, hi;  // gone when p < lo moving down an axis, or p > hi moving up
-  __device__ __forceinline__ explicit ExitTest(const MapSet& m) {
-    lo = -m.exit_margin;
-    hi = 1.0f + m.exit_margin;
-  }
-  __device__ __forceinline__ bool gone(V3 p, int ix, int iy, int iz) const {
-    return (ix == 1 ? p.x > hi : p.x < lo) || (iy == 3 ? p.y > hi : p.y < lo) || (iz == 5 ? p.z > hi : p.z < lo);
-  }
-};
+// Exact early exit: a sample whose position lies more than half the coarsest
+// texel outside [0,1] along an axis reads only border texels (0) at every
+// level -- a filtered fetch at level l reads texels whose centres lie within
+// one texel (2^l / N) of the position, and the coarsest level is L-1.  A cone
+// moving away from the volume along an axis is past margin = 3/4 of the
+// coarsest texel (MapSet::exit_margin, set by the host) beyond
+// `exit_distance`, and adds exact zeros from there on, so its march ends
+// there (the extra quarter texel absorbs the rounding of the division).
+// Diffuse cones that pass the room's walls (their alpha stays below 1 at the
+// coarse levels) otherwise march on to sqrt(3) outside the grid.
+__device__ __forceinline__ float exit_distance(const MapSet& m, V3 origin, V3 dir, float max_dist) {
+  const float lo = -m.exit_margin, hi = 1.0f + m.exit_margin;
+  float d = max_dist;
+  if (dir.x > 0.0f) d = fminf(d, (hi - origin.x) / dir.x);
+  if (dir.x < 0.0f) d = fminf(d, (lo - origin.x) / dir.x);
+  if (dir.y > 0.0f) d = fminf(d, (hi - origin.y) / dir.y);
+  if (dir.y < 0.0f) d = fminf(d, (lo - origin.y) / dir.y);
+  if (dir.z > 0.0f) d = fminf(d, (hi - origin.z) / dir.z);
+  if (dir.z < 0.0f) d = fminf(d, (lo - origin.z) / dir.z);
+  return d;  // (+inf margin: max_dist)
+}
 
 // Exact empty-space skip: true when every texel the sample at u with this
 // lod reads is 0 (MapSet::occ).  Its coarser quadrilinear level is c (level
@@ -206,7 +205,7 @@ struct ExitTest {
 // 1/64 texel of a texel boundary the texture unit's fixed-point coordinate
 // could pick the neighbouring pair: such samples are fetched.  A pair outside
 // the grid is tested at the nearest cell inside it (conservative: border
-// texels are 0, and cones leaving the grid stop by ExitTest).  (A position
+// texels are 0, and cones leaving the grid stop at exit_distance).  (A position
 // that is not finite or is huge ends up clamped or fetched; the texture path
 // returns 0 for it either way.)
 __device__ __forceinline__ bool sample_empty(const MapSet& m, V3 u, float lod) {
@@ -256,9 +255,8 @@ __device__ float4 trace_cone(const MapSet& m, V3 origin, V3 dir, float aperture,
   float dist = 3.0f * voxel_size;
   float diam = dist * aperture;
   V3 sp = dir * dist + origin;
-  const ExitTest exit(m);
-  while (acc.w < 1.0f && dist < max_dist) {
-    if (exit.gone(sp, ix, iy, iz)) break;
+  const float stop = exit_distance(m, origin, dir, max_dist);
+  while (acc.w < 1.0f && dist < stop) {
     const float mip = fmaxf(log2f(diam * cube_res), 0.0f);
     if (!(kSkipEmptyRGBA && m.skip_empty && sample_empty(m, sp, mip))) {  // an empty sample adds exact zeros
       const float4 s = sample_voxel<SAMPLER, ISO, STORAGE>(m, sp, ix, iy, iz, ad, mip);
@@ -285,9 +283,8 @@ __device__ float trace_alpha(const MapSet& m, V3 origin, V3 dir, float aperture,
   float dist = 3.0f * voxel_size;
   float diam = dist * aperture;
   V3 sp = dir * dist + origin;
-  const ExitTest exit(m);
-  while (a < 1.0f && dist < max_dist) {
-    if (exit.gone(sp, ix, iy, iz)) break;
+  const float stop = exit_distance(m, origin, dir, max_dist);
+  while (a < 1.0f && dist < stop) {
     const float mip = fmaxf(log2f(diam * cube_res), 0.0f);
     if (!(m.skip_empty && sample_empty3(m, sp, mip))) a = __fmaf_rn(sample_alpha(m, sp, ix, iy, iz, ad, mip), 1.0f - a, a);
     const float step = fmaxf(diam * 0.5f, voxel_size);
