@@ -484,7 +484,8 @@ def run_ours(args):
                      "unit": "GB/s", "frac": round(achieved / peak, 5), "traffic": traffic,
                      "peak_source": peak_kind,
                      "texture_path": {
-                         "note": "k_trace is texture-pipeline bound, not HBM bound (profiles/k_trace_1080p_256.md)",
+                         "note": "k_trace is bound by the texture pipeline and its step arithmetic, not by HBM "
+                                 "(profiles/k_trace_1080p_256.md)",
                          "quadrilinear_fetches_per_frame": fetches,
                          "fetches_per_clock_per_sm": round(fetches / (trace_ms * 1e-3) / sm_clock_hz / NUM_SMS, 3),
                          "texel_bytes_per_s": round(fetches * 64 / (trace_ms * 1e-3) / 1e12, 3),
