@@ -137,15 +137,17 @@ __device__ __forceinline__ float aniso_alpha(const MapSet& m, V3 u, int ix, int 
   return r;
 }
 
-// sum_k a_k * textureLod(map idx_k, u, lod), lod >= 0.
-template <int SAMPLER, bool ISO, int STORAGE>
+// sum_k a_k * textureLod(map idx_k, u, lod), lod >= 0.  Positions with a
+// coordinate of magnitude >= 1e6 (or not finite) sample 0; CHECK = false
+// when the caller knows the position is sane.
+template <int SAMPLER, bool ISO, int STORAGE, bool CHECK = true>
 __device__ __forceinline__ float4 sample_voxel(const MapSet& m, V3 u, int ix, int iy, int iz, V3 ad, float lod) {
   if (SAMPLER == VCT_SAMPLER_EXACT) {
     if (ISO) return texture_lod_exact<STORAGE>(m, 0, u, lod) * (ad.x + ad.y + ad.z);
     return texture_lod_exact<STORAGE>(m, ix, u, lod) * ad.x + texture_lod_exact<STORAGE>(m, iy, u, lod) * ad.y +
            texture_lod_exact<STORAGE>(m, iz, u, lod) * ad.z;
   }
-  if (!u_sane(u)) return f4(0.f, 0.f, 0.f, 0.f);
+  if (CHECK && !u_sane(u)) return f4(0.f, 0.f, 0.f, 0.f);
   const float wsum = ad.x + ad.y + ad.z;
   if (lod < 1.0f) {
     const float4 t0 = tex3D<float4>(m.l0_tex, u.x, u.y, u.z);
@@ -163,7 +165,6 @@ __device__ __forceinline__ float4 sample_voxel(const MapSet& m, V3 u, int ix, in
 // The alpha of sample_voxel (texture unit, anisotropic RGBA8 maps) from the
 // alpha-only chains, with the same arithmetic as the alpha channel there.
 __device__ __forceinline__ float sample_alpha(const MapSet& m, V3 u, int ix, int iy, int iz, V3 ad, float lod) {
-  if (!u_sane(u)) return 0.0f;
   const float wsum = ad.x + ad.y + ad.z;
   if (lod < 1.0f) {
     const float t0 = tex3D<float4>(m.l0_tex, u.x, u.y, u.z).w;
@@ -243,6 +244,14 @@ __device__ __forceinline__ bool sample_empty3(const MapSet& m, V3 u, float lod) 
 #endif
 constexpr bool kSkipEmptyRGBA = VCT_SKIP_EMPTY_RGBA != 0;  // also in the RGBA cones (else shadow cones only)
 
+// Whether every position of a march from `origin` along unit `dir` up to
+// `stop` is sane (|coordinate| < 1e6, finite); then the step loop needs no
+// per-sample check.
+__device__ __forceinline__ bool march_sane(V3 origin, V3 dir, float stop) {
+  const float reach = fmaxf(fabsf(origin.x), fmaxf(fabsf(origin.y), fabsf(origin.z))) + fmaxf(stop, 0.0f);
+  return reach < 1.0e6f && isfinite(dir.x + dir.y + dir.z);
+}
+
 // trace_cone, voxel_cone_tracing.frag:88-119.
 template <int SAMPLER, bool ISO, int STORAGE>
 __device__ float4 trace_cone(const MapSet& m, V3 origin, V3 dir, float aperture, float max_dist) {
@@ -256,10 +265,12 @@ __device__ float4 trace_cone(const MapSet& m, V3 origin, V3 dir, float aperture,
   float diam = dist * aperture;
   V3 sp = dir * dist + origin;
   const float stop = exit_distance(m, origin, dir, max_dist);
+  const bool check = !march_sane(origin, dir, stop);
   while (acc.w < 1.0f && dist < stop) {
-    const float mip = fmaxf(log2f(diam * cube_res), 0.0f);
-    if (!(kSkipEmptyRGBA && m.skip_empty && sample_empty(m, sp, mip))) {  // an empty sample adds exact zeros
-      const float4 s = sample_voxel<SAMPLER, ISO, STORAGE>(m, sp, ix, iy, iz, ad, mip);
+    const float mip = fmaxf(__log2f(diam * cube_res), 0.0f);
+    if (!(kSkipEmptyRGBA && m.skip_empty && sample_empty(m, sp, mip)) && !(check && !u_sane(sp))) {
+      // (an empty or insane sample adds exact zeros)
+      const float4 s = sample_voxel<SAMPLER, ISO, STORAGE, false>(m, sp, ix, iy, iz, ad, mip);
       acc = fma4(s, 1.0f - acc.w, acc);
     }
     const float step = fmaxf(diam * 0.5f, voxel_size);
@@ -284,9 +295,11 @@ __device__ float trace_alpha(const MapSet& m, V3 origin, V3 dir, float aperture,
   float diam = dist * aperture;
   V3 sp = dir * dist + origin;
   const float stop = exit_distance(m, origin, dir, max_dist);
+  const bool check = !march_sane(origin, dir, stop);
   while (a < 1.0f && dist < stop) {
-    const float mip = fmaxf(log2f(diam * cube_res), 0.0f);
-    if (!(m.skip_empty && sample_empty3(m, sp, mip))) a = __fmaf_rn(sample_alpha(m, sp, ix, iy, iz, ad, mip), 1.0f - a, a);
+    const float mip = fmaxf(__log2f(diam * cube_res), 0.0f);
+    if (!(m.skip_empty && sample_empty3(m, sp, mip)) && !(check && !u_sane(sp)))
+      a = __fmaf_rn(sample_alpha(m, sp, ix, iy, iz, ad, mip), 1.0f - a, a);
     const float step = fmaxf(diam * 0.5f, voxel_size);
     dist += step;
     diam = dist * aperture;
