@@ -679,10 +679,15 @@ __device__ __forceinline__ void brick_accumulate(const SceneParams& sp, int N, c
   for (int i = threadIdx.x; i < kBrickVox; i += kThreads) acc.clear(i);
   __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  for (uint32_t base = beg + warp * 32; base < end; base += kWarps * 32) {
-    const uint32_t e = base + lane;
+  // Rounds of up to kWarps * 32 pairs, split evenly between the warps (a
+  // brick with a few dozen pairs keeps every warp busy expanding samples).
+  for (uint32_t b0 = beg; b0 < end; b0 += kWarps * 32) {
+    const uint32_t n = min((uint32_t)(kWarps * 32), end - b0);
+    const uint32_t q = (n + kWarps - 1) / kWarps;
+    const uint32_t k = warp * q + lane;
+    const uint32_t e = b0 + k;
     int cnt = 0;
-    if (e < end) {
+    if (lane < q && k < n) {
       if (MODE == VCT_VOX_CONSERVATIVE)
         cnt = setup_sat(sp, N, __ldg(list + e), b3, reinterpret_cast<SetupSat&>(setup[warp][lane]));
       else
