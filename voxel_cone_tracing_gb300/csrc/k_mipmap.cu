@@ -332,9 +332,12 @@ __device__ __forceinline__ void mip_region(const MapSet& ms, int src_level, uint
 // has the copy of region i+1 in flight.  Every wait is bounded; a wait that
 // gives up sets FrameStatus::async_timeout (the host reports an error),
 // waits (bounded) for the copy it still has in flight and leaves.
+#ifndef VCT_MIP_TMA_MIN_BLOCKS
+#define VCT_MIP_TMA_MIN_BLOCKS 4  // resident CTAs per SM the RGBA8 TMA pass is compiled for
+#endif
 constexpr int kTmaBox = 16;
 template <int NMAPS, int STORAGE>
-__global__ void __launch_bounds__(kThreads) k_mip_tma(const __grid_constant__ CUtensorMap map, MapSet ms,
+__global__ void __launch_bounds__(kThreads, STORAGE == VCT_STORAGE_RGBA8 ? VCT_MIP_TMA_MIN_BLOCKS : 1) k_mip_tma(const __grid_constant__ CUtensorMap map, MapSet ms,
                                                       FrameStatus* status) {
   typedef typename Texel<STORAGE>::T T;
   constexpr int B3 = kTmaBox * kTmaBox * kTmaBox;
@@ -501,6 +504,8 @@ cudaError_t run_tma(const MapSet& ms, const CUtensorMap* map, FrameStatus* statu
   for (int l = 1; l <= 4; ++l) smem += (size_t)NMAPS * (B >> l) * (B >> l) * (B >> l) * sizeof(T);
   auto kern = k_mip_tma<NMAPS, STORAGE>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  e = cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100);  // room for more CTAs
   if (e != cudaSuccess) return e;
   int dev = 0, sms = 148, per_sm = 1;
   cudaGetDevice(&dev);
