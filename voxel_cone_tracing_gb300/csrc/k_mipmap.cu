@@ -337,7 +337,7 @@ __device__ __forceinline__ void mip_region(const MapSet& ms, int src_level, uint
 #endif
 constexpr int kTmaBox = 16;
 template <int NMAPS, int STORAGE>
-__global__ void __launch_bounds__(kThreads, STORAGE == VCT_STORAGE_RGBA8 ? VCT_MIP_TMA_MIN_BLOCKS : 1) k_mip_tma(const __grid_constant__ CUtensorMap map, MapSet ms,
+__global__ void __launch_bounds__(kThreads, STORAGE == VCT_STORAGE_RGBA8 ? VCT_MIP_TMA_MIN_BLOCKS : 3) k_mip_tma(const __grid_constant__ CUtensorMap map, MapSet ms,
                                                       FrameStatus* status) {
   typedef typename Texel<STORAGE>::T T;
   constexpr int B3 = kTmaBox * kTmaBox * kTmaBox;
@@ -505,8 +505,12 @@ cudaError_t run_tma(const MapSet& ms, const CUtensorMap* map, FrameStatus* statu
   auto kern = k_mip_tma<NMAPS, STORAGE>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  e = cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100);  // room for more CTAs
-  if (e != cudaSuccess) return e;
+  if (STORAGE == VCT_STORAGE_RGBA8) {
+    // shared memory for 4 CTAs per SM (the RGBA16F pass runs one per SM and
+    // keeps the default split, which leaves more L1 for its surface reads)
+    e = cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+    if (e != cudaSuccess) return e;
+  }
   int dev = 0, sms = 148, per_sm = 1;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
