@@ -37,7 +37,10 @@
 namespace vct {
 namespace {
 
-constexpr int kThreads = 128;
+#ifndef VCT_BRICK_THREADS
+#define VCT_BRICK_THREADS 128
+#endif
+constexpr int kThreads = VCT_BRICK_THREADS;  // threads of a brick CTA
 constexpr int kWarps = kThreads / 32;
 constexpr int kBrickVox = kBrick * kBrick * kBrick;
 constexpr float kBinMargin = 0.25f;   // voxels; >> snapping and FP32 error
