@@ -255,7 +255,7 @@ struct vct_batch {
       VCT_CUDA(cudaStreamSynchronize(stream));
       pending = false;
       const FrameStatus s = *h_status.p;
-      VCT_CHECK(heavy.grow(s, brick_count.n));  // exact either way: no redo
+      VCT_CHECK(heavy.grow(s, brick_count.n, stream));  // exact either way: no redo
       bool redo = false;
       if (s.pair_total > pair_list.n) {
         VCT_CHECK(pair_list.ensure((size_t)s.pair_total + s.pair_total / 4 + 4096));
@@ -451,7 +451,7 @@ vct_status build_batch(vct_batch* b, const vct_batch_scene* descs, uint32_t n) {
   VCT_CHECK(b->brick_count.ensure(nbk));
   VCT_CHECK(b->brick_offset.ensure(nbk + 1));
   VCT_CHECK(b->brick_cursor.ensure(nbk));
-  VCT_CHECK(b->heavy.reserve(nbk, 1024, 65536));
+  VCT_CHECK(b->heavy.reserve(nbk, 1024, 65536, b->stream));
   VCT_CHECK(b->scan_tmp.ensure(scan_tmp_words(nbk)));
   VCT_CHECK(b->pair_list.ensure((size_t)std::min<uint64_t>(0xffffff00ull, 4ull * total_tris + 65536ull)));
   VCT_CHECK(b->bin_big_count.ensure(1));

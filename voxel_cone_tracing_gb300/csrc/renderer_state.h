@@ -174,18 +174,18 @@ struct HeavyStore {
     return std::max({heavy_slot_bytes(VCT_STORAGE_RGBA8), heavy_slot_bytes(VCT_STORAGE_RGBA16F),
                      heavy_slot_bytes(kStorageAttr)});
   }
-  vct_status reserve(size_t n_bricks, uint32_t slots, uint32_t n_items) {
+  // Called between frames (no kernel of the owner in flight); `st` is the
+  // owner's stream, so the zeroing is ordered before its next frame.
+  vct_status reserve(size_t n_bricks, uint32_t slots, uint32_t n_items, cudaStream_t st) {
     VCT_CHECK(slot.ensure(n_bricks));
     VCT_CHECK(counters.ensure(3));
     if (slots > slot_cap) {
-      // Called between frames (no kernel in flight): the slots and their
-      // counters start at zero and every frame leaves them so.
+      // the slots and their counters start at zero and every frame leaves them so
       VCT_CHECK(brick.ensure(slots));
       VCT_CHECK(done.ensure(slots));
       VCT_CHECK(acc.ensure((size_t)slots * slot_bytes()));
-      VCT_CUDA(cudaMemset(done.p, 0, (size_t)slots * sizeof(uint32_t)));
-      VCT_CUDA(cudaMemset(acc.p, 0, (size_t)slots * slot_bytes()));
-      VCT_CUDA(cudaDeviceSynchronize());
+      VCT_CUDA(cudaMemsetAsync(done.p, 0, (size_t)slots * sizeof(uint32_t), st));
+      VCT_CUDA(cudaMemsetAsync(acc.p, 0, (size_t)slots * slot_bytes(), st));
       slot_cap = slots;
     }
     if (n_items > item_cap) {
@@ -195,10 +195,10 @@ struct HeavyStore {
     return VCT_OK;
   }
   // After a frame: room for its split with a margin.
-  vct_status grow(const FrameStatus& s, size_t n_bricks) {
+  vct_status grow(const FrameStatus& s, size_t n_bricks, cudaStream_t st) {
     if (s.heavy_total <= slot_cap && s.extra_total <= item_cap) return VCT_OK;
     return reserve(n_bricks, std::max(slot_cap, s.heavy_total + s.heavy_total / 4 + 64),
-                   std::max(item_cap, s.extra_total + s.extra_total / 4 + 1024));
+                   std::max(item_cap, s.extra_total + s.extra_total / 4 + 1024), st);
   }
   HeavyBricks view() const {
     HeavyBricks h;
@@ -504,7 +504,7 @@ struct vct_renderer {
     VCT_CHECK(brick_offset.ensure(nb + 1));
     VCT_CHECK(brick_cursor.ensure(nb));
     VCT_CHECK(scan_tmp.ensure(scan_tmp_words(nb)));
-    VCT_CHECK(heavy.reserve(nb, 256, 16384));
+    VCT_CHECK(heavy.reserve(nb, 256, 16384, stream));
     if (cfg.keep_counts) VCT_CHECK(counts.ensure((size_t)r * r * r));
     have_frame = false;
     return VCT_OK;
@@ -721,7 +721,7 @@ struct vct_renderer {
       frame_pending = false;
       const FrameStatus s = *h_status.p;
       if (s.async_timeout) return set_error(VCT_ERR_CUDA, "an asynchronous copy or tensor-core group did not complete");
-      VCT_CHECK(heavy.grow(s, brick_count.n));  // exact either way: no redo
+      VCT_CHECK(heavy.grow(s, brick_count.n, stream));  // exact either way: no redo
       bool redo = false;
       if (s.pair_total > pair_list.n) {
         VCT_CHECK(pair_list.ensure((size_t)s.pair_total + s.pair_total / 4 + 4096));
