@@ -256,6 +256,39 @@ def precision_leg(R, torch, steps, flush_mb=256):
     return out
 
 
+def overlap_leg(R, torch, scene, steps, flush):
+    """The bench frame with the G-buffer raster on a second stream beside
+    voxelize and mipmap (vct_config.overlap_raster = 1): a shorter frame,
+    but the overlapped stages slow each other down."""
+    r = R.Renderer(WIDTH, HEIGHT, grid_res=GRID, overlap_raster=1)
+    ids = R.load_scene(r, scene)
+    r.set_voxel_view_dir(7, 0.0)
+    stream = torch.cuda.Stream()
+    r.set_stream(stream.cuda_stream)
+    for _ in range(3):
+        R.queue_scene(r, scene, ids)
+        r.render()
+    r.synchronize()
+    stages, frame_ms = [], []
+    for _ in range(steps):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record(stream)
+        R.queue_scene(r, scene, ids)
+        r.render()
+        e.record(stream)
+        r.synchronize()
+        stages.append(r.stage_times())
+        frame_ms.append(s.elapsed_time(e))
+    r.close()
+    mean = lambda key: statistics.mean(st[key] for st in stages)  # noqa: E731
+    return {"workload": "bench frame, G-buffer raster beside voxelize and mipmap", "unit": UNIT,
+            "value": round(mean("voxelize") + mean("mipmap") + mean("trace"), 4),
+            "frame_ms": round(statistics.mean(frame_ms), 4),
+            "stages_ms": {k: round(mean(k), 4) for k in ("voxelize", "mipmap", "gbuffer", "trace")}}
+
+
 def injection_leg(R, torch, scene, steps, flush):
     """Deferred light injection on the bench frame: the light moves every
     frame, the geometry does not, so frames after the first skip
@@ -501,6 +534,7 @@ def run_ours(args):
     }
     if not args.no_mlp:
         line["mlp"] = mlp_leg(r, R, scene, ids, stream, flush, min(args.steps, 20), stages)
+    line["overlap_raster"] = overlap_leg(R, torch, scene, min(args.steps, 20), flush)
     line["injection"] = injection_leg(R, torch, scene, min(args.steps, 20), flush)
     if not args.no_precision:
         line["precision"] = precision_leg(R, torch, min(args.steps, 20))

@@ -117,7 +117,13 @@ typedef struct {
                          * grid, as the reference's loop does; 0 (default):
                          * a cone stops once every further sample can only
                          * read border texels (identical results)          */
-  int32_t reserved[5];
+  int32_t overlap_raster; /* 1: the G-buffer raster (and the learned
+                         * diffuse term) run on a second stream beside
+                         * voxelize and mipmap, which they do not depend on:
+                         * a shorter frame, longer voxelize and mipmap
+                         * stages; 0 (default): one stream, one stage
+                         * after the other                                */
+  int32_t reserved[4];
 } vct_config;
 
 typedef struct vct_renderer vct_renderer;
@@ -126,8 +132,11 @@ typedef struct vct_renderer vct_renderer;
 typedef struct {
   float voxelize;   /* clear + bin + voxelize level 0                     */
   float mipmap;     /* levels 1..L-1                                       */
-  float gbuffer;    /* forward raster + attribute resolve                  */
-  float trace;      /* cone-trace shading                                  */
+  float gbuffer;    /* forward raster + attribute resolve (with
+                     * overlap_raster it runs beside voxelize and mipmap,
+                     * and the stages can add up to more than total)      */
+  float trace;      /* cone-trace shading (+ the learned diffuse term's
+                     * inference when it replaces the diffuse cones)      */
   float total;      /* first to last event of the frame                    */
   uint32_t kernel_launches; /* engine kernels launched for the frame       */
   uint32_t voxelized;       /* 1: the frame voxelized its geometry; 0: light

@@ -138,3 +138,18 @@ def test_caller_stream(vct, scene):
     s = torch.cuda.Stream()
     _, b = _frame(vct, scene, lambda r: r.set_stream(s.cuda_stream))
     np.testing.assert_array_equal(a, b)
+
+
+def test_overlap_raster_same_frame(vct, scene):
+    """Every stage on one stream (default) and the G-buffer raster beside
+    voxelize and mipmap (overlap_raster = 1) give the same frame, also on a
+    caller's stream."""
+    import torch
+    _, a = _frame(vct, scene)
+    _, b = _frame(vct, scene, overlap_raster=1)
+    s = torch.cuda.Stream()
+    r, c = _frame(vct, scene, lambda r: r.set_stream(s.cuda_stream), overlap_raster=1)
+    np.testing.assert_array_equal(a, b)
+    np.testing.assert_array_equal(a, c)
+    t = r.stage_times()
+    assert t["gbuffer"] > 0.0 and t["total"] >= t["trace"]

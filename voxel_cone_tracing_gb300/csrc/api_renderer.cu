@@ -91,7 +91,7 @@ static vct_status check_config(const vct_config& c) {
     return set_error(VCT_ERR_INVALID_VALUE, "radiance_max %g > 1 needs RGBA16F storage", c.radiance_max);
   if (c.vox_mode < 0 || c.vox_mode > 1 || c.mip_mode < 0 || c.mip_mode > 1 || c.storage < 0 || c.storage > 1 ||
       c.sampler < 0 || c.sampler > 1 || c.cone_set < 0 || c.cone_set > 1 || c.shadow_from_maps < 0 ||
-      c.shadow_from_maps > 1 || c.full_march < 0 || c.full_march > 1)
+      c.shadow_from_maps > 1 || c.full_march < 0 || c.full_march > 1 || c.overlap_raster < 0 || c.overlap_raster > 1)
     return set_error(VCT_ERR_INVALID_VALUE, "config field out of range");
   return VCT_OK;
 }
@@ -351,13 +351,17 @@ extern "C" vct_status vct_get_stage_times(vct_renderer* r, vct_stage_times* out)
   if (!r || !out) return set_error(VCT_ERR_INVALID_VALUE, "NULL argument");
   VCT_CHECK(r->finish());
   if (!r->have_frame) return set_error(VCT_ERR_INVALID_VALUE, "no frame rendered yet");
-  float t[4];
-  for (int i = 0; i < 4; ++i) VCT_CUDA(cudaEventElapsedTime(&t[i], r->ev[i], r->ev[i + 1]));
+  // ev: voxelize start, voxelize end, mipmap end, trace start, trace end;
+  // evg (raster stream): raster start, raster end, learned term end.
+  float t[2], g[2], tr;
+  for (int i = 0; i < 2; ++i) VCT_CUDA(cudaEventElapsedTime(&t[i], r->ev[i], r->ev[i + 1]));
+  for (int i = 0; i < 2; ++i) VCT_CUDA(cudaEventElapsedTime(&g[i], r->evg[i], r->evg[i + 1]));
+  VCT_CUDA(cudaEventElapsedTime(&tr, r->ev[3], r->ev[4]));
   out->voxelize = t[0];
   out->mipmap = t[1];
-  out->gbuffer = t[2];
-  out->trace = t[3];
-  VCT_CUDA(cudaEventElapsedTime(&out->total, r->ev[0], r->ev[4]));
+  out->gbuffer = g[0];
+  out->trace = tr + g[1];
+  VCT_CUDA(cudaEventElapsedTime(&out->total, r->ev_start, r->ev[4]));
   out->kernel_launches = (uint32_t)r->launches;
   out->voxelized = r->last_revoxelized ? 1u : 0u;
   out->split_bricks = r->h_status.p->heavy_total;

@@ -378,7 +378,11 @@ struct vct_renderer {
   bool have_last = false;
   // GPU state
   cudaStream_t own_stream = nullptr, stream = nullptr;
+  cudaStream_t gb_stream = nullptr;  // G-buffer raster + learned diffuse term
+  cudaEvent_t ev_start = nullptr;
   cudaEvent_t ev[5] = {};
+  cudaEvent_t evg[3] = {};
+  cudaEvent_t ev_join = nullptr;
   cudaEvent_t ev_staged = nullptr;
   cudaEvent_t ev_done = nullptr;   // after the frame's status copy
   MapStore maps;
@@ -422,12 +426,18 @@ struct vct_renderer {
   bool have_sp = false;
 
   ~vct_renderer() {
+    if (gb_stream) cudaStreamSynchronize(gb_stream);
     if (stream) cudaStreamSynchronize(stream);
     free_maps();
     for (auto& e : ev)
       if (e) cudaEventDestroy(e);
+    for (auto& e : evg)
+      if (e) cudaEventDestroy(e);
+    if (ev_start) cudaEventDestroy(ev_start);
+    if (ev_join) cudaEventDestroy(ev_join);
     if (ev_staged) cudaEventDestroy(ev_staged);
     if (ev_done) cudaEventDestroy(ev_done);
+    if (gb_stream) cudaStreamDestroy(gb_stream);
     if (own_stream) cudaStreamDestroy(own_stream);
   }
 
@@ -485,6 +495,7 @@ struct vct_renderer {
   // set_grid_resolution (renderer.cpp:178-188): six 3D textures of `levels`
   // mip levels.  Here: level 0 once + one chain (levels 1..L-1) per map.
   vct_status alloc_maps(uint32_t r) {
+    if (gb_stream) VCT_CUDA(cudaStreamSynchronize(gb_stream));
     if (stream) VCT_CUDA(cudaStreamSynchronize(stream));
     free_inj();
     VCT_CHECK(maps.alloc(r, cfg.mip_mode, cfg.storage, cfg.shadow_from_maps == 0 && cfg.sampler == VCT_SAMPLER_HW));
@@ -518,7 +529,11 @@ struct vct_renderer {
     std::memcpy(proj, kIdentity, sizeof(proj));
     VCT_CUDA(cudaStreamCreateWithFlags(&own_stream, cudaStreamNonBlocking));
     stream = own_stream;
+    VCT_CUDA(cudaStreamCreateWithFlags(&gb_stream, cudaStreamNonBlocking));
     for (auto& e : ev) VCT_CUDA(cudaEventCreate(&e));
+    for (auto& e : evg) VCT_CUDA(cudaEventCreate(&e));
+    VCT_CUDA(cudaEventCreate(&ev_start));
+    VCT_CUDA(cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming));
     VCT_CUDA(cudaEventCreateWithFlags(&ev_staged, cudaEventDisableTiming));
     VCT_CUDA(cudaEventCreateWithFlags(&ev_done, cudaEventDisableTiming));
     // Default material (renderer.cpp:115-128, fill_default_mat_data :85-98).
@@ -667,6 +682,28 @@ struct vct_renderer {
 
     VCT_CUDA(cudaMemsetAsync(d_status.p, 0, sizeof(FrameStatus), stream));
     launches = 0;
+    VCT_CUDA(cudaEventRecord(ev_start, stream));
+    // The G-buffer raster reads only the scene and the camera, and the
+    // learned diffuse term only the G-buffer: with overlap_raster both run
+    // on a second stream beside voxelize and mipmap, and the trace waits
+    // for them.
+    const bool side = cfg.overlap_raster != 0;
+    cudaStream_t gs = side ? gb_stream : stream;
+    if (side) VCT_CUDA(cudaStreamWaitEvent(gb_stream, ev_start, 0));
+    VCT_CUDA(cudaEventRecord(evg[0], gs));
+    VCT_CUDA(launch_gbuffer(sp, cp, rb, gs, &launches));
+    VCT_CUDA(cudaEventRecord(evg[1], gs));
+    TraceParams tp = fi.tp;
+    tp.diffuse_in = nullptr;
+    if (diffuse_mode == VCT_DIFFUSE_MLP && mlp.trained && tp.enable_diffuse && tp.view_voxel_dir >= 7) {
+      // The learned term replaces the nine diffuse cones (its time counts as trace time).
+      VCT_CHECK(diffuse_px.ensure((size_t)W * H));
+      VCT_CUDA(launch_mlp_infer(mlp.params(), sp, gb_pos.p, gb_nrm.p, W * H, diffuse_px.p, gs, mlp.tc, d_status.p));
+      ++launches;
+      tp.diffuse_in = diffuse_px.p;
+    }
+    VCT_CUDA(cudaEventRecord(evg[2], gs));
+    if (side) VCT_CUDA(cudaEventRecord(ev_join, gb_stream));
     VCT_CUDA(cudaEventRecord(ev[0], stream));
     if (inject) {
       // Re-voxelize the attribute grids only when the geometry changed;
@@ -689,17 +726,8 @@ struct vct_renderer {
     VCT_CUDA(cudaEventRecord(ev[1], stream));
     VCT_CUDA(launch_mipmap(ms, cfg.mip_mode, stream, &launches, have_l0_map ? &l0_map : nullptr, d_status.p));
     VCT_CUDA(cudaEventRecord(ev[2], stream));
-    VCT_CUDA(launch_gbuffer(sp, cp, rb, stream, &launches));
+    if (side) VCT_CUDA(cudaStreamWaitEvent(stream, ev_join, 0));
     VCT_CUDA(cudaEventRecord(ev[3], stream));
-    TraceParams tp = fi.tp;
-    tp.diffuse_in = nullptr;
-    if (diffuse_mode == VCT_DIFFUSE_MLP && mlp.trained && tp.enable_diffuse && tp.view_voxel_dir >= 7) {
-      // The learned term replaces the nine diffuse cones (its time counts as trace time).
-      VCT_CHECK(diffuse_px.ensure((size_t)W * H));
-      VCT_CUDA(launch_mlp_infer(mlp.params(), sp, gb_pos.p, gb_nrm.p, W * H, diffuse_px.p, stream, mlp.tc, d_status.p));
-      ++launches;
-      tp.diffuse_in = diffuse_px.p;
-    }
     VCT_CUDA(launch_trace(sp, cp, ms, tp, gb_pos.p, gb_nrm.p, frame.p, cfg.keep_float_frame ? frame_f32.p : nullptr,
                           stream, &launches));
     last_sp = sp;

@@ -78,7 +78,8 @@ class Config(C.Structure):
     _fields_ = [("grid_res", C.c_int32), ("vox_mode", C.c_int32), ("mip_mode", C.c_int32),
                 ("storage", C.c_int32), ("sampler", C.c_int32), ("cone_set", C.c_int32),
                 ("keep_counts", C.c_int32), ("keep_float_frame", C.c_int32), ("radiance_max", C.c_float),
-                ("shadow_from_maps", C.c_int32), ("full_march", C.c_int32), ("reserved", C.c_int32 * 5)]
+                ("shadow_from_maps", C.c_int32), ("full_march", C.c_int32),
+                ("overlap_raster", C.c_int32), ("reserved", C.c_int32 * 4)]
 
 
 class StageTimes(C.Structure):
