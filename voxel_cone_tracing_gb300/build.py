@@ -21,6 +21,9 @@ DEMO_SRC = os.path.join(HERE, "demo", "vct_demo.cpp")
 DEMO = os.path.join(HERE, "vct_demo")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=off", "-I", CSRC]
+# Per-file flags: the cone tracer fuses products and sums only where its
+# code says so, so that its frames do not change with the code's arrangement.
+FILE_FLAGS = {"k_trace.cu": ["-fmad=false"]}
 # Extra nvcc flags (e.g. -DVCT_TRACE_MIN_BLOCKS=3 for tuning sweeps); the
 # library is rebuilt when they differ from the ones it was built with.
 EXTRA = os.environ.get("VCT_NVCC_FLAGS", "").split()
@@ -39,7 +42,8 @@ def sources() -> list:
 
 
 def _deps() -> list:
-    return sources() + glob.glob(os.path.join(CSRC, "*.h")) + glob.glob(os.path.join(CSRC, "*.cuh")) + \
+    return sources() + [os.path.abspath(__file__)] + glob.glob(os.path.join(CSRC, "*.h")) + \
+        glob.glob(os.path.join(CSRC, "*.cuh")) + \
         glob.glob(os.path.join(HERE, "..", "include", "*.h"))
 
 
@@ -81,7 +85,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
 
     def compile_one(src):
         obj = os.path.join(BUILD, os.path.basename(src) + ".o")
-        cmd = [cc, *ARCH, *FLAGS, *EXTRA, "-c", src, "-o", obj]
+        cmd = [cc, *ARCH, *FLAGS, *FILE_FLAGS.get(os.path.basename(src), []), *EXTRA, "-c", src, "-o", obj]
         if verbose:
             cmd.insert(1, "-Xptxas=-v")
         r = subprocess.run(cmd, capture_output=True, text=True)

@@ -5,6 +5,10 @@
 // (each warp a 16x2 strip) so that neighbouring lanes march neighbouring,
 // nearly parallel cones and hit the same texture-cache lines.
 //
+// This file is compiled with -fmad=false: a product and a sum are fused only
+// where the code says so (__fmaf_rn), so the results do not depend on how
+// the compiler arranges the code around them.
+//
 // Texture sampling is GL textureLod with GL_LINEAR_MIPMAP_LINEAR and
 // CLAMP_TO_BORDER(0) over levels 0..L-1 (texture_3d.cpp:10-15).  Level 0 is
 // one texture shared by the six maps (as in the reference, where all six
@@ -213,7 +217,7 @@ __device__ __forceinline__ bool sample_empty(const MapSet& m, V3 u, float lod) {
   const int c = min((int)lod + 1, m.L - 1);  // lod >= 0
   const int s = m.N >> c;
   const float fs = (float)s;
-  const float tx = u.x * fs - 0.5f, ty = u.y * fs - 0.5f, tz = u.z * fs - 0.5f;
+  const float tx = __fmaf_rn(u.x, fs, -0.5f), ty = __fmaf_rn(u.y, fs, -0.5f), tz = __fmaf_rn(u.z, fs, -0.5f);
   const float bx = floorf(tx), by = floorf(ty), bz = floorf(tz);
   const float fx = tx - bx, fy = ty - by, fz = tz - bz;
   constexpr float kEps = 1.0f / 64.0f;
@@ -229,20 +233,35 @@ __device__ __forceinline__ bool sample_empty(const MapSet& m, V3 u, float lod) {
 // tested at the nearest cell inside, conservatively).  Cheaper than
 // sample_empty (no boundary test); it finds nearly all the empty steps of
 // the narrow shadow cones.
-__device__ __forceinline__ bool sample_empty3(const MapSet& m, V3 u, float lod) {
+// (sample_empty3 in two parts: the occupancy word is loaded a step ahead by
+// the pipelined shadow march; the word shifted right by `bit` holds the bit.)
+__device__ __forceinline__ uint32_t empty3_word(const MapSet& m, V3 u, float lod, uint32_t& bit) {
   const int c = min((int)lod + 1, m.L - 1);  // lod >= 0
   const int s = m.N >> c;
   const float fs = (float)s;
   const int kx = min(max(__float2int_rd(u.x * fs), 0), s - 1), ky = min(max(__float2int_rd(u.y * fs), 0), s - 1),
             kz = min(max(__float2int_rd(u.z * fs), 0), s - 1);
-  const uint32_t w = __ldg(m.occ3[c] + ((uint32_t)kz * s + ky) * m.occ_wpr[c] + (kx >> 5));
-  return ((w >> (kx & 31)) & 1u) == 0u;
+  bit = (uint32_t)kx & 31u;
+  return __ldg(m.occ3[c] + ((uint32_t)kz * s + ky) * m.occ_wpr[c] + (kx >> 5));
+}
+
+__device__ __forceinline__ bool sample_empty3(const MapSet& m, V3 u, float lod) {
+  uint32_t bit;
+  const uint32_t w = empty3_word(m, u, lod, bit);
+  return ((w >> bit) & 1u) == 0u;
 }
 
 #ifndef VCT_SKIP_EMPTY_RGBA
 #define VCT_SKIP_EMPTY_RGBA 1
 #endif
 constexpr bool kSkipEmptyRGBA = VCT_SKIP_EMPTY_RGBA != 0;  // also in the RGBA cones (else shadow cones only)
+
+// The sample position origin + dir * dist of a march step, one rounding per
+// coordinate (an explicit fused multiply-add, so that it does not depend on
+// how the compiler arranges the step loop).
+__device__ __forceinline__ V3 march_pos(V3 origin, V3 dir, float dist) {
+  return v3(__fmaf_rn(dir.x, dist, origin.x), __fmaf_rn(dir.y, dist, origin.y), __fmaf_rn(dir.z, dist, origin.z));
+}
 
 // Whether every position of a march from `origin` along unit `dir` up to
 // `stop` is sane (|coordinate| < 1e6, finite); then the step loop needs no
@@ -252,9 +271,50 @@ __device__ __forceinline__ bool march_sane(V3 origin, V3 dir, float stop) {
   return reach < 1.0e6f && isfinite(dir.x + dir.y + dir.z);
 }
 
-// trace_cone, voxel_cone_tracing.frag:88-119.
-template <int SAMPLER, bool ISO, int STORAGE>
-__device__ float4 trace_cone(const MapSet& m, V3 origin, V3 dir, float aperture, float max_dist) {
+#ifndef VCT_TRACE_PIPE
+#define VCT_TRACE_PIPE 1
+#endif
+// Step loop of the texture-unit anisotropic march: 0 = one step after the
+// other; 1 = the next step's position, lod and empty-space test (with its
+// occupancy load) run while this step's texture fetches are in flight;
+// 2 = also the next step's fetches are issued before this step's results
+// are used (two sets of results live).  Same samples, same arithmetic.
+constexpr int kTracePipe = VCT_TRACE_PIPE;
+
+// The raw texture results of one step of the anisotropic march (the
+// fetches of sample_voxel, texture unit, anisotropic maps).
+struct Taps {
+  float4 t0, x, y, z;
+};
+
+__device__ __forceinline__ void issue_taps(const MapSet& m, V3 u, int ix, int iy, int iz, V3 ad, float lod, Taps& t) {
+  float l = lod - 1.0f;
+  if (lod < 1.0f) {
+    t.t0 = tex3D<float4>(m.l0_tex, u.x, u.y, u.z);
+    if (!(lod > 0.0f)) return;
+    l = 0.0f;
+  }
+  if (ad.x != 0.0f) t.x = tex3DLod<float4>(m.tex[ix], u.x, u.y, u.z, l);
+  if (ad.y != 0.0f) t.y = tex3DLod<float4>(m.tex[iy], u.x, u.y, u.z, l);
+  if (ad.z != 0.0f) t.z = tex3DLod<float4>(m.tex[iz], u.x, u.y, u.z, l);
+}
+
+// sample_voxel<HW, aniso> from the step's taps, operation for operation.
+__device__ __forceinline__ float4 combine_taps(const Taps& t, V3 ad, float lod) {
+  const float wsum = ad.x + ad.y + ad.z;
+  if (lod < 1.0f && !(lod > 0.0f)) return mul4(t.t0, wsum);
+  float4 r = f4(0.f, 0.f, 0.f, 0.f);
+  if (ad.x != 0.0f) r = mul4(t.x, ad.x);
+  if (ad.y != 0.0f) r = fma4(t.y, ad.y, r);
+  if (ad.z != 0.0f) r = fma4(t.z, ad.z, r);
+  if (lod < 1.0f) return fma4(r, lod, mul4(t.t0, __fmul_rn(1.0f - lod, wsum)));
+  return r;
+}
+
+// trace_cone for the texture unit and anisotropic maps with the step loop
+// software-pipelined (kTracePipe): the march, the samples taken and the
+// accumulation are those of the plain loop in trace_cone.
+__device__ float4 trace_cone_pipe(const MapSet& m, V3 origin, V3 dir, float aperture, float max_dist) {
   dir = normalize(dir);
   const int ix = dir.x < 0.0f ? 0 : 1, iy = dir.y < 0.0f ? 2 : 3, iz = dir.z < 0.0f ? 4 : 5;
   const V3 ad = vabs(dir);
@@ -263,7 +323,54 @@ __device__ float4 trace_cone(const MapSet& m, V3 origin, V3 dir, float aperture,
   float4 acc = f4(0.f, 0.f, 0.f, 0.f);
   float dist = 3.0f * voxel_size;
   float diam = dist * aperture;
-  V3 sp = dir * dist + origin;
+  V3 sp = march_pos(origin, dir, dist);
+  const float stop = exit_distance(m, origin, dir, max_dist);
+  const bool check = !march_sane(origin, dir, stop);
+  if (!(dist < stop)) return acc;
+  float mip = fmaxf(__log2f(diam * cube_res), 0.0f);
+  bool live = !(kSkipEmptyRGBA && m.skip_empty && sample_empty(m, sp, mip)) && !(check && !u_sane(sp));
+  Taps t;
+  if (live) issue_taps(m, sp, ix, iy, iz, ad, mip, t);
+  while (true) {
+    // the next step (taken only while this one leaves alpha below 1)
+    const float step = fmaxf(diam * 0.5f, voxel_size);
+    dist += step;
+    diam = dist * aperture;
+    sp = march_pos(origin, dir, dist);
+    const bool more = dist < stop;
+    const float mip_n = fmaxf(__log2f(diam * cube_res), 0.0f);
+    const bool live_n =
+        more && !(kSkipEmptyRGBA && m.skip_empty && sample_empty(m, sp, mip_n)) && !(check && !u_sane(sp));
+    if (kTracePipe >= 2) {
+      Taps tn;
+      if (live_n) issue_taps(m, sp, ix, iy, iz, ad, mip_n, tn);
+      if (live) acc = fma4(combine_taps(t, ad, mip), 1.0f - acc.w, acc);
+      if (!(acc.w < 1.0f) || !more) break;
+      t = tn;
+    } else {
+      if (live) acc = fma4(combine_taps(t, ad, mip), 1.0f - acc.w, acc);
+      if (!(acc.w < 1.0f) || !more) break;
+      if (live_n) issue_taps(m, sp, ix, iy, iz, ad, mip_n, t);
+    }
+    mip = mip_n;
+    live = live_n;
+  }
+  return acc;
+}
+
+// trace_cone, voxel_cone_tracing.frag:88-119.
+template <int SAMPLER, bool ISO, int STORAGE>
+__device__ float4 trace_cone(const MapSet& m, V3 origin, V3 dir, float aperture, float max_dist) {
+  if (kTracePipe > 0 && SAMPLER == VCT_SAMPLER_HW && !ISO) return trace_cone_pipe(m, origin, dir, aperture, max_dist);
+  dir = normalize(dir);
+  const int ix = dir.x < 0.0f ? 0 : 1, iy = dir.y < 0.0f ? 2 : 3, iz = dir.z < 0.0f ? 4 : 5;
+  const V3 ad = vabs(dir);
+  const float cube_res = (float)m.N;
+  const float voxel_size = 1.0f / cube_res;
+  float4 acc = f4(0.f, 0.f, 0.f, 0.f);
+  float dist = 3.0f * voxel_size;
+  float diam = dist * aperture;
+  V3 sp = march_pos(origin, dir, dist);
   const float stop = exit_distance(m, origin, dir, max_dist);
   const bool check = !march_sane(origin, dir, stop);
   while (acc.w < 1.0f && dist < stop) {
@@ -276,7 +383,7 @@ __device__ float4 trace_cone(const MapSet& m, V3 origin, V3 dir, float aperture,
     const float step = fmaxf(diam * 0.5f, voxel_size);
     dist += step;
     diam = dist * aperture;
-    sp = dir * dist + origin;
+    sp = march_pos(origin, dir, dist);
   }
   return acc;
 }
@@ -284,7 +391,9 @@ __device__ float4 trace_cone(const MapSet& m, V3 origin, V3 dir, float aperture,
 // trace_cone(...).a (trace_shadow, :121-124) with the texture unit over the
 // alpha-only chains: the same march and the same alpha arithmetic, two
 // texture fetches per step instead of three.
+__device__ float trace_alpha_pipe(const MapSet& m, V3 origin, V3 dir, float aperture, float max_dist);
 __device__ float trace_alpha(const MapSet& m, V3 origin, V3 dir, float aperture, float max_dist) {
+  if (kTracePipe > 0) return trace_alpha_pipe(m, origin, dir, aperture, max_dist);
   dir = normalize(dir);
   const int ix = dir.x < 0.0f ? 0 : 1, iy = dir.y < 0.0f ? 2 : 3, iz = dir.z < 0.0f ? 4 : 5;
   const V3 ad = vabs(dir);
@@ -293,7 +402,7 @@ __device__ float trace_alpha(const MapSet& m, V3 origin, V3 dir, float aperture,
   float a = 0.0f;
   float dist = 3.0f * voxel_size;
   float diam = dist * aperture;
-  V3 sp = dir * dist + origin;
+  V3 sp = march_pos(origin, dir, dist);
   const float stop = exit_distance(m, origin, dir, max_dist);
   const bool check = !march_sane(origin, dir, stop);
   while (a < 1.0f && dist < stop) {
@@ -303,7 +412,47 @@ __device__ float trace_alpha(const MapSet& m, V3 origin, V3 dir, float aperture,
     const float step = fmaxf(diam * 0.5f, voxel_size);
     dist += step;
     diam = dist * aperture;
-    sp = dir * dist + origin;
+    sp = march_pos(origin, dir, dist);
+  }
+  return a;
+}
+
+// trace_alpha with the occupancy word of the next step loaded while this
+// step is sampled (kTracePipe > 0): the same samples and arithmetic.
+__device__ float trace_alpha_pipe(const MapSet& m, V3 origin, V3 dir, float aperture, float max_dist) {
+  dir = normalize(dir);
+  const int ix = dir.x < 0.0f ? 0 : 1, iy = dir.y < 0.0f ? 2 : 3, iz = dir.z < 0.0f ? 4 : 5;
+  const V3 ad = vabs(dir);
+  const float cube_res = (float)m.N;
+  const float voxel_size = 1.0f / cube_res;
+  const bool skip = m.skip_empty != 0;
+  float a = 0.0f;
+  float dist = 3.0f * voxel_size;
+  float diam = dist * aperture;
+  V3 sp = march_pos(origin, dir, dist);
+  const float stop = exit_distance(m, origin, dir, max_dist);
+  const bool check = !march_sane(origin, dir, stop);
+  if (!(dist < stop)) return a;
+  float mip = fmaxf(__log2f(diam * cube_res), 0.0f);
+  uint32_t bit = 0, w = skip ? empty3_word(m, sp, mip, bit) : 1u;
+  while (true) {
+    const float step = fmaxf(diam * 0.5f, voxel_size);
+    const float dist_n = dist + step;
+    const float diam_n = dist_n * aperture;
+    const V3 sp_n = march_pos(origin, dir, dist_n);
+    const bool more = dist_n < stop;
+    const float mip_n = fmaxf(__log2f(diam_n * cube_res), 0.0f);
+    uint32_t bit_n = 0, w_n = 1u;
+    if (skip && more) w_n = empty3_word(m, sp_n, mip_n, bit_n);
+    if (((w >> bit) & 1u) != 0u && !(check && !u_sane(sp)))
+      a = __fmaf_rn(sample_alpha(m, sp, ix, iy, iz, ad, mip), 1.0f - a, a);
+    if (!(a < 1.0f) || !more) break;
+    dist = dist_n;
+    diam = diam_n;
+    sp = sp_n;
+    mip = mip_n;
+    w = w_n;
+    bit = bit_n;
   }
   return a;
 }
