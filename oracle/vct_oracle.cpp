@@ -852,9 +852,12 @@ template <class R> static bool sample_empty_rule(int N, int L, V3<R> u, R lod) {
   const R t[3] = {u.x * R(s) - R(0.5), u.y * R(s) - R(0.5), u.z * R(s) - R(0.5)};
   int k[3];
   for (int a = 0; a < 3; ++a) {
-    const R b = std::floor(t[a]), f = t[a] - b;
-    if (f < R(1) / R(64) || f > R(1) - R(1) / R(64)) return false;
-    k[a] = std::min(std::max((int)b, 0), s - 1);
+    // 8.8 fixed point: the top byte of the fraction within 4/256 of a
+    // texel boundary marks a sample that is fetched
+    const R q = std::floor(t[a] * R(256));
+    const R fr = q - R(256) * std::floor(q / R(256));
+    if (fr < R(4) || fr >= R(252)) return false;
+    k[a] = std::min(std::max((int)std::floor(t[a]), 0), s - 1);
   }
   return g_dilated[c][((size_t)k[2] * s + k[1]) * s + k[0]] == 0;
 }

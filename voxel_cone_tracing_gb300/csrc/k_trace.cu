@@ -208,7 +208,11 @@ __device__ __forceinline__ float exit_distance(const MapSet& m, V3 origin, V3 di
 // texels k .. k+1 along each axis, k = floor(u * (N >> c) - 0.5), and the
 // finer level's texels lie inside them, so the occ bit of k decides.  Within
 // 1/64 texel of a texel boundary the texture unit's fixed-point coordinate
-// could pick the neighbouring pair: such samples are fetched.  A pair outside
+// could pick the neighbouring pair: such samples are fetched.  The test runs
+// in 8.8 fixed point: q = floor(256 t) (t scaled by a power of two, so the
+// same rounding), k = q >> 8, and the fraction's top byte q & 255 in
+// [252, 255] or [0, 3] marks the band (a superset of |frac - 0| < 1/64 and
+// frac > 1 - 1/64: conservative).  A pair outside
 // the grid is tested at the nearest cell inside it (conservative: border
 // texels are 0, and cones leaving the grid stop at exit_distance).  (A position
 // that is not finite or is huge ends up clamped or fetched; the texture path
@@ -216,13 +220,13 @@ __device__ __forceinline__ float exit_distance(const MapSet& m, V3 origin, V3 di
 __device__ __forceinline__ bool sample_empty(const MapSet& m, V3 u, float lod) {
   const int c = min((int)lod + 1, m.L - 1);  // lod >= 0
   const int s = m.N >> c;
-  const float fs = (float)s;
-  const float tx = __fmaf_rn(u.x, fs, -0.5f), ty = __fmaf_rn(u.y, fs, -0.5f), tz = __fmaf_rn(u.z, fs, -0.5f);
-  const float bx = floorf(tx), by = floorf(ty), bz = floorf(tz);
-  const float fx = tx - bx, fy = ty - by, fz = tz - bz;
-  constexpr float kEps = 1.0f / 64.0f;
-  if (fminf(fx, fminf(fy, fz)) < kEps || fmaxf(fx, fmaxf(fy, fz)) > 1.0f - kEps) return false;
-  const int kx = min(max((int)bx, 0), s - 1), ky = min(max((int)by, 0), s - 1), kz = min(max((int)bz, 0), s - 1);
+  const float fs = (float)(s << 8);
+  // (huge or non-finite coordinates saturate or give 0: clamped or fetched)
+  const int qx = __float2int_rd(__fmaf_rn(u.x, fs, -128.0f)), qy = __float2int_rd(__fmaf_rn(u.y, fs, -128.0f)),
+            qz = __float2int_rd(__fmaf_rn(u.z, fs, -128.0f));
+  if ((((uint32_t)qx + 4u) & 255u) < 8u || (((uint32_t)qy + 4u) & 255u) < 8u || (((uint32_t)qz + 4u) & 255u) < 8u)
+    return false;
+  const int kx = min(max(qx >> 8, 0), s - 1), ky = min(max(qy >> 8, 0), s - 1), kz = min(max(qz >> 8, 0), s - 1);
   const uint32_t w = __ldg(m.occ[c] + ((uint32_t)kz * s + ky) * m.occ_wpr[c] + (kx >> 5));
   return ((w >> (kx & 31)) & 1u) == 0u;
 }
