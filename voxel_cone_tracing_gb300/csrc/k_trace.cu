@@ -1,9 +1,10 @@
 // k_trace.cu -- the ConeTracer: replaces the per-fragment cone marching of
 // voxel_cone_tracing.frag (main :246-275) over the G-buffer.
 //
-// One thread shades one visible pixel; a 16x16 CTA covers a 16x16 pixel tile
-// (each warp a 16x2 strip) so that neighbouring lanes march neighbouring,
-// nearly parallel cones and hit the same texture-cache lines.
+// One thread shades one visible pixel; a CTA covers a 16x8 pixel tile (each
+// warp a 16x2 strip; the batched kernel's CTAs 16x16) so that neighbouring
+// lanes march neighbouring, nearly parallel cones and hit the same
+// texture-cache lines.
 //
 // This file is compiled with -fmad=false: a product and a sum are fused only
 // where the code says so (__fmaf_rn), so the results do not depend on how
@@ -42,11 +43,21 @@ __device__ __forceinline__ float4 fma4(float4 a, float s, float4 c) {
   return f4(__fmaf_rn(a.x, s, c.x), __fmaf_rn(a.y, s, c.y), __fmaf_rn(a.z, s, c.z), __fmaf_rn(a.w, s, c.w));
 }
 
-#ifndef VCT_TRACE_MIN_BLOCKS
-#define VCT_TRACE_MIN_BLOCKS 4
+#ifndef VCT_TRACE_ROWS
+#define VCT_TRACE_ROWS 8
 #endif
-// Resident 256-thread CTAs per SM the texture-unit variant is compiled for
-// (register budget 65536 / (256 * 4) = 64 per thread).
+#ifndef VCT_TRACE_MIN_BLOCKS
+#define VCT_TRACE_MIN_BLOCKS 12
+#endif
+// A k_trace CTA shades a 16 x kTraceRows pixel tile (each warp a 16x2
+// strip); the texture-unit variant is compiled for kTraceMinBlocks resident
+// CTAs per SM (register budget 65536 / (16 * rows * blocks) per thread).
+// Measured on the 1080p bench frame (trace ms): 128 threads x 12 CTAs (40
+// registers, 48 warps per SM) 2.59; x 9 (56 registers) 2.64; 256 threads
+// x 4 (64 registers) 2.71, x 6 (40) 2.62; 32 registers 3.77 (spills);
+// 64-thread CTAs x 22 2.98.
+constexpr int kTraceRows = VCT_TRACE_ROWS;
+constexpr int kTraceThreads = 16 * kTraceRows;
 constexpr int kTraceMinBlocks = VCT_TRACE_MIN_BLOCKS;
 #ifndef VCT_TRACE_BATCH_MIN_BLOCKS
 #define VCT_TRACE_BATCH_MIN_BLOCKS 3
@@ -626,11 +637,11 @@ __device__ __forceinline__ void trace_px(const SceneParams& sp, const CameraPara
 }
 
 template <int SAMPLER, bool ISO, int STORAGE>
-__global__ void __launch_bounds__(256, SAMPLER == VCT_SAMPLER_HW ? kTraceMinBlocks : 1)
+__global__ void __launch_bounds__(kTraceThreads, SAMPLER == VCT_SAMPLER_HW ? kTraceMinBlocks : 1)
     k_trace(SceneParams sp, CameraParams cp, MapSet m, TraceParams tp, const float4* __restrict__ gb_pos,
             const float4* __restrict__ gb_nrm, uchar4* __restrict__ frame, float4* __restrict__ frame_f32) {
-  trace_px<SAMPLER, ISO, STORAGE>(sp, cp, m, tp, gb_pos, gb_nrm, frame, frame_f32,
-                                  blockIdx.x * 16 + (threadIdx.x & 15), blockIdx.y * 16 + (threadIdx.x >> 4));
+  trace_px<SAMPLER, ISO, STORAGE>(sp, cp, m, tp, gb_pos, gb_nrm, frame, frame_f32, blockIdx.x * 16 + (threadIdx.x & 15),
+                                  blockIdx.y * kTraceRows + (threadIdx.x >> 4));
 }
 
 // One pixel of a batch scene.  Called, not inlined, from the tile loop of
@@ -706,8 +717,8 @@ __global__ void __launch_bounds__(256, kTraceBatchMinBlocks) k_trace_batch(Batch
 template <int SAMPLER, bool ISO, int STORAGE>
 cudaError_t run(const SceneParams& sp, const CameraParams& cp, const MapSet& ms, const TraceParams& tp,
                 const float4* gb_pos, const float4* gb_nrm, uchar4* frame, float4* frame_f32, cudaStream_t st) {
-  dim3 grid((cp.W + 15) / 16, (cp.H + 15) / 16);
-  k_trace<SAMPLER, ISO, STORAGE><<<grid, 256, 0, st>>>(sp, cp, ms, tp, gb_pos, gb_nrm, frame, frame_f32);
+  dim3 grid((cp.W + 15) / 16, (cp.H + kTraceRows - 1) / kTraceRows);
+  k_trace<SAMPLER, ISO, STORAGE><<<grid, kTraceThreads, 0, st>>>(sp, cp, ms, tp, gb_pos, gb_nrm, frame, frame_f32);
   return cudaGetLastError();
 }
 
