@@ -271,6 +271,23 @@ __device__ __forceinline__ bool sample_empty3(const MapSet& m, V3 u, float lod) 
 #endif
 constexpr bool kSkipEmptyRGBA = VCT_SKIP_EMPTY_RGBA != 0;  // also in the RGBA cones (else shadow cones only)
 
+// The lod of a march step, max(log2(diam * N), 0) with the fast log2
+// (lg2.approx).  Its argument is at least 3 * aperture >= 0.05 (the first
+// step is at 3 voxels and apertures are >= 0.0174533), never subnormal, so
+// the flush-to-zero form gives the same result without the subnormal path.
+#ifndef VCT_LOD_FTZ
+#define VCT_LOD_FTZ 1
+#endif
+__device__ __forceinline__ float cone_lod(float x) {
+#if VCT_LOD_FTZ
+  float r;
+  asm("lg2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return fmaxf(r, 0.0f);
+#else
+  return fmaxf(__log2f(x), 0.0f);
+#endif
+}
+
 // The sample position origin + dir * dist of a march step, one rounding per
 // coordinate (an explicit fused multiply-add, so that it does not depend on
 // how the compiler arranges the step loop).
@@ -342,7 +359,7 @@ __device__ float4 trace_cone_pipe(const MapSet& m, V3 origin, V3 dir, float aper
   const float stop = exit_distance(m, origin, dir, max_dist);
   const bool check = !march_sane(origin, dir, stop);
   if (!(dist < stop)) return acc;
-  float mip = fmaxf(__log2f(diam * cube_res), 0.0f);
+  float mip = cone_lod(diam * cube_res);
   bool live = !(kSkipEmptyRGBA && m.skip_empty && sample_empty(m, sp, mip)) && !(check && !u_sane(sp));
   Taps t;
   if (live) issue_taps(m, sp, ix, iy, iz, ad, mip, t);
@@ -353,7 +370,7 @@ __device__ float4 trace_cone_pipe(const MapSet& m, V3 origin, V3 dir, float aper
     diam = dist * aperture;
     sp = march_pos(origin, dir, dist);
     const bool more = dist < stop;
-    const float mip_n = fmaxf(__log2f(diam * cube_res), 0.0f);
+    const float mip_n = cone_lod(diam * cube_res);
     const bool live_n =
         more && !(kSkipEmptyRGBA && m.skip_empty && sample_empty(m, sp, mip_n)) && !(check && !u_sane(sp));
     if (kTracePipe >= 2) {
@@ -389,7 +406,7 @@ __device__ float4 trace_cone(const MapSet& m, V3 origin, V3 dir, float aperture,
   const float stop = exit_distance(m, origin, dir, max_dist);
   const bool check = !march_sane(origin, dir, stop);
   while (acc.w < 1.0f && dist < stop) {
-    const float mip = fmaxf(__log2f(diam * cube_res), 0.0f);
+    const float mip = cone_lod(diam * cube_res);
     if (!(kSkipEmptyRGBA && m.skip_empty && sample_empty(m, sp, mip)) && !(check && !u_sane(sp))) {
       // (an empty or insane sample adds exact zeros)
       const float4 s = sample_voxel<SAMPLER, ISO, STORAGE, false>(m, sp, ix, iy, iz, ad, mip);
@@ -421,7 +438,7 @@ __device__ float trace_alpha(const MapSet& m, V3 origin, V3 dir, float aperture,
   const float stop = exit_distance(m, origin, dir, max_dist);
   const bool check = !march_sane(origin, dir, stop);
   while (a < 1.0f && dist < stop) {
-    const float mip = fmaxf(__log2f(diam * cube_res), 0.0f);
+    const float mip = cone_lod(diam * cube_res);
     if (!(m.skip_empty && sample_empty3(m, sp, mip)) && !(check && !u_sane(sp)))
       a = __fmaf_rn(sample_alpha(m, sp, ix, iy, iz, ad, mip), 1.0f - a, a);
     const float step = fmaxf(diam * 0.5f, voxel_size);
@@ -448,7 +465,7 @@ __device__ float trace_alpha_pipe(const MapSet& m, V3 origin, V3 dir, float aper
   const float stop = exit_distance(m, origin, dir, max_dist);
   const bool check = !march_sane(origin, dir, stop);
   if (!(dist < stop)) return a;
-  float mip = fmaxf(__log2f(diam * cube_res), 0.0f);
+  float mip = cone_lod(diam * cube_res);
   uint32_t bit = 0, w = skip ? empty3_word(m, sp, mip, bit) : 1u;
   while (true) {
     const float step = fmaxf(diam * 0.5f, voxel_size);
@@ -456,7 +473,7 @@ __device__ float trace_alpha_pipe(const MapSet& m, V3 origin, V3 dir, float aper
     const float diam_n = dist_n * aperture;
     const V3 sp_n = march_pos(origin, dir, dist_n);
     const bool more = dist_n < stop;
-    const float mip_n = fmaxf(__log2f(diam_n * cube_res), 0.0f);
+    const float mip_n = cone_lod(diam_n * cube_res);
     uint32_t bit_n = 0, w_n = 1u;
     if (skip && more) w_n = empty3_word(m, sp_n, mip_n, bit_n);
     if (((w >> bit) & 1u) != 0u && !(check && !u_sane(sp)))
