@@ -42,6 +42,12 @@ namespace {
 #endif
 constexpr int kThreads = VCT_BRICK_THREADS;  // threads of a brick CTA
 constexpr int kWarps = kThreads / 32;
+#ifndef VCT_BRICK_BALANCE
+#define VCT_BRICK_BALANCE 1
+#endif
+// 1: a brick CTA spreads each round's samples over all its threads (a scan
+// over the round's pairs); 0: each warp expands the samples of its own pairs.
+constexpr bool kBrickBalance = VCT_BRICK_BALANCE != 0;
 constexpr int kBrickVox = kBrick * kBrick * kBrick;
 constexpr float kBinMargin = 0.25f;   // voxels; >> snapping and FP32 error
 constexpr float kFix = 65535.0f;      // fixed-point scale of one contribution
@@ -682,6 +688,55 @@ __device__ __forceinline__ void brick_accumulate(const SceneParams& sp, int N, c
   for (int i = threadIdx.x; i < kBrickVox; i += kThreads) acc.clear(i);
   __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if constexpr (kBrickBalance) {
+    // Rounds of up to kThreads pairs: one setup per thread, an exclusive
+    // scan of the pairs' sample counts, then every thread expands samples
+    // it, it + kThreads, ... of the round (a triangle covering the whole
+    // brick does not hold up one warp while the others wait).
+    __shared__ int s_wsum[kWarps];
+    SetupOf<MODE>* su = &setup[0][0];
+    int* ex = &excl[0][0];  // kWarps * 33 >= kThreads entries
+    for (uint32_t b0 = beg; b0 < end; b0 += kThreads) {
+      const uint32_t n = min((uint32_t)kThreads, end - b0);
+      int cnt = 0;
+      if ((uint32_t)threadIdx.x < n) {
+        if (MODE == VCT_VOX_CONSERVATIVE)
+          cnt = setup_sat(sp, N, __ldg(list + b0 + threadIdx.x), b3, reinterpret_cast<SetupSat&>(su[threadIdx.x]));
+        else
+          cnt = setup_ref(sp, N, __ldg(list + b0 + threadIdx.x), b3, reinterpret_cast<SetupRef&>(su[threadIdx.x]));
+      }
+      int incl = cnt;
+      for (int o = 1; o < 32; o <<= 1) {
+        const int v = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += v;
+      }
+      if (lane == 31) s_wsum[warp] = incl;
+      __syncthreads();
+      int off = 0, total = 0;
+#pragma unroll
+      for (int w = 0; w < kWarps; ++w) {
+        const int v = s_wsum[w];
+        off += w < warp ? v : 0;
+        total += v;
+      }
+      ex[threadIdx.x] = off + incl - cnt;
+      __syncthreads();
+      for (int it = threadIdx.x; it < total; it += kThreads) {
+        int lo = 0, hi = (int)n - 1;  // owner = last pair with ex <= it
+        while (lo < hi) {
+          const int mid = (lo + hi + 1) >> 1;
+          if (ex[mid] <= it) lo = mid; else hi = mid - 1;
+        }
+        const int local = it - ex[lo];
+        if (MODE == VCT_VOX_CONSERVATIVE)
+          item_sat(sp, N, b3, reinterpret_cast<const SetupSat&>(su[lo]), local, acc);
+        else
+          item_ref(sp, N, b3, reinterpret_cast<const SetupRef&>(su[lo]), local, acc);
+      }
+      __syncthreads();  // the round's setups and offsets are free again
+    }
+    return;
+  }
   // Rounds of up to kWarps * 32 pairs, split evenly between the warps (a
   // brick with a few dozen pairs keeps every warp busy expanding samples).
   for (uint32_t b0 = beg; b0 < end; b0 += kWarps * 32) {
