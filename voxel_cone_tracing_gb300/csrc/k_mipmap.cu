@@ -243,17 +243,22 @@ __device__ __forceinline__ void mip_reduce(const MapSet& ms, int src_level, int 
       for (int r = threadIdx.x; r < b3; r += kThreads) {
         const int x = r % b, y = (r / b) % b, z = r / (b * b);
         T ch[8], v6[6];
+        bool any = false;
 #pragma unroll
-        for (int k = 0; k < 8; ++k)
+        for (int k = 0; k < 8; ++k) {
           ch[k] = cur[((2 * z + c_off[k][2]) * cur_b + (2 * y + c_off[k][1])) * cur_b + (2 * x + c_off[k][0])];
-        if constexpr (STORAGE == VCT_STORAGE_RGBA8) aniso6_rgba8(ch, v6);
-        else aniso6_rgba16f(ch, v6);
-        if (ms.skip_empty) {
-          bool any = false;
-#pragma unroll
-          for (int k = 0; k < 8; ++k) any |= nonzero(ch[k]);
-          occ_store<B>(ms, 1, ox, oy, oz, x, y, z, r, any, occ_box);
+          any |= nonzero(ch[k]);
         }
+        // Eight zero children reduce to 0 in every direction (most of level
+        // 0 is empty space): the blends are evaluated only where needed.
+        if (any) {
+          if constexpr (STORAGE == VCT_STORAGE_RGBA8) aniso6_rgba8(ch, v6);
+          else aniso6_rgba16f(ch, v6);
+        } else {
+#pragma unroll
+          for (int d = 0; d < 6; ++d) v6[d] = T{};
+        }
+        if (ms.skip_empty) occ_store<B>(ms, 1, ox, oy, oz, x, y, z, r, any, occ_box);
         const int dl = src_level + 1;
 #pragma unroll
         for (int d = 0; d < 6; ++d) {
@@ -275,10 +280,13 @@ __device__ __forceinline__ void mip_reduce(const MapSet& ms, int src_level, int 
       const int x = r % b, y = (r / b) % b, z = r / (b * b);
       const T* base = cur + (cur_shared ? 0 : d * cb3);
       T ch[8];
+      bool any = false;
 #pragma unroll
-      for (int k = 0; k < 8; ++k)
+      for (int k = 0; k < 8; ++k) {
         ch[k] = base[((2 * z + c_off[k][2]) * cur_b + (2 * y + c_off[k][1])) * cur_b + (2 * x + c_off[k][0])];
-      const T v = reduce<STORAGE>(ch, d, NMAPS == 1);
+        any |= nonzero(ch[k]);
+      }
+      const T v = any ? reduce<STORAGE>(ch, d, NMAPS == 1) : T{};  // zero children reduce to 0
       out[i] = v;
       const int dl = src_level + l;
       surf3Dwrite(v, ms.surf[d][dl], ((ox >> l) + x) * Texel<STORAGE>::kBytes, (oy >> l) + y, (oz >> l) + z);

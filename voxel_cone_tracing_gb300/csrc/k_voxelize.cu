@@ -48,6 +48,28 @@ constexpr int kWarps = kThreads / 32;
 // 1: a brick CTA spreads each round's samples over all its threads (a scan
 // over the round's pairs); 0: each warp expands the samples of its own pairs.
 constexpr bool kBrickBalance = VCT_BRICK_BALANCE != 0;
+#ifndef VCT_BRICK_ROUND
+#define VCT_BRICK_ROUND 0
+#endif
+// Pairs per round of the balanced expansion (0: one per thread); their
+// triangle setups are the larger part of a brick CTA's shared memory.
+constexpr int kRound = VCT_BRICK_ROUND > 0 ? VCT_BRICK_ROUND : kThreads;
+static_assert(kRound % 32 == 0 && kRound <= kThreads, "round of whole warps, at most one pair per thread");
+constexpr int kSetupSlots = kBrickBalance ? kRound : kThreads;
+constexpr int kExclSlots = kBrickBalance ? kRound : kWarps * 33;
+#ifndef VCT_BRICK_MIN_BLOCKS
+#define VCT_BRICK_MIN_BLOCKS 0
+#endif
+// Resident brick CTAs per SM the kernels are compiled for (0: the default
+// per coverage rule).  Both rules keep 7 per SM (30 KB of shared memory
+// each); the conservative rule's kernel is held to the 72 registers that 7
+// allow (unbounded it takes 98 and fits 5: 512^3 voxelize 1.47 -> 1.75 ms).
+// Measured with 64-pair rounds (20 KB) at 8-10 per SM: the 512^3 raster
+// rule gains 5%, the bench frame and the batch lose 4-8%.
+template <int MODE>
+constexpr int brick_min_blocks() {
+  return VCT_BRICK_MIN_BLOCKS > 0 ? VCT_BRICK_MIN_BLOCKS : (MODE == VCT_VOX_CONSERVATIVE ? 7 : 1);
+}
 constexpr int kBrickVox = kBrick * kBrick * kBrick;
 constexpr float kBinMargin = 0.25f;   // voxels; >> snapping and FP32 error
 constexpr float kFix = 65535.0f;      // fixed-point scale of one contribution
@@ -683,21 +705,21 @@ using SetupOf = typename std::conditional<MODE == VCT_VOX_CONSERVATIVE, SetupSat
 template <int MODE, int STORAGE>
 __device__ __forceinline__ void brick_accumulate(const SceneParams& sp, int N, const int b3[3],
                                                  const uint32_t* __restrict__ list, uint32_t beg, uint32_t end,
-                                                 AccT<STORAGE>& acc, SetupOf<MODE> (&setup)[kWarps][32],
-                                                 int (&excl)[kWarps][33]) {
+                                                 AccT<STORAGE>& acc, SetupOf<MODE> (&setup)[kSetupSlots],
+                                                 int (&excl)[kExclSlots]) {
   for (int i = threadIdx.x; i < kBrickVox; i += kThreads) acc.clear(i);
   __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if constexpr (kBrickBalance) {
-    // Rounds of up to kThreads pairs: one setup per thread, an exclusive
+    // Rounds of up to kRound pairs: one setup per thread, an exclusive
     // scan of the pairs' sample counts, then every thread expands samples
     // it, it + kThreads, ... of the round (a triangle covering the whole
     // brick does not hold up one warp while the others wait).
     __shared__ int s_wsum[kWarps];
-    SetupOf<MODE>* su = &setup[0][0];
-    int* ex = &excl[0][0];  // kWarps * 33 >= kThreads entries
-    for (uint32_t b0 = beg; b0 < end; b0 += kThreads) {
-      const uint32_t n = min((uint32_t)kThreads, end - b0);
+    SetupOf<MODE>* su = setup;
+    int* ex = excl;
+    for (uint32_t b0 = beg; b0 < end; b0 += kRound) {
+      const uint32_t n = min((uint32_t)kRound, end - b0);
       int cnt = 0;
       if ((uint32_t)threadIdx.x < n) {
         if (MODE == VCT_VOX_CONSERVATIVE)
@@ -719,7 +741,7 @@ __device__ __forceinline__ void brick_accumulate(const SceneParams& sp, int N, c
         off += w < warp ? v : 0;
         total += v;
       }
-      ex[threadIdx.x] = off + incl - cnt;
+      if (threadIdx.x < kRound) ex[threadIdx.x] = off + incl - cnt;
       __syncthreads();
       for (int it = threadIdx.x; it < total; it += kThreads) {
         int lo = 0, hi = (int)n - 1;  // owner = last pair with ex <= it
@@ -747,29 +769,29 @@ __device__ __forceinline__ void brick_accumulate(const SceneParams& sp, int N, c
     int cnt = 0;
     if (lane < q && k < n) {
       if (MODE == VCT_VOX_CONSERVATIVE)
-        cnt = setup_sat(sp, N, __ldg(list + e), b3, reinterpret_cast<SetupSat&>(setup[warp][lane]));
+        cnt = setup_sat(sp, N, __ldg(list + e), b3, reinterpret_cast<SetupSat&>(setup[warp * 32 + lane]));
       else
-        cnt = setup_ref(sp, N, __ldg(list + e), b3, reinterpret_cast<SetupRef&>(setup[warp][lane]));
+        cnt = setup_ref(sp, N, __ldg(list + e), b3, reinterpret_cast<SetupRef&>(setup[warp * 32 + lane]));
     }
     int incl = cnt;
     for (int o = 1; o < 32; o <<= 1) {
       int v = __shfl_up_sync(0xffffffffu, incl, o);
       if (lane >= o) incl += v;
     }
-    excl[warp][lane] = incl - cnt;
+    excl[warp * 33 + lane] = incl - cnt;
     const int total = __shfl_sync(0xffffffffu, incl, 31);
     __syncwarp();
     for (int it = lane; it < total; it += 32) {
       int lo = 0, hi = 31;  // owner = last lane with excl <= it
       while (lo < hi) {
         int mid = (lo + hi + 1) >> 1;
-        if (excl[warp][mid] <= it) lo = mid; else hi = mid - 1;
+        if (excl[warp * 33 + mid] <= it) lo = mid; else hi = mid - 1;
       }
-      const int local = it - excl[warp][lo];
+      const int local = it - excl[warp * 33 + lo];
       if (MODE == VCT_VOX_CONSERVATIVE)
-        item_sat(sp, N, b3, reinterpret_cast<const SetupSat&>(setup[warp][lo]), local, acc);
+        item_sat(sp, N, b3, reinterpret_cast<const SetupSat&>(setup[warp * 32 + lo]), local, acc);
       else
-        item_ref(sp, N, b3, reinterpret_cast<const SetupRef&>(setup[warp][lo]), local, acc);
+        item_ref(sp, N, b3, reinterpret_cast<const SetupRef&>(setup[warp * 32 + lo]), local, acc);
     }
     __syncwarp();
   }
@@ -841,8 +863,8 @@ template <int MODE, int STORAGE>
 __device__ __forceinline__ void brick_unit(const SceneParams& sp, int N, uint32_t brick,
                                            const uint32_t* __restrict__ offset, const uint32_t* __restrict__ list,
                                            uint32_t cap, cudaSurfaceObject_t l0, uint32_t* __restrict__ counts,
-                                           FrameStatus* st, AccT<STORAGE>& acc, SetupOf<MODE> (&setup)[kWarps][32],
-                                           int (&excl)[kWarps][33], const InjGrids& inj, void* l0_lin,
+                                           FrameStatus* st, AccT<STORAGE>& acc, SetupOf<MODE> (&setup)[kSetupSlots],
+                                           int (&excl)[kExclSlots], const InjGrids& inj, void* l0_lin,
                                            const HeavyBricks* hb, uint32_t slot_index, uint32_t chunk, bool item) {
   __shared__ uint32_t s_last;
   int b3[3];
@@ -899,14 +921,14 @@ __device__ __forceinline__ void brick_unit(const SceneParams& sp, int N, uint32_
 // split bricks from the launch-wide item queue (first in the grid, so that
 // the dense bricks' chunks start with the first bricks, not in the tail).
 template <int MODE, int STORAGE>
-__global__ void __launch_bounds__(kThreads) k_bricks(SceneParams sp, int N, const uint32_t* __restrict__ offset,
+__global__ void __launch_bounds__(kThreads, brick_min_blocks<MODE>()) k_bricks(SceneParams sp, int N, const uint32_t* __restrict__ offset,
                                                      const uint32_t* __restrict__ list, uint32_t cap,
                                                      cudaSurfaceObject_t l0, uint32_t* __restrict__ counts,
                                                      FrameStatus* st, InjGrids inj, void* l0_lin, HeavyBricks hb,
                                                      uint32_t n_extra) {
   __shared__ AccT<STORAGE> acc;
-  __shared__ SetupOf<MODE> setup[kWarps][32];
-  __shared__ int excl[kWarps][33];
+  __shared__ SetupOf<MODE> setup[kSetupSlots];
+  __shared__ int excl[kExclSlots];
   __shared__ uint32_t s_next;
   const bool extra = blockIdx.x < n_extra;
   const uint32_t n_items = extra ? min(hb.counters[1], hb.item_cap) : 0u;
@@ -938,10 +960,10 @@ __global__ void __launch_bounds__(kThreads) k_bricks(SceneParams sp, int N, cons
 // thousands of triangle samples).  The queue hands out the extra chunks of
 // the split bricks first (global brick indices), then the bricks.
 template <int MODE, int STORAGE>
-__global__ void __launch_bounds__(kThreads) k_bricks_batch(BatchWork w, BatchBuffers bb) {
+__global__ void __launch_bounds__(kThreads, brick_min_blocks<MODE>()) k_bricks_batch(BatchWork w, BatchBuffers bb) {
   __shared__ AccT<STORAGE> acc;
-  __shared__ SetupOf<MODE> setup[kWarps][32];
-  __shared__ int excl[kWarps][33];
+  __shared__ SetupOf<MODE> setup[kSetupSlots];
+  __shared__ int excl[kExclSlots];
   __shared__ uint32_t s_next;
   const HeavyBricks& hb = bb.heavy;
   const uint32_t n_items = hb.slot ? min(hb.counters[1], hb.item_cap) : 0u;
