@@ -410,7 +410,7 @@ __global__ void __launch_bounds__(kThreads) k_mip(MapSet ms, int src_level) {
 // The first pass (level 0 -> levels 1..4) of every scene of a batch in one
 // persistent launch.
 template <int NMAPS, int STORAGE>
-__global__ void __launch_bounds__(kThreads) k_mip_batch(BatchWork w) {
+__global__ void __launch_bounds__(kThreads, STORAGE == VCT_STORAGE_RGBA8 ? VCT_MIP_TMA_MIN_BLOCKS : 3) k_mip_batch(BatchWork w) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   for (uint32_t g = blockIdx.x; g < w.total; g += gridDim.x) {
     const int s = batch_scene_of(w, g);
