@@ -71,6 +71,7 @@ struct vct_batch {
   // batch-wide work arrays
   DevBuf<uint32_t> brick_count, brick_offset, brick_cursor, pair_list, scan_tmp, bin_big_count, queue;
   DevBuf<BinRec> bin_big;
+  DevBuf<uint2> bin_rec;  // per padded batch triangle (counting -> filling pass)
   uint32_t bin_big_cap = 0;
   HeavyStore heavy;
   DevBuf<unsigned char> rbig;
@@ -133,6 +134,7 @@ struct vct_batch {
     bb.rb.status = d_status.p;
     bb.frame = frame.p;
     bb.heavy = kHeavySplit ? heavy.view() : HeavyBricks{};
+    bb.bin_rec = bin_rec.p;
     return bb;
   }
 
@@ -454,6 +456,7 @@ vct_status build_batch(vct_batch* b, const vct_batch_scene* descs, uint32_t n) {
   VCT_CHECK(b->heavy.reserve(nbk, 1024, 65536, b->stream));
   VCT_CHECK(b->scan_tmp.ensure(scan_tmp_words(nbk)));
   VCT_CHECK(b->pair_list.ensure((size_t)std::min<uint64_t>(0xffffff00ull, 4ull * total_tris + 65536ull)));
+  VCT_CHECK(b->bin_rec.ensure(std::max<size_t>(b->tris.total(), 1)));
   VCT_CHECK(b->bin_big_count.ensure(1));
   VCT_CHECK(b->grow_bin_big(1 << 12));
   VCT_CHECK(b->rbig_count.ensure(2));

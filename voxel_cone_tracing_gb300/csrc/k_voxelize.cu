@@ -153,7 +153,7 @@ __device__ bool tri_box_f32(const float v[3][3], const float c[3], const float h
 
 // One (triangle, candidate brick) test of the binning passes.
 template <bool FILL>
-__device__ __forceinline__ void bin_one(const float v[3][3], int bx, int by, int bz, int nb, bool test, uint32_t t,
+__device__ __forceinline__ bool bin_one(const float v[3][3], int bx, int by, int bz, int nb, bool test, uint32_t t,
                                         uint32_t* __restrict__ count, uint32_t* __restrict__ cursor,
                                         uint32_t* __restrict__ list, uint32_t cap) {
   if (test) {
@@ -165,7 +165,7 @@ __device__ __forceinline__ void bin_one(const float v[3][3], int bx, int by, int
       c[d] = 0.5f * (lo + hi);
       h[d] = 0.5f * (hi - lo);
     }
-    if (!tri_box_f32(v, c, h)) return;
+    if (!tri_box_f32(v, c, h)) return false;
   }
   const uint32_t brick = ((uint32_t)bz * nb + by) * nb + bx;
   if (FILL) {
@@ -174,10 +174,18 @@ __device__ __forceinline__ void bin_one(const float v[3][3], int bx, int by, int
   } else {
     atomicAdd(count + brick, 1u);
   }
+  return true;
 }
 
 constexpr int kSoloBricks = 8;  // candidate bricks a lane bins on its own
 constexpr int kBigSplit = 8;     // CTAs that share one large triangle
+// Bin record of a triangle (counting pass -> filling pass): x = first
+// candidate brick (10 bits per axis), y = bits 0-7 which of its (at most
+// kSoloBricks) candidates passed the triangle/box test, bits 8-16 the
+// candidate extents - 1 (3 bits per axis), bit 31 = bin it again in the
+// filling pass (triangles the warp bins together).  Triangles of large-
+// triangle records and rejected ones have no bricks here.
+constexpr uint32_t kRecAgain = 1u << 31;
 
 // Bins every triangle to the bricks it may touch.  A lane handles its own
 // triangle when it has few candidate bricks.  A triangle with more
@@ -191,13 +199,30 @@ template <bool FILL>
 __device__ __forceinline__ void bin_tri(const SceneParams& sp, int N, uint32_t t, uint32_t* __restrict__ count,
                                         uint32_t* __restrict__ cursor, uint32_t* __restrict__ list, uint32_t cap,
                                         FrameStatus* st, BinRec* __restrict__ big, uint32_t big_cap,
-                                        uint32_t* __restrict__ big_count, uint32_t scene) {
+                                        uint32_t* __restrict__ big_count, uint32_t scene, uint2* __restrict__ rec) {
   const int lane = threadIdx.x & 31;
   const int nb = N / kBrick;
   float v[3][3] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};
   int blo[3] = {0, 0, 0}, bhi[3] = {-1, -1, -1};
   int vol = 0;
-  if (t < sp.total_tris) {
+  bool again = true;  // (filling pass) this lane's triangle is binned from scratch
+  if (FILL && rec && t < sp.total_tris) {
+    // Replay the counting pass's bricks (same pairs, no triangle reload).
+    const uint2 r = rec[t];
+    again = (r.y & kRecAgain) != 0u;
+    if (!again) {
+      const int x0 = (int)(r.x & 1023u), y0 = (int)((r.x >> 10) & 1023u), z0 = (int)(r.x >> 20);
+      const int ex = (int)((r.y >> 8) & 7u) + 1, ey = (int)((r.y >> 11) & 7u) + 1;
+      for (uint32_t m = r.y & 0xffu; m; m &= m - 1) {
+        const int i = __ffs(m) - 1;
+        const uint32_t brick = ((uint32_t)(z0 + i / (ex * ey)) * nb + (uint32_t)(y0 + (i / ex) % ey)) * nb +
+                               (uint32_t)(x0 + i % ex);
+        const uint32_t slot = atomicAdd(cursor + brick, 1u);
+        if (slot < cap) list[slot] = t;
+      }
+    }
+  }
+  if (again && t < sp.total_tris) {
     TriLoad tl;
     load_tri<false>(sp, t, tl);
     if (!tl.ok) {
@@ -220,10 +245,19 @@ __device__ __forceinline__ void bin_tri(const SceneParams& sp, int N, uint32_t t
     }
   }
   if (vol > 0 && vol <= kSoloBricks) {
+    uint32_t mask = 0u;
+    int i = 0;
     for (int bz = blo[2]; bz <= bhi[2]; ++bz)
       for (int by = blo[1]; by <= bhi[1]; ++by)
-        for (int bx = blo[0]; bx <= bhi[0]; ++bx)
-          bin_one<FILL>(v, bx, by, bz, nb, vol > 1, t, count, cursor, list, cap);
+        for (int bx = blo[0]; bx <= bhi[0]; ++bx, ++i)
+          if (bin_one<FILL>(v, bx, by, bz, nb, vol > 1, t, count, cursor, list, cap)) mask |= 1u << i;
+    if (!FILL && rec)
+      rec[t] = make_uint2((uint32_t)blo[0] | (uint32_t)blo[1] << 10 | (uint32_t)blo[2] << 20,
+                          mask | (uint32_t)(bhi[0] - blo[0]) << 8 | (uint32_t)(bhi[1] - blo[1]) << 11 |
+                              (uint32_t)(bhi[2] - blo[2]) << 14);
+  } else if (!FILL && rec && t < sp.total_tris) {
+    // no bricks, or a large triangle: binned by its record (k_bin_big) or by the warp
+    rec[t] = make_uint2(0u, vol > kSoloBricks && !big ? kRecAgain : 0u);
   }
   bool in_warp = vol > kSoloBricks;
   if (in_warp && big) {
@@ -268,9 +302,10 @@ template <bool FILL>
 __global__ void __launch_bounds__(256) k_bin(SceneParams sp, int N, uint32_t* __restrict__ count,
                                              uint32_t* __restrict__ cursor, uint32_t* __restrict__ list,
                                              uint32_t cap, FrameStatus* st, BinRec* __restrict__ big,
-                                             uint32_t big_cap, uint32_t* __restrict__ big_count) {
+                                             uint32_t big_cap, uint32_t* __restrict__ big_count,
+                                             uint2* __restrict__ rec) {
   bin_tri<FILL>(sp, N, blockIdx.x * blockDim.x + threadIdx.x, count, cursor, list, cap, st, big, big_cap, big_count,
-                0u);
+                0u, rec);
 }
 
 // Every scene's triangles in one persistent launch; scene triangle ranges
@@ -280,9 +315,11 @@ __global__ void __launch_bounds__(256) k_bin_batch(BatchWork w, BatchBuffers bb)
   for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < w.total; g += gridDim.x * blockDim.x) {
     const int s = batch_scene_of(w, g);
     const BatchScene& S = w.scenes[s];
-    bin_tri<FILL>(S.sp, S.N, g - __ldg(w.prefix + s), FILL ? nullptr : bb.brick_count + S.brick_base,
+    const uint32_t t = g - __ldg(w.prefix + s);
+    bin_tri<FILL>(S.sp, S.N, t, FILL ? nullptr : bb.brick_count + S.brick_base,
                   FILL ? bb.brick_cursor + S.brick_base : nullptr, bb.pair_list, bb.pair_cap, bb.status, bb.big,
-                  bb.big_cap, bb.big_count, (uint32_t)s);
+                  bb.big_cap, bb.big_count, (uint32_t)s,
+                  bb.bin_rec ? bb.bin_rec + (g - t) : nullptr);
   }
 }
 
@@ -1082,7 +1119,7 @@ cudaError_t launch_voxelize_linear(const SceneParams& sp, int N, int mode, const
   const unsigned tri_blocks = (sp.total_tris + 255) / 256;
   if (tri_blocks)
     k_bin<false><<<tri_blocks, 256, 0, st>>>(sp, N, vb.brick_count, nullptr, nullptr, 0, vb.status, nullptr, 0,
-                                             nullptr);
+                                             nullptr, nullptr);
   e = launch_exclusive_scan(vb.brick_count, vb.brick_offset, vb.brick_cursor, n_bricks, vb.scan_tmp, st);
   if (e != cudaSuccess) return e;
   e = cudaMemcpyAsync(&vb.status->pair_total, vb.brick_offset + n_bricks, sizeof(uint32_t), cudaMemcpyDeviceToDevice,
@@ -1090,7 +1127,7 @@ cudaError_t launch_voxelize_linear(const SceneParams& sp, int N, int mode, const
   if (e != cudaSuccess) return e;
   if (tri_blocks)
     k_bin<true><<<tri_blocks, 256, 0, st>>>(sp, N, nullptr, vb.brick_cursor, vb.pair_list, vb.pair_cap, vb.status,
-                                            nullptr, 0, nullptr);
+                                            nullptr, 0, nullptr, nullptr);
   if (mode == VCT_VOX_CONSERVATIVE)
     k_bricks_linear<VCT_VOX_CONSERVATIVE><<<(unsigned)n_bricks, kThreads, 0, st>>>(sp, N, vb.brick_offset,
                                                                                  vb.pair_list, vb.pair_cap, out);
@@ -1150,7 +1187,7 @@ cudaError_t launch_voxelize(const SceneParams& sp, int N, int mode, int storage,
   }
   if (tri_blocks) {
     k_bin<false><<<tri_blocks, 256, 0, st>>>(sp, N, vb.brick_count, nullptr, nullptr, 0, vb.status, vb.big,
-                                             vb.big_cap, vb.big_count);
+                                             vb.big_cap, vb.big_count, vb.bin_rec);
     ++nl;
     if (vb.big) {
       k_bin_big<false><<<big_grid, 256, 0, st>>>(N, vb.big, vb.big_cap, vb.big_count, vb.brick_count, nullptr, nullptr,
@@ -1175,7 +1212,7 @@ cudaError_t launch_voxelize(const SceneParams& sp, int N, int mode, int storage,
   }
   if (tri_blocks) {
     k_bin<true><<<tri_blocks, 256, 0, st>>>(sp, N, nullptr, vb.brick_cursor, vb.pair_list, vb.pair_cap, vb.status,
-                                            vb.big, vb.big_cap, vb.big_count);
+                                            vb.big, vb.big_cap, vb.big_count, vb.bin_rec);
     ++nl;
     if (vb.big) {
       k_bin_big<true><<<big_grid, 256, 0, st>>>(N, vb.big, vb.big_cap, vb.big_count, nullptr, vb.brick_cursor,

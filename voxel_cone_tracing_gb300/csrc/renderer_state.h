@@ -396,6 +396,7 @@ struct vct_renderer {
   HostBuf<DevInstance> h_inst;
   DevBuf<uint32_t> brick_count, brick_offset, brick_cursor, pair_list, scan_tmp, counts;
   DevBuf<BinRec> bin_big;           // large-triangle binning records
+  DevBuf<uint2> bin_rec;            // per triangle: counting pass -> filling pass
   DevBuf<uint32_t> bin_big_count;
   uint32_t bin_big_cap = 0;
   HeavyStore heavy;                 // dense bricks split across CTAs
@@ -653,6 +654,7 @@ struct vct_renderer {
 
     const uint32_t pairs_needed = (uint32_t)std::min<uint64_t>(0xffffff00ull, 4ull * total + 65536ull);
     if (pair_list.n < pairs_needed) VCT_CHECK(pair_list.ensure(pairs_needed));
+    VCT_CHECK(bin_rec.ensure(std::max<size_t>(total, 1)));
 
     VoxBuffers vb;
     vb.brick_count = brick_count.p;
@@ -668,6 +670,7 @@ struct vct_renderer {
     vb.big_count = bin_big_count.p;
     vb.level0_lin = have_l0_map ? (void*)l0_lin.p : nullptr;
     vb.heavy = kHeavySplit ? heavy.view() : HeavyBricks{};
+    vb.bin_rec = bin_rec.p;
 
     RasterBuffers rb;
     rb.vis = vis.p;

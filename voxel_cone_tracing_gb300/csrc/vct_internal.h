@@ -146,6 +146,8 @@ struct VoxBuffers {
   uint32_t* big_count;
   void* level0_lin;        // level 0 also in linear memory (x fastest), or null
   HeavyBricks heavy;       // dense-brick splitting (heavy.slot null: off)
+  uint2* bin_rec;          // per triangle: the counting pass's bricks, replayed
+                           // by the filling pass (total_tris; null: recompute)
 };
 
 struct RasterBuffers {
@@ -227,6 +229,7 @@ struct BatchBuffers {
   RasterBuffers rb;       // vis / gb_pos / gb_nrm point at pixel 0 of the batch
   uchar4* frame;
   HeavyBricks heavy;      // over the batch-wide (global) brick indices
+  uint2* bin_rec;         // per (padded) batch triangle, as VoxBuffers::bin_rec
 };
 
 // Tunable launch shapes of the batched kernels (chosen by the autotuner).
