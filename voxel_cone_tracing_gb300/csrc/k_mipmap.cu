@@ -564,12 +564,20 @@ __device__ __forceinline__ bool occ_raw_cell(const MapSet& ms, int c, int x, int
     const int s = ms.N >> c;
     return ms.occ_raw[c][((size_t)z * s + y) * s + x] != 0;
   }
+  // The OR of the cell's f^3 block of level-k bytes: every row loaded
+  // independently (no early exit, so the loads are in flight together).
   const int k = ms.occ_k, f = 1 << (c - k), sk = ms.N >> k;
+  uint32_t any = 0u;
   for (int dz = 0; dz < f; ++dz)
-    for (int dy = 0; dy < f; ++dy)
-      for (int dx = 0; dx < f; ++dx)
-        if (ms.occ_raw[k][((size_t)(z * f + dz) * sk + (y * f + dy)) * sk + x * f + dx]) return true;
-  return false;
+    for (int dy = 0; dy < f; ++dy) {
+      const uint8_t* row = ms.occ_raw[k] + ((size_t)(z * f + dz) * sk + (y * f + dy)) * sk + (size_t)x * f;
+      if (f == 4) {
+        any |= __ldg(reinterpret_cast<const uint32_t*>(row));  // 4-byte aligned: x * 4
+      } else {
+        for (int dx = 0; dx < f; ++dx) any |= __ldg(row + dx);
+      }
+    }
+  return any != 0u;
 }
 
 __device__ void occ_pack_word(const MapSet& ms, int c, uint32_t w) {
