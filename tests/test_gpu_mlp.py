@@ -182,3 +182,35 @@ def test_learned_diffuse_replaces_cones(vct):
     print(f"diffuse-only PSNR: learned {q_learned:.1f} dB, untrained {q_untrained:.1f} dB, report {rep}")
     assert q_learned >= 35.0
     assert q_learned >= q_untrained + 15.0
+
+
+def test_learned_diffuse_on_the_raster_stream(vct, tmp_path):
+    """With overlap_raster the learned term's inference runs on the G-buffer
+    raster's stream beside voxelize and mipmap: the frame equals the
+    one-stream frame of the same network bit for bit."""
+    w, h = 64, 48
+    scene = scenes.scene_small(width=w, height=h)
+    a = vct.Renderer(w, h, grid_res=32, keep_float_frame=1)
+    ids_a = vct.load_scene(a, scene)
+    a.set_voxel_view_dir(7, 0.0)
+    vct.queue_scene(a, scene, ids_a)
+    a.render()
+    a.mlp_init(vct.mlp_desc(n_max=128, seed=2))
+    a.mlp_train(vct.mlp_desc(n_max=128, seed=2, steps=20, batch=1 << 12, n_samples=1 << 14))
+    path = str(tmp_path / "net.bin")
+    a.mlp_save(path)
+    b = vct.Renderer(w, h, grid_res=32, keep_float_frame=1, overlap_raster=1)
+    ids_b = vct.load_scene(b, scene)
+    b.set_voxel_view_dir(7, 0.0)
+    b.mlp_load(path)
+    frames = []
+    for r, ids in ((a, ids_a), (b, ids_b)):
+        r.set_diffuse_mode(vct.DIFFUSE_MLP)
+        vct.queue_scene(r, scene, ids)
+        r.render()
+        frames.append(r.read_frame(vct.FRAME_RGBA32F).copy())
+        t = r.stage_times()
+        assert t["gbuffer"] > 0.0 and t["trace"] > 0.0
+    np.testing.assert_array_equal(frames[0], frames[1])
+    a.close()
+    b.close()
