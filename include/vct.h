@@ -257,7 +257,8 @@ vct_status vct_get_grid(vct_renderer* r, int32_t* res, int32_t* levels);
  * RGB, BF16 tensor cores, FP32 accumulation) trained on the GPU to predict
  * trace_diffuse (voxel_cone_tracing.frag:140-168), the average of the nine
  * diffuse cones; with VCT_DIFFUSE_MLP a frame evaluates it instead of
- * tracing those cones.  The cone tracer stays the default and the judge. */
+ * tracing those cones.  The cone tracer stays the default and the reference
+ * the network's per-pixel error is measured against. */
 enum { VCT_DIFFUSE_CONES = 0, VCT_DIFFUSE_MLP = 1 };
 
 typedef struct {
