@@ -182,6 +182,36 @@ __device__ __forceinline__ void write_alpha(const MapSet& ms, int level, int x, 
 __device__ __forceinline__ bool nonzero(uint32_t v) { return v != 0u; }
 __device__ __forceinline__ bool nonzero(uint2 v) { return (v.x | v.y) != 0u; }
 
+// The eight children of destination texel (x, y, z) from a level of edge
+// b2 (= 2 * the destination edge) at `src` in shared memory ([z][y][x]):
+// the children at 2x and 2x+1 (c_off entries k+4 and k) are neighbours,
+// and every row offset is even, so each pair is one aligned 8-byte (RGBA8)
+// or 16-byte (RGBA16F) load.  Returns whether any child is non-zero.
+__device__ __forceinline__ bool load_children(const uint32_t* src, int b2, int x, int y, int z, uint32_t* ch) {
+  bool any = false;
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const uint2 v = *reinterpret_cast<const uint2*>(src + ((2 * z + c_off[k][2]) * b2 + (2 * y + c_off[k][1])) * b2 +
+                                                    2 * x);
+    ch[k + 4] = v.x;
+    ch[k] = v.y;
+    any |= (v.x | v.y) != 0u;
+  }
+  return any;
+}
+__device__ __forceinline__ bool load_children(const uint2* src, int b2, int x, int y, int z, uint2* ch) {
+  bool any = false;
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const uint4 v = *reinterpret_cast<const uint4*>(src + ((2 * z + c_off[k][2]) * b2 + (2 * y + c_off[k][1])) * b2 +
+                                                    2 * x);
+    ch[k + 4] = make_uint2(v.x, v.y);
+    ch[k] = make_uint2(v.z, v.w);
+    any |= (v.x | v.y | v.z | v.w) != 0u;
+  }
+  return any;
+}
+
 // Occupancy of cell (x, y, z) (index r) of level l of the region at
 // (ox, oy, oz): into the region's shared copy and to global memory -- level 1
 // of 16^3 regions straight into the packed bits (a warp holds four rows of
@@ -243,12 +273,7 @@ __device__ __forceinline__ void mip_reduce(const MapSet& ms, int src_level, int 
       for (int r = threadIdx.x; r < b3; r += kThreads) {
         const int x = r % b, y = (r / b) % b, z = r / (b * b);
         T ch[8], v6[6];
-        bool any = false;
-#pragma unroll
-        for (int k = 0; k < 8; ++k) {
-          ch[k] = cur[((2 * z + c_off[k][2]) * cur_b + (2 * y + c_off[k][1])) * cur_b + (2 * x + c_off[k][0])];
-          any |= nonzero(ch[k]);
-        }
+        const bool any = load_children(cur, cur_b, x, y, z, ch);
         // Eight zero children reduce to 0 in every direction (most of level
         // 0 is empty space): the blends are evaluated only where needed.
         if (any) {
@@ -280,12 +305,7 @@ __device__ __forceinline__ void mip_reduce(const MapSet& ms, int src_level, int 
       const int x = r % b, y = (r / b) % b, z = r / (b * b);
       const T* base = cur + (cur_shared ? 0 : d * cb3);
       T ch[8];
-      bool any = false;
-#pragma unroll
-      for (int k = 0; k < 8; ++k) {
-        ch[k] = base[((2 * z + c_off[k][2]) * cur_b + (2 * y + c_off[k][1])) * cur_b + (2 * x + c_off[k][0])];
-        any |= nonzero(ch[k]);
-      }
+      const bool any = load_children(base, cur_b, x, y, z, ch);
       const T v = any ? reduce<STORAGE>(ch, d, NMAPS == 1) : T{};  // zero children reduce to 0
       out[i] = v;
       const int dl = src_level + l;
