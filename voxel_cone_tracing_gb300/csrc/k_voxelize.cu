@@ -33,6 +33,7 @@
 
 #include "vct_internal.h"
 #include "vct_math.cuh"
+#include "vct_snap.h"
 
 namespace vct {
 namespace {
@@ -529,13 +530,15 @@ __device__ int setup_ref(const SceneParams& sp, int N, uint32_t t, const int b3[
   else axis = 1;
   const int ia = axis == 2 ? 0 : (axis == 0 ? 1 : 0);
   const int ib = axis == 2 ? 1 : 2;
-  const double scale = (double)N * 256.0;
+  // Vertices snapped to 1/256 sample: round((g + 1) * N * 256), exactly,
+  // in integer arithmetic (N is a power of two; vct_snap.h).
+  const int shift = __ffs(N) - 1 + 8;
   int idx[3] = {0, 1, 2};
   long long A[3], B[3];
   float c[3];
   for (int k = 0; k < 3; ++k) {
-    A[k] = __double2ll_rn(__dmul_rn(__dadd_rn((double)tl.g[k][ia], 1.0), scale));
-    B[k] = __double2ll_rn(__dmul_rn(__dadd_rn((double)tl.g[k][ib], 1.0), scale));
+    A[k] = snap_fixed(tl.g[k][ia], shift);
+    B[k] = snap_fixed(tl.g[k][ib], shift);
     c[k] = tl.g[k][axis];
   }
   long long area = (A[1] - A[0]) * (B[2] - B[0]) - (B[1] - B[0]) * (A[2] - A[0]);
@@ -617,12 +620,14 @@ __device__ int setup_sat(const SceneParams& sp, int N, uint32_t t, const int b3[
   TriLoad tl;
   load_tri<true>(sp, t, tl);
   if (!tl.ok) return 0;
-  const double scale = (double)N * 128.0;
+  // Vertices snapped to 1/256 voxel: round((g + 1) * N * 128), exactly, in
+  // integer arithmetic (N is a power of two; vct_snap.h).
+  const int shift = __ffs(N) - 1 + 7;
   int lo[3], hi[3];
   for (int d = 0; d < 3; ++d) {
     long long mn = LLONG_MAX, mx = LLONG_MIN;
     for (int k = 0; k < 3; ++k) {
-      long long q = __double2ll_rn(__dmul_rn(__dadd_rn((double)tl.g[k][d], 1.0), scale));
+      long long q = snap_fixed(tl.g[k][d], shift);
       s.V[k][d] = (int)q;
       mn = min(mn, q);
       mx = max(mx, q);
