@@ -48,7 +48,7 @@ NUM_SMS = 152
 # skip: no fetch); counted by the instrumented oracle (oracle.trace_stats;
 # checked by tests/test_scenes.py::test_bench_frame_work).
 TRACE_FETCHES_PER_PIXEL_REF = 778.9
-TRACE_FETCHES_PER_PIXEL = 417.3
+TRACE_FETCHES_PER_PIXEL = 419.1
 INSTANCE_RECORD_BYTES = 144   # one per queued model (DevInstance)
 STATUS_BYTES = 48             # per-frame status read back with the frame
 

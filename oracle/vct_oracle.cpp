@@ -886,7 +886,8 @@ static ConeOut<R> trace_cone(const Maps& m, V3<R> origin, V3<R> dir, R aperture,
     if (gone) ++beyond;
     R mip = fmaxr(R(std::log2(diam * cube_res)), R(0));
     if (g_stats_on && !gone && !g_dilated.empty() &&
-        (t_cone_class == 2 ? sample_empty3_rule<R>(m.N, m.L, sp, mip) : sample_empty_rule<R>(m.N, m.L, sp, mip))) {
+        (t_cone_class == 2 ? sample_empty3_rule<R>(m.N, m.L, sp, mip)
+                           : mip < R(5) && sample_empty_rule<R>(m.N, m.L, sp, mip))) {  // RGBA cones: lod < 5 only
       ++empty;
       if (mip < R(1)) ++empty_lt1;
     }

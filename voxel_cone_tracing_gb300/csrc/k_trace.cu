@@ -270,6 +270,15 @@ __device__ __forceinline__ bool sample_empty3(const MapSet& m, V3 u, float lod) 
 #define VCT_SKIP_EMPTY_RGBA 1
 #endif
 constexpr bool kSkipEmptyRGBA = VCT_SKIP_EMPTY_RGBA != 0;  // also in the RGBA cones (else shadow cones only)
+#ifndef VCT_SKIP_MAX_LOD
+#define VCT_SKIP_MAX_LOD 5.0f
+#endif
+// RGBA cones test for empty space only below this lod: coarser samples are
+// fetched without the test (the coarse cells are rarely empty; fetching a
+// sample that is empty adds the same exact zeros).  Measured on the 1080p
+// bench frame (trace ms): no cap 2.580, below 6 2.552, 5.5 2.550, 5 2.540,
+// 4 2.572; the frames are bit-identical.
+constexpr float kSkipMaxLod = VCT_SKIP_MAX_LOD;
 
 // The lod of a march step, max(log2(diam * N), 0) with the fast log2
 // (lg2.approx).  Its argument is at least 3 * aperture >= 0.05 (the first
@@ -360,7 +369,7 @@ __device__ float4 trace_cone_pipe(const MapSet& m, V3 origin, V3 dir, float aper
   const bool check = !march_sane(origin, dir, stop);
   if (!(dist < stop)) return acc;
   float mip = cone_lod(diam * cube_res);
-  bool live = !(kSkipEmptyRGBA && m.skip_empty && sample_empty(m, sp, mip)) && !(check && !u_sane(sp));
+  bool live = !(kSkipEmptyRGBA && m.skip_empty && mip < kSkipMaxLod && sample_empty(m, sp, mip)) && !(check && !u_sane(sp));
   Taps t;
   if (live) issue_taps(m, sp, ix, iy, iz, ad, mip, t);
   while (true) {
@@ -372,7 +381,7 @@ __device__ float4 trace_cone_pipe(const MapSet& m, V3 origin, V3 dir, float aper
     const bool more = dist < stop;
     const float mip_n = cone_lod(diam * cube_res);
     const bool live_n =
-        more && !(kSkipEmptyRGBA && m.skip_empty && sample_empty(m, sp, mip_n)) && !(check && !u_sane(sp));
+        more && !(kSkipEmptyRGBA && m.skip_empty && mip_n < kSkipMaxLod && sample_empty(m, sp, mip_n)) && !(check && !u_sane(sp));
     if (kTracePipe >= 2) {
       Taps tn;
       if (live_n) issue_taps(m, sp, ix, iy, iz, ad, mip_n, tn);
@@ -407,7 +416,7 @@ __device__ float4 trace_cone(const MapSet& m, V3 origin, V3 dir, float aperture,
   const bool check = !march_sane(origin, dir, stop);
   while (acc.w < 1.0f && dist < stop) {
     const float mip = cone_lod(diam * cube_res);
-    if (!(kSkipEmptyRGBA && m.skip_empty && sample_empty(m, sp, mip)) && !(check && !u_sane(sp))) {
+    if (!(kSkipEmptyRGBA && m.skip_empty && mip < kSkipMaxLod && sample_empty(m, sp, mip)) && !(check && !u_sane(sp))) {
       // (an empty or insane sample adds exact zeros)
       const float4 s = sample_voxel<SAMPLER, ISO, STORAGE, false>(m, sp, ix, iy, iz, ad, mip);
       acc = fma4(s, 1.0f - acc.w, acc);
