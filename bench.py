@@ -38,17 +38,19 @@ METRIC = "ms/frame 1080p@256³ (voxelize+mip+trace)"
 UNIT = "ms/frame"
 WIDTH, HEIGHT, GRID = 1920, 1080, 256
 SCENE_SEED = 2000
-CPU_ROW_STRIDE = 64
-NUM_SMS = 152
-# Quadrilinear 3D fetches per pixel of this frame: 251.2 cone-march steps per
-# pixel (3 fetches each, +1 level-0 fetch for the 25.2 steps with lod < 1)
-# by the reference's sample rule; here the 58.0 shadow steps take 2 fetches
-# (alpha-only chains), the 24.6 steps beyond the grid are not taken (exact
-# early exit) and 86 more steps find only empty cells (exact empty-space
-# skip: no fetch); counted by the instrumented oracle (oracle.trace_stats;
-# checked by tests/test_scenes.py::test_bench_frame_work).
+CPU_WARMUP_ROW_STRIDE = 64   # warm-up frames of the CPU arm trace every 64th row only
+# Texture fetches per pixel of this frame that the texture-unit tracer
+# issues, counted by the instrumented oracle (oracle.trace_stats over every
+# 32nd row; checked by tests/test_scenes.py::test_bench_frame_work): 251.2
+# cone-march steps per pixel by the reference's sample rule (778.9
+# quadrilinear fetches: 3 per step, +1 level-0 fetch below lod 1); the engine
+# skips the steps beyond the grid (exact early exit), the empty steps (exact
+# empty-space skip), the maps whose anisotropic weight is exactly 0, and
+# reads packed alpha-only chains for the shadow cones: 265.6 two-level
+# (quadrilinear) and 83.6 one-level (trilinear) RGBA8 fetches per pixel.
 TRACE_FETCHES_PER_PIXEL_REF = 778.9
-TRACE_FETCHES_PER_PIXEL = 419.1
+TRACE_FETCH_QUAD_PER_PIXEL = 265.6
+TRACE_FETCH_TRI_PER_PIXEL = 83.6
 INSTANCE_RECORD_BYTES = 144   # one per queued model (DevInstance)
 STATUS_BYTES = 48             # per-frame status read back with the frame
 
@@ -134,17 +136,27 @@ def _oracle_params(threads):
     return O.Params(grid_res=GRID, width=WIDTH, height=HEIGHT, threads=threads)
 
 
-def cpu_frame_ms(scene, threads, row_stride):
-    """FP32 CPU restatement: voxelize + mip of the whole scene, cone trace of
-    every row_stride-th row, trace time scaled by row_stride."""
+def cpu_frame_ms(scene, threads, row_stride=1):
+    """FP32 CPU restatement of the frame: voxelize + mip + cone trace (of
+    every row_stride-th pixel row; 1 = the whole frame).  -> (voxelize + mip
+    + trace ms, per-stage ms)."""
     from oracle import oracle as O
     ms = O.time_frame(scene, _oracle_params(threads), row_stride)
-    return ms[0] + ms[1] + ms[3] * row_stride, ms
+    return ms[0] + ms[1] + ms[3], ms
 
 
-def _cpu_sample_text(row_stride):
-    return (f"FP32 C++ restatement, voxelize+mip of the full {WIDTH}x{HEIGHT}@{GRID}^3 frame, cone trace of every "
-            f"{row_stride}th pixel row (1/{row_stride} of the pixels), trace time x{row_stride}")
+CPU_SAMPLE = (f"FP32 C++ restatement of the whole frame: voxelize + mip of the {GRID}^3 grid and the cone trace "
+              f"of all {WIDTH}x{HEIGHT} pixels, every step; host threads over triangle chunks, voxel slabs and "
+              "32-pixel runs")
+
+
+def bench_config(sampler: str, parallelism: str) -> dict:
+    """The workload description both arms print (same keys, same workload)."""
+    return {"workload": "room + displaced icosphere (499,290 triangles), 1920x1080, 256^3 aniso RGBA8, "
+                        "9 diffuse + 1 specular + 1 shadow cone", "grid": GRID, "width": WIDTH, "height": HEIGHT,
+            "triangles": 499290, "voxelizer": "reference raster 2x", "sampler": sampler,
+            "l2": "flushed between timed frames (256 MB write)" if sampler == "texture unit" else "n/a (CPU)",
+            "parallelism": parallelism}
 
 
 def run_reference(args):
@@ -153,26 +165,29 @@ def run_reference(args):
         return 0
     threads = os.cpu_count() or 1
     scene = _scene()
-    stride = CPU_ROW_STRIDE
+    assert scene.n_tris == 499290
     for _ in range(max(args.warmup, 0)):
-        cpu_frame_ms(scene, threads, stride * 4)
-    vals = []
+        cpu_frame_ms(scene, threads, CPU_WARMUP_ROW_STRIDE)
+    vals, stages = [], []
     for _ in range(args.steps):
-        v, _ms = cpu_frame_ms(scene, threads, stride)
+        v, ms = cpu_frame_ms(scene, threads, 1)
         vals.append(v)
+        stages.append(ms)
     value = statistics.mean(vals)
+    frame = statistics.mean(float(sum(st)) for st in stages)  # + the G-buffer raster
     line = {
         "impl": "reference", "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(value, 3), "higher_is_better": False,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(frame, 3), "higher_is_better": False,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": "room + displaced icosphere (499,290 triangles), 1920x1080, 256^3 aniso RGBA8, "
-                               "9 diffuse + 1 specular + 1 shadow cone", "grid": GRID, "width": WIDTH,
-                   "height": HEIGHT, "triangles": scene.n_tris, "parallelism": "host threads"},
+        "config": bench_config("FP32 software", f"host threads x{threads}"),
+        "stages_ms": {k: round(statistics.mean(st[i] for st in stages), 2)
+                      for k, i in (("voxelize", 0), ("mipmap", 1), ("gbuffer", 2), ("trace", 3))},
         "cpu_baseline": {"value": round(value, 3), "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": _cpu_sample_text(stride)},
+                         "sample": CPU_SAMPLE},
         "e2e": {"value": round(value, 3), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-        "note": "reference is an OpenGL 4.5 program (GLSL in the GL driver); no graphics stack exists on this "
-                "box, so its algorithm is timed as the project's CPU restatement",
+        "note": "the reference is an OpenGL 4.5 program (GLSL in the GL driver); no graphics stack exists on this "
+                "box, so its algorithm is timed as the project's CPU restatement; warm-up frames trace every "
+                f"{CPU_WARMUP_ROW_STRIDE}th row only",
     }
     print(json.dumps(line))
     return 0
@@ -490,46 +505,64 @@ def run_ours(args):
     d2h = WIDTH * HEIGHT * 4 + STATUS_BYTES
 
     # ---- roofline of the dominant kernel (cone trace) ----------------------
+    # The trace reads its texels through the texture unit from L1 (the chain
+    # fits in L2 and neighbouring cones share cache lines): its bound is the
+    # texture unit's filtering rate, measured here on this device by
+    # vct_measure_texture_rate (two-level and one-level 3D RGBA8 fetches,
+    # every lane fetching, L1-resident).  The trace's fetches are counted by
+    # the instrumented oracle; a one-level fetch is charged rate_quad/rate_tri
+    # of a two-level one.  HBM is reported beside it.
+    probe = {k: R.measure_texture_rate(k) for k in (0, 1, 2)}
+    rate_quad, rate_tri = probe[0]["fetches_per_s"], probe[1]["fetches_per_s"]
+    px = WIDTH * HEIGHT
+    n_quad, n_tri = TRACE_FETCH_QUAD_PER_PIXEL * px, TRACE_FETCH_TRI_PER_PIXEL * px
+    trace_ms = mean("trace")
+    q_equiv = n_quad + n_tri * rate_quad / rate_tri
+    achieved_tex = q_equiv / (trace_ms * 1e-3) / 1e9
+    floor_ms = (n_quad / rate_quad + n_tri / rate_tri) * 1e3
+    sms = torch.cuda.get_device_properties(local).multi_processor_count
+    sm_clock_hz = (clk.summary().get("sm_mhz") or 2070.0) * 1e6
+    per_clk_sm = lambda rate: round(rate / sm_clock_hz / sms, 3)  # noqa: E731
     peak, peak_kind = _peaks()
     nmaps_levels = sum((GRID >> l) ** 3 for l in range(1, 7)) * 6
-    trace_bytes = WIDTH * HEIGHT * (32 + 4) + (GRID ** 3 + nmaps_levels) * 4
-    trace_ms = mean("trace")
-    achieved = trace_bytes / (trace_ms * 1e-3) / 1e9
+    trace_bytes = px * (32 + 4) + (GRID ** 3 + nmaps_levels) * 4
+    achieved_hbm = trace_bytes / (trace_ms * 1e-3) / 1e9
     traffic, tex_pct = None, None
     tp = os.path.join(ROOT, "profiles", "trace_traffic.json")
     if os.path.exists(tp):
         with open(tp) as f:
             prof = json.load(f)
         traffic, tex_pct = prof.get("dram_bytes_per_launch"), prof.get("tex_pipe_pct_of_peak")
-    fetches = TRACE_FETCHES_PER_PIXEL * WIDTH * HEIGHT
-    sm_clock_hz = (clk.summary().get("sm_mhz") or 2070.0) * 1e6
 
     line = {
         "metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": max(args.warmup, 3), "ms_per_step": round(ms_step, 4), "higher_is_better": False,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": "room + displaced icosphere (499,290 triangles), 1920x1080, 256^3 aniso RGBA8, "
-                               "9 diffuse + 1 specular + 1 shadow cone", "grid": GRID, "width": WIDTH,
-                   "height": HEIGHT, "triangles": scene.n_tris, "voxelizer": "reference raster 2x",
-                   "sampler": "texture unit", "l2": "flushed between timed frames (256 MB write)",
-                   "parallelism": f"replicas x{world}"},
+        "config": bench_config("texture unit", f"replicas x{world}"),
         "stages_ms": {"voxelize": round(mean("voxelize"), 4), "mipmap": round(mean("mipmap"), 4),
                       "gbuffer": round(mean("gbuffer"), 4), "trace": round(trace_ms, 4),
                       "frame": round(ms_step, 4)},
         "e2e": {"value": round(e2e_ms, 4), "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "statistic": "median of per-step host wall times", "mean": round(e2e_mean, 4)},
         "gpu_launches": int(sum(st["kernel_launches"] for st in stages)),
-        "roofline": {"kernel": "k_trace", "bound": "hbm", "achieved": round(achieved, 2), "peak": peak,
-                     "unit": "GB/s", "frac": round(achieved / peak, 5), "traffic": traffic,
-                     "peak_source": peak_kind,
-                     "texture_path": {
-                         "note": "k_trace is bound by the texture pipeline and its step arithmetic, not by HBM "
-                                 "(profiles/k_trace_1080p_256.md)",
-                         "quadrilinear_fetches_per_frame": fetches,
-                         "fetches_per_clock_per_sm": round(fetches / (trace_ms * 1e-3) / sm_clock_hz / NUM_SMS, 3),
-                         "texel_bytes_per_s": round(fetches * 64 / (trace_ms * 1e-3) / 1e12, 3),
-                         "texel_bytes_unit": "TB/s (16 RGBA8 texels per fetch, served by L1)",
-                         "ncu_tex_pipe_pct_of_peak": tex_pct}},
+        "roofline": {"kernel": "k_trace", "bound": "tex", "achieved": round(achieved_tex, 2),
+                     "peak": round(rate_quad / 1e9, 2), "unit": "Gfetch/s", "frac": round(achieved_tex * 1e9 / rate_quad, 4),
+                     "traffic": traffic, "peak_source": "measured in this run (vct_measure_texture_rate)",
+                     "fetches": {"two_level_per_pixel": TRACE_FETCH_QUAD_PER_PIXEL,
+                                 "one_level_per_pixel": TRACE_FETCH_TRI_PER_PIXEL,
+                                 "reference_rule_per_pixel": TRACE_FETCHES_PER_PIXEL_REF,
+                                 "two_level_equivalents_per_frame": round(q_equiv),
+                                 "unit": "3D RGBA8 texture fetches (achieved/peak in two-level equivalents)"},
+                     "fetch_floor_ms": round(floor_ms, 4),
+                     "probe": {"two_level_per_clk_per_sm": per_clk_sm(rate_quad),
+                               "one_level_per_clk_per_sm": per_clk_sm(rate_tri),
+                               "mip_integer_lod_per_clk_per_sm": per_clk_sm(probe[2]["fetches_per_s"]),
+                               "sms": sms, "sm_mhz": sm_clock_hz / 1e6},
+                     "trace_two_level_equivalents_per_clk_per_sm": per_clk_sm(q_equiv / (trace_ms * 1e-3)),
+                     "ncu_tex_pipe_pct_of_peak": tex_pct,
+                     "hbm": {"achieved": round(achieved_hbm, 2), "peak": peak, "unit": "GB/s",
+                             "frac": round(achieved_hbm / peak, 5), "peak_source": peak_kind,
+                             "algorithmic_bytes": trace_bytes}},
         "clocks": clk.summary(),
     }
     if not args.no_mlp:
@@ -542,11 +575,11 @@ def run_ours(args):
         line["batch"] = batch_leg(R, torch, min(max(args.steps, 3), 10), rank, world, pg)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
-        v, ms = cpu_frame_ms(scene, threads, CPU_ROW_STRIDE)
+        v, ms = cpu_frame_ms(scene, threads, 1)
         line["cpu_baseline"] = {"value": round(v, 2), "unit": UNIT, "cores": threads, "kind": "port",
-                                "sample": _cpu_sample_text(CPU_ROW_STRIDE),
+                                "sample": CPU_SAMPLE + " (one frame)",
                                 "stages_ms": {"voxelize": round(ms[0], 2), "mipmap": round(ms[1], 2),
-                                              "trace": round(ms[3] * CPU_ROW_STRIDE, 2)}}
+                                              "trace": round(ms[3], 2)}}
     if rank == 0:
         print(json.dumps(line))
     r.close()

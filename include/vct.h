@@ -338,15 +338,18 @@ typedef struct {
 /* Voxelize meshes (host array of descriptors) into level0_rgba8 (device,
  * grid_res^3 x 4 bytes, x fastest, fully overwritten) with the same kernels
  * and coverage rules as vct_render's level 0.  materials: device array;
- * lights: host array (at most 10 used).  Limits: grid_res a power of two in
- * [8, 256], <= 64 meshes, <= 4096 materials, <= 2^21 (triangle, 8^3-voxel
- * brick) pairs; beyond them the call fails with VCT_ERR_INVALID_VALUE (the
- * pair count is known only after binning, so that case fails after the GPU
- * work and leaves the output incomplete).  The first call on a device looks
- * up the library's device array once; calls share that array, so calls
- * whose GPU work overlaps (other streams / threads) race -- serialise them.
- * Synchronises `stream` (a cudaStream_t, NULL = default stream) before
- * returning. */
+ * lights: host array.  Limits: grid_res a power of two in [8, 256], <= 64
+ * meshes, <= 4096 materials, <= 10 lights, <= 2^21 (triangle, 8^3-voxel
+ * brick) pairs; beyond them the call fails with VCT_ERR_INVALID_VALUE.  Two
+ * failures are known only after the GPU work, which then leaves the output
+ * incomplete: more pairs than the limit, and vertex indices >= n_verts or
+ * material ids >= n_materials (the kernels clamp such ids, so they read
+ * nothing outside the caller's buffers).  Every call looks up the library's
+ * device array on the current device (the first lookup on a device loads
+ * the library's device code: make that call before any stream capture);
+ * calls share that array, so calls whose GPU work overlaps (other streams /
+ * threads) race -- serialise them.  Synchronises `stream` (a cudaStream_t,
+ * NULL = default stream) before returning. */
 vct_status vct_voxelize_noalloc(const vct_device_mesh* meshes, uint32_t n_meshes,
                                 const vct_material_data* materials, uint32_t n_materials,
                                 const vct_point_light* lights, uint32_t n_lights,
@@ -467,6 +470,19 @@ vct_status vct_batch_set_shape(vct_batch* b, const vct_batch_shape* shape);
  * the fastest, and reports it with the frame times before and after. */
 vct_status vct_batch_autotune(vct_batch* b, int32_t frames, vct_batch_shape* best, float* ms_before,
                               float* ms_after);
+
+/* ------------------------------------------------------- measurement --- */
+
+/* No counterpart in the reference: a measurement helper.  The cone tracer is
+ * bound by the texture unit, so its roofline is the rate at which the
+ * current device filters 3D RGBA8 fetches with every lane fetching and the
+ * texels L1-resident.  kind 0: tex3DLod of a mipmapped texture at a
+ * fractional lod (two levels, 16 texels); 1: tex3D of a non-mipmapped
+ * texture (8 texels); 2: tex3DLod at an integer lod (one level).  Runs
+ * iters (4..8192) fetches per thread on every SM, timed with CUDA events
+ * (best of 3 launches after a warm-up); returns fetches per second and the
+ * launch time in ms.  Allocates and frees its own 32^3 texture. */
+vct_status vct_measure_texture_rate(int32_t kind, uint32_t iters, double* fetches_per_s, double* ms);
 
 #ifdef __cplusplus
 }

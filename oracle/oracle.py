@@ -317,10 +317,12 @@ def trace_stats(scene, params: Params, level0, chains, gb: dict, row_stride: int
     beyond the grid (taken by the reference's loop, skipped by the engine's
     exact early exit) and the other steps the engine's occupancy rule finds
     empty (no fetch; `empty_lt1` of them with lod < 1) per cone class over
-    the traced rows (the algorithmic texture work of the trace)."""
+    the traced rows, and the single-level / two-level texture fetches the
+    engine's texture-unit path issues for the remaining steps (`fetch_tri`,
+    `fetch_quad`: the algorithmic texture work of the trace)."""
     w, h = params.width, params.height
     out = np.zeros((h, w, 4), np.float32)
-    st = np.zeros(32, np.uint64)
+    st = np.zeros(40, np.uint64)
     sh, pc = _SceneHold(scene), params.c()
     args = [np.ascontiguousarray(level0, np.uint8), np.ascontiguousarray(chains, np.uint8),
             np.ascontiguousarray(gb["tri_id"], np.uint32), np.ascontiguousarray(gb["pos"], np.float64),
@@ -328,7 +330,8 @@ def trace_stats(scene, params: Params, level0, chains, gb: dict, row_stride: int
     lib().orc_trace_stats(sh.ptr, C.addressof(pc), *[_ptr(a) for a in args], int(row_stride), _ptr(out), _ptr(st))
     names = ["diffuse", "specular", "shadow", "refraction"]
     res = {n: dict(cones=int(st[i]), steps=int(st[4 + i]), lod_lt1=int(st[8 + i]), beyond=int(st[20 + i]),
-                   empty=int(st[24 + i]), empty_lt1=int(st[28 + i])) for i, n in enumerate(names)}
+                   empty=int(st[24 + i]), empty_lt1=int(st[28 + i]), fetch_tri=int(st[32 + i]),
+                   fetch_quad=int(st[36 + i])) for i, n in enumerate(names)}
     res["lod_bands"] = [int(v) for v in st[12:20]]  # all classes: lod in [k, k+1), last = lod >= 7
     return res
 

@@ -776,10 +776,16 @@ template <class R> struct ConeOut { V4<R> c; int steps; };
 // than 3/4 of the coarsest texel outside [0,1] along an axis it travels
 // away on (they read border texels only; the engine does not take them);
 // then per class the other steps whose texels are all 0 by the engine's
-// occupancy rule (below), and how many of those have lod < 1.
+// occupancy rule (below), and how many of those have lod < 1; then per
+// class the texture fetches the engine's texture-unit path issues for the
+// steps it takes, split into single-level (trilinear: the shared level 0,
+// a chain at lod 0 when lod < 1, a chain clamped at its last level) and
+// two-level (quadrilinear) fetches.  A map whose weight is exactly 0 is not
+// fetched; shadow cones fetch the packed alpha chains (one fetch for the x
+// and y maps, one for the z maps).
 enum {
   kStatCones = 0, kStatSteps = 4, kStatLodLt1 = 8, kStatLodBand = 12, kStatBeyond = 20, kStatEmpty = 24,
-  kStatEmptyLt1 = 28, kStatN = 32
+  kStatEmptyLt1 = 28, kStatFetchTri = 32, kStatFetchQuad = 36, kStatN = 40
 };
 static std::atomic<uint64_t> g_stats[kStatN];
 // The engine's empty-space rule (csrc/k_trace.cu sample_empty): per level c
@@ -877,7 +883,9 @@ static ConeOut<R> trace_cone(const Maps& m, V3<R> origin, V3<R> dir, R aperture,
   R dist = R(3) * voxel_size;
   R diam = dist * aperture;
   V3<R> sp = dir * dist + origin;
-  int steps = 0, lod_lt1 = 0, beyond = 0, empty = 0, empty_lt1 = 0;
+  int steps = 0, lod_lt1 = 0, beyond = 0, empty = 0, empty_lt1 = 0, f_tri = 0, f_quad = 0;
+  const int maps_fetched = t_cone_class == 2 ? (ad.x != R(0) || ad.y != R(0)) + (ad.z != R(0))
+                                             : (ad.x != R(0)) + (ad.y != R(0)) + (ad.z != R(0));
   const R margin = R(0.75) * R(1 << (m.L - 1)) / cube_res;
   auto outside = [&](R p, bool up) { return up ? p > R(1) + margin : p < -margin; };
   bool gone = false;
@@ -885,11 +893,18 @@ static ConeOut<R> trace_cone(const Maps& m, V3<R> origin, V3<R> dir, R aperture,
     gone = gone || outside(sp.x, ix == 1) || outside(sp.y, iy == 3) || outside(sp.z, iz == 5);
     if (gone) ++beyond;
     R mip = fmaxr(R(std::log2(diam * cube_res)), R(0));
-    if (g_stats_on && !gone && !g_dilated.empty() &&
-        (t_cone_class == 2 ? sample_empty3_rule<R>(m.N, m.L, sp, mip)
-                           : mip < R(5) && sample_empty_rule<R>(m.N, m.L, sp, mip))) {  // RGBA cones: lod < 5 only
-      ++empty;
-      if (mip < R(1)) ++empty_lt1;
+    if (g_stats_on && !gone && !g_dilated.empty()) {
+      if (t_cone_class == 2 ? sample_empty3_rule<R>(m.N, m.L, sp, mip)
+                            : mip < R(5) && sample_empty_rule<R>(m.N, m.L, sp, mip)) {  // RGBA cones: lod < 5 only
+        ++empty;
+        if (mip < R(1)) ++empty_lt1;
+      } else if (mip < R(1)) {
+        f_tri += 1 + (mip > R(0) ? maps_fetched : 0);
+      } else if (mip - R(1) >= R(m.L - 2) || mip == std::floor(mip)) {
+        f_tri += maps_fetched;
+      } else {
+        f_quad += maps_fetched;
+      }
     }
     V4<R> smp = texture_lod<R>(m, ix, sp, mip) * ad.x + texture_lod<R>(m, iy, sp, mip) * ad.y +
                 texture_lod<R>(m, iz, sp, mip) * ad.z;
@@ -909,6 +924,8 @@ static ConeOut<R> trace_cone(const Maps& m, V3<R> origin, V3<R> dir, R aperture,
     g_stats[kStatBeyond + t_cone_class] += (uint64_t)beyond;
     g_stats[kStatEmpty + t_cone_class] += (uint64_t)empty;
     g_stats[kStatEmptyLt1 + t_cone_class] += (uint64_t)empty_lt1;
+    g_stats[kStatFetchTri + t_cone_class] += (uint64_t)f_tri;
+    g_stats[kStatFetchQuad + t_cone_class] += (uint64_t)f_quad;
   }
   return {acc, steps};
 }
@@ -1060,9 +1077,15 @@ static void trace_impl(const orc_scene* s, const orc_params* p, const uint8_t* l
   const int W = p->width, H = p->height;
   if (row_stride < 1) row_stride = 1;
   const int rows = (H + row_stride - 1) / row_stride;
-  parallel_for(std::max(1, p->threads), rows, [&](int ri) {
-    int y = ri * row_stride;
-    for (int x = 0; x < W; ++x) {
+  // Work items are 32-pixel runs of a traced row, so that every thread gets
+  // a share of the frame whatever the row count (a sampled frame may have
+  // fewer rows than threads).
+  const int kRun = 32;
+  const int runs = (W + kRun - 1) / kRun;
+  parallel_for(std::max(1, p->threads), rows * runs, [&](int item) {
+    const int y = (item / runs) * row_stride;
+    const int x0 = (item % runs) * kRun, x1 = std::min(W, x0 + kRun);
+    for (int x = x0; x < x1; ++x) {
       size_t px = (size_t)y * W + x;
       float* o = out + 4 * px;
       for (int q = 0; q < 4; ++q) o[q] = kClear[q];

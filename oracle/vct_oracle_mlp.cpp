@@ -9,7 +9,8 @@
 // b = (N_max / N_min)^(1/15); x = p * N_l; the 8 corners of floor(x) are
 // looked up densely (c.x + c.y (N_l+1) + c.z (N_l+1)^2, corners clamped to
 // N_l) when (N_l+1)^3 <= T, else by the spatial hash
-// (c.x * 1 ^ c.y * 2654435761 ^ c.z * 805459861) mod T; trilinear weights
+// (c.x * 1 ^ c.y * 2654435761 ^ c.z * 805459861) mod T of Mueller et al.,
+// "Instant Neural Graphics Primitives" (SIGGRAPH 2022); trilinear weights
 // from frac(x).  Input vector (64): 32 hash features, normalize(normal),
 // albedo, a constant 1, zeros.  Layers: W1..W4 64x64 (ReLU), W5 16x64 (first
 // 3 outputs used, linear).  No biases.  Loss = mean over samples of the sum

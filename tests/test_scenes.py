@@ -55,7 +55,7 @@ def test_draw_objects_cover_mesh():
 
 def test_bench_frame_work(oracle):
     """Instrumented oracle on the benchmark frame (every 32nd row): the
-    per-pixel quadrilinear fetch count bench.py reports."""
+    per-pixel texture fetch counts bench.py reports."""
     import bench
     s = scenes.scene_sphere(seed=bench.SCENE_SEED, width=bench.WIDTH, height=bench.HEIGHT)
     p = oracle.Params(grid_res=bench.GRID, width=bench.WIDTH, height=bench.HEIGHT)
@@ -71,6 +71,11 @@ def test_bench_frame_work(oracle):
     assert st["diffuse"]["cones"] == 9 * px
     assert 3 * steps + lt1 == pytest.approx(bench.TRACE_FETCHES_PER_PIXEL_REF, rel=0.02)
     assert st["shadow"]["beyond"] == 0  # shadow cones end at the light, inside the grid
-    engine = sum((2 if k == "shadow" else 3) * (v["steps"] - v["beyond"] - v["empty"]) + v["lod_lt1"] - v["empty_lt1"]
-                 for k, v in st.items()) / px
-    assert engine == pytest.approx(bench.TRACE_FETCHES_PER_PIXEL, rel=0.02)
+    quad = sum(v["fetch_quad"] for v in st.values()) / px
+    tri = sum(v["fetch_tri"] for v in st.values()) / px
+    assert quad == pytest.approx(bench.TRACE_FETCH_QUAD_PER_PIXEL, rel=0.02)
+    assert tri == pytest.approx(bench.TRACE_FETCH_TRI_PER_PIXEL, rel=0.02)
+    # at most 3 fetches per RGBA step and 2 per shadow step, +1 below lod 1
+    upper = sum((2 if k == "shadow" else 3) * (v["steps"] - v["beyond"] - v["empty"]) + v["lod_lt1"] - v["empty_lt1"]
+                for k, v in st.items()) / px
+    assert quad + tri <= upper

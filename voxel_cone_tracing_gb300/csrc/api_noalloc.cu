@@ -20,12 +20,19 @@
 // so such a call reports the error after the work ran (its output is then
 // incomplete).
 //
-// The first call on a device looks up the device address of the array
-// (cudaGetSymbolAddress, once per device, with that device current).  All
-// calls share the array and it keeps the last call's contents; everything
-// that must start at zero is cleared by each call.  Calls whose GPU work
-// overlaps (other streams, other host threads) race on the array: issue them
-// one after another.
+// Every call looks up the device address of the array on the current device
+// (cudaGetSymbolAddress, with that device current); on a device's first call
+// that lookup loads the library's device code, so make the first call on a
+// device before any stream capture.  All calls share the array and it keeps
+// the last call's contents; everything that must start at zero is cleared by
+// each call.  Calls whose GPU work overlaps (other streams, other host
+// threads) race on the array: issue them one after another.
+//
+// Vertex indices and material ids live in caller memory on the device, so
+// they cannot be checked before the launch: the kernels clamp them (no read
+// leaves the caller's buffers) and a small kernel counts the ones out of
+// range, which makes the call fail with VCT_ERR_INVALID_VALUE after the work
+// ran (its output is then not the meshes' voxelization).
 #include <cstring>
 #include <mutex>
 
@@ -39,7 +46,6 @@ constexpr uint32_t kNaMaxPairs = 1u << 21;
 constexpr uint32_t kNaMaxMeshes = 64;
 constexpr uint32_t kNaMaxMaterials = 4096;
 constexpr int kNaScanTmp = kNaMaxBricks / 4096 + 8;
-constexpr int kNaMaxDevices = 64;
 
 struct NoAllocScratch {
   uint32_t brick_count[kNaMaxBricks];
@@ -54,26 +60,32 @@ struct NoAllocScratch {
 
 static __device__ __align__(256) unsigned char g_scratch[sizeof(NoAllocScratch)];
 
-std::mutex g_mu;
-NoAllocScratch* g_scratch_ptr[kNaMaxDevices] = {};
+std::once_flag g_identity_once;
 uint32_t g_identity[kNaMaxMaterials];
 
-// Device address of the scratch array on the current device (set up once
-// per device).
+// Device address of the scratch array on the current device.
 vct_status scratch_on_device(NoAllocScratch** out) {
-  int dev = 0;
-  VCT_CUDA(cudaGetDevice(&dev));
-  if (dev < 0 || dev >= kNaMaxDevices) return set_error(VCT_ERR_UNSUPPORTED, "device %d", dev);
-  std::lock_guard<std::mutex> lk(g_mu);
-  if (!g_scratch_ptr[dev]) {
-    void* p = nullptr;
-    cudaError_t e = cudaGetSymbolAddress(&p, g_scratch);
-    if (e != cudaSuccess) return cuda_status(e, "cudaGetSymbolAddress(voxelizer scratch)");
-    g_scratch_ptr[dev] = static_cast<NoAllocScratch*>(p);
+  void* p = nullptr;
+  cudaError_t e = cudaGetSymbolAddress(&p, g_scratch);
+  if (e != cudaSuccess) return cuda_status(e, "cudaGetSymbolAddress(voxelizer scratch)");
+  std::call_once(g_identity_once, [] {
     for (uint32_t i = 0; i < kNaMaxMaterials; ++i) g_identity[i] = i;
-  }
-  *out = g_scratch_ptr[dev];
+  });
+  *out = static_cast<NoAllocScratch*>(p);
   return VCT_OK;
+}
+
+// Counts the vertex indices >= n_verts and material ids >= n_materials of
+// one device mesh into *bad.
+__global__ void k_count_bad_ids(const uint32_t* __restrict__ indices, const uint32_t* __restrict__ tri_material,
+                                uint32_t n_tris, uint32_t n_verts, uint32_t n_materials, uint32_t* bad) {
+  uint32_t nb = 0;
+  for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < n_tris; t += gridDim.x * blockDim.x) {
+    nb += __ldg(tri_material + t) >= n_materials;
+    for (int k = 0; k < 3; ++k) nb += __ldg(indices + 3 * (size_t)t + k) >= n_verts;
+  }
+  for (int o = 16; o > 0; o >>= 1) nb += __shfl_xor_sync(0xffffffffu, nb, o);
+  if ((threadIdx.x & 31) == 0 && nb) atomicAdd(bad, nb);
 }
 
 }  // namespace
@@ -95,12 +107,16 @@ extern "C" vct_status vct_voxelize_noalloc(const vct_device_mesh* meshes, uint32
                      kNaMaxMaterials);
   if (vox_mode != VCT_VOX_REF_RASTER2X && vox_mode != VCT_VOX_CONSERVATIVE)
     return set_error(VCT_ERR_INVALID_VALUE, "vox_mode %d", vox_mode);
+  if (n_lights > (uint32_t)kMaxLights)
+    return set_error(VCT_ERR_INVALID_VALUE, "%u lights: this entry point takes at most %d", n_lights, kMaxLights);
   if (!(cube_size > 0.0f) || !std::isfinite(cube_size))
     return set_error(VCT_ERR_INVALID_VALUE, "cube_size %g", (double)cube_size);
   uint64_t total = 0;
   for (uint32_t i = 0; i < n_meshes; ++i) {
     if (meshes[i].n_tris && (!meshes[i].verts || !meshes[i].indices || !meshes[i].tri_material))
       return set_error(VCT_ERR_INVALID_VALUE, "mesh %u: NULL device pointer", i);
+    if (meshes[i].n_tris && !meshes[i].n_verts)
+      return set_error(VCT_ERR_INVALID_VALUE, "mesh %u: %u triangles and no vertices", i, meshes[i].n_tris);
     total += meshes[i].n_tris;
   }
   if (total > kNaMaxPairs)
@@ -128,16 +144,23 @@ extern "C" vct_status vct_voxelize_noalloc(const vct_device_mesh* meshes, uint32
     VCT_CUDA(cudaMemcpyAsync(s->inst, inst, n_meshes * sizeof(DevInstance), cudaMemcpyHostToDevice, st));
   VCT_CUDA(cudaMemcpyAsync(s->material_of_id, g_identity, n_materials * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
   VCT_CUDA(cudaMemsetAsync(&s->status, 0, sizeof(FrameStatus), st));
+  for (uint32_t i = 0; i < n_meshes; ++i) {
+    if (!meshes[i].n_tris) continue;
+    const unsigned blocks = std::min<unsigned>((meshes[i].n_tris + 255) / 256, 1024u);
+    k_count_bad_ids<<<blocks, 256, 0, st>>>(meshes[i].indices, meshes[i].tri_material, meshes[i].n_tris,
+                                            meshes[i].n_verts, n_materials, &s->status.bad_ids);
+  }
 
   SceneParams sp;
   std::memset(&sp, 0, sizeof(sp));
   sp.inst = s->inst;
   sp.materials = materials;
   sp.obj_material = s->material_of_id;
+  sp.n_obj = n_materials;
   sp.n_instances = n_meshes;
   sp.total_tris = (uint32_t)total;
   sp.n_materials = n_materials;
-  sp.n_lights = (int32_t)std::min<uint32_t>(n_lights, kMaxLights);
+  sp.n_lights = (int32_t)n_lights;
   sp.cube_size = cube_size;
   sp.radiance_max = 1.0f;
   for (int i = 0; i < sp.n_lights; ++i) sp.lights[i] = lights[i];
@@ -157,6 +180,10 @@ extern "C" vct_status vct_voxelize_noalloc(const vct_device_mesh* meshes, uint32
   FrameStatus hs;
   VCT_CUDA(cudaMemcpyAsync(&hs, &s->status, sizeof(hs), cudaMemcpyDeviceToHost, st));
   VCT_CUDA(cudaStreamSynchronize(st));
+  if (hs.bad_ids)
+    return set_error(VCT_ERR_INVALID_VALUE,
+                     "%u vertex indices / material ids out of range (indices < n_verts, ids < n_materials)",
+                     hs.bad_ids);
   if (hs.pair_total > kNaMaxPairs)
     return set_error(VCT_ERR_INVALID_VALUE,
                      "the scene needs %u triangle-brick pairs; this entry point holds at most %u (output incomplete)",

@@ -58,6 +58,10 @@ __device__ __forceinline__ float bf_lo(uint32_t v) { return __uint_as_float(v <<
 __device__ __forceinline__ float bf_hi(uint32_t v) { return __uint_as_float(v & 0xffff0000u); }
 
 // Grid index of one corner of level l (dense when the level fits the table).
+// Sparse levels use the spatial hash of the multiresolution hash encoding
+// (Mueller, Evans, Schied, Keller: "Instant Neural Graphics Primitives with a
+// Multiresolution Hash Encoding", SIGGRAPH 2022): per-axis primes 1,
+// 2654435761, 805459861 combined by XOR, modulo the table size.
 __device__ __forceinline__ uint32_t grid_index(const MlpParams& p, int l, int cx, int cy, int cz) {
   const int R = p.res[l];
   if ((p.dense_mask >> l) & 1) {

@@ -98,7 +98,10 @@ __device__ __forceinline__ void load_tri(const SceneParams& sp, uint32_t t, TriL
   const uint32_t lt = t - in.tri_base;
   tl.ok = true;
   for (int k = 0; k < 3; ++k) {
-    const uint32_t vi = __ldg(in.indices + 3 * (size_t)lt + k);
+    // Indices and material ids of host-side meshes are checked when they are
+    // loaded; those of caller-owned device meshes are clamped here (and
+    // counted by the caller's entry point), so that no id reads out of bounds.
+    const uint32_t vi = min(__ldg(in.indices + 3 * (size_t)lt + k), in.n_verts - 1u);
     const float4* vp = reinterpret_cast<const float4*>(in.verts + vi);
     const float4 a = __ldg(vp), b = __ldg(vp + 1);
     for (int r = 0; r < 3; ++r) {
@@ -109,7 +112,7 @@ __device__ __forceinline__ void load_tri(const SceneParams& sp, uint32_t t, TriL
     }
     if (NORMALS) tl.n[k] = normalize(nm_mul(in.NM, a.w, b.x, b.y));
   }
-  if (NORMALS) tl.mat = __ldg(sp.obj_material + __ldg(in.tri_obj + lt));
+  if (NORMALS) tl.mat = __ldg(sp.obj_material + min(__ldg(in.tri_obj + lt), sp.n_obj - 1u));
 }
 
 // ------------------------------------------------ conservative brick test --

@@ -43,6 +43,7 @@ struct SceneParams {
   const DevInstance* inst;
   const vct_material_data* materials;
   const uint32_t* obj_material;   // draw object -> material id
+  uint32_t n_obj;                 // entries of obj_material (0: ids not clamped)
   uint32_t n_instances;
   uint32_t total_tris;
   uint32_t n_materials;
@@ -63,7 +64,8 @@ struct FrameStatus {
   uint32_t async_timeout;   // a bounded wait for a bulk copy gave up (never expected)
   uint32_t heavy_total;     // dense bricks split across CTAs (accumulator slots needed)
   uint32_t extra_total;     // extra chunk work items of the split bricks
-  uint32_t pad[3];
+  uint32_t bad_ids;         // out-of-range vertex indices / material ids (device-side meshes)
+  uint32_t pad[2];
 };
 
 // Dense bricks: a brick with more than kHeavyChunk (triangle, brick) pairs

@@ -43,7 +43,7 @@ EXPORTS = [
     "vct_batch_set_camera", "vct_batch_render", "vct_batch_synchronize", "vct_batch_set_stream",
     "vct_batch_read_frame", "vct_batch_read_voxels", "vct_batch_stage_times", "vct_batch_get_shape",
     "vct_batch_set_shape", "vct_batch_autotune", "vct_set_light_injection", "vct_read_injection_grids",
-    "vct_mlp_set_tensor_kernels",
+    "vct_mlp_set_tensor_kernels", "vct_measure_texture_rate",
 ]
 DIFFUSE_CONES, DIFFUSE_MLP = 0, 1
 MLP_WEIGHTS = 5 * 64 * 64
@@ -138,7 +138,7 @@ def lib() -> C.CDLL:
             "vct_batch_stage_times": (I32, [P, P]), "vct_batch_get_shape": (I32, [P, P]),
             "vct_batch_set_shape": (I32, [P, P]), "vct_batch_autotune": (I32, [P, I32, P, P, P]),
             "vct_set_light_injection": (I32, [P, I32]), "vct_read_injection_grids": (I32, [P, P, P, P]),
-            "vct_mlp_set_tensor_kernels": (I32, [P, I32]),
+            "vct_mlp_set_tensor_kernels": (I32, [P, I32]), "vct_measure_texture_rate": (I32, [I32, U32, P, P]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
@@ -407,6 +407,15 @@ def voxelize_noalloc(meshes, materials_ptr: int, n_materials: int, lights: np.nd
     _check(lib().vct_voxelize_noalloc(C.addressof(arr), len(meshes), C.c_void_p(materials_ptr), int(n_materials),
                                       l.ctypes.data if l.size else None, l.size, float(cube_size), int(grid_res),
                                       int(vox_mode), C.c_void_p(out_ptr), C.c_void_p(stream or 0)))
+
+
+def measure_texture_rate(kind: int, iters: int = 2048) -> dict:
+    """vct_measure_texture_rate: 3D RGBA8 texture fetches per second of the
+    current device (kind 0: two-level, 1: level-0 trilinear, 2: one level of
+    a mipmapped texture)."""
+    rate, ms = C.c_double(), C.c_double()
+    _check(lib().vct_measure_texture_rate(int(kind), int(iters), C.addressof(rate), C.addressof(ms)))
+    return {"fetches_per_s": rate.value, "ms": ms.value}
 
 
 # --------------------------------------------------------------- Texture3D --
