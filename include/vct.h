@@ -314,6 +314,26 @@ vct_status vct_mlp_set_tensor_kernels(vct_renderer* r, int32_t use_tcgen05);
 vct_status vct_mlp_train_samples(vct_renderer* r, const float* samples, uint32_t n,
                                  const vct_mlp_desc* d, vct_mlp_report* report);
 
+/* The judge of the learned term: a frame that evaluates the network also
+ * traces the nine diffuse cones (texture-unit sampler) at one pixel of every
+ * stride x stride tile (the pixel within the tile changes from frame to
+ * frame) and compares them with the network's prediction (PSNR over the
+ * three channels, peak 1).  Below min_psnr_db the frame is rendered again
+ * with the cones before render() returns, and later frames keep the cones
+ * (vct_set_diffuse_mode(VCT_DIFFUSE_MLP) after training again re-enables
+ * the network).  stride 0 turns the judge off; default 8 and 40 dB. */
+vct_status vct_mlp_set_judge(vct_renderer* r, int32_t stride, float min_psnr_db);
+typedef struct {
+  float last_psnr_db;     /* judge's PSNR of the last judged frame (-1: none) */
+  uint32_t judged_pixels; /* pixels it compared                              */
+  uint32_t fallbacks;     /* frames it sent back to the cones                */
+  int32_t diffuse_mode;   /* VCT_DIFFUSE_* now in effect                     */
+  int32_t stride;
+  float min_psnr_db;
+  uint32_t reserved[4];
+} vct_mlp_judge_report;
+vct_status vct_mlp_get_judge(vct_renderer* r, vct_mlp_judge_report* out);
+
 /* ------------------------------------------ allocation-free voxelizer --- */
 
 /* No counterpart in the reference: an engine addition for callers that

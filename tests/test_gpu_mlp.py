@@ -157,6 +157,7 @@ def test_learned_diffuse_replaces_cones(vct):
     ids = vct.load_scene(r, scene)
     r.set_voxel_view_dir(7, 0.0)
     r.set_rendering_phases(False, True, False, False)  # diffuse indirect only
+    r.set_mlp_judge(0)  # the network's own output, also when it is poor
 
     def frame():
         vct.queue_scene(r, scene, ids)
@@ -205,6 +206,7 @@ def test_learned_diffuse_on_the_raster_stream(vct, tmp_path):
     b.mlp_load(path)
     frames = []
     for r, ids in ((a, ids_a), (b, ids_b)):
+        r.set_mlp_judge(0)  # a 20-step network: compare its output, not the fallback
         r.set_diffuse_mode(vct.DIFFUSE_MLP)
         vct.queue_scene(r, scene, ids)
         r.render()
@@ -214,3 +216,55 @@ def test_learned_diffuse_on_the_raster_stream(vct, tmp_path):
     np.testing.assert_array_equal(frames[0], frames[1])
     a.close()
     b.close()
+
+
+def test_judge_sends_a_stale_network_back_to_the_cones(vct):
+    """The cone tracer judges the learned term: trained on one light, the
+    network matches its cones there; with the light moved (the voxels are lit
+    anew, the network still predicts the old light) the judge's PSNR drops,
+    and with a threshold between the two the moved-light frame is rendered
+    with the cones again -- identical to a cone-traced frame -- and later
+    frames keep the cones until the network is re-enabled."""
+    w, h = 96, 64
+    scene = scenes.scene_small(width=w, height=h)
+    r = vct.Renderer(w, h, grid_res=64, keep_float_frame=1)
+    ids = vct.load_scene(r, scene)
+    r.set_voxel_view_dir(7, 0.0)
+    moved = scene.lights.copy()
+    moved["position"] = (0.35, 0.1, 0.3)
+    moved["intensity"] = 3.0
+
+    def frame(lights):
+        for mid in ids:
+            r.queue_model(mid)
+        for l in lights:
+            r.queue_point_light(l)
+        r.render()
+        return r.read_frame(vct.FRAME_RGBA32F).copy()
+
+    cones_moved = frame(moved)
+    frame(scene.lights)
+    r.mlp_init(vct.mlp_desc(n_max=256, seed=4))
+    r.mlp_train(vct.mlp_desc(n_max=256, seed=4, steps=600, batch=1 << 16, n_samples=1 << 20))
+    r.set_mlp_judge(2, 0.0)  # judge every frame, never fall back
+    r.set_diffuse_mode(vct.DIFFUSE_MLP)
+    frame(scene.lights)
+    same = r.mlp_judge()
+    frame(moved)
+    stale = r.mlp_judge()
+    print(f"judge PSNR: trained light {same['last_psnr_db']:.1f} dB, moved light {stale['last_psnr_db']:.1f} dB "
+          f"({same['judged_pixels']} / {stale['judged_pixels']} pixels)")
+    assert same["judged_pixels"] > 500 and same["fallbacks"] == 0 and same["diffuse_mode"] == vct.DIFFUSE_MLP
+    assert stale["last_psnr_db"] < same["last_psnr_db"] - 6.0
+    r.set_mlp_judge(2, 0.5 * (same["last_psnr_db"] + stale["last_psnr_db"]))
+    got = frame(moved)
+    rep = r.mlp_judge()
+    assert rep["fallbacks"] == 1 and rep["diffuse_mode"] == vct.DIFFUSE_CONES
+    np.testing.assert_array_equal(got, cones_moved)
+    np.testing.assert_array_equal(frame(moved), cones_moved)  # later frames keep the cones
+    assert r.mlp_judge()["fallbacks"] == 1
+    r.set_diffuse_mode(vct.DIFFUSE_MLP)
+    frame(scene.lights)  # the trained light passes again
+    rep = r.mlp_judge()
+    assert rep["fallbacks"] == 1 and rep["diffuse_mode"] == vct.DIFFUSE_MLP
+    r.close()

@@ -3,6 +3,7 @@
 // scene of the last frame, the Adam training loop, checkpoints, and the
 // evaluation / gradient hooks the tests use.
 #include <cstdio>
+#include <cstring>
 
 #include "renderer_state.h"
 
@@ -227,6 +228,32 @@ extern "C" vct_status vct_set_diffuse_mode(vct_renderer* r, int32_t mode) {
   if (mode == VCT_DIFFUSE_MLP && !r->mlp.trained)
     return set_error(VCT_ERR_INVALID_VALUE, "the learned diffuse term is not trained (vct_mlp_train / vct_mlp_load)");
   r->diffuse_mode = mode;
+  return VCT_OK;
+}
+
+extern "C" vct_status vct_mlp_set_judge(vct_renderer* r, int32_t stride, float min_psnr_db) {
+  clear_error();
+  if (!r) return set_error(VCT_ERR_INVALID_VALUE, "NULL renderer");
+  if (stride < 0 || stride > 256) return set_error(VCT_ERR_INVALID_VALUE, "judge stride %d (0 = off, 1..256)", stride);
+  if (!(min_psnr_db >= 0.0f) || !(min_psnr_db < 200.0f))
+    return set_error(VCT_ERR_INVALID_VALUE, "judge threshold %g dB", (double)min_psnr_db);
+  VCT_CHECK(r->finish());
+  r->judge_stride = stride;
+  r->judge_min_psnr = min_psnr_db;
+  return VCT_OK;
+}
+
+extern "C" vct_status vct_mlp_get_judge(vct_renderer* r, vct_mlp_judge_report* out) {
+  clear_error();
+  if (!r || !out) return set_error(VCT_ERR_INVALID_VALUE, "NULL argument");
+  VCT_CHECK(r->finish());
+  std::memset(out, 0, sizeof(*out));
+  out->last_psnr_db = r->judge_last_psnr;
+  out->judged_pixels = r->judge_last_n;
+  out->fallbacks = r->judge_fallbacks;
+  out->diffuse_mode = r->diffuse_mode;
+  out->stride = r->judge_stride;
+  out->min_psnr_db = r->judge_min_psnr;
   return VCT_OK;
 }
 

@@ -75,6 +75,7 @@ void load_mtl(const std::string& path, std::vector<vct_material_data>& mats, std
   }
   std::string line;
   vct_material_data* m = nullptr;
+  bool has_d = false;  // tinyobjloader: `d` wins over `Tr` in either order
   while (std::getline(f, line)) {
     std::istringstream ss(line);
     std::string tag;
@@ -91,6 +92,7 @@ void load_mtl(const std::string& path, std::vector<vct_material_data>& mats, std
       names[name] = (int)mats.size();
       mats.push_back(d);
       m = &mats.back();
+      has_d = false;
       continue;
     }
     if (!m) continue;
@@ -102,8 +104,8 @@ void load_mtl(const std::string& path, std::vector<vct_material_data>& mats, std
     else if (tag == "Ke") rd3(m->emission);
     else if (tag == "Ns") ss >> m->shininess;
     else if (tag == "Ni") ss >> m->ior;
-    else if (tag == "d") ss >> m->dissolve;
-    else if (tag == "Tr") { float tr; ss >> tr; m->dissolve = 1.0f - tr; }
+    else if (tag == "d") { ss >> m->dissolve; has_d = true; }
+    else if (tag == "Tr") { float tr = 0.0f; ss >> tr; if (!has_d) m->dissolve = 1.0f - tr; }
     else if (tag == "illum") ss >> m->illum;
     else if (tag == "Pr") ss >> m->roughness;
     else if (tag == "Pm") ss >> m->metallic;

@@ -763,7 +763,58 @@ __global__ void __launch_bounds__(256) k_trace_points(MapSet m, int cone_set, fl
   q[11] = d.z;
 }
 
+// The judge of the learned diffuse term (launch_judge_diffuse): one pixel
+// per stride x stride tile, the same visibility and within_cube test as
+// trace_px, the nine cones of trace_diffuse with the texture unit against
+// the network's prediction of them.
+template <bool ISO>
+__global__ void __launch_bounds__(128) k_judge_diffuse(SceneParams sp, MapSet m, TraceParams tp, int W, int H,
+                                                       const float4* __restrict__ gb_pos,
+                                                       const float4* __restrict__ gb_nrm,
+                                                       const float4* __restrict__ net, int stride, int ox, int oy,
+                                                       FrameStatus* __restrict__ status) {
+  const int px = (blockIdx.x * 16 + (threadIdx.x & 15)) * stride + ox;
+  const int py = (blockIdx.y * 8 + (threadIdx.x >> 4)) * stride + oy;
+  float e = 0.0f;
+  uint32_t n = 0;
+  if (px < W && py < H) {
+    const size_t p = (size_t)py * W + px;
+    const float4 g0 = gb_pos[p], g1 = gb_nrm[p];
+    if (__float_as_uint(g1.w) != 0xffffffffu) {
+      const V3 pos = v3(g0.x / sp.cube_size, g0.y / sp.cube_size, g0.z / sp.cube_size) * 0.5f + v3(0.5f, 0.5f, 0.5f);
+      if (fabsf(pos.x) < 1.0f && fabsf(pos.y) < 1.0f && fabsf(pos.z) < 1.0f) {
+        const V3 d = trace_diffuse<VCT_SAMPLER_HW, ISO, VCT_STORAGE_RGBA8>(m, tp.cone_set, pos, v3(g1.x, g1.y, g1.z));
+        const float4 q = net[p];
+        e = (d.x - q.x) * (d.x - q.x) + (d.y - q.y) * (d.y - q.y) + (d.z - q.z) * (d.z - q.z);
+        n = 1;
+      }
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    e += __shfl_xor_sync(0xffffffffu, e, o);
+    n += __shfl_xor_sync(0xffffffffu, n, o);
+  }
+  if ((threadIdx.x & 31) == 0 && n) {
+    atomicAdd(&status->judge_sse, e);
+    atomicAdd(&status->judge_n, n);
+  }
+}
+
 }  // namespace
+
+cudaError_t launch_judge_diffuse(const SceneParams& sp, const CameraParams& cp, const MapSet& ms, const TraceParams& tp,
+                                 const float4* gb_pos, const float4* gb_nrm, const float4* net, int stride, int ox,
+                                 int oy, FrameStatus* status, cudaStream_t st) {
+  if (stride < 1) return cudaSuccess;
+  const int tw = (cp.W - ox + stride - 1) / stride, th = (cp.H - oy + stride - 1) / stride;
+  if (tw <= 0 || th <= 0) return cudaSuccess;
+  dim3 grid((tw + 15) / 16, (th + 7) / 8);
+  if (tp.mip_mode == VCT_MIP_ISO)
+    k_judge_diffuse<true><<<grid, 128, 0, st>>>(sp, ms, tp, cp.W, cp.H, gb_pos, gb_nrm, net, stride, ox, oy, status);
+  else
+    k_judge_diffuse<false><<<grid, 128, 0, st>>>(sp, ms, tp, cp.W, cp.H, gb_pos, gb_nrm, net, stride, ox, oy, status);
+  return cudaGetLastError();
+}
 
 cudaError_t launch_trace_points(const SceneParams&, const MapSet& ms, int mip_mode, int cone_set, float* samples,
                                 int n, cudaStream_t st) {

@@ -421,6 +421,17 @@ struct vct_renderer {
   bool last_revoxelized = true;
   // learned diffuse term
   int diffuse_mode = VCT_DIFFUSE_CONES;
+  // The judge of the learned term: frames that evaluate the network also
+  // trace the nine cones at one pixel per judge_stride^2 tile and compare;
+  // below judge_min_psnr the frame is rendered again with the cones and
+  // later frames keep the cones until the network is trained again.
+  int judge_stride = 8;
+  float judge_min_psnr = 40.0f;
+  uint32_t judge_frame = 0;
+  bool judge_pending = false;
+  float judge_last_psnr = -1.0f;
+  uint32_t judge_last_n = 0;
+  uint32_t judge_fallbacks = 0;
   MlpState mlp;
   DevBuf<float4> diffuse_px;
   SceneParams last_sp;  // scene of the last encoded frame (training samples come from it)
@@ -733,6 +744,15 @@ struct vct_renderer {
     VCT_CUDA(cudaEventRecord(ev[3], stream));
     VCT_CUDA(launch_trace(sp, cp, ms, tp, gb_pos.p, gb_nrm.p, frame.p, cfg.keep_float_frame ? frame_f32.p : nullptr,
                           stream, &launches));
+    judge_pending = tp.diffuse_in != nullptr && judge_stride > 0;
+    if (judge_pending) {
+      const int ox = (int)((judge_frame * 5u) % (uint32_t)judge_stride);
+      const int oy = (int)((judge_frame * 3u) % (uint32_t)judge_stride);
+      ++judge_frame;
+      VCT_CUDA(launch_judge_diffuse(sp, cp, ms, tp, gb_pos.p, gb_nrm.p, tp.diffuse_in, judge_stride, ox, oy,
+                                    d_status.p, stream));
+      ++launches;
+    }
     last_sp = sp;
     have_sp = true;
     VCT_CUDA(cudaEventRecord(ev[4], stream));
@@ -765,6 +785,20 @@ struct vct_renderer {
       if (s.bigtri_total > bin_big_cap) {
         VCT_CHECK(grow_bin_big(s.bigtri_total + s.bigtri_total / 4 + 256));
         redo = true;
+      }
+      if (!redo && judge_pending) {
+        judge_pending = false;
+        if (s.judge_n) {
+          const double mse = (double)s.judge_sse / (3.0 * s.judge_n);
+          judge_last_psnr = mse > 0.0 ? (float)(10.0 * std::log10(1.0 / mse)) : 999.0f;
+          judge_last_n = s.judge_n;
+          if (judge_last_psnr < judge_min_psnr) {
+            // the network no longer predicts its cones: fall back to them
+            diffuse_mode = VCT_DIFFUSE_CONES;
+            ++judge_fallbacks;
+            redo = true;
+          }
+        }
       }
       if (!redo) return VCT_OK;
       if (!have_last) return VCT_OK;

@@ -65,7 +65,8 @@ struct FrameStatus {
   uint32_t heavy_total;     // dense bricks split across CTAs (accumulator slots needed)
   uint32_t extra_total;     // extra chunk work items of the split bricks
   uint32_t bad_ids;         // out-of-range vertex indices / material ids (device-side meshes)
-  uint32_t pad[2];
+  float judge_sse;          // learned diffuse term vs its nine cones: summed squared error
+  uint32_t judge_n;         //   over this many judged pixels (3 channels each)
 };
 
 // Dense bricks: a brick with more than kHeavyChunk (triangle, brick) pairs
@@ -370,6 +371,13 @@ cudaError_t launch_mlp_eval(const MlpParams& p, const float* samples, int n, flo
 cudaError_t launch_tri_area(const SceneParams& sp, float* area, cudaStream_t st);
 cudaError_t launch_sample_surface(const SceneParams& sp, const float* cdf, int n, uint64_t seed, float* samples,
                                   cudaStream_t st);
+// The judge of the learned diffuse term: at one pixel of every stride x
+// stride tile (tile offset (ox, oy)), trace_diffuse's cones against the
+// network's value in `net`; adds the squared error and the pixel count to
+// status->judge_sse / judge_n.
+cudaError_t launch_judge_diffuse(const SceneParams& sp, const CameraParams& cp, const MapSet& ms, const TraceParams& tp,
+                                 const float4* gb_pos, const float4* gb_nrm, const float4* net, int stride, int ox,
+                                 int oy, FrameStatus* status, cudaStream_t st);
 cudaError_t launch_trace_points(const SceneParams& sp, const MapSet& ms, int mip_mode, int cone_set, float* samples,
                                 int n, cudaStream_t st);
 

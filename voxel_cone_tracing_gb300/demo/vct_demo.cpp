@@ -4,7 +4,13 @@
 // of swapped to a GLFW window.
 //
 //   vct_demo [--assets DIR] [--out PREFIX] [--frames N] [--width W]
-//            [--height H] [--grid N] [--rotate RAD]
+//            [--height H] [--grid N] [--rotate RAD] [--sampler hw|exact]
+//            [--dump-matrices FILE]
+//
+// --sampler selects the texture unit (default) or FP32 software filtering;
+// --dump-matrices writes, per frame, the view, projection and the object's
+// model matrix the frame used (48 floats, column-major, text) so that a
+// checker can rebuild the same frame.
 //
 // Scene (main.cpp:85-118): assets/CornellBox-Glossy.obj at the identity, and
 // assets/suzanne.obj at (0, 1.1, -0.5), scale 0.3, with the glossy
@@ -206,6 +212,8 @@ int main(int argc, char** argv) {
   std::string assets, out = "vct_frame";
   int frames = 1, width = 800, height = 600, grid = 128;  // main.cpp:28-29; renderer.cpp:146
   float rot_step = 0.05f;
+  int sampler = VCT_SAMPLER_HW;
+  std::string dump;
   for (int i = 1; i < argc; ++i) {
     const std::string a = argv[i];
     auto next = [&]() -> const char* {
@@ -219,12 +227,20 @@ int main(int argc, char** argv) {
     else if (a == "--height") height = std::atoi(next());
     else if (a == "--grid") grid = std::atoi(next());
     else if (a == "--rotate") rot_step = (float)std::atof(next());
+    else if (a == "--dump-matrices") dump = next();
+    else if (a == "--sampler") {
+      const std::string v = next();
+      if (v == "hw") sampler = VCT_SAMPLER_HW;
+      else if (v == "exact") sampler = VCT_SAMPLER_EXACT;
+      else { std::fprintf(stderr, "--sampler takes hw or exact\n"); return 2; }
+    }
     else { std::fprintf(stderr, "unknown argument %s\n", a.c_str()); return 2; }
   }
 
   vct_config cfg;
   vct_config_default(&cfg);
   cfg.grid_res = grid;
+  cfg.sampler = sampler;
   vct::Renderer renderer(width, height, &cfg);
   if (renderer.last_status() != VCT_OK) {
     std::fprintf(stderr, "vct_demo: %s\n", vct_last_error());
@@ -274,12 +290,21 @@ int main(int argc, char** argv) {
   ceiling_light.color[0] = ceiling_light.color[1] = ceiling_light.color[2] = 1.0f;
   ceiling_light.intensity = 1.0f;
 
+  FILE* dump_fp = nullptr;
+  if (!dump.empty() && !(dump_fp = std::fopen(dump.c_str(), "w"))) {
+    std::fprintf(stderr, "vct_demo: cannot write %s\n", dump.c_str());
+    return 1;
+  }
   std::vector<uint8_t> rgba((size_t)width * height * 4);
   for (int f = 0; f < frames; ++f) {
     renderer.set_voxel_view_dir(7, 0.0f);
     const mat4 m = mul(mul(translate(dynamic_object_position), rotate_y(dynamic_object_rot)),
                        scale(dynamic_object_scale));  // main.cpp:369-372
     renderer.set_model_transform(dynamic_object, m);
+    if (dump_fp) {
+      for (const mat4* q : {(const mat4*)&view, (const mat4*)&proj, &m})
+        for (int k = 0; k < 16; ++k) std::fprintf(dump_fp, "%.9g%c", q->m[k], k == 15 ? '\n' : ' ');
+    }
     renderer.set_model_transform(box, mat4::identity());
     renderer.queue_model(box);
     renderer.queue_model(dynamic_object);
@@ -300,6 +325,10 @@ int main(int argc, char** argv) {
     std::printf("frame %d: voxelize %.3f ms, mipmap %.3f ms, gbuffer %.3f ms, trace %.3f ms -> %s%s\n", f,
                 t.voxelize, t.mipmap, t.gbuffer, t.trace, out.c_str(), name);
     dynamic_object_rot += rot_step;
+  }
+  if (dump_fp && std::fclose(dump_fp) != 0) {
+    std::fprintf(stderr, "vct_demo: cannot write %s\n", dump.c_str());
+    return 1;
   }
   return 0;
 }

@@ -43,7 +43,7 @@ EXPORTS = [
     "vct_batch_set_camera", "vct_batch_render", "vct_batch_synchronize", "vct_batch_set_stream",
     "vct_batch_read_frame", "vct_batch_read_voxels", "vct_batch_stage_times", "vct_batch_get_shape",
     "vct_batch_set_shape", "vct_batch_autotune", "vct_set_light_injection", "vct_read_injection_grids",
-    "vct_mlp_set_tensor_kernels", "vct_measure_texture_rate",
+    "vct_mlp_set_tensor_kernels", "vct_measure_texture_rate", "vct_mlp_set_judge", "vct_mlp_get_judge",
 ]
 DIFFUSE_CONES, DIFFUSE_MLP = 0, 1
 MLP_WEIGHTS = 5 * 64 * 64
@@ -58,6 +58,12 @@ class MLPDesc(C.Structure):
 class MLPReport(C.Structure):
     _fields_ = [("loss_first", C.c_float), ("loss_last", C.c_float), ("ms_samples", C.c_float),
                 ("ms_train", C.c_float), ("steps", C.c_uint32), ("n_samples", C.c_uint32)]
+
+
+class JudgeReport(C.Structure):
+    _fields_ = [("last_psnr_db", C.c_float), ("judged_pixels", C.c_uint32), ("fallbacks", C.c_uint32),
+                ("diffuse_mode", C.c_int32), ("stride", C.c_int32), ("min_psnr_db", C.c_float),
+                ("reserved", C.c_uint32 * 4)]
 
 
 def mlp_desc(**kw) -> MLPDesc:
@@ -139,6 +145,7 @@ def lib() -> C.CDLL:
             "vct_batch_set_shape": (I32, [P, P]), "vct_batch_autotune": (I32, [P, I32, P, P, P]),
             "vct_set_light_injection": (I32, [P, I32]), "vct_read_injection_grids": (I32, [P, P, P, P]),
             "vct_mlp_set_tensor_kernels": (I32, [P, I32]), "vct_measure_texture_rate": (I32, [I32, U32, P, P]),
+            "vct_mlp_set_judge": (I32, [P, I32, F]), "vct_mlp_get_judge": (I32, [P, P]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
@@ -366,6 +373,16 @@ class Renderer:
         _check(lib().vct_mlp_gradients(self._r, s.ctypes.data, s.shape[0], loss.ctypes.data, dw.ctypes.data,
                                        dt.ctypes.data))
         return float(loss[0]), dw, dt
+
+    def set_mlp_judge(self, stride: int, min_psnr_db: float = 40.0) -> None:
+        """vct_mlp_set_judge: cone-traced check of the learned term at one
+        pixel per stride x stride tile (0 = off)."""
+        _check(lib().vct_mlp_set_judge(self._r, int(stride), float(min_psnr_db)))
+
+    def mlp_judge(self) -> dict:
+        rep = JudgeReport()
+        _check(lib().vct_mlp_get_judge(self._r, C.addressof(rep)))
+        return {k: getattr(rep, k) for k, _ in JudgeReport._fields_ if k != "reserved"}
 
     def mlp_set_tensor_kernels(self, use_tcgen05: bool) -> None:
         _check(lib().vct_mlp_set_tensor_kernels(self._r, int(bool(use_tcgen05))))
