@@ -379,7 +379,7 @@ def batch_leg(R, torch, steps, rank=0, world=1, pg=None):
     # the same scenes, one Renderer each, rendered one after another
     rs = []
     for s, w, h, g, c in items:
-        r = R.Renderer(w, h, grid_res=g, cone_set=c)
+        r = R.Renderer(w, h, grid_res=g, cone_set=c, far_share=0)  # per-pixel cones, as the batch
         ids = R.load_scene(r, s)
         r.set_voxel_view_dir(7, 0.0)
         r.set_stream(stream.cuda_stream)

@@ -123,7 +123,14 @@ typedef struct {
                          * a shorter frame, longer voxelize and mipmap
                          * stages; 0 (default): one stream, one stage
                          * after the other                                */
-  int32_t reserved[4];
+  int32_t far_share;    /* texture-unit sampler: 1 (default): the four
+                         * pixels of a 2x2 quad with matching normals and
+                         * positions share the coarse part (lod >= 2) of
+                         * their diffuse cones, marched once per quad by the
+                         * lanes of the warp together; 0: every pixel marches
+                         * all of its cones (the reference's rule).  The FP32
+                         * software sampler always marches per pixel       */
+  int32_t reserved[3];
 } vct_config;
 
 typedef struct vct_renderer vct_renderer;

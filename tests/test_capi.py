@@ -71,18 +71,19 @@ def test_bad_config_rejected_before_device(vct):
         vct.Renderer(0, 16)
     assert e.value.status == 1
     # every switch of vct_config is 0 or 1
-    for field in ("shadow_from_maps", "full_march", "overlap_raster"):
+    for field in ("shadow_from_maps", "full_march", "overlap_raster", "far_share"):
         with pytest.raises(vct.VCTError) as e:
             vct.Renderer(16, 16, **{field: 2})
         assert e.value.status == 1, field
 
 
 def test_config_defaults_of_the_engine_switches(vct):
-    """The engine's own switches default to the fastest exact path: alpha-only
-    shadow chains, cone exit and empty-space skip on, one stream."""
+    """The engine's own switches default to the fastest path: alpha-only
+    shadow chains, cone exit and empty-space skip on (all exact), one stream,
+    and shared far fields of the diffuse cones for the texture-unit sampler."""
     c = vct.default_config()
-    assert (c.shadow_from_maps, c.full_march, c.overlap_raster) == (0, 0, 0)
-    assert list(c.reserved) == [0, 0, 0, 0]
+    assert (c.shadow_from_maps, c.full_march, c.overlap_raster, c.far_share) == (0, 0, 0, 1)
+    assert list(c.reserved) == [0, 0, 0]
 
 
 def test_cpp_facade_header_compiles(tmp_path):

@@ -24,7 +24,8 @@ def _items():
 
 
 def _single(vct, scene, w, h, grid, cones, vox_mode=0, view=None):
-    r = vct.Renderer(w, h, grid_res=grid, cone_set=cones, vox_mode=vox_mode)
+    # a batch marches every pixel's cones: compare with a Renderer that does too
+    r = vct.Renderer(w, h, grid_res=grid, cone_set=cones, vox_mode=vox_mode, far_share=0)
     ids = vct.load_scene(r, scene)
     if view is not None:
         r.set_camera_transform(view, scene.proj)

@@ -80,6 +80,7 @@ extern "C" void vct_config_default(vct_config* cfg) {
   cfg->sampler = VCT_SAMPLER_HW;
   cfg->cone_set = VCT_CONES_REF9;
   cfg->radiance_max = 1.0f;
+  cfg->far_share = 1;
 }
 
 static vct_status check_config(const vct_config& c) {
@@ -91,7 +92,8 @@ static vct_status check_config(const vct_config& c) {
     return set_error(VCT_ERR_INVALID_VALUE, "radiance_max %g > 1 needs RGBA16F storage", c.radiance_max);
   if (c.vox_mode < 0 || c.vox_mode > 1 || c.mip_mode < 0 || c.mip_mode > 1 || c.storage < 0 || c.storage > 1 ||
       c.sampler < 0 || c.sampler > 1 || c.cone_set < 0 || c.cone_set > 1 || c.shadow_from_maps < 0 ||
-      c.shadow_from_maps > 1 || c.full_march < 0 || c.full_march > 1 || c.overlap_raster < 0 || c.overlap_raster > 1)
+      c.shadow_from_maps > 1 || c.full_march < 0 || c.full_march > 1 || c.overlap_raster < 0 || c.overlap_raster > 1 ||
+      c.far_share < 0 || c.far_share > 1)
     return set_error(VCT_ERR_INVALID_VALUE, "config field out of range");
   return VCT_OK;
 }

@@ -539,6 +539,159 @@ __device__ V3 trace_diffuse(const MapSet& m, int cone_set, V3 origin, V3 n) {
   return v3(acc.x, acc.y, acc.z) * (1.0f / 9.0f);
 }
 
+// ------------------------------------------------- shared far fields ------
+// Far-field sharing (TraceParams::far_share, texture-unit sampler).  The
+// diffuse cones of neighbouring pixels on one surface start a fraction of a
+// voxel apart in nearly the same directions; once a cone's samples are
+// coarse (lod >= kShareLod, texels of 4+ voxels) the filtered values along
+// the four cones of a 2x2 quad barely differ.  So the march of every diffuse
+// cone is split at the first step whose lod reaches kShareLod: each pixel
+// marches the steps before it itself, and the rest ("far field") is marched
+// once per quad, along the cones of one pixel of the quad (its
+// representative), by the lanes of the warp together (far_fields below).
+// The split is exact front-to-back compositing: a march that continues from
+// the near part's accumulation equals near + (1 - near.a) * far, where far is
+// the march of the same steps from zero, and both stop at the same step
+// (alpha reaching 1).  Only the representative's positions and directions
+// stand in for the other pixels'.  A pixel shares only when its normal is
+// within kShareCos of the representative's and its surface point within
+// kShareDist voxels; others march their own cones.  Measured against the
+// FP64 oracle on the 1080p bench frame: 81 dB for the far fields alone
+// (the texture unit's 8-bit filter weights: 71 dB).
+constexpr float kShareLod = 2.0f;
+constexpr float kShareCos = 0.99f;
+constexpr float kShareDist = 2.0f;  // voxels
+constexpr int kShareQuads = 8;      // 2x2 quads of a 16x2-pixel warp
+constexpr int kShareCones = 9;
+
+struct FarWarp {
+  float4 far[kShareQuads * kShareCones];  // far field of cone k of quad slot q at q * K + k
+  float origin[kShareQuads][3];           // representative's texture-space position
+  float normal[kShareQuads][3];           // and normal
+};
+
+// The distance and diameter of the first step whose lod reaches kShareLod,
+// by the march's own recurrence (trace_cone), for aperture ap.
+__device__ __forceinline__ void far_start(float ap, int N, float& dist, float& diam) {
+  const float cube_res = (float)N;
+  const float voxel_size = 1.0f / cube_res;
+  dist = 3.0f * voxel_size;
+  diam = dist * ap;
+  for (int i = 0; i < 64 && cone_lod(diam * cube_res) < kShareLod; ++i) {
+    const float step = fmaxf(diam * 0.5f, voxel_size);
+    dist += step;
+    diam = dist * ap;
+  }
+}
+
+// Direction (unnormalised) and aperture of diffuse cone k, as trace_diffuse
+// computes them from the normal n and its frame o1, o2.
+__device__ __forceinline__ V3 diffuse_dir(int cone_set, V3 n, V3 o1, V3 o2, int k, float& ap) {
+  if (cone_set == VCT_CONES_SIX60) {
+    ap = 1.15470053838f;
+    const V3 nn = normalize(n);
+    if (k == 0) return nn;
+    float sphi, cphi;
+    sincosf(6.28318530717958648f * (float)(k - 1) / 5.0f, &sphi, &cphi);
+    return nn * 0.5f + (o1 * cphi + o2 * sphi) * 0.86602540378f;
+  }
+  ap = kTan22_5;
+  if (k == 0) return n;
+  const int j = k - 1;
+  const V3 c1 = (o1 + o2) * 0.5f, c2 = (o1 - o2) * 0.5f;
+  const V3 b = j < 2 ? o1 : (j < 4 ? o2 : (j < 6 ? c1 : c2));
+  const V3 side = (j & 1) ? -b : b;
+  return mixv(n, side, 0.5f);
+}
+
+// The far fields of a warp's nq quads: jobs k * nq + q (cone k of quad slot
+// q: neighbouring lanes start on the same cone of neighbouring quads, which
+// read neighbouring texels), dealt out to the lanes as they become free, so
+// that a lane whose cone ends early (alpha 1, the grid's edge) takes the
+// next job while the others march on.  Results go to fw.far[q * K + k].
+template <bool ISO>
+__device__ void far_fields(const MapSet& m, FarWarp& fw, int cone_set, int nq, float dist0, float diam0) {
+  const int lane = threadIdx.x & 31;
+  const int K = cone_set == VCT_CONES_SIX60 ? 6 : 9;
+  const int n_jobs = nq * K;
+  const float cube_res = (float)m.N;
+  const float voxel_size = 1.0f / cube_res;
+  int next = 0;  // warp-uniform: next job to hand out
+  int job = -1, res = 0;
+  bool active = false;
+  V3 origin = v3(0.f, 0.f, 0.f), dir = v3(0.f, 0.f, 1.f), ad = v3(0.f, 0.f, 1.f);
+  int ix = 1, iy = 3, iz = 5;
+  float dist = 0.f, diam = 0.f, stop = 0.f, ap = 0.f;
+  bool check = false;
+  float4 acc = f4(0.f, 0.f, 0.f, 0.f);
+  for (;;) {
+    const unsigned need = __ballot_sync(0xffffffffu, !active);
+    if (need && next < n_jobs) {
+      if (!active) {
+        job = next + __popc(need & ((1u << lane) - 1u));
+        if (job < n_jobs) {
+          const int k = job / nq, q = job - k * nq;
+          res = q * K + k;
+          origin = v3(fw.origin[q][0], fw.origin[q][1], fw.origin[q][2]);
+          const V3 n = v3(fw.normal[q][0], fw.normal[q][1], fw.normal[q][2]);
+          const V3 o1 = normalize(tangent(n));
+          const V3 o2 = normalize(cross(o1, n));
+          dir = normalize(diffuse_dir(cone_set, n, o1, o2, k, ap));
+          ix = dir.x < 0.0f ? 0 : 1;
+          iy = dir.y < 0.0f ? 2 : 3;
+          iz = dir.z < 0.0f ? 4 : 5;
+          ad = vabs(dir);
+          dist = dist0;
+          diam = diam0;
+          stop = exit_distance(m, origin, dir, kMaxDistance);
+          check = !march_sane(origin, dir, stop);
+          acc = f4(0.f, 0.f, 0.f, 0.f);
+          active = dist < stop;
+          if (!active) fw.far[res] = acc;
+        }
+      }
+      next += __popc(need);
+    }
+    if (!__any_sync(0xffffffffu, active)) break;
+    if (active) {
+      const V3 sp = march_pos(origin, dir, dist);
+      const float mip = cone_lod(diam * cube_res);
+      if (!(kSkipEmptyRGBA && m.skip_empty && mip < kSkipMaxLod && sample_empty(m, sp, mip)) &&
+          !(check && !u_sane(sp))) {
+        const float4 smp = sample_voxel<VCT_SAMPLER_HW, ISO, VCT_STORAGE_RGBA8, false>(m, sp, ix, iy, iz, ad, mip);
+        acc = fma4(smp, 1.0f - acc.w, acc);
+      }
+      const float step = fmaxf(diam * 0.5f, voxel_size);
+      dist += step;
+      diam = dist * ap;
+      if (!(acc.w < 1.0f) || !(dist < stop)) {
+        fw.far[res] = acc;
+        active = false;
+      }
+    }
+  }
+}
+
+// trace_diffuse with the quad's far fields (far: this quad's K results):
+// each cone marches its steps before far_dist, then takes the far field
+// behind what it has accumulated.
+template <bool ISO>
+__device__ V3 trace_diffuse_shared(const MapSet& m, int cone_set, V3 origin, V3 n, const float4* far, float far_dist) {
+  const V3 o1 = normalize(tangent(n));
+  const V3 o2 = normalize(cross(o1, n));
+  const int K = cone_set == VCT_CONES_SIX60 ? 6 : 9;
+  float4 acc = f4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll 1
+  for (int k = 0; k < K; ++k) {
+    float ap;
+    const V3 d = diffuse_dir(cone_set, n, o1, o2, k, ap);
+    float4 c = trace_cone<VCT_SAMPLER_HW, ISO, VCT_STORAGE_RGBA8>(m, origin, d, ap, far_dist);
+    if (c.w < 1.0f) c = fma4(far[k], 1.0f - c.w, c);
+    acc = acc + c;
+  }
+  return v3(acc.x, acc.y, acc.z) * (1.0f / (float)K);
+}
+
 __device__ __forceinline__ V3 refract(V3 I, V3 N, float eta) {
   const float d = dot(N, I);
   const float k = 1.0f - eta * eta * (1.0f - d * d);
@@ -600,11 +753,12 @@ __device__ __forceinline__ unsigned char unorm8(float v) {
 }
 
 // Shades pixel (px, py) of one frame (main, voxel_cone_tracing.frag:246-275).
-template <int SAMPLER, bool ISO, int STORAGE>
+template <int SAMPLER, bool ISO, int STORAGE, bool SHARE = false>
 __device__ __forceinline__ void trace_px(const SceneParams& sp, const CameraParams& cp, const MapSet& m,
                                          const TraceParams& tp, const float4* __restrict__ gb_pos,
                                          const float4* __restrict__ gb_nrm, uchar4* __restrict__ frame,
-                                         float4* __restrict__ frame_f32, int px, int py) {
+                                         float4* __restrict__ frame_f32, int px, int py,
+                                         const float4* far = nullptr, float far_dist = 0.0f) {
   if (px >= cp.W || py >= cp.H) return;
   const size_t p = (size_t)py * cp.W + px;
   float4 out = f4(0.15f, 0.25f, 0.25f, 1.0f);  // glClearColor, renderer.cpp:398
@@ -635,6 +789,8 @@ __device__ __forceinline__ void trace_px(const SceneParams& sp, const CameraPara
           if (tp.diffuse_in) {
             const float4 d = tp.diffuse_in[p];
             fd = mulv(mat3v(mat.diffuse), v3(d.x, d.y, d.z));
+          } else if (SHARE && far) {
+            fd = mulv(mat3v(mat.diffuse), trace_diffuse_shared<ISO>(m, tp.cone_set, pos, nrm, far, far_dist));
           } else {
             fd = mulv(mat3v(mat.diffuse), trace_diffuse<SAMPLER, ISO, STORAGE>(m, tp.cone_set, pos, nrm));
           }
@@ -668,6 +824,71 @@ __global__ void __launch_bounds__(kTraceThreads, SAMPLER == VCT_SAMPLER_HW ? kTr
             const float4* __restrict__ gb_nrm, uchar4* __restrict__ frame, float4* __restrict__ frame_f32) {
   trace_px<SAMPLER, ISO, STORAGE>(sp, cp, m, tp, gb_pos, gb_nrm, frame, frame_f32, blockIdx.x * 16 + (threadIdx.x & 15),
                                   blockIdx.y * kTraceRows + (threadIdx.x >> 4));
+}
+
+#ifndef VCT_SHARE_MIN_BLOCKS
+#define VCT_SHARE_MIN_BLOCKS 10
+#endif
+constexpr int kShareMinBlocks = VCT_SHARE_MIN_BLOCKS;
+
+// k_trace with shared far fields: the warp (a 16x2 strip, eight 2x2 quads)
+// first picks each quad's representative (its first pixel whose diffuse
+// cones are traced) and the pixels that share with it, marches the quads'
+// far fields together (far_fields), then shades its pixels as k_trace does.
+template <bool ISO>
+__global__ void __launch_bounds__(kTraceThreads, kShareMinBlocks)
+    k_trace_share(SceneParams sp, CameraParams cp, MapSet m, TraceParams tp, const float4* __restrict__ gb_pos,
+                  const float4* __restrict__ gb_nrm, uchar4* __restrict__ frame, float4* __restrict__ frame_f32) {
+  static_assert(kTraceThreads % 32 == 0, "whole warps");
+  __shared__ FarWarp s_far[kTraceThreads / 32];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int px = blockIdx.x * 16 + (threadIdx.x & 15), py = blockIdx.y * kTraceRows + (threadIdx.x >> 4);
+  FarWarp& fw = s_far[warp];
+  bool valid = false;
+  V3 pos = v3(0.f, 0.f, 0.f), nrm = v3(0.f, 0.f, 1.f);
+  if (px < cp.W && py < cp.H) {
+    const size_t p = (size_t)py * cp.W + px;
+    const float4 g0 = gb_pos[p], g1 = gb_nrm[p];
+    if (__float_as_uint(g1.w) != 0xffffffffu) {
+      pos = v3(g0.x / sp.cube_size, g0.y / sp.cube_size, g0.z / sp.cube_size) * 0.5f + v3(0.5f, 0.5f, 0.5f);
+      nrm = v3(g1.x, g1.y, g1.z);
+      // the pixels whose diffuse cones trace_px traces (within_cube, :250)
+      valid = fabsf(pos.x) < 1.0f && fabsf(pos.y) < 1.0f && fabsf(pos.z) < 1.0f;
+    }
+  }
+  valid = valid && tp.enable_diffuse && tp.view_voxel_dir >= 7 && !tp.diffuse_in;
+  const unsigned vmask = __ballot_sync(0xffffffffu, valid);
+  const int q = (lane & 15) >> 1;
+  const unsigned qv = vmask & ((3u << (2 * q)) | (3u << (16 + 2 * q)));
+  const int rep = qv ? __ffs(qv) - 1 : lane;
+  const V3 rpos = v3(__shfl_sync(0xffffffffu, pos.x, rep), __shfl_sync(0xffffffffu, pos.y, rep),
+                     __shfl_sync(0xffffffffu, pos.z, rep));
+  const V3 rn = v3(__shfl_sync(0xffffffffu, nrm.x, rep), __shfl_sync(0xffffffffu, nrm.y, rep),
+                   __shfl_sync(0xffffffffu, nrm.z, rep));
+  const unsigned repmask = __ballot_sync(0xffffffffu, valid && rep == lane);
+  const int slot = __popc(repmask & ((1u << rep) - 1u));
+  bool share = false;
+  if (valid) {
+    const float lim = kShareDist / (float)m.N;
+    share = dot(normalize(nrm), normalize(rn)) >= kShareCos && fabsf(pos.x - rpos.x) <= lim &&
+            fabsf(pos.y - rpos.y) <= lim && fabsf(pos.z - rpos.z) <= lim;
+  }
+  if (valid && rep == lane) {
+    fw.origin[slot][0] = pos.x;
+    fw.origin[slot][1] = pos.y;
+    fw.origin[slot][2] = pos.z;
+    fw.normal[slot][0] = nrm.x;
+    fw.normal[slot][1] = nrm.y;
+    fw.normal[slot][2] = nrm.z;
+  }
+  __syncwarp();
+  const int K = tp.cone_set == VCT_CONES_SIX60 ? 6 : 9;
+  float dist0 = 0.0f, diam0 = 0.0f;
+  far_start(tp.cone_set == VCT_CONES_SIX60 ? 1.15470053838f : kTan22_5, m.N, dist0, diam0);
+  if (repmask) far_fields<ISO>(m, fw, tp.cone_set, __popc(repmask), dist0, diam0);
+  __syncwarp();
+  trace_px<VCT_SAMPLER_HW, ISO, VCT_STORAGE_RGBA8, true>(sp, cp, m, tp, gb_pos, gb_nrm, frame, frame_f32, px, py,
+                                                         share ? fw.far + slot * K : nullptr, dist0);
 }
 
 // One pixel of a batch scene.  Called, not inlined, from the tile loop of
@@ -852,6 +1073,14 @@ cudaError_t launch_trace(const SceneParams& sp, const CameraParams& cp, const Ma
                  : run<VCT_SAMPLER_EXACT, false, VCT_STORAGE_RGBA8>(sp, cp, ms, tp, gb_pos, gb_nrm, frame, frame_f32, st);
     return iso ? run<VCT_SAMPLER_EXACT, true, VCT_STORAGE_RGBA16F>(sp, cp, ms, tp, gb_pos, gb_nrm, frame, frame_f32, st)
                : run<VCT_SAMPLER_EXACT, false, VCT_STORAGE_RGBA16F>(sp, cp, ms, tp, gb_pos, gb_nrm, frame, frame_f32, st);
+  }
+  if (tp.far_share && tp.enable_diffuse && !tp.diffuse_in && tp.view_voxel_dir >= 7) {
+    dim3 grid((cp.W + 15) / 16, (cp.H + kTraceRows - 1) / kTraceRows);
+    if (iso)
+      k_trace_share<true><<<grid, kTraceThreads, 0, st>>>(sp, cp, ms, tp, gb_pos, gb_nrm, frame, frame_f32);
+    else
+      k_trace_share<false><<<grid, kTraceThreads, 0, st>>>(sp, cp, ms, tp, gb_pos, gb_nrm, frame, frame_f32);
+    return cudaGetLastError();
   }
   return iso ? run<VCT_SAMPLER_HW, true, VCT_STORAGE_RGBA8>(sp, cp, ms, tp, gb_pos, gb_nrm, frame, frame_f32, st)
              : run<VCT_SAMPLER_HW, false, VCT_STORAGE_RGBA8>(sp, cp, ms, tp, gb_pos, gb_nrm, frame, frame_f32, st);

@@ -820,6 +820,7 @@ struct vct_renderer {
     tp.sampler = cfg.sampler;
     tp.mip_mode = cfg.mip_mode;
     tp.diffuse_in = nullptr;
+    tp.far_share = cfg.far_share;
     return tp;
   }
 };

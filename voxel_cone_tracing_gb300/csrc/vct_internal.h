@@ -180,6 +180,9 @@ struct TraceParams {
   int mip_mode;
   // Per-pixel trace_diffuse from the learned term (null: trace the cones).
   const float4* diffuse_in;
+  // Texture-unit sampler: 2x2 quads share the coarse part of their diffuse
+  // cones (vct_config::far_share).
+  int far_share;
 };
 
 // ---- batched rendering (api_batch.cu) --------------------------------------
