@@ -47,10 +47,16 @@ CPU_WARMUP_ROW_STRIDE = 64   # warm-up frames of the CPU arm trace every 64th ro
 # skips the steps beyond the grid (exact early exit), the empty steps (exact
 # empty-space skip), the maps whose anisotropic weight is exactly 0, and
 # reads packed alpha-only chains for the shadow cones: 265.6 two-level
-# (quadrilinear) and 83.6 one-level (trilinear) RGBA8 fetches per pixel.
+# (quadrilinear) and 83.5 one-level (trilinear) RGBA8 fetches per pixel when
+# every pixel marches all its cones (far_share 0).  With shared far fields
+# (far_share 1, the default; 2x2 quads march their diffuse cones after the
+# first step once), counted over whole quads: 87.25 two-level and 34.0
+# one-level fetches per pixel.
 TRACE_FETCHES_PER_PIXEL_REF = 778.9
-TRACE_FETCH_QUAD_PER_PIXEL = 265.6
-TRACE_FETCH_TRI_PER_PIXEL = 83.6
+TRACE_FETCH_QUAD_PER_PIXEL = 87.25
+TRACE_FETCH_TRI_PER_PIXEL = 34.0
+TRACE_FETCH_QUAD_PER_PIXEL_NOSHARE = 265.6
+TRACE_FETCH_TRI_PER_PIXEL_NOSHARE = 83.5
 INSTANCE_RECORD_BYTES = 144   # one per queued model (DevInstance)
 STATUS_BYTES = 48             # per-frame status read back with the frame
 
@@ -550,6 +556,8 @@ def run_ours(args):
                      "traffic": traffic, "peak_source": "measured in this run (vct_measure_texture_rate)",
                      "fetches": {"two_level_per_pixel": TRACE_FETCH_QUAD_PER_PIXEL,
                                  "one_level_per_pixel": TRACE_FETCH_TRI_PER_PIXEL,
+                                 "per_pixel_cones": {"two_level_per_pixel": TRACE_FETCH_QUAD_PER_PIXEL_NOSHARE,
+                                                     "one_level_per_pixel": TRACE_FETCH_TRI_PER_PIXEL_NOSHARE},
                                  "reference_rule_per_pixel": TRACE_FETCHES_PER_PIXEL_REF,
                                  "two_level_equivalents_per_frame": round(q_equiv),
                                  "unit": "3D RGBA8 texture fetches (achieved/peak in two-level equivalents)"},

@@ -57,7 +57,8 @@ class _Params(C.Structure):
                 ("enable_direct", C.c_int32), ("enable_diffuse", C.c_int32),
                 ("enable_specular", C.c_int32), ("enable_shadow", C.c_int32),
                 ("view_voxel_dir", C.c_int32), ("view_voxel_lod", C.c_float),
-                ("cone_set", C.c_int32), ("threads", C.c_int32), ("radiance_max", C.c_float)]
+                ("cone_set", C.c_int32), ("threads", C.c_int32), ("radiance_max", C.c_float),
+                ("far_share", C.c_int32)]
 
 
 _lib = None
@@ -116,7 +117,7 @@ class Params:
     def __init__(self, grid_res=64, width=64, height=64, vox_mode=VOX_REF_RASTER2X, mip_mode=MIP_ANISO,
                  enable_direct=True, enable_diffuse=True, enable_specular=True, enable_shadow=True,
                  view_voxel_dir=7, view_voxel_lod=0.0, cone_set=CONES_REF9, threads=None, levels=None,
-                 radiance_max=1.0):
+                 radiance_max=1.0, far_share=0):
         self.grid_res, self.width, self.height = grid_res, width, height
         self.levels = levels if levels is not None else levels_for(grid_res)
         self.vox_mode, self.mip_mode = vox_mode, mip_mode
@@ -126,6 +127,7 @@ class Params:
         self.cone_set = cone_set
         self.threads = threads if threads else (os.cpu_count() or 1)
         self.radiance_max = radiance_max
+        self.far_share = far_share
 
     def c(self) -> _Params:
         p = _Params()
@@ -319,7 +321,8 @@ def trace_stats(scene, params: Params, level0, chains, gb: dict, row_stride: int
     empty (no fetch; `empty_lt1` of them with lod < 1) per cone class over
     the traced rows, and the single-level / two-level texture fetches the
     engine's texture-unit path issues for the remaining steps (`fetch_tri`,
-    `fetch_quad`: the algorithmic texture work of the trace)."""
+    `fetch_quad`: the algorithmic texture work of the trace).  A negative
+    row_stride samples pairs of rows (whole 2x2 quads, for far_share)."""
     w, h = params.width, params.height
     out = np.zeros((h, w, 4), np.float32)
     st = np.zeros(40, np.uint64)

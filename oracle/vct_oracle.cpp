@@ -872,15 +872,19 @@ static thread_local int t_cone_class = 0;
 
 // trace_cone, voxel_cone_tracing.frag:88-119 (face_indices :71-78,
 // sample_voxel :80-86).
+static thread_local bool t_stats_skip = false;  // (a shared far field counted by another pixel)
+
+// start_dist > 0: the march starts at that step of the schedule (a far
+// field, see trace_diffuse) with nothing accumulated.
 template <class R>
-static ConeOut<R> trace_cone(const Maps& m, V3<R> origin, V3<R> dir, R aperture, R max_dist) {
+static ConeOut<R> trace_cone(const Maps& m, V3<R> origin, V3<R> dir, R aperture, R max_dist, R start_dist = R(0)) {
   dir = normalize(dir);
   const int ix = dir.x < R(0) ? 0 : 1, iy = dir.y < R(0) ? 2 : 3, iz = dir.z < R(0) ? 4 : 5;
   const V3<R> ad = vabs(dir);
   const R cube_res = R(m.N);
   const R voxel_size = R(1) / cube_res;
   V4<R> acc;
-  R dist = R(3) * voxel_size;
+  R dist = start_dist > R(0) ? start_dist : R(3) * voxel_size;
   R diam = dist * aperture;
   V3<R> sp = dir * dist + origin;
   int steps = 0, lod_lt1 = 0, beyond = 0, empty = 0, empty_lt1 = 0, f_tri = 0, f_quad = 0;
@@ -893,7 +897,7 @@ static ConeOut<R> trace_cone(const Maps& m, V3<R> origin, V3<R> dir, R aperture,
     gone = gone || outside(sp.x, ix == 1) || outside(sp.y, iy == 3) || outside(sp.z, iz == 5);
     if (gone) ++beyond;
     R mip = fmaxr(R(std::log2(diam * cube_res)), R(0));
-    if (g_stats_on && !gone && !g_dilated.empty()) {
+    if (g_stats_on && !t_stats_skip && !gone && !g_dilated.empty()) {
       if (t_cone_class == 2 ? sample_empty3_rule<R>(m.N, m.L, sp, mip)
                             : mip < R(5) && sample_empty_rule<R>(m.N, m.L, sp, mip)) {  // RGBA cones: lod < 5 only
         ++empty;
@@ -915,9 +919,9 @@ static ConeOut<R> trace_cone(const Maps& m, V3<R> origin, V3<R> dir, R aperture,
     sp = dir * dist + origin;
     ++steps;
     if (mip < R(1)) ++lod_lt1;
-    if (g_stats_on) g_stats[kStatLodBand + (mip >= R(7) ? 7 : (int)mip)] += 1;
+    if (g_stats_on && !t_stats_skip) g_stats[kStatLodBand + (mip >= R(7) ? 7 : (int)mip)] += 1;
   }
-  if (g_stats_on) {
+  if (g_stats_on && !t_stats_skip) {
     g_stats[kStatCones + t_cone_class] += 1;
     g_stats[kStatSteps + t_cone_class] += (uint64_t)steps;
     g_stats[kStatLodLt1 + t_cone_class] += (uint64_t)lod_lt1;
@@ -940,13 +944,74 @@ template <class R> static inline V3<R> mixv(V3<R> a, V3<R> b, R t) { return a * 
 static const double kTan22_5 = 0.55785173935;   // TAN_22_5, :136 (kept verbatim)
 static const double kMaxDistance = 1.73205080757;  // MAX_DISTANCE, :138
 
+// The engine's shared far fields (orc_params::far_share; csrc/k_trace.cu
+// k_trace_share), restated: the pixels of a 2x2 quad (even x, even y
+// corner) take as representative the quad's first pixel, in the order
+// (x0,y0), (x0+1,y0), (x0,y0+1), (x0+1,y0+1), whose diffuse cones are
+// traced.  A pixel shares when its normal is within cos 0.99 of the
+// representative's and its texture-space position within 2 voxels along
+// every axis.  A shared diffuse cone k takes its own first sample (step 0,
+// 3 voxels out), then adds the representative's cone k marched from the
+// second step of the schedule (distance far_dist) with nothing accumulated
+// ("far field"): near + (1 - near.a) * far while near.a < 1.
+template <class R> struct ShareQuad {
+  bool on = false, count_far = false;
+  V3<R> pos, n;  // representative's texture-space position and normal
+  R far_dist = R(0);
+};
+
+template <class R> static R far_start_dist(int N, R ap) {  // the second step of trace_cone's schedule
+  const R voxel = R(1) / R(N);
+  const R dist = R(3) * voxel;
+  return dist + fmaxr(dist * ap / R(2), voxel);
+}
+
+template <class R>
+static V4<R> diffuse_cone(const Maps& m, V3<R> origin, V3<R> dir, V3<R> rep_dir, R ap, R md,
+                          const ShareQuad<R>* sq) {
+  if (!sq || !sq->on) return trace_cone<R>(m, origin, dir, ap, md).c;
+  V4<R> near = trace_cone<R>(m, origin, dir, ap, sq->far_dist).c;
+  t_stats_skip = !sq->count_far;
+  V4<R> far = trace_cone<R>(m, sq->pos, rep_dir, ap, md, sq->far_dist).c;
+  t_stats_skip = false;
+  return near.a < R(1) ? near + far * (R(1) - near.a) : near;
+}
+
 // trace_diffuse, voxel_cone_tracing.frag:140-168 (9 cones, equal weights).
 // cone_set SIX60 (no reference counterpart): the normal plus 5 cones 60
 // degrees off it, evenly spaced in azimuth in the same tangent frame, each
 // of aperture 2*tan(30 deg), equal weights.
-template <class R> static V3<R> trace_diffuse(const Maps& m, int cone_set, V3<R> origin, V3<R> n) {
+template <class R> static V3<R> trace_diffuse(const Maps& m, int cone_set, V3<R> origin, V3<R> n,
+                                              const ShareQuad<R>* sq = nullptr) {
   const V3<R> o1 = normalize(tangent(n));
   const V3<R> o2 = normalize(cross(o1, n));
+  if (sq && sq->on) {
+    const V3<R> rn = sq->n;
+    const V3<R> q1 = normalize(tangent(rn)), q2 = normalize(cross(q1, rn));
+    V4<R> acc;
+    if (cone_set == ORC_CONES_SIX60) {
+      const R ap = R(2) * R(std::tan(3.14159265358979323846 / 6.0));
+      const V3<R> nn = normalize(n), rnn = normalize(rn);
+      acc = acc + diffuse_cone<R>(m, origin, nn, rnn, ap, R(kMaxDistance), sq);
+      for (int k = 0; k < 5; ++k) {
+        R phi = R(2.0 * 3.14159265358979323846 * k / 5.0);
+        const R c = R(std::cos(phi)), sn = R(std::sin(phi)), h = R(0.86602540378443864676);
+        acc = acc + diffuse_cone<R>(m, origin, nn * R(0.5) + (o1 * c + o2 * sn) * h,
+                                    rnn * R(0.5) + (q1 * c + q2 * sn) * h, ap, R(kMaxDistance), sq);
+      }
+      return V3<R>(acc.r, acc.g, acc.b) * (R(1) / R(6));
+    }
+    const R ap = R(kTan22_5), md = R(kMaxDistance), h = R(0.5);
+    const V3<R> c1 = (o1 + o2) * R(0.5), c2 = (o1 - o2) * R(0.5);
+    const V3<R> d1 = (q1 + q2) * R(0.5), d2 = (q1 - q2) * R(0.5);
+    const V3<R> pb[4] = {o1, o2, c1, c2}, rb[4] = {q1, q2, d1, d2};
+    acc = acc + diffuse_cone<R>(m, origin, n, rn, ap, md, sq);
+    for (int j = 0; j < 8; ++j) {
+      const R sgn = (j & 1) ? R(-1) : R(1);
+      acc = acc + diffuse_cone<R>(m, origin, mixv(n, pb[j >> 1] * sgn, h), mixv(rn, rb[j >> 1] * sgn, h), ap, md, sq);
+    }
+    return V3<R>(acc.r, acc.g, acc.b) * (R(1) / R(9));
+  }
   V4<R> acc;
   if (cone_set == ORC_CONES_SIX60) {
     const R ap = R(2) * R(std::tan(3.14159265358979323846 / 6.0));
@@ -1029,7 +1094,7 @@ static V3<R> direct_light(const orc_scene* s, const Maps& m, int enable_shadow, 
 // main, voxel_cone_tracing.frag:246-275, for one visible surface point.
 template <class R>
 static V4<R> shade_pixel(const orc_scene* s, const orc_params* p, const Maps& m, V3<R> world, V3<R> nrm,
-                         uint32_t mat_id, bool* written) {
+                         uint32_t mat_id, bool* written, const ShareQuad<R>* sq = nullptr) {
   const orc_material& mat = s->materials[mat_id < s->n_materials ? mat_id : 0];
   const R cube = R(s->cube_size);
   V3<R> pos = V3<R>(world.x / cube, world.y / cube, world.z / cube) * R(0.5) + V3<R>(R(0.5), R(0.5), R(0.5));
@@ -1045,7 +1110,7 @@ static V4<R> shade_pixel(const orc_scene* s, const orc_params* p, const Maps& m,
   V3<R> view_dir = normalize(world - cam);
   V3<R> fd, fdir, fs;
   t_cone_class = 0;
-  if (p->enable_diffuse) fd = mulv(mat_of<R>(mat, 0), trace_diffuse<R>(m, p->cone_set, pos, nrm));
+  if (p->enable_diffuse) fd = mulv(mat_of<R>(mat, 0), trace_diffuse<R>(m, p->cone_set, pos, nrm, sq));
   if (p->enable_direct) fdir = direct_light<R>(s, m, p->enable_shadow, mat, pos, nrm, view_dir);
   R sap = specular_aperture<R>(mat);
   if (p->enable_specular) {
@@ -1075,15 +1140,37 @@ static void trace_impl(const orc_scene* s, const orc_params* p, const uint8_t* l
   Maps m{level0, chains, p->grid_res, p->levels, orc_chain_texels(p->grid_res, p->levels), p->mip_mode == ORC_MIP_ISO,
          level0f, chainsf};
   const int W = p->width, H = p->height;
+  // row_stride < 0: pairs of rows (k |row_stride|, k |row_stride| + 1), so
+  // that sampled rows hold whole 2x2 quads (shared far fields)
+  const bool pairs = row_stride < -1;
+  if (pairs) row_stride = -row_stride;
   if (row_stride < 1) row_stride = 1;
-  const int rows = (H + row_stride - 1) / row_stride;
+  const int rows = pairs ? 2 * ((H + row_stride - 1) / row_stride) : (H + row_stride - 1) / row_stride;
   // Work items are 32-pixel runs of a traced row, so that every thread gets
   // a share of the frame whatever the row count (a sampled frame may have
   // fewer rows than threads).
   const int kRun = 32;
   const int runs = (W + kRun - 1) / kRun;
+  // Shared far fields: which pixels' diffuse cones are traced (the quad's
+  // candidates for representative), and the far fields' start distance.
+  const double cube = s->cube_size;
+  auto tex_pos = [&](size_t q, int a) { return pos[3 * q + a] / cube * 0.5 + 0.5; };
+  auto diffuse_traced = [&](int x, int y) {
+    if (x >= W || y >= H) return false;
+    const size_t q = (size_t)y * W + x;
+    if (tri_id[q] == 0xffffffffu || !p->enable_diffuse || p->view_voxel_dir < 7) return false;
+    for (int a = 0; a < 3; ++a)
+      if (!(std::fabs(tex_pos(q, a)) < 1.0)) return false;
+    return true;
+  };
+  const bool share_on = p->far_share != 0 && p->view_voxel_dir >= 7;
+  const R far_dist = far_start_dist<R>(p->grid_res, p->cone_set == ORC_CONES_SIX60
+                                                        ? R(2) * R(std::tan(3.14159265358979323846 / 6.0))
+                                                        : R(kTan22_5));
   parallel_for(std::max(1, p->threads), rows * runs, [&](int item) {
-    const int y = (item / runs) * row_stride;
+    const int ri = item / runs;
+    const int y = pairs ? (ri >> 1) * row_stride + (ri & 1) : ri * row_stride;
+    if (y >= H) return;
     const int x0 = (item % runs) * kRun, x1 = std::min(W, x0 + kRun);
     for (int x = x0; x < x1; ++x) {
       size_t px = (size_t)y * W + x;
@@ -1092,8 +1179,30 @@ static void trace_impl(const orc_scene* s, const orc_params* p, const uint8_t* l
       if (tri_id[px] == 0xffffffffu) continue;
       V3<R> w(R(pos[3 * px]), R(pos[3 * px + 1]), R(pos[3 * px + 2]));
       V3<R> n(R(nrm[3 * px]), R(nrm[3 * px + 1]), R(nrm[3 * px + 2]));
+      ShareQuad<R> sq;
+      if (share_on && diffuse_traced(x, y)) {
+        const int qx = x & ~1, qy = y & ~1;
+        const int order[4][2] = {{qx, qy}, {qx + 1, qy}, {qx, qy + 1}, {qx + 1, qy + 1}};
+        for (const auto& c : order) {
+          if (!diffuse_traced(c[0], c[1])) continue;
+          const size_t rp = (size_t)c[1] * W + c[0];
+          V3<double> na(nrm[3 * px], nrm[3 * px + 1], nrm[3 * px + 2]);
+          V3<double> nb(nrm[3 * rp], nrm[3 * rp + 1], nrm[3 * rp + 2]);
+          const double lim = 2.0 / p->grid_res;
+          bool ok = dot(normalize(na), normalize(nb)) >= 0.99;
+          for (int a = 0; a < 3; ++a) ok = ok && std::fabs(tex_pos(px, a) - tex_pos(rp, a)) <= lim;
+          if (ok) {
+            sq.on = true;
+            sq.count_far = rp == px;
+            sq.pos = V3<R>(R(tex_pos(rp, 0)), R(tex_pos(rp, 1)), R(tex_pos(rp, 2)));
+            sq.n = V3<R>(R(nrm[3 * rp]), R(nrm[3 * rp + 1]), R(nrm[3 * rp + 2]));
+            sq.far_dist = far_dist;
+          }
+          break;  // the first traced pixel is the representative
+        }
+      }
       bool written;
-      V4<R> c = shade_pixel<R>(s, p, m, w, n, mat[px], &written);
+      V4<R> c = shade_pixel<R>(s, p, m, w, n, mat[px], &written, &sq);
       if (!written) continue;  // fragment returned without writing: keep the clear colour
       o[0] = (float)c.r; o[1] = (float)c.g; o[2] = (float)c.b; o[3] = (float)c.a;
     }

@@ -94,6 +94,10 @@ typedef struct {
   int32_t threads;          /* host threads, >= 1 */
   float radiance_max;       /* voxel colour clamp: rgb to [0, radiance_max]
                              * (<= 0 means 1, the reference's clamp) */
+  int32_t far_share;        /* 0: every pixel marches all its cones (the
+                             * reference); 1: the engine's shared far fields
+                             * (2x2 quads share the diffuse cones' steps with
+                             * lod >= 2; see trace_diffuse) */
 } orc_params;
 
 /* Number of texels in one directional chain (levels 1..L-1). */
@@ -172,9 +176,13 @@ void orc_trace_f32(const orc_scene* s, const orc_params* p,
  * and lod >= 7; [20..23] per class the steps taken more than 3/4 of the
  * coarsest texel outside [0,1] along an axis the cone moves away on (border
  * texels only); [24..27] per class the other steps whose texels are all 0
- * by the engine's occupancy rule, [28..31] those of them with lod < 1.
- * stats holds 32 entries.  Not thread-safe against concurrent
- * orc_trace_stats. */
+ * by the engine's occupancy rule, [28..31] those of them with lod < 1;
+ * [32..35] and [36..39] per class the one-level and two-level texture
+ * fetches the engine's texture-unit path issues for the steps it takes
+ * (with far_share, a shared far field is counted once, by the quad's
+ * representative).  stats holds 40 entries.  row_stride < -1 traces pairs
+ * of rows (k |row_stride|, k |row_stride| + 1), i.e. whole 2x2 quads.  Not
+ * thread-safe against concurrent orc_trace_stats. */
 void orc_trace_stats(const orc_scene* s, const orc_params* p, const uint8_t* level0,
                      const uint8_t* chains, const uint32_t* tri_id, const double* pos,
                      const double* nrm, const uint32_t* mat, int32_t row_stride,

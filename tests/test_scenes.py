@@ -73,8 +73,18 @@ def test_bench_frame_work(oracle):
     assert st["shadow"]["beyond"] == 0  # shadow cones end at the light, inside the grid
     quad = sum(v["fetch_quad"] for v in st.values()) / px
     tri = sum(v["fetch_tri"] for v in st.values()) / px
-    assert quad == pytest.approx(bench.TRACE_FETCH_QUAD_PER_PIXEL, rel=0.02)
-    assert tri == pytest.approx(bench.TRACE_FETCH_TRI_PER_PIXEL, rel=0.02)
+    assert quad == pytest.approx(bench.TRACE_FETCH_QUAD_PER_PIXEL_NOSHARE, rel=0.02)
+    assert tri == pytest.approx(bench.TRACE_FETCH_TRI_PER_PIXEL_NOSHARE, rel=0.02)
+    # shared far fields (the default): pairs of rows, i.e. whole 2x2 quads
+    ps = oracle.Params(grid_res=bench.GRID, width=bench.WIDTH, height=bench.HEIGHT, far_share=1)
+    sh = oracle.trace_stats(s, ps, l0, ch, gb, row_stride=-32)
+    sh.pop("lod_bands")
+    assert sum(v["fetch_quad"] for v in sh.values()) / (2 * px) == pytest.approx(bench.TRACE_FETCH_QUAD_PER_PIXEL,
+                                                                                rel=0.02)
+    assert sum(v["fetch_tri"] for v in sh.values()) / (2 * px) == pytest.approx(bench.TRACE_FETCH_TRI_PER_PIXEL,
+                                                                               rel=0.02)
+    for k in ("shadow", "specular"):  # only the diffuse cones share
+        assert sh[k]["fetch_quad"] / (2 * px) == pytest.approx(st[k]["fetch_quad"] / px, rel=0.02)
     # at most 3 fetches per RGBA step and 2 per shadow step, +1 below lod 1
     upper = sum((2 if k == "shadow" else 3) * (v["steps"] - v["beyond"] - v["empty"]) + v["lod_lt1"] - v["empty_lt1"]
                 for k, v in st.items()) / px

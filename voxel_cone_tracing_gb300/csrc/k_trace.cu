@@ -542,47 +542,35 @@ __device__ V3 trace_diffuse(const MapSet& m, int cone_set, V3 origin, V3 n) {
 // ------------------------------------------------- shared far fields ------
 // Far-field sharing (TraceParams::far_share, texture-unit sampler).  The
 // diffuse cones of neighbouring pixels on one surface start a fraction of a
-// voxel apart in nearly the same directions; once a cone's samples are
-// coarse (lod >= kShareLod, texels of 4+ voxels) the filtered values along
-// the four cones of a 2x2 quad barely differ.  So the march of every diffuse
-// cone is split at the first step whose lod reaches kShareLod: each pixel
-// marches the steps before it itself, and the rest ("far field") is marched
-// once per quad, along the cones of one pixel of the quad (its
-// representative), by the lanes of the warp together (far_fields below).
-// The split is exact front-to-back compositing: a march that continues from
-// the near part's accumulation equals near + (1 - near.a) * far, where far is
-// the march of the same steps from zero, and both stop at the same step
-// (alpha reaching 1).  Only the representative's positions and directions
-// stand in for the other pixels'.  A pixel shares only when its normal is
-// within kShareCos of the representative's and its surface point within
-// kShareDist voxels; others march their own cones.  Measured against the
-// FP64 oracle on the 1080p bench frame: 81 dB for the far fields alone
-// (the texture unit's 8-bit filter weights: 71 dB).
-constexpr float kShareLod = 2.0f;
+// voxel apart in nearly the same directions, and after their first sample
+// (3 voxels out, lod log2(3 aperture)) their samples are coarse texels whose
+// filtered values barely differ across a 2x2 quad.  So every diffuse cone is
+// split after its first step: each pixel takes that sample itself, and the
+// rest of the march (the "far field") is done once per quad, along the cones
+// of one pixel of the quad (its representative), by the lanes of the warp
+// together (far_fields below).  The split is exact front-to-back
+// compositing: a march that continues from the first sample s equals
+// s + (1 - s.a) * far, where far is the march of the remaining steps from
+// zero, and both stop at the same step (alpha reaching 1).  Only the
+// representative's positions and directions stand in for the other
+// pixels'.  A pixel shares only when its normal is within kShareCos of the
+// representative's and its surface point within kShareDist voxels along
+// every axis; others march their own cones.  Measured against the FP64
+// oracle on the 1080p bench frame: 80.6 dB for the sharing alone (the
+// texture unit's 8-bit filter weights: 71 dB), with the diffuse cones' texture
+// fetches cut by two thirds.
 constexpr float kShareCos = 0.99f;
 constexpr float kShareDist = 2.0f;  // voxels
 constexpr int kShareQuads = 8;      // 2x2 quads of a 16x2-pixel warp
 constexpr int kShareCones = 9;
+constexpr int kShareJobs = kShareQuads * kShareCones;
 
 struct FarWarp {
-  float4 far[kShareQuads * kShareCones];  // far field of cone k of quad slot q at q * K + k
-  float origin[kShareQuads][3];           // representative's texture-space position
-  float normal[kShareQuads][3];           // and normal
+  float4 far[kShareJobs];   // far field of cone k of quad slot q at q * K + k
+  float4 job[kShareJobs];   // job j = k * nq + q: unit direction, exit distance
+  float origin[kShareQuads][3];  // representative's texture-space position
+  float normal[kShareQuads][3];  // and normal
 };
-
-// The distance and diameter of the first step whose lod reaches kShareLod,
-// by the march's own recurrence (trace_cone), for aperture ap.
-__device__ __forceinline__ void far_start(float ap, int N, float& dist, float& diam) {
-  const float cube_res = (float)N;
-  const float voxel_size = 1.0f / cube_res;
-  dist = 3.0f * voxel_size;
-  diam = dist * ap;
-  for (int i = 0; i < 64 && cone_lod(diam * cube_res) < kShareLod; ++i) {
-    const float step = fmaxf(diam * 0.5f, voxel_size);
-    dist += step;
-    diam = dist * ap;
-  }
-}
 
 // Direction (unnormalised) and aperture of diffuse cone k, as trace_diffuse
 // computes them from the normal n and its frame o1, o2.
@@ -604,51 +592,61 @@ __device__ __forceinline__ V3 diffuse_dir(int cone_set, V3 n, V3 o1, V3 o2, int 
   return mixv(n, side, 0.5f);
 }
 
-// The far fields of a warp's nq quads: jobs k * nq + q (cone k of quad slot
-// q: neighbouring lanes start on the same cone of neighbouring quads, which
-// read neighbouring texels), dealt out to the lanes as they become free, so
-// that a lane whose cone ends early (alpha 1, the grid's edge) takes the
-// next job while the others march on.  Results go to fw.far[q * K + k].
+// The far fields of a warp's nq quads.  Job j = k * nq + q is cone k of quad
+// slot q (neighbouring lanes start on the same cone of neighbouring quads,
+// which read neighbouring texels).  The lanes first set up every job's
+// direction and exit distance together (fw.job), then march: a lane whose
+// cone ends (alpha 1, the grid's edge) takes the next job while the others
+// march on.  The march starts at the second step of the schedule (dist1,
+// diam1) with nothing accumulated.  Results go to fw.far[q * K + k].
 template <bool ISO>
-__device__ void far_fields(const MapSet& m, FarWarp& fw, int cone_set, int nq, float dist0, float diam0) {
+__device__ void far_fields(const MapSet& m, FarWarp& fw, int cone_set, int nq, float dist1, float diam1) {
   const int lane = threadIdx.x & 31;
   const int K = cone_set == VCT_CONES_SIX60 ? 6 : 9;
   const int n_jobs = nq * K;
+  for (int j = lane; j < n_jobs; j += 32) {
+    const int k = j / nq, q = j - k * nq;
+    const V3 n = v3(fw.normal[q][0], fw.normal[q][1], fw.normal[q][2]);
+    const V3 o1 = normalize(tangent(n));
+    const V3 o2 = normalize(cross(o1, n));
+    float ap;
+    const V3 d = normalize(diffuse_dir(cone_set, n, o1, o2, k, ap));
+    const V3 o = v3(fw.origin[q][0], fw.origin[q][1], fw.origin[q][2]);
+    fw.job[j] = f4(d.x, d.y, d.z, exit_distance(m, o, d, kMaxDistance));
+  }
+  __syncwarp();
+  const float ap = cone_set == VCT_CONES_SIX60 ? 1.15470053838f : kTan22_5;
   const float cube_res = (float)m.N;
   const float voxel_size = 1.0f / cube_res;
   int next = 0;  // warp-uniform: next job to hand out
-  int job = -1, res = 0;
+  int res = 0;
   bool active = false;
   V3 origin = v3(0.f, 0.f, 0.f), dir = v3(0.f, 0.f, 1.f), ad = v3(0.f, 0.f, 1.f);
   int ix = 1, iy = 3, iz = 5;
-  float dist = 0.f, diam = 0.f, stop = 0.f, ap = 0.f;
+  float dist = 0.f, diam = 0.f, stop = 0.f;
   bool check = false;
   float4 acc = f4(0.f, 0.f, 0.f, 0.f);
   for (;;) {
     const unsigned need = __ballot_sync(0xffffffffu, !active);
     if (need && next < n_jobs) {
-      if (!active) {
-        job = next + __popc(need & ((1u << lane) - 1u));
-        if (job < n_jobs) {
-          const int k = job / nq, q = job - k * nq;
-          res = q * K + k;
-          origin = v3(fw.origin[q][0], fw.origin[q][1], fw.origin[q][2]);
-          const V3 n = v3(fw.normal[q][0], fw.normal[q][1], fw.normal[q][2]);
-          const V3 o1 = normalize(tangent(n));
-          const V3 o2 = normalize(cross(o1, n));
-          dir = normalize(diffuse_dir(cone_set, n, o1, o2, k, ap));
-          ix = dir.x < 0.0f ? 0 : 1;
-          iy = dir.y < 0.0f ? 2 : 3;
-          iz = dir.z < 0.0f ? 4 : 5;
-          ad = vabs(dir);
-          dist = dist0;
-          diam = diam0;
-          stop = exit_distance(m, origin, dir, kMaxDistance);
-          check = !march_sane(origin, dir, stop);
-          acc = f4(0.f, 0.f, 0.f, 0.f);
-          active = dist < stop;
-          if (!active) fw.far[res] = acc;
-        }
+      const int job = next + __popc(need & ((1u << lane) - 1u));
+      if (!active && job < n_jobs) {
+        const int k = job / nq, q = job - k * nq;
+        res = q * K + k;
+        const float4 jb = fw.job[job];
+        dir = v3(jb.x, jb.y, jb.z);
+        stop = jb.w;
+        origin = v3(fw.origin[q][0], fw.origin[q][1], fw.origin[q][2]);
+        ix = dir.x < 0.0f ? 0 : 1;
+        iy = dir.y < 0.0f ? 2 : 3;
+        iz = dir.z < 0.0f ? 4 : 5;
+        ad = vabs(dir);
+        dist = dist1;
+        diam = diam1;
+        check = !march_sane(origin, dir, stop);
+        acc = f4(0.f, 0.f, 0.f, 0.f);
+        active = dist < stop;
+        if (!active) fw.far[res] = acc;
       }
       next += __popc(need);
     }
@@ -673,20 +671,34 @@ __device__ void far_fields(const MapSet& m, FarWarp& fw, int cone_set, int nq, f
 }
 
 // trace_diffuse with the quad's far fields (far: this quad's K results):
-// each cone marches its steps before far_dist, then takes the far field
-// behind what it has accumulated.
+// each cone takes its first sample (step 0 of trace_cone) itself, then the
+// far field behind it.
 template <bool ISO>
-__device__ V3 trace_diffuse_shared(const MapSet& m, int cone_set, V3 origin, V3 n, const float4* far, float far_dist) {
+__device__ V3 trace_diffuse_shared(const MapSet& m, int cone_set, V3 origin, V3 n, const float4* far) {
   const V3 o1 = normalize(tangent(n));
   const V3 o2 = normalize(cross(o1, n));
   const int K = cone_set == VCT_CONES_SIX60 ? 6 : 9;
+  const float cube_res = (float)m.N;
   float4 acc = f4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll 1
   for (int k = 0; k < K; ++k) {
     float ap;
-    const V3 d = diffuse_dir(cone_set, n, o1, o2, k, ap);
-    float4 c = trace_cone<VCT_SAMPLER_HW, ISO, VCT_STORAGE_RGBA8>(m, origin, d, ap, far_dist);
-    if (c.w < 1.0f) c = fma4(far[k], 1.0f - c.w, c);
+    const V3 dir = normalize(diffuse_dir(cone_set, n, o1, o2, k, ap));
+    const float dist = 3.0f * (1.0f / cube_res);
+    const float diam = dist * ap;
+    const float stop = exit_distance(m, origin, dir, kMaxDistance);
+    float4 c = f4(0.f, 0.f, 0.f, 0.f);
+    if (dist < stop) {
+      const V3 sp = march_pos(origin, dir, dist);
+      const float mip = cone_lod(diam * cube_res);
+      if (!(kSkipEmptyRGBA && m.skip_empty && mip < kSkipMaxLod && sample_empty(m, sp, mip)) &&
+          !(!march_sane(origin, dir, stop) && !u_sane(sp))) {
+        const int ix = dir.x < 0.0f ? 0 : 1, iy = dir.y < 0.0f ? 2 : 3, iz = dir.z < 0.0f ? 4 : 5;
+        const float4 smp = sample_voxel<VCT_SAMPLER_HW, ISO, VCT_STORAGE_RGBA8, false>(m, sp, ix, iy, iz, vabs(dir), mip);
+        c = fma4(smp, 1.0f, c);
+      }
+      if (c.w < 1.0f) c = fma4(far[k], 1.0f - c.w, c);
+    }
     acc = acc + c;
   }
   return v3(acc.x, acc.y, acc.z) * (1.0f / (float)K);
@@ -758,7 +770,7 @@ __device__ __forceinline__ void trace_px(const SceneParams& sp, const CameraPara
                                          const TraceParams& tp, const float4* __restrict__ gb_pos,
                                          const float4* __restrict__ gb_nrm, uchar4* __restrict__ frame,
                                          float4* __restrict__ frame_f32, int px, int py,
-                                         const float4* far = nullptr, float far_dist = 0.0f) {
+                                         const float4* far = nullptr) {
   if (px >= cp.W || py >= cp.H) return;
   const size_t p = (size_t)py * cp.W + px;
   float4 out = f4(0.15f, 0.25f, 0.25f, 1.0f);  // glClearColor, renderer.cpp:398
@@ -790,7 +802,7 @@ __device__ __forceinline__ void trace_px(const SceneParams& sp, const CameraPara
             const float4 d = tp.diffuse_in[p];
             fd = mulv(mat3v(mat.diffuse), v3(d.x, d.y, d.z));
           } else if (SHARE && far) {
-            fd = mulv(mat3v(mat.diffuse), trace_diffuse_shared<ISO>(m, tp.cone_set, pos, nrm, far, far_dist));
+            fd = mulv(mat3v(mat.diffuse), trace_diffuse_shared<ISO>(m, tp.cone_set, pos, nrm, far));
           } else {
             fd = mulv(mat3v(mat.diffuse), trace_diffuse<SAMPLER, ISO, STORAGE>(m, tp.cone_set, pos, nrm));
           }
@@ -827,7 +839,7 @@ __global__ void __launch_bounds__(kTraceThreads, SAMPLER == VCT_SAMPLER_HW ? kTr
 }
 
 #ifndef VCT_SHARE_MIN_BLOCKS
-#define VCT_SHARE_MIN_BLOCKS 10
+#define VCT_SHARE_MIN_BLOCKS 8
 #endif
 constexpr int kShareMinBlocks = VCT_SHARE_MIN_BLOCKS;
 
@@ -883,12 +895,15 @@ __global__ void __launch_bounds__(kTraceThreads, kShareMinBlocks)
   }
   __syncwarp();
   const int K = tp.cone_set == VCT_CONES_SIX60 ? 6 : 9;
-  float dist0 = 0.0f, diam0 = 0.0f;
-  far_start(tp.cone_set == VCT_CONES_SIX60 ? 1.15470053838f : kTan22_5, m.N, dist0, diam0);
-  if (repmask) far_fields<ISO>(m, fw, tp.cone_set, __popc(repmask), dist0, diam0);
+  // the second step of the march schedule (trace_cone's recurrence)
+  const float ap = tp.cone_set == VCT_CONES_SIX60 ? 1.15470053838f : kTan22_5;
+  const float voxel_size = 1.0f / (float)m.N;
+  const float dist0 = 3.0f * voxel_size;
+  const float dist1 = dist0 + fmaxf(dist0 * ap * 0.5f, voxel_size);
+  if (repmask) far_fields<ISO>(m, fw, tp.cone_set, __popc(repmask), dist1, dist1 * ap);
   __syncwarp();
   trace_px<VCT_SAMPLER_HW, ISO, VCT_STORAGE_RGBA8, true>(sp, cp, m, tp, gb_pos, gb_nrm, frame, frame_f32, px, py,
-                                                         share ? fw.far + slot * K : nullptr, dist0);
+                                                         share ? fw.far + slot * K : nullptr);
 }
 
 // One pixel of a batch scene.  Called, not inlined, from the tile loop of
