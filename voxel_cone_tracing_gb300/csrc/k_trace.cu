@@ -561,6 +561,15 @@ __device__ V3 trace_diffuse(const MapSet& m, int cone_set, V3 origin, V3 n) {
 // fetches cut by two thirds.
 constexpr float kShareCos = 0.99f;
 constexpr float kShareDist = 2.0f;  // voxels
+#ifndef VCT_FAR_PIPE
+#define VCT_FAR_PIPE 1
+#endif
+constexpr bool kFarPipe = VCT_FAR_PIPE != 0;  // software-pipelined far-field march
+#ifndef VCT_FIRST_UNROLL
+#define VCT_FIRST_UNROLL 1  // the per-pixel first samples of the diffuse cones: cones in flight together
+#endif
+#define VCT_STR(x) #x
+#define VCT_UNROLL_N(n) _Pragma(VCT_STR(unroll n))
 constexpr int kShareQuads = 8;      // 2x2 quads of a 16x2-pixel warp
 constexpr int kShareCones = 9;
 constexpr int kShareJobs = kShareQuads * kShareCones;
@@ -626,6 +635,73 @@ __device__ void far_fields(const MapSet& m, FarWarp& fw, int cone_set, int nq, f
   float dist = 0.f, diam = 0.f, stop = 0.f;
   bool check = false;
   float4 acc = f4(0.f, 0.f, 0.f, 0.f);
+  if constexpr (kFarPipe) {
+    // Software-pipelined like trace_cone_pipe: a lane computes its next step
+    // (position, lod, empty-space test with its occupancy load) while the
+    // current step's texture fetches are in flight, and issues the next
+    // step's fetches as soon as the current one is added.  Same samples, same
+    // arithmetic as the loop below.
+    float mip = 0.f;
+    bool live = false;
+    Taps t;
+    for (;;) {
+      const unsigned need = __ballot_sync(0xffffffffu, !active);
+      if (need && next < n_jobs) {
+        const int job = next + __popc(need & ((1u << lane) - 1u));
+        if (!active && job < n_jobs) {
+          const int k = job / nq, q = job - k * nq;
+          res = q * K + k;
+          const float4 jb = fw.job[job];
+          dir = v3(jb.x, jb.y, jb.z);
+          stop = jb.w;
+          origin = v3(fw.origin[q][0], fw.origin[q][1], fw.origin[q][2]);
+          ix = dir.x < 0.0f ? 0 : 1;
+          iy = dir.y < 0.0f ? 2 : 3;
+          iz = dir.z < 0.0f ? 4 : 5;
+          ad = vabs(dir);
+          dist = dist1;
+          diam = diam1;
+          check = !march_sane(origin, dir, stop);
+          acc = f4(0.f, 0.f, 0.f, 0.f);
+          active = dist < stop;
+          if (!active) {
+            fw.far[res] = acc;
+          } else {
+            const V3 sp = march_pos(origin, dir, dist);
+            mip = cone_lod(diam * cube_res);
+            live = !(kSkipEmptyRGBA && m.skip_empty && mip < kSkipMaxLod && sample_empty(m, sp, mip)) &&
+                   !(check && !u_sane(sp));
+            if (live) issue_taps(m, sp, ix, iy, iz, ad, mip, t);
+          }
+        }
+        next += __popc(need);
+      }
+      if (!__any_sync(0xffffffffu, active)) break;
+      if (active) {
+        const float step = fmaxf(diam * 0.5f, voxel_size);
+        const float dist_n = dist + step;
+        const float diam_n = dist_n * ap;
+        const V3 sp_n = march_pos(origin, dir, dist_n);
+        const bool more = dist_n < stop;
+        const float mip_n = cone_lod(diam_n * cube_res);
+        const bool live_n = more &&
+                            !(kSkipEmptyRGBA && m.skip_empty && mip_n < kSkipMaxLod && sample_empty(m, sp_n, mip_n)) &&
+                            !(check && !u_sane(sp_n));
+        if (live) acc = fma4(combine_taps(t, ad, mip), 1.0f - acc.w, acc);
+        if (!(acc.w < 1.0f) || !more) {
+          fw.far[res] = acc;
+          active = false;
+        } else {
+          dist = dist_n;
+          diam = diam_n;
+          mip = mip_n;
+          live = live_n;
+          if (live) issue_taps(m, sp_n, ix, iy, iz, ad, mip, t);
+        }
+      }
+    }
+    return;
+  }
   for (;;) {
     const unsigned need = __ballot_sync(0xffffffffu, !active);
     if (need && next < n_jobs) {
@@ -680,7 +756,7 @@ __device__ V3 trace_diffuse_shared(const MapSet& m, int cone_set, V3 origin, V3 
   const int K = cone_set == VCT_CONES_SIX60 ? 6 : 9;
   const float cube_res = (float)m.N;
   float4 acc = f4(0.f, 0.f, 0.f, 0.f);
-#pragma unroll 1
+  VCT_UNROLL_N(VCT_FIRST_UNROLL)
   for (int k = 0; k < K; ++k) {
     float ap;
     const V3 dir = normalize(diffuse_dir(cone_set, n, o1, o2, k, ap));
