@@ -49,12 +49,12 @@ CPU_WARMUP_ROW_STRIDE = 64   # warm-up frames of the CPU arm trace every 64th ro
 # reads packed alpha-only chains for the shadow cones: 265.6 two-level
 # (quadrilinear) and 83.5 one-level (trilinear) RGBA8 fetches per pixel when
 # every pixel marches all its cones (far_share 0).  With shared far fields
-# (far_share 1, the default; 2x2 quads march their diffuse cones after the
-# first step once), counted over whole quads: 87.25 two-level and 34.0
-# one-level fetches per pixel.
+# (far_share 1, the default: groups of 4x2 pixels march their diffuse cones
+# after the first step once), counted over whole groups: 58.1 two-level and
+# 25.9 one-level fetches per pixel.
 TRACE_FETCHES_PER_PIXEL_REF = 778.9
-TRACE_FETCH_QUAD_PER_PIXEL = 87.25
-TRACE_FETCH_TRI_PER_PIXEL = 34.0
+TRACE_FETCH_QUAD_PER_PIXEL = 58.14
+TRACE_FETCH_TRI_PER_PIXEL = 25.88
 TRACE_FETCH_QUAD_PER_PIXEL_NOSHARE = 265.6
 TRACE_FETCH_TRI_PER_PIXEL_NOSHARE = 83.5
 INSTANCE_RECORD_BYTES = 144   # one per queued model (DevInstance)

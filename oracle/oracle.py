@@ -322,7 +322,7 @@ def trace_stats(scene, params: Params, level0, chains, gb: dict, row_stride: int
     the traced rows, and the single-level / two-level texture fetches the
     engine's texture-unit path issues for the remaining steps (`fetch_tri`,
     `fetch_quad`: the algorithmic texture work of the trace).  A negative
-    row_stride samples pairs of rows (whole 2x2 quads, for far_share)."""
+    row_stride samples pairs of rows (whole W x 2 groups, for far_share)."""
     w, h = params.width, params.height
     out = np.zeros((h, w, 4), np.float32)
     st = np.zeros(40, np.uint64)

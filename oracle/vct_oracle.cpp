@@ -944,11 +944,11 @@ template <class R> static inline V3<R> mixv(V3<R> a, V3<R> b, R t) { return a * 
 static const double kTan22_5 = 0.55785173935;   // TAN_22_5, :136 (kept verbatim)
 static const double kMaxDistance = 1.73205080757;  // MAX_DISTANCE, :138
 
-// The engine's shared far fields (orc_params::far_share; csrc/k_trace.cu
-// k_trace_share), restated: the pixels of a 2x2 quad (even x, even y
-// corner) take as representative the quad's first pixel, in the order
-// (x0,y0), (x0+1,y0), (x0,y0+1), (x0+1,y0+1), whose diffuse cones are
-// traced.  A pixel shares when its normal is within cos 0.99 of the
+// The engine's shared far fields (orc_params::far_share = the group width W;
+// csrc/k_trace.cu k_trace_share), restated: the pixels of a W x 2 group
+// (corner x0 a multiple of W, y0 even) take as representative the group's
+// first pixel, in the order (x0,y0) .. (x0+W-1,y0), (x0,y0+1) ..
+// (x0+W-1,y0+1), whose diffuse cones are traced.  A pixel shares when its normal is within cos 0.99 of the
 // representative's and its texture-space position within 2 voxels along
 // every axis.  A shared diffuse cone k takes its own first sample (step 0,
 // 3 voxels out), then adds the representative's cone k marched from the
@@ -1181,9 +1181,18 @@ static void trace_impl(const orc_scene* s, const orc_params* p, const uint8_t* l
       V3<R> n(R(nrm[3 * px]), R(nrm[3 * px + 1]), R(nrm[3 * px + 2]));
       ShareQuad<R> sq;
       if (share_on && diffuse_traced(x, y)) {
-        const int qx = x & ~1, qy = y & ~1;
-        const int order[4][2] = {{qx, qy}, {qx + 1, qy}, {qx, qy + 1}, {qx + 1, qy + 1}};
-        for (const auto& c : order) {
+        const int gw = std::min(std::max(p->far_share, 1), 16);
+        const int qx = x - x % gw, qy = y & ~1;
+        int order[32][2];
+        int no = 0;
+        for (int r = 0; r < 2; ++r)
+          for (int i = 0; i < gw; ++i) {
+            order[no][0] = qx + i;
+            order[no][1] = qy + r;
+            ++no;
+          }
+        for (int oi = 0; oi < no; ++oi) {
+          const int* c = order[oi];
           if (!diffuse_traced(c[0], c[1])) continue;
           const size_t rp = (size_t)c[1] * W + c[0];
           V3<double> na(nrm[3 * px], nrm[3 * px + 1], nrm[3 * px + 2]);

@@ -95,9 +95,9 @@ typedef struct {
   float radiance_max;       /* voxel colour clamp: rgb to [0, radiance_max]
                              * (<= 0 means 1, the reference's clamp) */
   int32_t far_share;        /* 0: every pixel marches all its cones (the
-                             * reference); 1: the engine's shared far fields
-                             * (2x2 quads share the diffuse cones' steps with
-                             * lod >= 2; see trace_diffuse) */
+                             * reference); W > 0: the engine's shared far
+                             * fields in groups of W x 2 pixels (see
+                             * trace_diffuse) */
 } orc_params;
 
 /* Number of texels in one directional chain (levels 1..L-1). */
@@ -179,7 +179,7 @@ void orc_trace_f32(const orc_scene* s, const orc_params* p,
  * by the engine's occupancy rule, [28..31] those of them with lod < 1;
  * [32..35] and [36..39] per class the one-level and two-level texture
  * fetches the engine's texture-unit path issues for the steps it takes
- * (with far_share, a shared far field is counted once, by the quad's
+ * (with far_share, a shared far field is counted once, by the group's
  * representative).  stats holds 40 entries.  row_stride < -1 traces pairs
  * of rows (k |row_stride|, k |row_stride| + 1), i.e. whole 2x2 quads.  Not
  * thread-safe against concurrent orc_trace_stats. */

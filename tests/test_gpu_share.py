@@ -1,14 +1,16 @@
 """Shared far fields (vct_config.far_share, the default of the texture-unit
-sampler): the four pixels of a 2x2 quad share the coarse part (lod >= 2) of
-their diffuse cones, marched once per quad by the lanes of a warp together.
+sampler): every diffuse cone takes its first sample per pixel; the rest of
+the march is done once per group of 4x2 pixels (FAR_SHARE_GROUP_W x 2) along
+the cones of the group's representative, by the lanes of a warp together.
 
 Tolerances: against the same frame with every pixel marching all its cones
-(far_share 0): PSNR >= 50 dB on the small scenes (96x64 and smaller frames:
-a quad covers more of the scene), >= 60 dB on the 1080p bench frame; against the FP64 oracle's per-pixel rule (from the GPU's own
-maps and G-buffer): PSNR >= 40 dB, the tolerance of the texture-unit
-sampler; against the oracle's restatement of the sharing rule: PSNR >= 50 dB
-(what remains is the texture unit's filtering); frames repeat bit for bit
-(the far-field jobs are dealt to lanes in a fixed order)."""
+(far_share 0): PSNR >= 45 dB on the small scenes (96x64 and smaller frames:
+a group covers more of the scene), >= 60 dB on the 1080p bench frame;
+against the FP64 oracle's per-pixel rule (from the GPU's own maps and
+G-buffer): PSNR >= 40 dB, the tolerance of the texture-unit sampler; against
+the oracle's restatement of the sharing rule: PSNR >= 50 dB (what remains
+is the texture unit's filtering); frames repeat bit for bit (the far-field
+jobs are dealt to lanes in a fixed order)."""
 import numpy as np
 import pytest
 
@@ -66,14 +68,14 @@ def test_shared_far_fields_small(vct, oracle, case, size):
                       cone_set=cfg.get("cone_set", 0))
     l0, ch, gb = a.read_voxels(0), _chains(a, p.n_maps), _gb64(a.read_gbuffer())
     ref = oracle.trace(scene, p, l0, ch, gb)
-    p.far_share = 1
+    p.far_share = vct.FAR_SHARE_GROUP_W
     ref_sh = oracle.trace(scene, p, l0, ch, gb)  # the oracle's restatement of the sharing rule
     qo = psnr(np.clip(fa, 0, 1), np.clip(ref, 0, 1))
     qs = psnr(np.clip(fa, 0, 1), np.clip(ref_sh, 0, 1))
     qr = psnr(np.clip(ref_sh, 0, 1), np.clip(ref, 0, 1))
     print(f"{case} {w}x{h}: shared vs per-pixel {q:.1f} dB; vs oracle {qo:.1f} dB, vs the oracle's sharing rule "
           f"{qs:.1f} dB (that rule vs per-pixel: {qr:.1f} dB)")
-    assert q >= 50.0
+    assert q >= 45.0
     assert qo >= 40.0
     assert qs >= 50.0
 

@@ -76,7 +76,9 @@ def test_bench_frame_work(oracle):
     assert quad == pytest.approx(bench.TRACE_FETCH_QUAD_PER_PIXEL_NOSHARE, rel=0.02)
     assert tri == pytest.approx(bench.TRACE_FETCH_TRI_PER_PIXEL_NOSHARE, rel=0.02)
     # shared far fields (the default): pairs of rows, i.e. whole 2x2 quads
-    ps = oracle.Params(grid_res=bench.GRID, width=bench.WIDTH, height=bench.HEIGHT, far_share=1)
+    from voxel_cone_tracing_gb300 import renderer
+    ps = oracle.Params(grid_res=bench.GRID, width=bench.WIDTH, height=bench.HEIGHT,
+                       far_share=renderer.FAR_SHARE_GROUP_W)
     sh = oracle.trace_stats(s, ps, l0, ch, gb, row_stride=-32)
     sh.pop("lod_bands")
     assert sum(v["fetch_quad"] for v in sh.values()) / (2 * px) == pytest.approx(bench.TRACE_FETCH_QUAD_PER_PIXEL,

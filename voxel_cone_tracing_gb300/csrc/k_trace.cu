@@ -544,21 +544,22 @@ __device__ V3 trace_diffuse(const MapSet& m, int cone_set, V3 origin, V3 n) {
 // diffuse cones of neighbouring pixels on one surface start a fraction of a
 // voxel apart in nearly the same directions, and after their first sample
 // (3 voxels out, lod log2(3 aperture)) their samples are coarse texels whose
-// filtered values barely differ across a 2x2 quad.  So every diffuse cone is
-// split after its first step: each pixel takes that sample itself, and the
-// rest of the march (the "far field") is done once per quad, along the cones
-// of one pixel of the quad (its representative), by the lanes of the warp
-// together (far_fields below).  The split is exact front-to-back
-// compositing: a march that continues from the first sample s equals
-// s + (1 - s.a) * far, where far is the march of the remaining steps from
-// zero, and both stop at the same step (alpha reaching 1).  Only the
+// filtered values barely differ across a few pixels.  So every diffuse cone
+// is split after its first step: each pixel takes that sample itself, and the
+// rest of the march (the "far field") is done once per group of kShareW x 2
+// pixels, along the cones of one pixel of the group (its representative),
+// by the lanes of the warp together (far_fields below).  The split is exact
+// front-to-back compositing: a march that continues from the first sample s
+// equals s + (1 - s.a) * far, where far is the march of the remaining steps
+// from zero, and both stop at the same step (alpha reaching 1).  Only the
 // representative's positions and directions stand in for the other
 // pixels'.  A pixel shares only when its normal is within kShareCos of the
 // representative's and its surface point within kShareDist voxels along
 // every axis; others march their own cones.  Measured against the FP64
-// oracle on the 1080p bench frame: 80.6 dB for the sharing alone (the
-// texture unit's 8-bit filter weights: 71 dB), with the diffuse cones' texture
-// fetches cut by two thirds.
+// oracle on the 1080p bench frame (sharing alone, the texture unit's 8-bit
+// filter weights being 71 dB): 2x2 groups 80.6 dB, 4x2 groups 73.1 dB, with
+// the diffuse cones' two-level texture fetches cut from 238 to 60 and 31
+// per pixel.
 constexpr float kShareCos = 0.99f;
 constexpr float kShareDist = 2.0f;  // voxels
 #ifndef VCT_FAR_PIPE
@@ -570,12 +571,18 @@ constexpr bool kFarPipe = VCT_FAR_PIPE != 0;  // software-pipelined far-field ma
 #endif
 #define VCT_STR(x) #x
 #define VCT_UNROLL_N(n) _Pragma(VCT_STR(unroll n))
-constexpr int kShareQuads = 8;      // 2x2 quads of a 16x2-pixel warp
+#ifndef VCT_SHARE_GROUP_W
+#define VCT_SHARE_GROUP_W 4
+#endif
+// A sharing group is kShareW x 2 pixels of a warp's 16x2 strip.
+constexpr int kShareW = VCT_SHARE_GROUP_W;
+static_assert(kShareW == 2 || kShareW == 4 || kShareW == 8, "group width divides the 16-pixel strip");
+constexpr int kShareQuads = 16 / kShareW;  // groups of a warp
 constexpr int kShareCones = 9;
 constexpr int kShareJobs = kShareQuads * kShareCones;
 
 struct FarWarp {
-  float4 far[kShareJobs];   // far field of cone k of quad slot q at q * K + k
+  float4 far[kShareJobs];   // far field of cone k of group slot q at q * K + k
   float4 job[kShareJobs];   // job j = k * nq + q: unit direction, exit distance
   float origin[kShareQuads][3];  // representative's texture-space position
   float normal[kShareQuads][3];  // and normal
@@ -601,8 +608,8 @@ __device__ __forceinline__ V3 diffuse_dir(int cone_set, V3 n, V3 o1, V3 o2, int 
   return mixv(n, side, 0.5f);
 }
 
-// The far fields of a warp's nq quads.  Job j = k * nq + q is cone k of quad
-// slot q (neighbouring lanes start on the same cone of neighbouring quads,
+// The far fields of a warp's nq groups.  Job j = k * nq + q is cone k of group
+// slot q (neighbouring lanes start on the same cone of neighbouring groups,
 // which read neighbouring texels).  The lanes first set up every job's
 // direction and exit distance together (fw.job), then march: a lane whose
 // cone ends (alpha 1, the grid's edge) takes the next job while the others
@@ -635,8 +642,9 @@ __device__ void far_fields(const MapSet& m, FarWarp& fw, int cone_set, int nq, f
   float dist = 0.f, diam = 0.f, stop = 0.f;
   bool check = false;
   float4 acc = f4(0.f, 0.f, 0.f, 0.f);
-  if constexpr (kFarPipe) {
-    // Software-pipelined like trace_cone_pipe: a lane computes its next step
+  if constexpr (kFarPipe && !ISO) {
+    // Software-pipelined like trace_cone_pipe (anisotropic maps; the
+    // isotropic march below samples one chain): a lane computes its next step
     // (position, lod, empty-space test with its occupancy load) while the
     // current step's texture fetches are in flight, and issues the next
     // step's fetches as soon as the current one is added.  Same samples, same
@@ -746,7 +754,7 @@ __device__ void far_fields(const MapSet& m, FarWarp& fw, int cone_set, int nq, f
   }
 }
 
-// trace_diffuse with the quad's far fields (far: this quad's K results):
+// trace_diffuse with the group's far fields (far: this group's K results):
 // each cone takes its first sample (step 0 of trace_cone) itself, then the
 // far field behind it.
 template <bool ISO>
@@ -762,19 +770,18 @@ __device__ V3 trace_diffuse_shared(const MapSet& m, int cone_set, V3 origin, V3 
     const V3 dir = normalize(diffuse_dir(cone_set, n, o1, o2, k, ap));
     const float dist = 3.0f * (1.0f / cube_res);
     const float diam = dist * ap;
-    const float stop = exit_distance(m, origin, dir, kMaxDistance);
+    // (the origin is a surface point inside the grid and the first step
+    // three voxels: the sample position is sane, and one beyond the grid's
+    // exit margin reads border texels, 0, as the unshortened march would)
     float4 c = f4(0.f, 0.f, 0.f, 0.f);
-    if (dist < stop) {
-      const V3 sp = march_pos(origin, dir, dist);
-      const float mip = cone_lod(diam * cube_res);
-      if (!(kSkipEmptyRGBA && m.skip_empty && mip < kSkipMaxLod && sample_empty(m, sp, mip)) &&
-          !(!march_sane(origin, dir, stop) && !u_sane(sp))) {
-        const int ix = dir.x < 0.0f ? 0 : 1, iy = dir.y < 0.0f ? 2 : 3, iz = dir.z < 0.0f ? 4 : 5;
-        const float4 smp = sample_voxel<VCT_SAMPLER_HW, ISO, VCT_STORAGE_RGBA8, false>(m, sp, ix, iy, iz, vabs(dir), mip);
-        c = fma4(smp, 1.0f, c);
-      }
-      if (c.w < 1.0f) c = fma4(far[k], 1.0f - c.w, c);
+    const V3 sp = march_pos(origin, dir, dist);
+    const float mip = cone_lod(diam * cube_res);
+    if (!(kSkipEmptyRGBA && m.skip_empty && mip < kSkipMaxLod && sample_empty(m, sp, mip))) {
+      const int ix = dir.x < 0.0f ? 0 : 1, iy = dir.y < 0.0f ? 2 : 3, iz = dir.z < 0.0f ? 4 : 5;
+      const float4 smp = sample_voxel<VCT_SAMPLER_HW, ISO, VCT_STORAGE_RGBA8, false>(m, sp, ix, iy, iz, vabs(dir), mip);
+      c = fma4(smp, 1.0f, c);
     }
+    if (c.w < 1.0f) c = fma4(far[k], 1.0f - c.w, c);
     acc = acc + c;
   }
   return v3(acc.x, acc.y, acc.z) * (1.0f / (float)K);
@@ -919,10 +926,11 @@ __global__ void __launch_bounds__(kTraceThreads, SAMPLER == VCT_SAMPLER_HW ? kTr
 #endif
 constexpr int kShareMinBlocks = VCT_SHARE_MIN_BLOCKS;
 
-// k_trace with shared far fields: the warp (a 16x2 strip, eight 2x2 quads)
-// first picks each quad's representative (its first pixel whose diffuse
-// cones are traced) and the pixels that share with it, marches the quads'
-// far fields together (far_fields), then shades its pixels as k_trace does.
+// k_trace with shared far fields: the warp (a 16x2 strip of kShareW x 2
+// groups) first picks each group's representative (its first pixel, row by
+// row, whose diffuse cones are traced) and the pixels that share with it,
+// marches the groups' far fields together (far_fields), then shades its
+// pixels as k_trace does.
 template <bool ISO>
 __global__ void __launch_bounds__(kTraceThreads, kShareMinBlocks)
     k_trace_share(SceneParams sp, CameraParams cp, MapSet m, TraceParams tp, const float4* __restrict__ gb_pos,
@@ -946,8 +954,9 @@ __global__ void __launch_bounds__(kTraceThreads, kShareMinBlocks)
   }
   valid = valid && tp.enable_diffuse && tp.view_voxel_dir >= 7 && !tp.diffuse_in;
   const unsigned vmask = __ballot_sync(0xffffffffu, valid);
-  const int q = (lane & 15) >> 1;
-  const unsigned qv = vmask & ((3u << (2 * q)) | (3u << (16 + 2 * q)));
+  const int q = (lane & 15) / kShareW;
+  const unsigned gbits = (1u << kShareW) - 1u;
+  const unsigned qv = vmask & ((gbits << (kShareW * q)) | (gbits << (16 + kShareW * q)));
   const int rep = qv ? __ffs(qv) - 1 : lane;
   const V3 rpos = v3(__shfl_sync(0xffffffffu, pos.x, rep), __shfl_sync(0xffffffffu, pos.y, rep),
                      __shfl_sync(0xffffffffu, pos.z, rep));

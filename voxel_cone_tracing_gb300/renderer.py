@@ -46,6 +46,9 @@ EXPORTS = [
     "vct_mlp_set_tensor_kernels", "vct_measure_texture_rate", "vct_mlp_set_judge", "vct_mlp_get_judge",
 ]
 DIFFUSE_CONES, DIFFUSE_MLP = 0, 1
+# vct_config.far_share = 1 shares the diffuse cones' far fields within groups
+# of FAR_SHARE_GROUP_W x 2 pixels (k_trace.cu kShareW).
+FAR_SHARE_GROUP_W = 4
 MLP_WEIGHTS = 5 * 64 * 64
 
 
