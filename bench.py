@@ -199,17 +199,29 @@ def run_reference(args):
     return 0
 
 
-def mlp_leg(r, R, scene, ids, stream, flush, steps, plain_stages):
+def mlp_leg(r, R, scene, ids, stream, flush, steps, plain_stages, per_pixel_trace_ms=None):
     """Learned diffuse term: train on this frame's scene (2^24 cone-traced
     surface samples, 1000 Adam steps of 2^18), then time frames that
-    evaluate the network instead of the nine diffuse cones, and compare the
-    frame with the cone-traced one (RGBA8, PSNR)."""
+    evaluate the network instead of the nine diffuse cones (the judge checks
+    1/64 of the pixels against their cones every frame), and compare the
+    frame with the cone-traced one (RGBA8, PSNR).  Then move the light (as
+    the injection leg does) and the camera, and report the network's PSNR
+    against the cones there and what the judge decides."""
     import numpy as np
     import torch
 
-    def frame():
-        R.queue_scene(r, scene, ids)
+    def frame(lights=None, view=None):
+        if view is not None:
+            r.set_camera_transform(view, scene.proj)
+        for mid in ids:
+            r.queue_model(mid)
+        for l in (scene.lights if lights is None else lights):
+            r.queue_point_light(l)
         r.render()
+
+    def psnr(a, b):
+        mse = float(np.mean((a[..., :3] - b[..., :3]) ** 2))
+        return round(10 * np.log10(1.0 / mse), 2) if mse > 0 else None
 
     r.set_diffuse_mode(R.DIFFUSE_CONES)
     frame()
@@ -227,17 +239,73 @@ def mlp_leg(r, R, scene, ids, stream, flush, steps, plain_stages):
         r.synchronize()
         stages.append(r.stage_times())
     got = r.read_frame().astype(np.float64) / 255.0
+    judge = r.mlp_judge()
+    # generalisation: the light moved, then the camera moved
+    moved = scene.lights.copy()
+    moved["position"] = scene.lights["position"] + (0.06, 0.0, -0.03)
+    from voxel_cone_tracing_gb300 import scenes as S
+    view2 = S.look_at((0.12, 0.05, 0.48), (0.0, -0.05, -0.2))
+    out = {}
+    for name, kw in (("light_moved", dict(lights=moved)), ("camera_moved", dict(view=view2))):
+        r.set_diffuse_mode(R.DIFFUSE_CONES)
+        frame(**kw)
+        cones = r.read_frame().astype(np.float64) / 255.0
+        r.set_mlp_judge(0)
+        r.set_diffuse_mode(R.DIFFUSE_MLP)
+        frame(**kw)
+        net = r.read_frame().astype(np.float64) / 255.0
+        r.set_mlp_judge(8, 40.0)
+        frame(**kw)
+        j = r.mlp_judge()
+        out[name] = {"psnr_db_vs_cones": psnr(net, cones), "judge_psnr_db": round(j["last_psnr_db"], 2),
+                     "judge_fell_back": j["diffuse_mode"] == R.DIFFUSE_CONES}
+    r.set_camera_transform(scene.view, scene.proj)
     r.set_diffuse_mode(R.DIFFUSE_CONES)
-    mse = float(np.mean((got[..., :3] - ref[..., :3]) ** 2))
     trace_mlp = statistics.mean(s["trace"] for s in stages)
     trace_cones = statistics.mean(s["trace"] for s in plain_stages)
     value = statistics.mean(s["voxelize"] + s["mipmap"] + s["trace"] for s in stages)
-    return {"value": round(value, 4), "unit": UNIT, "trace_ms": round(trace_mlp, 4),
-            "trace_ms_cones": round(trace_cones, 4), "trace_speedup": round(trace_cones / trace_mlp, 3),
-            "psnr_db_vs_cones": round(10 * np.log10(1.0 / mse), 2) if mse > 0 else None,
-            "train": {"samples": rep["n_samples"], "steps": rep["steps"], "loss_first": rep["loss_first"],
-                      "loss_last": rep["loss_last"], "ms_samples": round(rep["ms_samples"], 2),
-                      "ms_train": round(rep["ms_train"], 2)}}
+    res = {"value": round(value, 4), "unit": UNIT, "trace_ms": round(trace_mlp, 4),
+           "trace_ms_cones": round(trace_cones, 4), "trace_speedup": round(trace_cones / trace_mlp, 3),
+           "psnr_db_vs_cones": psnr(got, ref),
+           "judge": {"stride": judge["stride"], "min_psnr_db": judge["min_psnr_db"],
+                     "last_psnr_db": round(judge["last_psnr_db"], 2), "fallbacks": judge["fallbacks"]},
+           "after_training": out,
+           "train": {"samples": rep["n_samples"], "steps": rep["steps"], "loss_first": rep["loss_first"],
+                     "loss_last": rep["loss_last"], "ms_samples": round(rep["ms_samples"], 2),
+                     "ms_train": round(rep["ms_train"], 2)}}
+    if per_pixel_trace_ms:
+        res["trace_ms_cones_per_pixel"] = round(per_pixel_trace_ms, 4)
+        res["trace_speedup_vs_per_pixel_cones"] = round(per_pixel_trace_ms / trace_mlp, 3)
+    return res
+
+
+def per_pixel_leg(R, torch, scene, steps, flush):
+    """The bench frame with every pixel marching all of its cones
+    (far_share 0, the reference's rule): the exact-rule tracer's stages."""
+    r = R.Renderer(WIDTH, HEIGHT, grid_res=GRID, far_share=0)
+    ids = R.load_scene(r, scene)
+    r.set_voxel_view_dir(7, 0.0)
+    stream = torch.cuda.Stream()
+    r.set_stream(stream.cuda_stream)
+    for _ in range(3):
+        R.queue_scene(r, scene, ids)
+        r.render()
+    r.synchronize()
+    stages = []
+    for _ in range(steps):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        R.queue_scene(r, scene, ids)
+        r.render()
+        r.synchronize()
+        stages.append(r.stage_times())
+    r.close()
+    mean = lambda key: statistics.mean(st[key] for st in stages)  # noqa: E731
+    return {"workload": "bench frame, every pixel marching all its cones (far_share 0)", "unit": UNIT,
+            "value": round(mean("voxelize") + mean("mipmap") + mean("trace"), 4),
+            "stages_ms": {k: round(mean(k), 4) for k in ("voxelize", "mipmap", "gbuffer", "trace")},
+            "fetches": {"two_level_per_pixel": TRACE_FETCH_QUAD_PER_PIXEL_NOSHARE,
+                        "one_level_per_pixel": TRACE_FETCH_TRI_PER_PIXEL_NOSHARE}}
 
 
 def precision_leg(R, torch, steps, flush_mb=256):
@@ -551,7 +619,7 @@ def run_ours(args):
         "e2e": {"value": round(e2e_ms, 4), "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "statistic": "median of per-step host wall times", "mean": round(e2e_mean, 4)},
         "gpu_launches": int(sum(st["kernel_launches"] for st in stages)),
-        "roofline": {"kernel": "k_trace", "bound": "tex", "achieved": round(achieved_tex, 2),
+        "roofline": {"kernel": "k_trace_share", "bound": "tex", "achieved": round(achieved_tex, 2),
                      "peak": round(rate_quad / 1e9, 2), "unit": "Gfetch/s", "frac": round(achieved_tex * 1e9 / rate_quad, 4),
                      "traffic": traffic, "peak_source": "measured in this run (vct_measure_texture_rate)",
                      "fetches": {"two_level_per_pixel": TRACE_FETCH_QUAD_PER_PIXEL,
@@ -573,8 +641,10 @@ def run_ours(args):
                              "algorithmic_bytes": trace_bytes}},
         "clocks": clk.summary(),
     }
+    line["per_pixel_cones"] = per_pixel_leg(R, torch, scene, min(args.steps, 20), flush)
     if not args.no_mlp:
-        line["mlp"] = mlp_leg(r, R, scene, ids, stream, flush, min(args.steps, 20), stages)
+        line["mlp"] = mlp_leg(r, R, scene, ids, stream, flush, min(args.steps, 20), stages,
+                              line["per_pixel_cones"]["stages_ms"]["trace"])
     line["overlap_raster"] = overlap_leg(R, torch, scene, min(args.steps, 20), flush)
     line["injection"] = injection_leg(R, torch, scene, min(args.steps, 20), flush)
     if not args.no_precision:
