@@ -1086,36 +1086,61 @@ __global__ void __launch_bounds__(256) k_trace_points(MapSet m, int cone_set, fl
 
 // The judge of the learned diffuse term (launch_judge_diffuse): one pixel
 // per stride x stride tile, the same visibility and within_cube test as
-// trace_px, the nine cones of trace_diffuse with the texture unit against
-// the network's prediction of them.
+// trace_px, the cones of trace_diffuse with the texture unit against the
+// network's prediction of them.  A CTA judges 32 pixels with one thread per
+// (pixel, cone), so that the few judged pixels still fill the GPU; the
+// cones of a pixel are summed in trace_diffuse's order.
+constexpr int kJudgePixels = 32;
 template <bool ISO>
-__global__ void __launch_bounds__(128) k_judge_diffuse(SceneParams sp, MapSet m, TraceParams tp, int W, int H,
-                                                       const float4* __restrict__ gb_pos,
-                                                       const float4* __restrict__ gb_nrm,
-                                                       const float4* __restrict__ net, int stride, int ox, int oy,
-                                                       FrameStatus* __restrict__ status) {
-  const int px = (blockIdx.x * 16 + (threadIdx.x & 15)) * stride + ox;
-  const int py = (blockIdx.y * 8 + (threadIdx.x >> 4)) * stride + oy;
-  float e = 0.0f;
-  uint32_t n = 0;
-  if (px < W && py < H) {
-    const size_t p = (size_t)py * W + px;
-    const float4 g0 = gb_pos[p], g1 = gb_nrm[p];
-    if (__float_as_uint(g1.w) != 0xffffffffu) {
-      const V3 pos = v3(g0.x / sp.cube_size, g0.y / sp.cube_size, g0.z / sp.cube_size) * 0.5f + v3(0.5f, 0.5f, 0.5f);
-      if (fabsf(pos.x) < 1.0f && fabsf(pos.y) < 1.0f && fabsf(pos.z) < 1.0f) {
-        const V3 d = trace_diffuse<VCT_SAMPLER_HW, ISO, VCT_STORAGE_RGBA8>(m, tp.cone_set, pos, v3(g1.x, g1.y, g1.z));
-        const float4 q = net[p];
-        e = (d.x - q.x) * (d.x - q.x) + (d.y - q.y) * (d.y - q.y) + (d.z - q.z) * (d.z - q.z);
-        n = 1;
+__global__ void __launch_bounds__(kJudgePixels * 9) k_judge_diffuse(SceneParams sp, MapSet m, TraceParams tp, int W,
+                                                                    int H, const float4* __restrict__ gb_pos,
+                                                                    const float4* __restrict__ gb_nrm,
+                                                                    const float4* __restrict__ net, int stride, int ox,
+                                                                    int oy, int tw, int n_judged,
+                                                                    FrameStatus* __restrict__ status) {
+  __shared__ float4 s_cone[9][kJudgePixels];
+  const int j = threadIdx.x % kJudgePixels, k = threadIdx.x / kJudgePixels;
+  const int K = tp.cone_set == VCT_CONES_SIX60 ? 6 : 9;
+  const int i = blockIdx.x * kJudgePixels + j;
+  bool judged = false;
+  size_t p = 0;
+  if (i < n_judged) {
+    const int px = (i % tw) * stride + ox, py = (i / tw) * stride + oy;
+    if (px < W && py < H) {
+      p = (size_t)py * W + px;
+      const float4 g0 = gb_pos[p], g1 = gb_nrm[p];
+      if (__float_as_uint(g1.w) != 0xffffffffu) {
+        const V3 pos =
+            v3(g0.x / sp.cube_size, g0.y / sp.cube_size, g0.z / sp.cube_size) * 0.5f + v3(0.5f, 0.5f, 0.5f);
+        judged = fabsf(pos.x) < 1.0f && fabsf(pos.y) < 1.0f && fabsf(pos.z) < 1.0f;
+        if (judged && k < K) {
+          const V3 n = v3(g1.x, g1.y, g1.z);
+          const V3 o1 = normalize(tangent(n));
+          const V3 o2 = normalize(cross(o1, n));
+          float ap;
+          const V3 d = diffuse_dir(tp.cone_set, n, o1, o2, k, ap);
+          s_cone[k][j] = trace_cone<VCT_SAMPLER_HW, ISO, VCT_STORAGE_RGBA8>(m, pos, d, ap, kMaxDistance);
+        }
       }
     }
+  }
+  __syncthreads();
+  if (k != 0) return;  // one warp sums
+  float e = 0.0f;
+  uint32_t n = 0;
+  if (judged) {
+    float4 acc = f4(0.f, 0.f, 0.f, 0.f);
+    for (int c = 0; c < K; ++c) acc = acc + s_cone[c][j];
+    const V3 d = v3(acc.x, acc.y, acc.z) * (1.0f / (float)K);
+    const float4 q = net[p];
+    e = (d.x - q.x) * (d.x - q.x) + (d.y - q.y) * (d.y - q.y) + (d.z - q.z) * (d.z - q.z);
+    n = 1;
   }
   for (int o = 16; o > 0; o >>= 1) {
     e += __shfl_xor_sync(0xffffffffu, e, o);
     n += __shfl_xor_sync(0xffffffffu, n, o);
   }
-  if ((threadIdx.x & 31) == 0 && n) {
+  if (threadIdx.x == 0 && n) {
     atomicAdd(&status->judge_sse, e);
     atomicAdd(&status->judge_n, n);
   }
@@ -1129,11 +1154,14 @@ cudaError_t launch_judge_diffuse(const SceneParams& sp, const CameraParams& cp, 
   if (stride < 1) return cudaSuccess;
   const int tw = (cp.W - ox + stride - 1) / stride, th = (cp.H - oy + stride - 1) / stride;
   if (tw <= 0 || th <= 0) return cudaSuccess;
-  dim3 grid((tw + 15) / 16, (th + 7) / 8);
+  const int n_judged = tw * th;
+  const unsigned blocks = (unsigned)((n_judged + kJudgePixels - 1) / kJudgePixels);
   if (tp.mip_mode == VCT_MIP_ISO)
-    k_judge_diffuse<true><<<grid, 128, 0, st>>>(sp, ms, tp, cp.W, cp.H, gb_pos, gb_nrm, net, stride, ox, oy, status);
+    k_judge_diffuse<true><<<blocks, kJudgePixels * 9, 0, st>>>(sp, ms, tp, cp.W, cp.H, gb_pos, gb_nrm, net, stride, ox,
+                                                              oy, tw, n_judged, status);
   else
-    k_judge_diffuse<false><<<grid, 128, 0, st>>>(sp, ms, tp, cp.W, cp.H, gb_pos, gb_nrm, net, stride, ox, oy, status);
+    k_judge_diffuse<false><<<blocks, kJudgePixels * 9, 0, st>>>(sp, ms, tp, cp.W, cp.H, gb_pos, gb_nrm, net, stride,
+                                                               ox, oy, tw, n_judged, status);
   return cudaGetLastError();
 }
 
