@@ -423,8 +423,9 @@ def batch_leg(R, torch, steps, rank=0, world=1, pg=None):
     990-865k triangles, frames 256^2-1920x1080, 9 or 6 diffuse cones), one
     frame of all of them per step: every stage pass one persistent launch
     over all scenes, the frame captured once in a CUDA graph and replayed,
-    launch shapes chosen by the autotuner.  Compared with the same 64 scenes
-    rendered one after another by 64 Renderers on one stream.  With N ranks
+    launch shapes chosen by the autotuner, shared far fields as a Renderer's
+    default.  Compared with the same 64 scenes rendered one after another by
+    64 Renderers (same settings) on one stream.  With N ranks
     the scenes are split between them by cost (no data moves between
     GPUs); times are the max over ranks."""
     from voxel_cone_tracing_gb300 import replicas, scenes
@@ -453,7 +454,7 @@ def batch_leg(R, torch, steps, rank=0, world=1, pg=None):
     # the same scenes, one Renderer each, rendered one after another
     rs = []
     for s, w, h, g, c in items:
-        r = R.Renderer(w, h, grid_res=g, cone_set=c, far_share=0)  # per-pixel cones, as the batch
+        r = R.Renderer(w, h, grid_res=g, cone_set=c)
         ids = R.load_scene(r, s)
         r.set_voxel_view_dir(7, 0.0)
         r.set_stream(stream.cuda_stream)

@@ -458,20 +458,30 @@ typedef struct {
 typedef struct {
   int32_t vox_mode;   /* VCT_VOX_* for every scene */
   int32_t use_graph;  /* capture the frame once in a CUDA graph, then replay it */
-  int32_t reserved[6];
+  int32_t far_share;  /* 1: shared far fields of the diffuse cones, as
+                       * vct_config.far_share (vct_batch_config_default sets
+                       * it); 0: every pixel marches all its cones          */
+  int32_t reserved[5];
 } vct_batch_config;
+
+/* vox_mode VCT_VOX_REF_RASTER2X, no graph, far_share 1 (a Renderer's default). */
+void vct_batch_config_default(vct_batch_config* cfg);
 
 /* Launch shapes of the batched kernels: persistent CTAs per SM of the
  * binning, brick and trace launches, the trace's tile scheduling (1 =
- * atomic tile queue, 0 = static stride), and the trace's form: 0 = one
+ * atomic tile queue, 0 = static stride), the trace's form: 0 = one
  * persistent launch over all scenes, 1 = one launch of the one-scene trace
- * kernel per scene, spread over parallel streams (graph branches). */
+ * kernel per scene, spread over parallel streams (graph branches), and the
+ * tile of the per-scene shared-far-field trace.  Every shape renders the
+ * same frames. */
 typedef struct {
   int32_t bin_ctas_per_sm;
   int32_t bricks_ctas_per_sm;
   int32_t trace_ctas_per_sm;
   int32_t trace_dynamic;
   int32_t trace_per_scene;
+  int32_t trace_tile_rows;  /* per-scene shared-far-field trace: CTA tile 16 x 8
+                             * or 16 x 16 pixels (the same frame either way) */
 } vct_batch_shape;
 
 typedef struct vct_batch vct_batch;

@@ -23,9 +23,8 @@ def _items():
     return out
 
 
-def _single(vct, scene, w, h, grid, cones, vox_mode=0, view=None):
-    # a batch marches every pixel's cones: compare with a Renderer that does too
-    r = vct.Renderer(w, h, grid_res=grid, cone_set=cones, vox_mode=vox_mode, far_share=0)
+def _single(vct, scene, w, h, grid, cones, vox_mode=0, view=None, far_share=1):
+    r = vct.Renderer(w, h, grid_res=grid, cone_set=cones, vox_mode=vox_mode, far_share=far_share)
     ids = vct.load_scene(r, scene)
     if view is not None:
         r.set_camera_transform(view, scene.proj)
@@ -35,9 +34,9 @@ def _single(vct, scene, w, h, grid, cones, vox_mode=0, view=None):
     return r
 
 
-def _check_scene(vct, b, i, item, vox_mode=0, view=None):
+def _check_scene(vct, b, i, item, vox_mode=0, view=None, far_share=1):
     scene, w, h, grid, cones = item
-    r = _single(vct, scene, w, h, grid, cones, vox_mode, view)
+    r = _single(vct, scene, w, h, grid, cones, vox_mode, view, far_share)
     np.testing.assert_array_equal(b.read_frame(i), r.read_frame(), err_msg=f"scene {i} frame")
     np.testing.assert_array_equal(b.read_voxels(i, 0), r.read_voxels(0), err_msg=f"scene {i} level 0")
     n, levels = r.grid()
@@ -60,18 +59,22 @@ def test_batch_rejects_bad_scenes(vct):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("per_scene", [0, 1], ids=["persistent_trace", "per_scene_trace"])
+@pytest.mark.parametrize("far_share", [1, 0], ids=["shared_far", "per_pixel"])
+@pytest.mark.parametrize("per_scene", [0, 1, 16], ids=["persistent_trace", "per_scene_trace", "per_scene_16_rows"])
 @pytest.mark.parametrize("use_graph", [False, True], ids=["eager", "graph"])
-def test_batch_matches_renderer(vct, use_graph, per_scene):
+def test_batch_matches_renderer(vct, use_graph, per_scene, far_share):
+    """Every trace form (one persistent launch; one launch per scene with
+    16x8 or 16x16 tiles) renders each scene exactly as a Renderer with the
+    same far_share does."""
     items = _items()
-    b = vct.Batch(items, use_graph=use_graph)
-    b.shape = dict(b.shape, trace_per_scene=per_scene)
+    b = vct.Batch(items, use_graph=use_graph, far_share=far_share)
+    b.shape = dict(b.shape, trace_per_scene=int(per_scene != 0), trace_tile_rows=16 if per_scene == 16 else 8)
     b.render()
     b.render()  # a second frame (a graph replay) gives the same result
     t = b.stage_times()
     assert t["kernel_launches"] > 0 and t["total"] > 0
     for i, item in enumerate(items):
-        _check_scene(vct, b, i, item)
+        _check_scene(vct, b, i, item, far_share=far_share)
 
 
 @pytest.mark.gpu
@@ -108,7 +111,7 @@ def test_batch_autotune_keeps_results(vct):
     assert rep["shape"] == b.shape
     assert rep["ms_after"] <= rep["ms_before"] + 1e-6
     assert rep["shape"]["trace_ctas_per_sm"] in (2, 3) and rep["shape"]["trace_dynamic"] in (0, 1)
-    assert rep["shape"]["trace_per_scene"] in (0, 1)
+    assert rep["shape"]["trace_per_scene"] in (0, 1) and rep["shape"]["trace_tile_rows"] in (8, 16)
     b.render()
     for i in range(len(items)):
         np.testing.assert_array_equal(b.read_frame(i), before[i])
@@ -156,13 +159,14 @@ def test_batch_scenes_against_oracle(vct, oracle):
     with 9 cones).  Level 0 within 1 LSB of the oracle's with the same
     occupancy, every directional mip level bit-exact from the GPU's level 0,
     and the RGBA8 frame against the oracle's own voxelize -> mip -> G-buffer
-    -> trace at PSNR >= 40 dB (texture-unit sampler, end to end)."""
+    -> trace (its restatement of the shared far fields, the batch's default)
+    at PSNR >= 40 dB (texture-unit sampler, end to end)."""
     bench_items = scenes.batch_scenes(n=7)
     items = [_items()[0], _items()[4], bench_items[0], bench_items[1], bench_items[6]]
     b = vct.Batch(items, use_graph=True)
     b.render()
     for i, (scene, w, h, grid, cones) in enumerate(items):
-        p = oracle.Params(grid_res=grid, width=w, height=h, cone_set=cones)
+        p = oracle.Params(grid_res=grid, width=w, height=h, cone_set=cones, far_share=vct.FAR_SHARE_GROUP_W)
         ref = oracle.render(scene, p)
         l0 = b.read_voxels(i, 0)
         d = np.abs(l0.astype(int) - ref["level0"].astype(int))

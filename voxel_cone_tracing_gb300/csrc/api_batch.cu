@@ -59,7 +59,7 @@ struct vct_batch {
   vct_batch_config cfg;
   std::vector<std::unique_ptr<SceneRes>> scenes;
   int sms = 148;
-  BatchShape shape = {8, 8, 3, 1, 1};
+  BatchShape shape = {8, 8, 3, 1, 1, 8};
   // device descriptors
   DevBuf<BatchScene> d_scenes;
   HostBuf<CameraParams> h_cams;
@@ -207,7 +207,9 @@ struct vct_batch {
       for (size_t i = 0; i < trace_order.size(); ++i) {
         const int s = trace_order[i];
         const SceneRes& r = *scenes[s];
-        VCT_CUDA(launch_trace(r.sp, h_cams.p[s], r.maps.ms, r.tp, gb_pos.p + px_base[s], gb_nrm.p + px_base[s],
+        TraceParams tp = r.tp;
+        tp.tile_rows = shape.trace_tile_rows;
+        VCT_CUDA(launch_trace(r.sp, h_cams.p[s], r.maps.ms, tp, gb_pos.p + px_base[s], gb_nrm.p + px_base[s],
                               frame.p + px_base[s], nullptr, side[i % kSide], &launches));
       }
       for (int k = 0; k < kSide; ++k) {
@@ -215,7 +217,7 @@ struct vct_batch {
         VCT_CUDA(cudaStreamWaitEvent(stream, join_ev[k], 0));
       }
     } else {
-      VCT_CUDA(launch_trace_batch(work(tiles, true), bb, shape, sms, stream, &launches));
+      VCT_CUDA(launch_trace_batch(work(tiles, true), bb, shape, sms, stream, &launches, cfg.far_share != 0));
     }
     VCT_CUDA(record(4));
     VCT_CUDA(cudaMemcpyAsync(h_status.p, d_status.p, sizeof(FrameStatus), cudaMemcpyDeviceToHost, stream));
@@ -320,7 +322,7 @@ vct_status upload(DevBuf<T>& d, const T* h, size_t n) {
   return VCT_OK;
 }
 
-vct_status build_scene(const vct_batch_scene& d, SceneRes& r) {
+vct_status build_scene(const vct_batch_scene& d, SceneRes& r, int far_share) {
   r.W = d.width;
   r.H = d.height;
   r.N = d.grid_res;
@@ -371,6 +373,7 @@ vct_status build_scene(const vct_batch_scene& d, SceneRes& r) {
   r.tp.cone_set = d.cone_set;
   r.tp.sampler = VCT_SAMPLER_HW;
   r.tp.mip_mode = VCT_MIP_ANISO;
+  r.tp.far_share = far_share;
   std::memcpy(r.view, d.view, sizeof(r.view));
   std::memcpy(r.proj, d.proj, sizeof(r.proj));
   return VCT_OK;
@@ -400,7 +403,7 @@ vct_status build_batch(vct_batch* b, const vct_batch_scene* descs, uint32_t n) {
   uint64_t total_tris = 0;
   for (uint32_t i = 0; i < n; ++i) {
     b->scenes.emplace_back(new SceneRes());
-    VCT_CHECK(build_scene(descs[i], *b->scenes.back()));
+    VCT_CHECK(build_scene(descs[i], *b->scenes.back(), b->cfg.far_share));
     const SceneRes& r = *b->scenes.back();
     const uint32_t nb = (uint32_t)(r.N / kBrick);
     c_tris.push_back((r.n_tris + 31u) & ~31u);
@@ -485,6 +488,7 @@ extern "C" vct_status vct_batch_create(const vct_batch_scene* scenes, uint32_t n
   if (cfg) c = *cfg;
   if (c.vox_mode != VCT_VOX_REF_RASTER2X && c.vox_mode != VCT_VOX_CONSERVATIVE)
     return set_error(VCT_ERR_INVALID_VALUE, "vox_mode %d", c.vox_mode);
+  if (c.far_share != 0 && c.far_share != 1) return set_error(VCT_ERR_INVALID_VALUE, "far_share %d", c.far_share);
   for (uint32_t i = 0; i < n_scenes; ++i) VCT_CHECK(check_scene(scenes[i], i));
   VCT_CHECK(ensure_device());
   std::unique_ptr<vct_batch> b(new vct_batch());
@@ -495,6 +499,13 @@ extern "C" vct_status vct_batch_create(const vct_batch_scene* scenes, uint32_t n
 }
 
 extern "C" void vct_batch_destroy(vct_batch* b) { delete b; }
+
+extern "C" void vct_batch_config_default(vct_batch_config* cfg) {
+  if (!cfg) return;
+  std::memset(cfg, 0, sizeof(*cfg));
+  cfg->vox_mode = VCT_VOX_REF_RASTER2X;
+  cfg->far_share = 1;
+}
 
 extern "C" vct_status vct_batch_set_camera(vct_batch* b, uint32_t scene, const float view[16],
                                            const float proj[16]) {
@@ -597,6 +608,7 @@ extern "C" vct_status vct_batch_get_shape(vct_batch* b, vct_batch_shape* out) {
   out->trace_ctas_per_sm = b->shape.trace_ctas_per_sm;
   out->trace_dynamic = b->shape.trace_dynamic;
   out->trace_per_scene = b->shape.trace_per_scene;
+  out->trace_tile_rows = b->shape.trace_tile_rows;
   return VCT_OK;
 }
 
@@ -605,7 +617,8 @@ extern "C" vct_status vct_batch_set_shape(vct_batch* b, const vct_batch_shape* s
   if (!b || !s) return set_error(VCT_ERR_INVALID_VALUE, "NULL argument");
   if (s->bin_ctas_per_sm < 1 || s->bin_ctas_per_sm > 32 || s->bricks_ctas_per_sm < 1 ||
       s->bricks_ctas_per_sm > 32 || s->trace_ctas_per_sm < 1 || s->trace_ctas_per_sm > 3 ||
-      (s->trace_dynamic != 0 && s->trace_dynamic != 1) || (s->trace_per_scene != 0 && s->trace_per_scene != 1))
+      (s->trace_dynamic != 0 && s->trace_dynamic != 1) || (s->trace_per_scene != 0 && s->trace_per_scene != 1) ||
+      (s->trace_tile_rows != 8 && s->trace_tile_rows != 16))
     return set_error(VCT_ERR_INVALID_VALUE, "launch shape out of range");
   VCT_CHECK(b->finish());
   b->shape.bin_ctas_per_sm = s->bin_ctas_per_sm;
@@ -613,6 +626,7 @@ extern "C" vct_status vct_batch_set_shape(vct_batch* b, const vct_batch_shape* s
   b->shape.trace_ctas_per_sm = s->trace_ctas_per_sm;
   b->shape.trace_dynamic = s->trace_dynamic;
   b->shape.trace_per_scene = s->trace_per_scene;
+  b->shape.trace_tile_rows = s->trace_tile_rows;
   b->drop_graph();  // launch shapes are baked into a captured graph
   return VCT_OK;
 }
@@ -655,6 +669,7 @@ extern "C" vct_status vct_batch_autotune(vct_batch* b, int32_t frames, vct_batch
   const int trace_c[] = {2, 3};
   const int dyn_c[] = {0, 1};
   const int per_scene_c[] = {0, 1};
+  const int rows_c[] = {8, 16};
   auto try_field = [&](int BatchShape::*field, const auto& cand) -> vct_status {
     const int nc = (int)(sizeof(cand) / sizeof(cand[0]));
     for (int k = 0; k < nc; ++k) {
@@ -673,6 +688,7 @@ extern "C" vct_status vct_batch_autotune(vct_batch* b, int32_t frames, vct_batch
     return VCT_OK;
   };
   VCT_CHECK(try_field(&BatchShape::trace_per_scene, per_scene_c));
+  if (cur.trace_per_scene && b->cfg.far_share) VCT_CHECK(try_field(&BatchShape::trace_tile_rows, rows_c));
   VCT_CHECK(try_field(&BatchShape::trace_dynamic, dyn_c));
   VCT_CHECK(try_field(&BatchShape::trace_ctas_per_sm, trace_c));
   VCT_CHECK(try_field(&BatchShape::bricks_ctas_per_sm, brick_c));
@@ -685,6 +701,7 @@ extern "C" vct_status vct_batch_autotune(vct_batch* b, int32_t frames, vct_batch
     best->trace_ctas_per_sm = cur.trace_ctas_per_sm;
     best->trace_dynamic = cur.trace_dynamic;
     best->trace_per_scene = cur.trace_per_scene;
+    best->trace_tile_rows = cur.trace_tile_rows;
   }
   if (ms_before) *ms_before = base;
   if (ms_after) *ms_after = cur_ms;

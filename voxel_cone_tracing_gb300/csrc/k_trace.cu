@@ -926,20 +926,18 @@ __global__ void __launch_bounds__(kTraceThreads, SAMPLER == VCT_SAMPLER_HW ? kTr
 #endif
 constexpr int kShareMinBlocks = VCT_SHARE_MIN_BLOCKS;
 
-// k_trace with shared far fields: the warp (a 16x2 strip of kShareW x 2
-// groups) first picks each group's representative (its first pixel, row by
-// row, whose diffuse cones are traced) and the pixels that share with it,
-// marches the groups' far fields together (far_fields), then shades its
-// pixels as k_trace does.
+// One pixel of k_trace_share: the warp (a 16x2 strip of kShareW x 2
+// groups, its rows starting at an even frame row) first picks each group's
+// representative (its first pixel, row by row, whose diffuse cones are
+// traced) and the pixels that share with it, marches the groups' far fields
+// together (far_fields), then shades its pixels as k_trace does.  Called by
+// all 32 lanes of a warp together; fw is the warp's shared-memory block.
 template <bool ISO>
-__global__ void __launch_bounds__(kTraceThreads, kShareMinBlocks)
-    k_trace_share(SceneParams sp, CameraParams cp, MapSet m, TraceParams tp, const float4* __restrict__ gb_pos,
-                  const float4* __restrict__ gb_nrm, uchar4* __restrict__ frame, float4* __restrict__ frame_f32) {
-  static_assert(kTraceThreads % 32 == 0, "whole warps");
-  __shared__ FarWarp s_far[kTraceThreads / 32];
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int px = blockIdx.x * 16 + (threadIdx.x & 15), py = blockIdx.y * kTraceRows + (threadIdx.x >> 4);
-  FarWarp& fw = s_far[warp];
+__device__ __forceinline__ void trace_px_share(const SceneParams& sp, const CameraParams& cp, const MapSet& m,
+                                               const TraceParams& tp, const float4* __restrict__ gb_pos,
+                                               const float4* __restrict__ gb_nrm, uchar4* __restrict__ frame,
+                                               float4* __restrict__ frame_f32, int px, int py, FarWarp& fw) {
+  const int lane = threadIdx.x & 31;
   bool valid = false;
   V3 pos = v3(0.f, 0.f, 0.f), nrm = v3(0.f, 0.f, 1.f);
   if (px < cp.W && py < cp.H) {
@@ -989,6 +987,19 @@ __global__ void __launch_bounds__(kTraceThreads, kShareMinBlocks)
   __syncwarp();
   trace_px<VCT_SAMPLER_HW, ISO, VCT_STORAGE_RGBA8, true>(sp, cp, m, tp, gb_pos, gb_nrm, frame, frame_f32, px, py,
                                                          share ? fw.far + slot * K : nullptr);
+  __syncwarp();  // fw is free for the warp's next use
+}
+
+// k_trace with shared far fields: a CTA shades a 16 x ROWS tile (8 or 16
+// rows: the same warps, 16x2 strips, so the same frame either way).
+template <bool ISO, int ROWS>
+__global__ void __launch_bounds__(16 * ROWS, kShareMinBlocks * 8 / ROWS)
+    k_trace_share(SceneParams sp, CameraParams cp, MapSet m, TraceParams tp, const float4* __restrict__ gb_pos,
+                  const float4* __restrict__ gb_nrm, uchar4* __restrict__ frame, float4* __restrict__ frame_f32) {
+  static_assert(ROWS % 2 == 0, "whole 16x2 warps");
+  __shared__ FarWarp s_far[ROWS / 2];
+  trace_px_share<ISO>(sp, cp, m, tp, gb_pos, gb_nrm, frame, frame_f32, blockIdx.x * 16 + (threadIdx.x & 15),
+                      blockIdx.y * ROWS + (threadIdx.x >> 4), s_far[threadIdx.x >> 5]);
 }
 
 // One pixel of a batch scene.  Called, not inlined, from the tile loop of
@@ -1011,6 +1022,15 @@ __device__ VCT_BATCH_PX_FN void trace_batch_px(const float4* __restrict__ gb_pos
                                             uchar4* __restrict__ frame, int px, int py) {
   trace_px<VCT_SAMPLER_HW, ISO, VCT_STORAGE_RGBA8>(s_batch_scene.sp, s_batch_cam, s_batch_scene.ms,
                                                    s_batch_scene.tp, gb_pos, gb_nrm, frame, nullptr, px, py);
+}
+
+// trace_px_share on the CTA's current batch scene (k_trace_batch_share);
+// called, not inlined, for the same reason as trace_batch_px.
+__device__ VCT_BATCH_PX_FN void trace_batch_px_share(const float4* __restrict__ gb_pos,
+                                                  const float4* __restrict__ gb_nrm, uchar4* __restrict__ frame,
+                                                  int px, int py, FarWarp& fw) {
+  trace_px_share<false>(s_batch_scene.sp, s_batch_cam, s_batch_scene.ms, s_batch_scene.tp, gb_pos, gb_nrm, frame,
+                        nullptr, px, py, fw);
 }
 
 // The 16x16 tiles of every scene of a batch in one persistent launch.  With
@@ -1050,6 +1070,56 @@ __global__ void __launch_bounds__(256, kTraceBatchMinBlocks) k_trace_batch(Batch
     const uint32_t lt = g - __ldg(w.prefix + s), tiles_x = (uint32_t)(s_sc.W + 15) / 16;
     trace_batch_px<ISO>(bb.rb.gb_pos + s_sc.px_base, bb.rb.gb_nrm + s_sc.px_base, bb.frame + s_sc.px_base,
                         (int)(lt % tiles_x) * 16 + (threadIdx.x & 15), (int)(lt / tiles_x) * 16 + (threadIdx.x >> 4));
+    if (w.queue) {
+      __syncthreads();  // every thread has read s_next
+      if (threadIdx.x == 0) s_next = atomicAdd(w.queue, 1u);
+      __syncthreads();
+      g = s_next;
+    } else {
+      g += gridDim.x;
+    }
+  }
+}
+
+// k_trace_batch with shared far fields (the batch's far_share): every 16x16
+// tile is eight 16x2 warps, as in k_trace_share, so each scene's frame equals
+// a Renderer's with far_share 1.  Anisotropic maps (the batch's).
+#ifndef VCT_TRACE_BATCH_SHARE_MIN_BLOCKS
+#define VCT_TRACE_BATCH_SHARE_MIN_BLOCKS 4
+#endif
+constexpr int kTraceBatchShareMinBlocks = VCT_TRACE_BATCH_SHARE_MIN_BLOCKS;
+__global__ void __launch_bounds__(256, kTraceBatchShareMinBlocks) k_trace_batch_share(BatchWork w, BatchBuffers bb) {
+  __shared__ FarWarp s_far[8];
+  __shared__ uint32_t s_next;
+  __shared__ int s_cur;
+  BatchScene& s_sc = s_batch_scene;
+  CameraParams& s_cam = s_batch_cam;
+  static_assert(sizeof(BatchScene) % 4 == 0 && sizeof(CameraParams) % 4 == 0, "word copies");
+  uint32_t g = blockIdx.x;
+  if (threadIdx.x == 0) s_cur = -1;
+  if (w.queue) {
+    if (threadIdx.x == 0) s_next = atomicAdd(w.queue, 1u);
+    __syncthreads();
+    g = s_next;
+  }
+  __syncthreads();
+  while (g < w.total) {
+    const int s = batch_scene_of(w, g);
+    if (s != s_cur) {  // CTA-uniform
+      __syncthreads();  // the previous tile is done with the old scene
+      const uint32_t* src = reinterpret_cast<const uint32_t*>(w.scenes + s);
+      for (int i = threadIdx.x; i < (int)(sizeof(BatchScene) / 4); i += blockDim.x)
+        reinterpret_cast<uint32_t*>(&s_sc)[i] = __ldg(src + i);
+      const uint32_t* csrc = reinterpret_cast<const uint32_t*>(w.cams + s);
+      for (int i = threadIdx.x; i < (int)(sizeof(CameraParams) / 4); i += blockDim.x)
+        reinterpret_cast<uint32_t*>(&s_cam)[i] = __ldg(csrc + i);
+      __syncthreads();
+      if (threadIdx.x == 0) s_cur = s;
+    }
+    const uint32_t lt = g - __ldg(w.prefix + s), tiles_x = (uint32_t)(s_sc.W + 15) / 16;
+    trace_batch_px_share(bb.rb.gb_pos + s_sc.px_base, bb.rb.gb_nrm + s_sc.px_base, bb.frame + s_sc.px_base,
+                         (int)(lt % tiles_x) * 16 + (threadIdx.x & 15), (int)(lt / tiles_x) * 16 + (threadIdx.x >> 4),
+                         s_far[threadIdx.x >> 5]);
     if (w.queue) {
       __syncthreads();  // every thread has read s_next
       if (threadIdx.x == 0) s_next = atomicAdd(w.queue, 1u);
@@ -1175,13 +1245,20 @@ cudaError_t launch_trace_points(const SceneParams&, const MapSet& ms, int mip_mo
 }
 
 cudaError_t launch_trace_batch(const BatchWork& tiles, const BatchBuffers& bb, const BatchShape& shape, int sms,
-                               cudaStream_t st, int* launches) {
+                               cudaStream_t st, int* launches, bool share) {
   if (!tiles.total) return cudaSuccess;
   BatchWork w = tiles;
   if (!shape.trace_dynamic) w.queue = nullptr;
   else {
     cudaError_t e = cudaMemsetAsync(w.queue, 0, sizeof(uint32_t), st);
     if (e != cudaSuccess) return e;
+  }
+  if (share) {
+    const int per_sm = std::min(std::max(shape.trace_ctas_per_sm, 1), kTraceBatchShareMinBlocks);
+    const unsigned grid = (unsigned)std::max(1, std::min<int>(sms * per_sm, (int)tiles.total));
+    k_trace_batch_share<<<grid, 256, 0, st>>>(w, bb);
+    if (launches) ++*launches;
+    return cudaGetLastError();
   }
   const int per_sm = std::min(std::max(shape.trace_ctas_per_sm, 1), kTraceBatchMinBlocks);
   const unsigned grid = (unsigned)std::max(1, std::min<int>(sms * per_sm, (int)tiles.total));
@@ -1203,11 +1280,15 @@ cudaError_t launch_trace(const SceneParams& sp, const CameraParams& cp, const Ma
                : run<VCT_SAMPLER_EXACT, false, VCT_STORAGE_RGBA16F>(sp, cp, ms, tp, gb_pos, gb_nrm, frame, frame_f32, st);
   }
   if (tp.far_share && tp.enable_diffuse && !tp.diffuse_in && tp.view_voxel_dir >= 7) {
-    dim3 grid((cp.W + 15) / 16, (cp.H + kTraceRows - 1) / kTraceRows);
-    if (iso)
-      k_trace_share<true><<<grid, kTraceThreads, 0, st>>>(sp, cp, ms, tp, gb_pos, gb_nrm, frame, frame_f32);
-    else
-      k_trace_share<false><<<grid, kTraceThreads, 0, st>>>(sp, cp, ms, tp, gb_pos, gb_nrm, frame, frame_f32);
+    if (tp.tile_rows == 16) {
+      dim3 grid((cp.W + 15) / 16, (cp.H + 15) / 16);
+      if (iso) k_trace_share<true, 16><<<grid, 256, 0, st>>>(sp, cp, ms, tp, gb_pos, gb_nrm, frame, frame_f32);
+      else k_trace_share<false, 16><<<grid, 256, 0, st>>>(sp, cp, ms, tp, gb_pos, gb_nrm, frame, frame_f32);
+    } else {
+      dim3 grid((cp.W + 15) / 16, (cp.H + 7) / 8);
+      if (iso) k_trace_share<true, 8><<<grid, 128, 0, st>>>(sp, cp, ms, tp, gb_pos, gb_nrm, frame, frame_f32);
+      else k_trace_share<false, 8><<<grid, 128, 0, st>>>(sp, cp, ms, tp, gb_pos, gb_nrm, frame, frame_f32);
+    }
     return cudaGetLastError();
   }
   return iso ? run<VCT_SAMPLER_HW, true, VCT_STORAGE_RGBA8>(sp, cp, ms, tp, gb_pos, gb_nrm, frame, frame_f32, st)

@@ -821,6 +821,7 @@ struct vct_renderer {
     tp.mip_mode = cfg.mip_mode;
     tp.diffuse_in = nullptr;
     tp.far_share = cfg.far_share;
+    tp.tile_rows = 0;
     return tp;
   }
 };

@@ -180,9 +180,12 @@ struct TraceParams {
   int mip_mode;
   // Per-pixel trace_diffuse from the learned term (null: trace the cones).
   const float4* diffuse_in;
-  // Texture-unit sampler: 2x2 quads share the coarse part of their diffuse
+  // Texture-unit sampler: pixel groups share the far fields of their diffuse
   // cones (vct_config::far_share).
   int far_share;
+  // Rows of a CTA's 16-pixel-wide tile of the shared-far-field tracer: 8
+  // (0 means 8) or 16.  The frame is the same either way.
+  int tile_rows;
 };
 
 // ---- batched rendering (api_batch.cu) --------------------------------------
@@ -245,6 +248,7 @@ struct BatchShape {
   int trace_ctas_per_sm;
   int trace_dynamic;   // 1: tiles from an atomic queue; 0: static stride
   int trace_per_scene; // 1: one launch of the one-scene trace kernel per scene
+  int trace_tile_rows; // 8 or 16: CTA tile rows of the per-scene shared-far-field trace
 };
 
 // ---- learned diffuse term (k_mlp.cu) --------------------------------------
@@ -354,8 +358,10 @@ cudaError_t launch_mipmap_batch(const BatchWork& regions, const BatchWork* tail,
                                 cudaStream_t st, int* launches);
 cudaError_t launch_gbuffer_batch(const BatchWork& tris, const BatchWork& tiles, size_t total_px,
                                  const BatchBuffers& bb, int sms, cudaStream_t st, int* launches);
+// share: every scene shares the far fields of its diffuse cones (the batch's
+// far_share; k_trace_batch_share).
 cudaError_t launch_trace_batch(const BatchWork& tiles, const BatchBuffers& bb, const BatchShape& shape, int sms,
-                               cudaStream_t st, int* launches);
+                               cudaStream_t st, int* launches, bool share);
 
 // Learned diffuse term.
 cudaError_t launch_mlp_init(float* prm, __nv_bfloat16* prm_bf, size_t n, float scale, uint64_t seed, cudaStream_t st);

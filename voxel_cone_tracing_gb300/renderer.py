@@ -44,6 +44,7 @@ EXPORTS = [
     "vct_batch_read_frame", "vct_batch_read_voxels", "vct_batch_stage_times", "vct_batch_get_shape",
     "vct_batch_set_shape", "vct_batch_autotune", "vct_set_light_injection", "vct_read_injection_grids",
     "vct_mlp_set_tensor_kernels", "vct_measure_texture_rate", "vct_mlp_set_judge", "vct_mlp_get_judge",
+    "vct_batch_config_default",
 ]
 DIFFUSE_CONES, DIFFUSE_MLP = 0, 1
 # vct_config.far_share = 1 shares the diffuse cones' far fields within groups
@@ -149,6 +150,7 @@ def lib() -> C.CDLL:
             "vct_set_light_injection": (I32, [P, I32]), "vct_read_injection_grids": (I32, [P, P, P, P]),
             "vct_mlp_set_tensor_kernels": (I32, [P, I32]), "vct_measure_texture_rate": (I32, [I32, U32, P, P]),
             "vct_mlp_set_judge": (I32, [P, I32, F]), "vct_mlp_get_judge": (I32, [P, P]),
+            "vct_batch_config_default": (None, [P]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
@@ -513,12 +515,14 @@ class BatchScene(C.Structure):
 
 
 class BatchConfig(C.Structure):
-    _fields_ = [("vox_mode", C.c_int32), ("use_graph", C.c_int32), ("reserved", C.c_int32 * 6)]
+    _fields_ = [("vox_mode", C.c_int32), ("use_graph", C.c_int32), ("far_share", C.c_int32),
+                ("reserved", C.c_int32 * 5)]
 
 
 class BatchShape(C.Structure):
     _fields_ = [("bin_ctas_per_sm", C.c_int32), ("bricks_ctas_per_sm", C.c_int32),
-                ("trace_ctas_per_sm", C.c_int32), ("trace_dynamic", C.c_int32), ("trace_per_scene", C.c_int32)]
+                ("trace_ctas_per_sm", C.c_int32), ("trace_dynamic", C.c_int32), ("trace_per_scene", C.c_int32),
+                ("trace_tile_rows", C.c_int32)]
 
 
 class Batch:
@@ -526,7 +530,7 @@ class Batch:
     of ``items`` is (scene, width, height, grid_res, cone_set); geometry,
     materials, lights, camera and cube size come from the scene."""
 
-    def __init__(self, items, vox_mode: int = VOX_REF_RASTER2X, use_graph: bool = False):
+    def __init__(self, items, vox_mode: int = VOX_REF_RASTER2X, use_graph: bool = False, far_share: int = 1):
         keep = []
         descs = (BatchScene * len(items))()
         self.sizes = []
@@ -552,7 +556,8 @@ class Batch:
             d.proj[:] = [float(x) for x in np.asarray(scene.proj, np.float32).reshape(-1)]
             self.sizes.append((int(w), int(h), int(grid)))
         cfg = BatchConfig()
-        cfg.vox_mode, cfg.use_graph = int(vox_mode), int(bool(use_graph))
+        lib().vct_batch_config_default(C.byref(cfg))
+        cfg.vox_mode, cfg.use_graph, cfg.far_share = int(vox_mode), int(bool(use_graph)), int(far_share)
         self._b = C.c_void_p()
         _check(lib().vct_batch_create(descs, len(items), C.byref(cfg), C.byref(self._b)))
 
