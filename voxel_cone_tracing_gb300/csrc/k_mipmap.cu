@@ -24,6 +24,7 @@
 
 #include "vct_async.cuh"
 #include "vct_internal.h"
+#include "vct_mip.cuh"
 
 namespace vct {
 namespace {
@@ -38,12 +39,6 @@ __constant__ int c_pairs[6][4][2] = {
     {{0, 4}, {1, 5}, {2, 6}, {3, 7}}, {{4, 0}, {5, 1}, {6, 2}, {7, 3}},
     {{0, 2}, {1, 3}, {5, 7}, {4, 6}}, {{2, 0}, {3, 1}, {7, 5}, {6, 4}},
     {{0, 1}, {2, 3}, {4, 5}, {6, 7}}, {{1, 0}, {3, 2}, {5, 4}, {7, 6}}};
-// The same table as a compile-time constant for fully unrolled loops.
-__device__ constexpr int c_pairs_h[6][4][2] = {
-    {{0, 4}, {1, 5}, {2, 6}, {3, 7}}, {{4, 0}, {5, 1}, {6, 2}, {7, 3}},
-    {{0, 2}, {1, 3}, {5, 7}, {4, 6}}, {{2, 0}, {3, 1}, {7, 5}, {6, 4}},
-    {{0, 1}, {2, 3}, {4, 5}, {6, 7}}, {{1, 0}, {3, 2}, {5, 4}, {7, 6}}};
-
 template <int STORAGE> struct Texel;
 template <> struct Texel<VCT_STORAGE_RGBA8> {
   typedef uint32_t T;
@@ -53,8 +48,6 @@ template <> struct Texel<VCT_STORAGE_RGBA16F> {
   typedef uint2 T;
   static constexpr int kBytes = 8;
 };
-
-__device__ __forceinline__ uint32_t ch8(uint32_t t, int c) { return (t >> (8 * c)) & 0xffu; }
 
 __device__ __forceinline__ uint32_t aniso_rgba8(const uint32_t* ch, int d) {
   uint32_t out = 0;
@@ -119,33 +112,6 @@ template <int STORAGE>
 __device__ __forceinline__ typename Texel<STORAGE>::T reduce(const typename Texel<STORAGE>::T* ch, int d, bool iso) {
   if constexpr (STORAGE == VCT_STORAGE_RGBA8) return iso ? iso_rgba8(ch) : aniso_rgba8(ch, d);
   else return iso ? iso_rgba16f(ch) : aniso_rgba16f(ch, d);
-}
-
-// All six directions of one destination texel from the same 8 children
-// (level 1, where every map reads the shared level 0): each child's channels
-// are unpacked once; same exact rule as aniso_rgba8.
-__device__ __forceinline__ void aniso6_rgba8(const uint32_t* ch, uint32_t* out) {
-  uint32_t c[8][4];
-#pragma unroll
-  for (int k = 0; k < 8; ++k)
-#pragma unroll
-    for (int q = 0; q < 4; ++q) c[k][q] = ch8(ch[k], q);
-#pragma unroll
-  for (int d = 0; d < 6; ++d) {
-    uint32_t o = 0;
-#pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      uint32_t S = 0;
-#pragma unroll
-      for (int p = 0; p < 4; ++p) {
-        const int f = c_pairs_h[d][p][0], b = c_pairs_h[d][p][1];
-        S += c[f][q] * 255u + (255u - c[f][3]) * c[b][q];
-      }
-      const uint32_t v = (S + 510u) / 1020u;
-      o |= (v > 255u ? 255u : v) << (8 * q);
-    }
-    out[d] = o;
-  }
 }
 
 __device__ __forceinline__ void aniso6_rgba16f(const uint2* ch, uint2* out) {
@@ -551,15 +517,20 @@ cudaError_t run_tma(const MapSet& ms, const CUtensorMap* map, FrameStatus* statu
 }
 
 template <int NMAPS, int STORAGE>
-cudaError_t run_all(const MapSet& ms, cudaStream_t st, int* launches, const CUtensorMap* map, FrameStatus* status) {
-  const int K1 = ms.L - 1 < 4 ? ms.L - 1 : 4;
-  if (K1 < 1) return cudaSuccess;
-  // The TMA-staged first pass needs four levels below a 16^3 box.
-  cudaError_t e = (map && status && K1 == 4 && ms.N % kTmaBox == 0) ? run_tma<NMAPS, STORAGE>(ms, map, status, st)
-                                                                     : run_pass_k<NMAPS, true, STORAGE>(ms, 0, K1, st);
-  if (e != cudaSuccess) return e;
-  if (launches) ++*launches;
-  int done = K1;
+cudaError_t run_all(const MapSet& ms, cudaStream_t st, int* launches, const CUtensorMap* map, FrameStatus* status,
+                    int first_level) {
+  cudaError_t e = cudaSuccess;
+  int done = first_level;
+  if (done == 0) {
+    const int K1 = ms.L - 1 < 4 ? ms.L - 1 : 4;
+    if (K1 < 1) return cudaSuccess;
+    // The TMA-staged first pass needs four levels below a 16^3 box.
+    e = (map && status && K1 == 4 && ms.N % kTmaBox == 0) ? run_tma<NMAPS, STORAGE>(ms, map, status, st)
+                                                          : run_pass_k<NMAPS, true, STORAGE>(ms, 0, K1, st);
+    if (e != cudaSuccess) return e;
+    if (launches) ++*launches;
+    done = K1;
+  }
   while (done < ms.L - 1) {
     int K = ms.L - 1 - done;
     if (K > 4) K = 4;
@@ -716,15 +687,16 @@ __global__ void k_box_mip_rgba8(cudaSurfaceObject_t src, int sw, int sh, int sd,
 }  // namespace
 
 cudaError_t launch_mipmap(const MapSet& ms, int mip_mode, cudaStream_t st, int* launches, const void* tmap,
-                          FrameStatus* status) {
+                          FrameStatus* status, int first_level) {
   const CUtensorMap* map = static_cast<const CUtensorMap*>(tmap);
+  const int fl = first_level;
   cudaError_t e;
   if (mip_mode == VCT_MIP_ISO) {
-    e = ms.storage == VCT_STORAGE_RGBA8 ? run_all<1, VCT_STORAGE_RGBA8>(ms, st, launches, map, status)
-                                        : run_all<1, VCT_STORAGE_RGBA16F>(ms, st, launches, map, status);
+    e = ms.storage == VCT_STORAGE_RGBA8 ? run_all<1, VCT_STORAGE_RGBA8>(ms, st, launches, map, status, fl)
+                                        : run_all<1, VCT_STORAGE_RGBA16F>(ms, st, launches, map, status, fl);
   } else {
-    e = ms.storage == VCT_STORAGE_RGBA8 ? run_all<6, VCT_STORAGE_RGBA8>(ms, st, launches, map, status)
-                                        : run_all<6, VCT_STORAGE_RGBA16F>(ms, st, launches, map, status);
+    e = ms.storage == VCT_STORAGE_RGBA8 ? run_all<6, VCT_STORAGE_RGBA8>(ms, st, launches, map, status, fl)
+                                        : run_all<6, VCT_STORAGE_RGBA16F>(ms, st, launches, map, status, fl);
   }
   if (e != cudaSuccess || !ms.skip_empty || ms.L < 2) return e;
   const uint32_t total = occ_words(ms);

@@ -33,6 +33,7 @@
 
 #include "vct_internal.h"
 #include "vct_math.cuh"
+#include "vct_mip.cuh"
 #include "vct_snap.h"
 
 namespace vct {
@@ -843,13 +844,143 @@ __device__ __forceinline__ void brick_accumulate(const SceneParams& sp, int N, c
   __syncthreads();
 }
 
+// ---- fused mip levels 1-3 (RGBA8, six maps; BrickMips) ----------------------
+// The brick holds whole 4^3, 2^3 and 1^3 blocks of levels 1-3, so its CTA
+// writes them from its level-0 texels in shared memory with the MipBuilder's
+// exact rule (vct_mip.cuh), plus the alpha-only chains and the occupancy
+// bytes of those levels (a cell is occupied when its block of level 0 holds a
+// non-zero texel); the MipBuilder then starts from level 3.  This replaces
+// the first pass's re-read of level 0 (and the linear copy it read).
+struct BrickMipScratch {
+  uint32_t l0[kBrick * kBrick * kBrick];
+  uint32_t l1[6][64];
+  uint32_t l2[6][8];
+  uint32_t l3[6];
+  uint8_t occ1[64];
+  uint8_t occ2[8];
+};
+
+__device__ __forceinline__ void brick_alpha(const BrickMips& bm, int level, int x, int y, int z, const uint32_t* v,
+                                            int stride) {
+  surf3Dwrite(make_uchar4(v[0] >> 24, v[stride] >> 24, v[2 * stride] >> 24, v[3 * stride] >> 24),
+              bm.alpha[0][level], x * 4, y, z);
+  surf3Dwrite(make_uchar2(v[4 * stride] >> 24, v[5 * stride] >> 24), bm.alpha[1][level], x * 2, y, z);
+}
+
+__device__ __forceinline__ void brick_occ(const BrickMips& bm, int N, int level, int x, int y, int z, bool any) {
+  if (!bm.occ_raw[level]) return;
+  const int s = N >> level;
+  bm.occ_raw[level][((size_t)z * s + y) * s + x] = any ? 1 : 0;
+}
+
+// Levels 1-3 of brick b3 from scr.l0 ([z][y][x], written and synchronised
+// by the caller); all threads of the CTA.
+__device__ void brick_mips(const BrickMips& bm, int N, const int b3[3], BrickMipScratch& scr) {
+  const int t = threadIdx.x;
+  if (t < 64) {  // level 1: one texel, all six maps (their children are the shared level 0)
+    const int x = t & 3, y = (t >> 2) & 3, z = t >> 4;
+    uint32_t ch[8];
+    bool any = false;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      ch[k] = scr.l0[((2 * z + c_mip_off[k][2]) * 8 + 2 * y + c_mip_off[k][1]) * 8 + 2 * x + c_mip_off[k][0]];
+      any |= ch[k] != 0u;
+    }
+    uint32_t v6[6] = {0u, 0u, 0u, 0u, 0u, 0u};
+    if (any) aniso6_rgba8(ch, v6);  // (eight zero children reduce to 0)
+    const int X = b3[0] * 4 + x, Y = b3[1] * 4 + y, Z = b3[2] * 4 + z;
+#pragma unroll
+    for (int d = 0; d < 6; ++d) {
+      surf3Dwrite(v6[d], bm.surf[d][1], X * 4, Y, Z);
+      scr.l1[d][t] = v6[d];
+    }
+    if (bm.has_alpha) brick_alpha(bm, 1, X, Y, Z, v6, 1);
+    scr.occ1[t] = any ? 1 : 0;
+    brick_occ(bm, N, 1, X, Y, Z, any);
+  }
+  __syncthreads();
+  if (t < 48) {  // level 2: texel r of map d from that map's level 1
+    const int d = t >> 3, r = t & 7, x = r & 1, y = (r >> 1) & 1, z = r >> 2;
+    uint32_t ch[8];
+    bool any = false;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      ch[k] = scr.l1[d][((2 * z + c_mip_off[k][2]) * 4 + 2 * y + c_mip_off[k][1]) * 4 + 2 * x + c_mip_off[k][0]];
+      any |= ch[k] != 0u;
+    }
+    const uint32_t v = any ? aniso_rgba8_map(ch, d) : 0u;
+    surf3Dwrite(v, bm.surf[d][2], (b3[0] * 2 + x) * 4, b3[1] * 2 + y, b3[2] * 2 + z);
+    scr.l2[d][r] = v;
+  } else if (t >= 64 && t < 72) {  // occupancy of level 2 from level 1's
+    const int r = t - 64, x = r & 1, y = (r >> 1) & 1, z = r >> 2;
+    bool any = false;
+#pragma unroll
+    for (int k = 0; k < 8; ++k)
+      any |= scr.occ1[((2 * z + c_mip_off[k][2]) * 4 + 2 * y + c_mip_off[k][1]) * 4 + 2 * x + c_mip_off[k][0]] != 0;
+    scr.occ2[r] = any ? 1 : 0;
+    brick_occ(bm, N, 2, b3[0] * 2 + x, b3[1] * 2 + y, b3[2] * 2 + z, any);
+  }
+  __syncthreads();
+  if (t < 8) {
+    if (bm.has_alpha) brick_alpha(bm, 2, b3[0] * 2 + (t & 1), b3[1] * 2 + ((t >> 1) & 1), b3[2] * 2 + (t >> 2),
+                                  &scr.l2[0][t], 8);
+  } else if (t >= 32 && t < 38) {  // level 3: the brick's one texel of map d
+    const int d = t - 32;
+    uint32_t ch[8];
+    bool any = false;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      ch[k] = scr.l2[d][(c_mip_off[k][2] * 2 + c_mip_off[k][1]) * 2 + c_mip_off[k][0]];
+      any |= ch[k] != 0u;
+    }
+    const uint32_t v = any ? aniso_rgba8_map(ch, d) : 0u;
+    surf3Dwrite(v, bm.surf[d][3], b3[0] * 4, b3[1], b3[2]);
+    scr.l3[d] = v;
+  } else if (t == 64) {
+    bool any = false;
+    for (int k = 0; k < 8; ++k) any |= scr.occ2[k] != 0;
+    brick_occ(bm, N, 3, b3[0], b3[1], b3[2], any);
+  }
+  __syncthreads();
+  if (t == 0 && bm.has_alpha) brick_alpha(bm, 3, b3[0], b3[1], b3[2], scr.l3, 1);
+}
+
+// Levels 1-3 of an empty brick: zeros (the texels and the occupancy).
+__device__ void brick_mips_zero(const BrickMips& bm, int N, const int b3[3]) {
+  const int t = threadIdx.x;
+  const uint32_t zero[6] = {0u, 0u, 0u, 0u, 0u, 0u};
+  int level = 0, x = 0, y = 0, z = 0;
+  if (t < 64) {
+    level = 1;
+    x = b3[0] * 4 + (t & 3);
+    y = b3[1] * 4 + ((t >> 2) & 3);
+    z = b3[2] * 4 + (t >> 4);
+  } else if (t < 72) {
+    level = 2;
+    x = b3[0] * 2 + (t & 1);
+    y = b3[1] * 2 + ((t >> 1) & 1);
+    z = b3[2] * 2 + ((t >> 2) & 1);
+  } else if (t == 72) {
+    level = 3;
+    x = b3[0];
+    y = b3[1];
+    z = b3[2];
+  }
+  if (!level) return;
+#pragma unroll
+  for (int d = 0; d < 6; ++d) surf3Dwrite(0u, bm.surf[d][level], x * 4, y, z);
+  if (bm.has_alpha) brick_alpha(bm, level, x, y, z, zero, 1);
+  brick_occ(bm, N, level, x, y, z, false);
+}
+
 // Writes the brick at b3 from its sums: order-independent mean, round to
 // nearest (ties up); empty voxels = 0.  `acc` may be in shared or global
 // memory.
 template <int STORAGE>
 __device__ __forceinline__ void brick_finalize(const SceneParams& sp, int N, const int b3[3], const AccT<STORAGE>& acc,
                                                cudaSurfaceObject_t l0, uint32_t* __restrict__ counts,
-                                               FrameStatus* st, const InjGrids& inj, void* l0_lin) {
+                                               FrameStatus* st, const InjGrids& inj, void* l0_lin,
+                                               const BrickMips* bm = nullptr, BrickMipScratch* scr = nullptr) {
   for (int i = threadIdx.x; i < kBrickVox; i += kThreads) {
     const uint32_t n = acc.n[i];
     const int lx = i & 7, ly = (i >> 3) & 7, lz = i >> 6;
@@ -872,6 +1003,7 @@ __device__ __forceinline__ void brick_finalize(const SceneParams& sp, int N, con
                              unorm8_mean(acc.c[3][i], n));
       surf3Dwrite(o, l0, x * 4, y, z);
       if (l0_lin) static_cast<uchar4*>(l0_lin)[((size_t)z * N + y) * N + x] = o;
+      if (bm) scr->l0[i] = (uint32_t)o.x | (uint32_t)o.y << 8 | (uint32_t)o.z << 16 | (uint32_t)o.w << 24;
     } else {
       ushort4 o = make_ushort4(0, 0, 0, 0);
       if (n) {
@@ -885,6 +1017,12 @@ __device__ __forceinline__ void brick_finalize(const SceneParams& sp, int N, con
       if (l0_lin) static_cast<ushort4*>(l0_lin)[((size_t)z * N + y) * N + x] = o;
     }
     if (counts) counts[((size_t)z * N + y) * N + x] = n;
+  }
+  if constexpr (STORAGE == VCT_STORAGE_RGBA8) {
+    if (bm) {
+      __syncthreads();
+      brick_mips(*bm, N, b3, *scr);
+    }
   }
 }
 
@@ -910,7 +1048,9 @@ __device__ __forceinline__ void brick_unit(const SceneParams& sp, int N, uint32_
                                            uint32_t cap, cudaSurfaceObject_t l0, uint32_t* __restrict__ counts,
                                            FrameStatus* st, AccT<STORAGE>& acc, SetupOf<MODE> (&setup)[kSetupSlots],
                                            int (&excl)[kExclSlots], const InjGrids& inj, void* l0_lin,
-                                           const HeavyBricks* hb, uint32_t slot_index, uint32_t chunk, bool item) {
+                                           const HeavyBricks* hb, uint32_t slot_index, uint32_t chunk, bool item,
+                                           const BrickMips* bm = nullptr) {
+  static_assert(sizeof(BrickMipScratch) <= sizeof(setup), "fused mips fit in the triangle setups' memory");
   __shared__ uint32_t s_last;
   int b3[3];
   brick_coords(N, brick, b3);
@@ -933,6 +1073,7 @@ __device__ __forceinline__ void brick_unit(const SceneParams& sp, int N, uint32_
       }
       if (counts) counts[((size_t)z * N + y) * N + x] = 0u;
     }
+    if (bm) brick_mips_zero(*bm, N, b3);
     return;
   }
   // Only a dense brick looks up its slot.
@@ -959,18 +1100,22 @@ __device__ __forceinline__ void brick_unit(const SceneParams& sp, int N, uint32_
     if (threadIdx.x == 0) hb->done[slot] = 0;
     __syncthreads();
   }
-  brick_finalize<STORAGE>(sp, N, b3, acc, l0, counts, st, inj, l0_lin);
+  // (the triangle setups are done with: their memory holds the fused mips)
+  brick_finalize<STORAGE>(sp, N, b3, acc, l0, counts, st, inj, l0_lin, bm,
+                          reinterpret_cast<BrickMipScratch*>(&setup[0]));
 }
 
 // One CTA per brick, after `n_extra` CTAs that run the extra chunks of
 // split bricks from the launch-wide item queue (first in the grid, so that
 // the dense bricks' chunks start with the first bricks, not in the tail).
-template <int MODE, int STORAGE>
-__global__ void __launch_bounds__(kThreads, brick_min_blocks<MODE>()) k_bricks(SceneParams sp, int N, const uint32_t* __restrict__ offset,
+// (FUSE: the fused mips' level-1 reduction holds 32 unpacked children; the
+// kernel is held to the registers of 7 resident CTAs, as without it.)
+template <int MODE, int STORAGE, bool FUSE = false>
+__global__ void __launch_bounds__(kThreads, FUSE ? 7 : brick_min_blocks<MODE>()) k_bricks(SceneParams sp, int N, const uint32_t* __restrict__ offset,
                                                      const uint32_t* __restrict__ list, uint32_t cap,
                                                      cudaSurfaceObject_t l0, uint32_t* __restrict__ counts,
                                                      FrameStatus* st, InjGrids inj, void* l0_lin, HeavyBricks hb,
-                                                     uint32_t n_extra) {
+                                                     uint32_t n_extra, const __grid_constant__ BrickMips bm) {
   __shared__ AccT<STORAGE> acc;
   __shared__ SetupOf<MODE> setup[kSetupSlots];
   __shared__ int excl[kExclSlots];
@@ -995,7 +1140,7 @@ __global__ void __launch_bounds__(kThreads, brick_min_blocks<MODE>()) k_bricks(S
       chunk = w.y;
     }
     brick_unit<MODE, STORAGE>(sp, N, brick, offset, list, cap, l0, counts, st, acc, setup, excl, inj, l0_lin, &hb,
-                              brick, chunk, extra);
+                              brick, chunk, extra, FUSE ? &bm : nullptr);
     __syncthreads();  // done with acc
   }
 }
@@ -1230,12 +1375,23 @@ cudaError_t launch_voxelize(const SceneParams& sp, int N, int mode, int storage,
   }
   const InjGrids g = inj ? *inj : InjGrids{};
   void* lin = inj ? nullptr : vb.level0_lin;
+  const bool fuse_mips = vb.mips && !inj && storage == VCT_STORAGE_RGBA8;
+  BrickMips bm;
+  std::memset(&bm, 0, sizeof(bm));
+  if (fuse_mips) bm = *vb.mips;
   // Before the bricks: two CTAs per SM that run the extra chunks.
   const uint32_t n_extra = hb.slot ? std::min<uint32_t>(hb.item_cap, (uint32_t)(sms * std::min(fit, 2))) : 0u;
   dispatch_bricks(mode, storage, inj != nullptr, [&](auto mode_tag, auto storage_tag) {
-    k_bricks<decltype(mode_tag)::value, decltype(storage_tag)::value>
-        <<<(unsigned)(n_extra + n_bricks), kThreads, 0, st>>>(sp, N, vb.brick_offset, vb.pair_list, vb.pair_cap, l0,
-                                                               vb.counts, vb.status, g, lin, hb, n_extra);
+    constexpr int M = decltype(mode_tag)::value, S = decltype(storage_tag)::value;
+    if constexpr (S == VCT_STORAGE_RGBA8) {
+      if (fuse_mips) {
+        k_bricks<M, S, true><<<(unsigned)(n_extra + n_bricks), kThreads, 0, st>>>(
+            sp, N, vb.brick_offset, vb.pair_list, vb.pair_cap, l0, vb.counts, vb.status, g, lin, hb, n_extra, bm);
+        return;
+      }
+    }
+    k_bricks<M, S><<<(unsigned)(n_extra + n_bricks), kThreads, 0, st>>>(
+        sp, N, vb.brick_offset, vb.pair_list, vb.pair_cap, l0, vb.counts, vb.status, g, lin, hb, n_extra, bm);
   });
   ++nl;
   if (launches) *launches += nl;

@@ -682,6 +682,24 @@ struct vct_renderer {
     vb.level0_lin = have_l0_map ? (void*)l0_lin.p : nullptr;
     vb.heavy = kHeavySplit ? heavy.view() : HeavyBricks{};
     vb.bin_rec = bin_rec.p;
+    // RGBA8 anisotropic maps: the brick kernel writes mip levels 1-3 itself
+    // (not for light injection, whose level 0 comes from k_inject).
+    BrickMips bm;
+    std::memset(&bm, 0, sizeof(bm));
+    const bool fuse = kFuseBrickMips && !inject && cfg.storage == VCT_STORAGE_RGBA8 &&
+                      cfg.mip_mode == VCT_MIP_ANISO && ms.L >= 4;
+    if (fuse) {
+      for (int d = 0; d < 6; ++d)
+        for (int l = 1; l <= 3; ++l) bm.surf[d][l] = ms.surf[d][l];
+      bm.has_alpha = ms.alpha_tex[0] != 0;
+      for (int k = 0; k < 2 && bm.has_alpha; ++k)
+        for (int l = 1; l <= 3; ++l) bm.alpha[k][l] = ms.alpha_surf[k][l];
+      for (int l = 1; l <= 3 && ms.skip_empty; ++l) bm.occ_raw[l] = ms.occ_raw[l];
+      vb.mips = &bm;
+      vb.level0_lin = nullptr;  // no TMA-staged first pass to read it
+    } else {
+      vb.mips = nullptr;
+    }
 
     RasterBuffers rb;
     rb.vis = vis.p;
@@ -738,7 +756,13 @@ struct vct_renderer {
       VCT_CUDA(launch_voxelize(sp, (int)res, cfg.vox_mode, cfg.storage, vb, ms.l0_surf, stream, &launches));
     }
     VCT_CUDA(cudaEventRecord(ev[1], stream));
-    VCT_CUDA(launch_mipmap(ms, cfg.mip_mode, stream, &launches, have_l0_map ? &l0_map : nullptr, d_status.p));
+    if (fuse) {
+      MapSet m3 = ms;
+      m3.occ_k = 3;  // the levels whose occupancy bytes the brick kernel wrote
+      VCT_CUDA(launch_mipmap(m3, cfg.mip_mode, stream, &launches, nullptr, d_status.p, 3));
+    } else {
+      VCT_CUDA(launch_mipmap(ms, cfg.mip_mode, stream, &launches, have_l0_map ? &l0_map : nullptr, d_status.p));
+    }
     VCT_CUDA(cudaEventRecord(ev[2], stream));
     if (side) VCT_CUDA(cudaStreamWaitEvent(stream, ev_join, 0));
     VCT_CUDA(cudaEventRecord(ev[3], stream));

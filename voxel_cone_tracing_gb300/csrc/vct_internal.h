@@ -135,6 +135,20 @@ struct MapSet {
   int occ_wpr[kMaxLevels];
 };
 
+// Levels 1-3 of the six RGBA8 directional chains written by the brick
+// kernel itself (the MipBuilder then starts from level 3): the chains'
+// surfaces, the alpha-only chains and the occupancy bytes of those levels.
+#ifndef VCT_FUSE_BRICK_MIPS
+#define VCT_FUSE_BRICK_MIPS 1  // -DVCT_FUSE_BRICK_MIPS=0: the MipBuilder builds every level
+#endif
+constexpr bool kFuseBrickMips = VCT_FUSE_BRICK_MIPS != 0;
+struct BrickMips {
+  cudaSurfaceObject_t surf[6][4];   // [map][level 1..3]
+  cudaSurfaceObject_t alpha[2][4];  // [chain][level 1..3] (has_alpha)
+  uint8_t* occ_raw[4];              // [level 1..3] (null: no occupancy)
+  int has_alpha;
+};
+
 struct VoxBuffers {
   uint32_t* brick_count;   // n_bricks
   uint32_t* brick_offset;  // n_bricks + 1
@@ -151,6 +165,7 @@ struct VoxBuffers {
   HeavyBricks heavy;       // dense-brick splitting (heavy.slot null: off)
   uint2* bin_rec;          // per triangle: the counting pass's bricks, replayed
                            // by the filling pass (total_tris; null: recompute)
+  const BrickMips* mips;   // RGBA8: the brick kernel writes levels 1-3 too (null: off)
 };
 
 struct RasterBuffers {
@@ -290,8 +305,10 @@ cudaError_t launch_voxelize_linear(const SceneParams& sp, int N, int mode, const
                                    cudaStream_t st);
 // `tmap` (a CUtensorMap over the linear level 0, or null): the first pass
 // stages level 0 through TMA bulk-tensor copies; `status` receives timeouts.
+// first_level 3: levels 1-3 are already written (BrickMips; then ms.occ_k
+// must be 3, the levels whose occupancy bytes the brick kernel wrote).
 cudaError_t launch_mipmap(const MapSet& ms, int mip_mode, cudaStream_t st, int* launches, const void* tmap = nullptr,
-                          FrameStatus* status = nullptr);
+                          FrameStatus* status = nullptr, int first_level = 0);
 cudaError_t launch_gbuffer(const SceneParams& sp, const CameraParams& cp, const RasterBuffers& rb,
                            cudaStream_t st, int* launches);
 cudaError_t launch_trace(const SceneParams& sp, const CameraParams& cp, const MapSet& ms, const TraceParams& tp,

@@ -1,0 +1,83 @@
+// vct_mip.cuh -- the exact RGBA8 anisotropic mip rule (mipmap.comp:40-98),
+// shared by the MipBuilder (k_mipmap.cu) and the brick kernel's fused first
+// levels (k_voxelize.cu).
+//
+// With texels k/255 the stored value of mean(alpha_blend(front, back)) over
+// the four (front, back) child pairs of a direction is round(S / 1020) with
+// S = sum over the pairs of (F*255 + (255-F.a)*B) per channel, ties up,
+// clamped to 255 -- the exact real value of the GLSL expression, rounded to
+// unorm8 as imageStore does.
+#pragma once
+
+#include <cstdint>
+
+namespace vct {
+
+// voxel_offsets, mipmap.comp:10-20: child k of texel x is 2x + c_mip_off[k].
+__device__ constexpr int c_mip_off[8][3] = {{1, 1, 1}, {1, 1, 0}, {1, 0, 1}, {1, 0, 0},
+                                            {0, 1, 1}, {0, 1, 0}, {0, 0, 1}, {0, 0, 0}};
+// (front, back) child pairs per map (0:-x 1:+x 2:-y 3:+y 4:-z 5:+z), mipmap.comp:59-98.
+__device__ constexpr int c_pairs_h[6][4][2] = {
+    {{0, 4}, {1, 5}, {2, 6}, {3, 7}}, {{4, 0}, {5, 1}, {6, 2}, {7, 3}},
+    {{0, 2}, {1, 3}, {5, 7}, {4, 6}}, {{2, 0}, {3, 1}, {7, 5}, {6, 4}},
+    {{0, 1}, {2, 3}, {4, 5}, {6, 7}}, {{1, 0}, {3, 2}, {5, 4}, {7, 6}}};
+
+__device__ __forceinline__ uint32_t ch8(uint32_t t, int c) { return (t >> (8 * c)) & 0xffu; }
+
+// All six directions of one destination texel from the same 8 children
+// (level 1, where every map reads the shared level 0): each child's channels
+// are unpacked once.
+__device__ __forceinline__ void aniso6_rgba8(const uint32_t* ch, uint32_t* out) {
+  uint32_t c[8][4];
+#pragma unroll
+  for (int k = 0; k < 8; ++k)
+#pragma unroll
+    for (int q = 0; q < 4; ++q) c[k][q] = ch8(ch[k], q);
+#pragma unroll
+  for (int d = 0; d < 6; ++d) {
+    uint32_t o = 0;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      uint32_t S = 0;
+#pragma unroll
+      for (int p = 0; p < 4; ++p) {
+        const int f = c_pairs_h[d][p][0], b = c_pairs_h[d][p][1];
+        S += c[f][q] * 255u + (255u - c[f][3]) * c[b][q];
+      }
+      const uint32_t v = (S + 510u) / 1020u;
+      o |= (v > 255u ? 255u : v) << (8 * q);
+    }
+    out[d] = o;
+  }
+}
+
+// Direction D of one destination texel from that map's own 8 children.
+template <int D>
+__device__ __forceinline__ uint32_t aniso_rgba8_map(const uint32_t* ch) {
+  uint32_t o = 0;
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    uint32_t S = 0;
+#pragma unroll
+    for (int p = 0; p < 4; ++p) {
+      const uint32_t f = ch[c_pairs_h[D][p][0]], b = ch[c_pairs_h[D][p][1]];
+      S += ch8(f, q) * 255u + (255u - ch8(f, 3)) * ch8(b, q);
+    }
+    const uint32_t v = (S + 510u) / 1020u;
+    o |= (v > 255u ? 255u : v) << (8 * q);
+  }
+  return o;
+}
+
+__device__ __forceinline__ uint32_t aniso_rgba8_map(const uint32_t* ch, int d) {
+  switch (d) {
+    case 0: return aniso_rgba8_map<0>(ch);
+    case 1: return aniso_rgba8_map<1>(ch);
+    case 2: return aniso_rgba8_map<2>(ch);
+    case 3: return aniso_rgba8_map<3>(ch);
+    case 4: return aniso_rgba8_map<4>(ch);
+    default: return aniso_rgba8_map<5>(ch);
+  }
+}
+
+}  // namespace vct
