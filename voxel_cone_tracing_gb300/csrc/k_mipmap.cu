@@ -564,6 +564,9 @@ __device__ __forceinline__ bool occ_raw_cell(const MapSet& ms, int c, int x, int
       const uint8_t* row = ms.occ_raw[k] + ((size_t)(z * f + dz) * sk + (y * f + dy)) * sk + (size_t)x * f;
       if (f == 4) {
         any |= __ldg(reinterpret_cast<const uint32_t*>(row));  // 4-byte aligned: x * 4
+      } else if (f == 8) {
+        const uint2 v = __ldg(reinterpret_cast<const uint2*>(row));  // 8-byte aligned: x * 8
+        any |= v.x | v.y;
       } else {
         for (int dx = 0; dx < f; ++dx) any |= __ldg(row + dx);
       }

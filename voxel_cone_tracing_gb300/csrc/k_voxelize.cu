@@ -1057,7 +1057,13 @@ __device__ __forceinline__ void brick_unit(const SceneParams& sp, int N, uint32_
   const uint32_t beg0 = min(offset[brick], cap), end = min(offset[brick + 1], cap);
   if (beg0 == end) {
     // No triangle touches this brick (most of the grid): store cleared texels
-    // without the accumulator or its barriers.
+    // without the accumulator or its barriers -- unless they are zero already
+    // (BrickMips::dirty; the per-voxel counts are not tracked by it).
+    if (bm && bm->dirty && !counts) {
+      if (!bm->dirty[brick]) return;  // CTA-uniform
+      __syncthreads();                // every thread has read the flag
+      if (threadIdx.x == 0) bm->dirty[brick] = 0;
+    }
     for (int i = threadIdx.x; i < kBrickVox; i += kThreads) {
       const int x = b3[0] * kBrick + (i & 7), y = b3[1] * kBrick + ((i >> 3) & 7), z = b3[2] * kBrick + (i >> 6);
       if (STORAGE == kStorageAttr) {
@@ -1101,6 +1107,7 @@ __device__ __forceinline__ void brick_unit(const SceneParams& sp, int N, uint32_
     __syncthreads();
   }
   // (the triangle setups are done with: their memory holds the fused mips)
+  if (bm && bm->dirty && threadIdx.x == 0) bm->dirty[brick] = 1;
   brick_finalize<STORAGE>(sp, N, b3, acc, l0, counts, st, inj, l0_lin, bm,
                           reinterpret_cast<BrickMipScratch*>(&setup[0]));
 }

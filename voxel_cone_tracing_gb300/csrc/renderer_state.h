@@ -390,6 +390,8 @@ struct vct_renderer {
   DevBuf<unsigned char> l0_lin;  // level 0 also in linear memory (the MipBuilder's TMA source)
   CUtensorMap l0_map;
   bool have_l0_map = false;
+  DevBuf<uint8_t> brick_dirty;  // BrickMips::dirty
+  bool dirty_unknown = true;
   DevBuf<vct_material_data> d_materials;
   DevBuf<uint32_t> d_obj_material;
   DevBuf<DevInstance> d_inst;
@@ -515,6 +517,7 @@ struct vct_renderer {
     const int L = ms.L;
     const uint32_t tb = cfg.storage == VCT_STORAGE_RGBA16F ? 8u : 4u;
     have_l0_map = false;
+    dirty_unknown = true;
     if (r >= 16) {
       VCT_CHECK(l0_lin.ensure((size_t)r * r * r * tb));
       VCT_CHECK(encode_box_map(&l0_map, l0_lin.p, r, tb));
@@ -526,6 +529,7 @@ struct vct_renderer {
     VCT_CHECK(brick_count.ensure(nb));
     VCT_CHECK(brick_offset.ensure(nb + 1));
     VCT_CHECK(brick_cursor.ensure(nb));
+    VCT_CHECK(brick_dirty.ensure(nb));
     VCT_CHECK(scan_tmp.ensure(scan_tmp_words(nb)));
     VCT_CHECK(heavy.reserve(nb, 256, 16384, stream));
     if (cfg.keep_counts) VCT_CHECK(counts.ensure((size_t)r * r * r));
@@ -695,10 +699,17 @@ struct vct_renderer {
       for (int k = 0; k < 2 && bm.has_alpha; ++k)
         for (int l = 1; l <= 3; ++l) bm.alpha[k][l] = ms.alpha_surf[k][l];
       for (int l = 1; l <= 3 && ms.skip_empty; ++l) bm.occ_raw[l] = ms.occ_raw[l];
+      if (dirty_unknown) {  // new maps, or another writer touched them: every brick writes
+        const size_t nb = (size_t)(res / kBrick) * (res / kBrick) * (res / kBrick);
+        VCT_CUDA(cudaMemsetAsync(brick_dirty.p, 1, nb, stream));
+        dirty_unknown = false;
+      }
+      bm.dirty = brick_dirty.p;
       vb.mips = &bm;
       vb.level0_lin = nullptr;  // no TMA-staged first pass to read it
     } else {
       vb.mips = nullptr;
+      dirty_unknown = true;  // this frame writes every level without the flags
     }
 
     RasterBuffers rb;

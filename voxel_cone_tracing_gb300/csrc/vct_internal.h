@@ -146,6 +146,10 @@ struct BrickMips {
   cudaSurfaceObject_t surf[6][4];   // [map][level 1..3]
   cudaSurfaceObject_t alpha[2][4];  // [chain][level 1..3] (has_alpha)
   uint8_t* occ_raw[4];              // [level 1..3] (null: no occupancy)
+  // Per brick: 1 when its level-0 texels, levels 1-3 or occupancy bytes may
+  // hold non-zero data from an earlier frame.  A brick that is empty in this
+  // frame and not dirty holds zeros already and writes nothing.
+  uint8_t* dirty;
   int has_alpha;
 };
 
