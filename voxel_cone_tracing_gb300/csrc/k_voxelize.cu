@@ -874,49 +874,41 @@ __device__ __forceinline__ void brick_occ(const BrickMips& bm, int N, int level,
 }
 
 // Levels 1-3 of brick b3 from scr.l0 ([z][y][x], written and synchronised
-// by the caller); all threads of the CTA.
+// by the caller); all threads of the CTA.  Each (texel, map) item takes one
+// thread, the map a run-time index (aniso_rgba8_dir), so that the whole CTA
+// works on level 1 and the code exists once: six unrolled copies of the rule
+// made the kernel miss its instruction cache.
 __device__ void brick_mips(const BrickMips& bm, int N, const int b3[3], BrickMipScratch& scr) {
+  static_assert(kThreads >= 128, "level 2 and its occupancy take threads 64-119");
   const int t = threadIdx.x;
-  if (t < 64) {  // level 1: one texel, all six maps (their children are the shared level 0)
+  for (int i = t; i < 6 * 64; i += kThreads) {  // level 1: map i / 64 (warp-uniform), texel i % 64
+    const int d = i >> 6, r = i & 63, x = r & 3, y = (r >> 2) & 3, z = r >> 4;
+    const uint32_t v = aniso_rgba8_dir(d, [&](int k) { return scr.l0[mip_child(8, x, y, z, k)]; });
+    surf3Dwrite(v, bm.surf[d][1], (b3[0] * 4 + x) * 4, b3[1] * 4 + y, b3[2] * 4 + z);
+    scr.l1[d][r] = v;
+  }
+  if (t < 64) {  // occupancy of level 1: the texel's block of level 0
     const int x = t & 3, y = (t >> 2) & 3, z = t >> 4;
-    uint32_t ch[8];
     bool any = false;
 #pragma unroll
-    for (int k = 0; k < 8; ++k) {
-      ch[k] = scr.l0[((2 * z + c_mip_off[k][2]) * 8 + 2 * y + c_mip_off[k][1]) * 8 + 2 * x + c_mip_off[k][0]];
-      any |= ch[k] != 0u;
-    }
-    uint32_t v6[6] = {0u, 0u, 0u, 0u, 0u, 0u};
-    if (any) aniso6_rgba8(ch, v6);  // (eight zero children reduce to 0)
-    const int X = b3[0] * 4 + x, Y = b3[1] * 4 + y, Z = b3[2] * 4 + z;
-#pragma unroll
-    for (int d = 0; d < 6; ++d) {
-      surf3Dwrite(v6[d], bm.surf[d][1], X * 4, Y, Z);
-      scr.l1[d][t] = v6[d];
-    }
-    if (bm.has_alpha) brick_alpha(bm, 1, X, Y, Z, v6, 1);
+    for (int k = 0; k < 8; ++k) any |= scr.l0[mip_child(8, x, y, z, k)] != 0u;
     scr.occ1[t] = any ? 1 : 0;
-    brick_occ(bm, N, 1, X, Y, Z, any);
+    brick_occ(bm, N, 1, b3[0] * 4 + x, b3[1] * 4 + y, b3[2] * 4 + z, any);
   }
   __syncthreads();
-  if (t < 48) {  // level 2: texel r of map d from that map's level 1
-    const int d = t >> 3, r = t & 7, x = r & 1, y = (r >> 1) & 1, z = r >> 2;
-    uint32_t ch[8];
-    bool any = false;
-#pragma unroll
-    for (int k = 0; k < 8; ++k) {
-      ch[k] = scr.l1[d][((2 * z + c_mip_off[k][2]) * 4 + 2 * y + c_mip_off[k][1]) * 4 + 2 * x + c_mip_off[k][0]];
-      any |= ch[k] != 0u;
-    }
-    const uint32_t v = any ? aniso_rgba8_map(ch, d) : 0u;
+  if (t < 64) {
+    if (bm.has_alpha) brick_alpha(bm, 1, b3[0] * 4 + (t & 3), b3[1] * 4 + ((t >> 2) & 3), b3[2] * 4 + (t >> 4),
+                                  &scr.l1[0][t], 64);
+  } else if (t < 64 + 48) {  // level 2: texel r of map d from that map's level 1
+    const int j = t - 64, d = j >> 3, r = j & 7, x = r & 1, y = (r >> 1) & 1, z = r >> 2;
+    const uint32_t v = aniso_rgba8_dir(d, [&](int k) { return scr.l1[d][mip_child(4, x, y, z, k)]; });
     surf3Dwrite(v, bm.surf[d][2], (b3[0] * 2 + x) * 4, b3[1] * 2 + y, b3[2] * 2 + z);
     scr.l2[d][r] = v;
-  } else if (t >= 64 && t < 72) {  // occupancy of level 2 from level 1's
-    const int r = t - 64, x = r & 1, y = (r >> 1) & 1, z = r >> 2;
+  } else if (t < 64 + 48 + 8) {  // occupancy of level 2 from level 1's
+    const int r = t - 112, x = r & 1, y = (r >> 1) & 1, z = r >> 2;
     bool any = false;
 #pragma unroll
-    for (int k = 0; k < 8; ++k)
-      any |= scr.occ1[((2 * z + c_mip_off[k][2]) * 4 + 2 * y + c_mip_off[k][1]) * 4 + 2 * x + c_mip_off[k][0]] != 0;
+    for (int k = 0; k < 8; ++k) any |= scr.occ1[mip_child(4, x, y, z, k)] != 0;
     scr.occ2[r] = any ? 1 : 0;
     brick_occ(bm, N, 2, b3[0] * 2 + x, b3[1] * 2 + y, b3[2] * 2 + z, any);
   }
@@ -926,14 +918,7 @@ __device__ void brick_mips(const BrickMips& bm, int N, const int b3[3], BrickMip
                                   &scr.l2[0][t], 8);
   } else if (t >= 32 && t < 38) {  // level 3: the brick's one texel of map d
     const int d = t - 32;
-    uint32_t ch[8];
-    bool any = false;
-#pragma unroll
-    for (int k = 0; k < 8; ++k) {
-      ch[k] = scr.l2[d][(c_mip_off[k][2] * 2 + c_mip_off[k][1]) * 2 + c_mip_off[k][0]];
-      any |= ch[k] != 0u;
-    }
-    const uint32_t v = any ? aniso_rgba8_map(ch, d) : 0u;
+    const uint32_t v = aniso_rgba8_dir(d, [&](int k) { return scr.l2[d][mip_child(2, 0, 0, 0, k)]; });
     surf3Dwrite(v, bm.surf[d][3], b3[0] * 4, b3[1], b3[2]);
     scr.l3[d] = v;
   } else if (t == 64) {

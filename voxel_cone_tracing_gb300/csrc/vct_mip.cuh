@@ -51,33 +51,36 @@ __device__ __forceinline__ void aniso6_rgba8(const uint32_t* ch, uint32_t* out) 
   }
 }
 
-// Direction D of one destination texel from that map's own 8 children.
-template <int D>
-__device__ __forceinline__ uint32_t aniso_rgba8_map(const uint32_t* ch) {
+// Index of child k (as in c_mip_off) of destination texel (x, y, z) in a
+// cube of side s2 = twice the destination's, stored [z][y][x].
+__device__ __forceinline__ int mip_child(int s2, int x, int y, int z, int k) {
+  return ((2 * z + 1 - (k & 1)) * s2 + 2 * y + 1 - ((k >> 1) & 1)) * s2 + 2 * x + 1 - ((k >> 2) & 1);
+}
+
+// Direction d (a run-time value: one code path for all six maps) of one
+// destination texel whose children come from child(k).  The (front, back)
+// pairs of map d are the children with d's axis bit (x: 4, y: 2, z: 1 in k)
+// clear and set, front the clear one for the minus direction (c_pairs_h);
+// S is a sum, so the pairs' order does not matter and the result equals
+// the table's rule.
+template <class Child>
+__device__ __forceinline__ uint32_t aniso_rgba8_dir(int d, Child child) {
+  const int bit = 4 >> (d >> 1), sel = (d & 1) ? bit : 0;
+  uint32_t S[4] = {0u, 0u, 0u, 0u};
+#pragma unroll
+  for (int p = 0; p < 4; ++p) {
+    const int k = ((p & (bit - 1)) | ((p & ~(bit - 1)) << 1)) | sel;
+    const uint32_t f = child(k), b = child(k ^ bit), fa = 255u - ch8(f, 3);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) S[q] += ch8(f, q) * 255u + fa * ch8(b, q);
+  }
   uint32_t o = 0;
 #pragma unroll
   for (int q = 0; q < 4; ++q) {
-    uint32_t S = 0;
-#pragma unroll
-    for (int p = 0; p < 4; ++p) {
-      const uint32_t f = ch[c_pairs_h[D][p][0]], b = ch[c_pairs_h[D][p][1]];
-      S += ch8(f, q) * 255u + (255u - ch8(f, 3)) * ch8(b, q);
-    }
-    const uint32_t v = (S + 510u) / 1020u;
+    const uint32_t v = (S[q] + 510u) / 1020u;
     o |= (v > 255u ? 255u : v) << (8 * q);
   }
   return o;
-}
-
-__device__ __forceinline__ uint32_t aniso_rgba8_map(const uint32_t* ch, int d) {
-  switch (d) {
-    case 0: return aniso_rgba8_map<0>(ch);
-    case 1: return aniso_rgba8_map<1>(ch);
-    case 2: return aniso_rgba8_map<2>(ch);
-    case 3: return aniso_rgba8_map<3>(ch);
-    case 4: return aniso_rgba8_map<4>(ch);
-    default: return aniso_rgba8_map<5>(ch);
-  }
 }
 
 }  // namespace vct
