@@ -421,10 +421,11 @@ def injection_leg(R, torch, scene, steps, flush):
 def batch_leg(R, torch, steps, rank=0, world=1, pg=None):
     """Batched workload: 64 seeded scenes of uneven size (grids 32^3-256^3,
     990-865k triangles, frames 256^2-1920x1080, 9 or 6 diffuse cones), one
-    frame of all of them per step: every stage pass one persistent launch
-    over all scenes, the frame captured once in a CUDA graph and replayed,
-    launch shapes chosen by the autotuner, shared far fields as a Renderer's
-    default.  Compared with the same 64 scenes rendered one after another by
+    frame of all of them per step: every stage pass one launch over all
+    scenes (the trace may be one launch per scene, if the autotuner finds
+    that faster; `one_launch_per_stage` times the single-launch trace too),
+    the frame captured once in a CUDA graph and replayed, launch shapes
+    chosen by the autotuner, shared far fields as a Renderer's default.  Compared with the same 64 scenes rendered one after another by
     64 Renderers (same settings) on one stream.  With N ranks
     the scenes are split between them by cost (no data moves between
     GPUs); times are the max over ranks."""
@@ -450,6 +451,20 @@ def batch_leg(R, torch, steps, rank=0, world=1, pg=None):
         stages.append(st)
         dev.append(st["total"])
     launches = stages[-1]["kernel_launches"]
+    # the same batch with every stage one launch (the trace one CTA per tile
+    # of every scene) instead of the tuned trace form
+    b.shape = dict(b.shape, trace_per_scene=0, trace_ctas_per_sm=0)
+    for _ in range(2):
+        b.render()
+    b.synchronize()
+    one = []
+    for _ in range(steps):
+        b.render()
+        b.synchronize()
+        one.append(b.stage_times())
+    one_launch = {"shape": b.shape, "value": round(statistics.mean(t["total"] for t in one), 3),
+                  "trace_ms": round(statistics.mean(t["trace"] for t in one), 3),
+                  "kernel_launches_per_frame": one[-1]["kernel_launches"]}
     b.close()
     # the same scenes, one Renderer each, rendered one after another
     rs = []
@@ -488,7 +503,7 @@ def batch_leg(R, torch, steps, rank=0, world=1, pg=None):
                         "6-9 diffuse cones", "unit": "ms/batch frame",
             "value": round(dev_ms, 3), "wall_ms": round(wall_ms, 3), "ranks": world,
             "stages_ms": {k: round(mean(k), 3) for k in ("voxelize", "mipmap", "gbuffer", "trace")},
-            "kernel_launches_per_frame": launches, "autotune": tune,
+            "kernel_launches_per_frame": launches, "autotune": tune, "one_launch_per_stage": one_launch,
             "sequential_renderers": {"device_ms": round(statistics.mean(seq_dev), 3),
                                      "stages_ms": {k: round(statistics.mean(s[k] for s in seq_stages), 3)
                                                    for k in ("voxelize", "mipmap", "gbuffer", "trace")},

@@ -468,12 +468,13 @@ typedef struct {
 void vct_batch_config_default(vct_batch_config* cfg);
 
 /* Launch shapes of the batched kernels: persistent CTAs per SM of the
- * binning, brick and trace launches, the trace's tile scheduling (1 =
- * atomic tile queue, 0 = static stride), the trace's form: 0 = one
- * persistent launch over all scenes, 1 = one launch of the one-scene trace
- * kernel per scene, spread over parallel streams (graph branches), and the
- * tile of the per-scene shared-far-field trace.  Every shape renders the
- * same frames. */
+ * binning, brick and trace launches (trace 1-3, or 0: one launch with one
+ * CTA per 16 x 16 tile of every scene, not persistent), the persistent
+ * trace's tile scheduling (1 = atomic tile queue, 0 = static stride), the
+ * trace's form: 0 = one launch over all scenes, 1 = one launch of the
+ * one-scene trace kernel per scene, spread over parallel streams (graph
+ * branches), and the tile of the per-scene shared-far-field trace.  Every
+ * shape renders the same frames. */
 typedef struct {
   int32_t bin_ctas_per_sm;
   int32_t bricks_ctas_per_sm;

@@ -60,15 +60,17 @@ def test_batch_rejects_bad_scenes(vct):
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("far_share", [1, 0], ids=["shared_far", "per_pixel"])
-@pytest.mark.parametrize("per_scene", [0, 1, 16], ids=["persistent_trace", "per_scene_trace", "per_scene_16_rows"])
+@pytest.mark.parametrize("form", ["persistent", "tiles", "per_scene", "per_scene_16_rows"])
 @pytest.mark.parametrize("use_graph", [False, True], ids=["eager", "graph"])
-def test_batch_matches_renderer(vct, use_graph, per_scene, far_share):
-    """Every trace form (one persistent launch; one launch per scene with
-    16x8 or 16x16 tiles) renders each scene exactly as a Renderer with the
-    same far_share does."""
+def test_batch_matches_renderer(vct, use_graph, form, far_share):
+    """Every trace form (one persistent launch; one launch with one CTA per
+    tile; one launch per scene with 16x8 or 16x16 tiles) renders each scene
+    exactly as a Renderer with the same far_share does."""
     items = _items()
     b = vct.Batch(items, use_graph=use_graph, far_share=far_share)
-    b.shape = dict(b.shape, trace_per_scene=int(per_scene != 0), trace_tile_rows=16 if per_scene == 16 else 8)
+    b.shape = dict(b.shape, trace_per_scene=int(form.startswith("per_scene")),
+                   trace_tile_rows=16 if form == "per_scene_16_rows" else 8,
+                   trace_ctas_per_sm=0 if form == "tiles" else 2)
     b.render()
     b.render()  # a second frame (a graph replay) gives the same result
     t = b.stage_times()
@@ -87,11 +89,11 @@ def test_batch_conservative_voxelizer(vct):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("per_scene", [0, 1], ids=["persistent_trace", "per_scene_trace"])
-def test_batch_camera_update_under_graph(vct, per_scene):
+@pytest.mark.parametrize("form", ["persistent", "tiles", "per_scene"])
+def test_batch_camera_update_under_graph(vct, form):
     items = _items()[:4]
     b = vct.Batch(items, use_graph=True)
-    b.shape = dict(b.shape, trace_per_scene=per_scene)
+    b.shape = dict(b.shape, trace_per_scene=int(form == "per_scene"), trace_ctas_per_sm=0 if form == "tiles" else 2)
     b.render()
     scene = items[2][0]
     view = scenes.look_at((0.1, 0.05, 0.45), (0.0, -0.1, -0.5))
@@ -110,7 +112,7 @@ def test_batch_autotune_keeps_results(vct):
     rep = b.autotune(frames=1)
     assert rep["shape"] == b.shape
     assert rep["ms_after"] <= rep["ms_before"] + 1e-6
-    assert rep["shape"]["trace_ctas_per_sm"] in (2, 3) and rep["shape"]["trace_dynamic"] in (0, 1)
+    assert rep["shape"]["trace_ctas_per_sm"] in (0, 2, 3) and rep["shape"]["trace_dynamic"] in (0, 1)
     assert rep["shape"]["trace_per_scene"] in (0, 1) and rep["shape"]["trace_tile_rows"] in (8, 16)
     b.render()
     for i in range(len(items)):

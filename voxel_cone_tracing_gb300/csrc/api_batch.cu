@@ -616,7 +616,7 @@ extern "C" vct_status vct_batch_set_shape(vct_batch* b, const vct_batch_shape* s
   clear_error();
   if (!b || !s) return set_error(VCT_ERR_INVALID_VALUE, "NULL argument");
   if (s->bin_ctas_per_sm < 1 || s->bin_ctas_per_sm > 32 || s->bricks_ctas_per_sm < 1 ||
-      s->bricks_ctas_per_sm > 32 || s->trace_ctas_per_sm < 1 || s->trace_ctas_per_sm > 3 ||
+      s->bricks_ctas_per_sm > 32 || s->trace_ctas_per_sm < 0 || s->trace_ctas_per_sm > 3 ||
       (s->trace_dynamic != 0 && s->trace_dynamic != 1) || (s->trace_per_scene != 0 && s->trace_per_scene != 1) ||
       (s->trace_tile_rows != 8 && s->trace_tile_rows != 16))
     return set_error(VCT_ERR_INVALID_VALUE, "launch shape out of range");
@@ -668,29 +668,51 @@ extern "C" vct_status vct_batch_autotune(vct_batch* b, int32_t frames, vct_batch
   const int brick_c[] = {2, 4, 8};
   const int trace_c[] = {2, 3};
   const int dyn_c[] = {0, 1};
-  const int per_scene_c[] = {0, 1};
-  const int rows_c[] = {8, 16};
-  auto try_field = [&](int BatchShape::*field, const auto& cand) -> vct_status {
-    const int nc = (int)(sizeof(cand) / sizeof(cand[0]));
-    for (int k = 0; k < nc; ++k) {
-      if (cur.*field == cand[k]) continue;
-      BatchShape s = cur;
-      s.*field = cand[k];
-      b->shape = s;
-      b->drop_graph();
-      float ms = 0.0f;
-      VCT_CHECK(time_frames(b, frames, &ms));
-      if (ms < cur_ms) {
-        cur_ms = ms;
-        cur = s;
-      }
+  auto try_shape = [&](const BatchShape& s) -> vct_status {
+    if (std::memcmp(&s, &cur, sizeof(s)) == 0) return VCT_OK;
+    b->shape = s;
+    b->drop_graph();
+    float ms = 0.0f;
+    VCT_CHECK(time_frames(b, frames, &ms));
+    if (ms < cur_ms) {
+      cur_ms = ms;
+      cur = s;
     }
     return VCT_OK;
   };
-  VCT_CHECK(try_field(&BatchShape::trace_per_scene, per_scene_c));
-  if (cur.trace_per_scene && b->cfg.far_share) VCT_CHECK(try_field(&BatchShape::trace_tile_rows, rows_c));
-  VCT_CHECK(try_field(&BatchShape::trace_dynamic, dyn_c));
-  VCT_CHECK(try_field(&BatchShape::trace_ctas_per_sm, trace_c));
+  auto try_field = [&](int BatchShape::*field, const auto& cand) -> vct_status {
+    const int nc = (int)(sizeof(cand) / sizeof(cand[0]));
+    for (int k = 0; k < nc; ++k) {
+      BatchShape s = cur;
+      s.*field = cand[k];
+      VCT_CHECK(try_shape(s));
+    }
+    return VCT_OK;
+  };
+  // The trace's form first, from the same starting point: one launch per
+  // scene (16x8 or, with shared far fields, 16x16 tiles), one launch with
+  // one CTA per tile, or one persistent launch (2 or 3 CTAs per SM).
+  {
+    const BatchShape start = cur;
+    BatchShape forms[5];
+    int nf = 0;
+    for (int rows = 8; rows <= 16; rows += 8) {
+      if (rows == 16 && !b->cfg.far_share) continue;
+      forms[nf] = start;
+      forms[nf].trace_per_scene = 1;
+      forms[nf++].trace_tile_rows = rows;
+    }
+    for (int c : {0, 2, 3}) {
+      forms[nf] = start;
+      forms[nf].trace_per_scene = 0;
+      forms[nf++].trace_ctas_per_sm = c;
+    }
+    for (int k = 0; k < nf; ++k) VCT_CHECK(try_shape(forms[k]));
+  }
+  if (!cur.trace_per_scene && cur.trace_ctas_per_sm) {  // the persistent form's scheduling
+    VCT_CHECK(try_field(&BatchShape::trace_dynamic, dyn_c));
+    VCT_CHECK(try_field(&BatchShape::trace_ctas_per_sm, trace_c));
+  }
   VCT_CHECK(try_field(&BatchShape::bricks_ctas_per_sm, brick_c));
   VCT_CHECK(try_field(&BatchShape::bin_ctas_per_sm, bin_c));
   b->shape = cur;

@@ -1131,6 +1131,37 @@ __global__ void __launch_bounds__(256, kTraceBatchShareMinBlocks) k_trace_batch_
   }
 }
 
+// One CTA per 16x16 tile of every scene of the batch, in one launch
+// (BatchShape::trace_ctas_per_sm 0).  Without a tile loop the shading is
+// inlined, as in the one-scene kernels, while the scene's descriptor and
+// camera come from shared memory: a CTA looks up its scene, copies them
+// there and traces its tile.
+template <bool SHARE>
+__global__ void __launch_bounds__(256, SHARE ? kTraceBatchShareMinBlocks : kTraceBatchMinBlocks)
+    k_trace_batch_tiles(BatchWork w, BatchBuffers bb) {
+  __shared__ FarWarp s_far[SHARE ? 8 : 1];
+  BatchScene& s_sc = s_batch_scene;
+  CameraParams& s_cam = s_batch_cam;
+  const uint32_t g = blockIdx.x;
+  const int s = batch_scene_of_warp(w, g);  // every warp finds it: no barrier before the copy
+  const uint32_t* src = reinterpret_cast<const uint32_t*>(w.scenes + s);
+  for (int i = threadIdx.x; i < (int)(sizeof(BatchScene) / 4); i += blockDim.x)
+    reinterpret_cast<uint32_t*>(&s_sc)[i] = __ldg(src + i);
+  const uint32_t* csrc = reinterpret_cast<const uint32_t*>(w.cams + s);
+  for (int i = threadIdx.x; i < (int)(sizeof(CameraParams) / 4); i += blockDim.x)
+    reinterpret_cast<uint32_t*>(&s_cam)[i] = __ldg(csrc + i);
+  __syncthreads();
+  const uint32_t lt = g - __ldg(w.prefix + s), tiles_x = (uint32_t)(s_sc.W + 15) / 16;
+  const int px = (int)(lt % tiles_x) * 16 + (threadIdx.x & 15), py = (int)(lt / tiles_x) * 16 + (threadIdx.x >> 4);
+  const float4* gp = bb.rb.gb_pos + s_sc.px_base;
+  const float4* gn = bb.rb.gb_nrm + s_sc.px_base;
+  uchar4* fr = bb.frame + s_sc.px_base;
+  if constexpr (SHARE)
+    trace_px_share<false>(s_sc.sp, s_cam, s_sc.ms, s_sc.tp, gp, gn, fr, nullptr, px, py, s_far[threadIdx.x >> 5]);
+  else
+    trace_px<VCT_SAMPLER_HW, false, VCT_STORAGE_RGBA8>(s_sc.sp, s_cam, s_sc.ms, s_sc.tp, gp, gn, fr, nullptr, px, py);
+}
+
 template <int SAMPLER, bool ISO, int STORAGE>
 cudaError_t run(const SceneParams& sp, const CameraParams& cp, const MapSet& ms, const TraceParams& tp,
                 const float4* gb_pos, const float4* gb_nrm, uchar4* frame, float4* frame_f32, cudaStream_t st) {
@@ -1248,6 +1279,12 @@ cudaError_t launch_trace_batch(const BatchWork& tiles, const BatchBuffers& bb, c
                                cudaStream_t st, int* launches, bool share) {
   if (!tiles.total) return cudaSuccess;
   BatchWork w = tiles;
+  if (shape.trace_ctas_per_sm == 0) {  // one CTA per tile
+    if (share) k_trace_batch_tiles<true><<<tiles.total, 256, 0, st>>>(w, bb);
+    else k_trace_batch_tiles<false><<<tiles.total, 256, 0, st>>>(w, bb);
+    if (launches) ++*launches;
+    return cudaGetLastError();
+  }
   if (!shape.trace_dynamic) w.queue = nullptr;
   else {
     cudaError_t e = cudaMemsetAsync(w.queue, 0, sizeof(uint32_t), st);

@@ -243,6 +243,22 @@ __device__ __forceinline__ int batch_scene_of(const BatchWork& w, uint32_t g) {
   return lo;
 }
 
+// batch_scene_of for a whole warp (all 32 lanes): the lanes test 32 scenes'
+// prefixes at a time, so the lookup takes one round of loads per 32 scenes
+// instead of a chain of dependent loads.  The prefixes are non-decreasing,
+// so the scene is the number of prefixes <= g, minus one.
+__device__ __forceinline__ int batch_scene_of_warp(const BatchWork& w, uint32_t g) {
+  const int lane = threadIdx.x & 31;
+  int count = 0;
+  for (int base = 0; base < w.n; base += 32) {
+    const int i = base + lane;
+    const uint32_t m = __ballot_sync(0xffffffffu, i < w.n && __ldg(w.prefix + i) <= g);
+    count += __popc(m);
+    if (m != 0xffffffffu) break;  // warp-uniform
+  }
+  return count - 1;
+}
+
 // Batch-wide work arrays.
 struct BatchBuffers {
   uint32_t* brick_count;
