@@ -88,7 +88,10 @@ typedef enum {
 } vct_status;
 
 enum { VCT_VOX_REF_RASTER2X = 0, VCT_VOX_CONSERVATIVE = 1 };
-enum { VCT_MIP_ANISO = 0, VCT_MIP_ISO = 1 };
+/* VCT_MIP_BOTH: the six directional chains (traced, as VCT_MIP_ANISO) and an
+ * isotropic chain (map 6: the box mean of VCT_MIP_ISO), built in one pass
+ * from the same staged children; view_voxel_dir 6 shows the isotropic chain. */
+enum { VCT_MIP_ANISO = 0, VCT_MIP_ISO = 1, VCT_MIP_BOTH = 2 };
 enum { VCT_STORAGE_RGBA8 = 0, VCT_STORAGE_RGBA16F = 1 };
 enum { VCT_SAMPLER_HW = 0, VCT_SAMPLER_EXACT = 1 };
 enum { VCT_CONES_REF9 = 0, VCT_CONES_SIX60 = 1 };

@@ -70,6 +70,9 @@ def test_bad_config_rejected_before_device(vct):
     with pytest.raises(vct.VCTError) as e:
         vct.Renderer(0, 16)
     assert e.value.status == 1
+    with pytest.raises(vct.VCTError) as e:
+        vct.Renderer(16, 16, mip_mode=vct.MIP_BOTH + 1)
+    assert e.value.status == 1
     # every switch of vct_config is 0 or 1
     for field in ("shadow_from_maps", "full_march", "overlap_raster", "far_share"):
         with pytest.raises(vct.VCTError) as e:

@@ -90,7 +90,7 @@ static vct_status check_config(const vct_config& c) {
     return set_error(VCT_ERR_INVALID_VALUE, "radiance_max %g: need 0 <= radiance_max <= 65504", c.radiance_max);
   if (c.radiance_max > 1.0f && c.storage != VCT_STORAGE_RGBA16F)
     return set_error(VCT_ERR_INVALID_VALUE, "radiance_max %g > 1 needs RGBA16F storage", c.radiance_max);
-  if (c.vox_mode < 0 || c.vox_mode > 1 || c.mip_mode < 0 || c.mip_mode > 1 || c.storage < 0 || c.storage > 1 ||
+  if (c.vox_mode < 0 || c.vox_mode > 1 || c.mip_mode < 0 || c.mip_mode > 2 || c.storage < 0 || c.storage > 1 ||
       c.sampler < 0 || c.sampler > 1 || c.cone_set < 0 || c.cone_set > 1 || c.shadow_from_maps < 0 ||
       c.shadow_from_maps > 1 || c.full_march < 0 || c.full_march > 1 || c.overlap_raster < 0 || c.overlap_raster > 1 ||
       c.far_share < 0 || c.far_share > 1)

@@ -216,7 +216,7 @@ __device__ __forceinline__ void mip_reduce(const MapSet& ms, int src_level, int 
 #pragma unroll 1
   for (int l = 1; l <= K; ++l) {
     const int b = B >> l, b3 = b * b * b, cb3 = cur_b * cur_b * cur_b;
-    if (FROM_L0 && ms.skip_empty && !(NMAPS == 6 && l == 1)) {
+    if (FROM_L0 && ms.skip_empty && !(NMAPS >= 6 && l == 1)) {
       const int cb = b * 2;
       for (int r = threadIdx.x; r < b3; r += kThreads) {
         const int x = r % b, y = (r / b) % b, z = r / (b * b);
@@ -233,9 +233,10 @@ __device__ __forceinline__ void mip_reduce(const MapSet& ms, int src_level, int 
       occ_prev = occ_off;
       occ_off += b3;
     }
-    if (FROM_L0 && NMAPS == 6 && l == 1) {
+    if (FROM_L0 && NMAPS >= 6 && l == 1) {
       // The six maps of level 1 read the same children: one thread per
-      // destination texel evaluates all six directions.
+      // destination texel evaluates all six directions (and, with the
+      // isotropic map 6, the box mean too).
       for (int r = threadIdx.x; r < b3; r += kThreads) {
         const int x = r % b, y = (r / b) % b, z = r / (b * b);
         T ch[8], v6[6];
@@ -256,6 +257,11 @@ __device__ __forceinline__ void mip_reduce(const MapSet& ms, int src_level, int 
           out[d * b3 + r] = v6[d];
           surf3Dwrite(v6[d], ms.surf[d][dl], ((ox >> 1) + x) * Texel<STORAGE>::kBytes, (oy >> 1) + y, (oz >> 1) + z);
         }
+        if constexpr (NMAPS == 7) {
+          const T v = any ? reduce<STORAGE>(ch, 0, true) : T{};
+          out[6 * b3 + r] = v;
+          surf3Dwrite(v, ms.surf[6][dl], ((ox >> 1) + x) * Texel<STORAGE>::kBytes, (oy >> 1) + y, (oz >> 1) + z);
+        }
         if constexpr (STORAGE == VCT_STORAGE_RGBA8)
           if (ms.alpha_tex[0]) write_alpha(ms, dl, (ox >> 1) + x, (oy >> 1) + y, (oz >> 1) + z, v6, 1);
       }
@@ -272,13 +278,13 @@ __device__ __forceinline__ void mip_reduce(const MapSet& ms, int src_level, int 
       const T* base = cur + (cur_shared ? 0 : d * cb3);
       T ch[8];
       const bool any = load_children(base, cur_b, x, y, z, ch);
-      const T v = any ? reduce<STORAGE>(ch, d, NMAPS == 1) : T{};  // zero children reduce to 0
+      const T v = any ? reduce<STORAGE>(ch, d, NMAPS == 1 || d == 6) : T{};  // zero children reduce to 0
       out[i] = v;
       const int dl = src_level + l;
       surf3Dwrite(v, ms.surf[d][dl], ((ox >> l) + x) * Texel<STORAGE>::kBytes, (oy >> l) + y, (oz >> l) + z);
     }
     __syncthreads();
-    if constexpr (NMAPS == 6 && STORAGE == VCT_STORAGE_RGBA8) {
+    if constexpr (NMAPS >= 6 && STORAGE == VCT_STORAGE_RGBA8) {
       if (ms.alpha_tex[0]) {
         // The alpha copies of this level, from the six maps in shared memory
         // (read only; the next level writes past them).
@@ -531,9 +537,11 @@ cudaError_t run_all(const MapSet& ms, cudaStream_t st, int* launches, const CUte
     if (launches) ++*launches;
     done = K1;
   }
+  // (seven RGBA16F source boxes of 16^3 would not fit in shared memory)
+  constexpr int kTailMax = NMAPS == 7 && STORAGE == VCT_STORAGE_RGBA16F ? 3 : 4;
   while (done < ms.L - 1) {
     int K = ms.L - 1 - done;
-    if (K > 4) K = 4;
+    if (K > kTailMax) K = kTailMax;
     e = run_pass_k<NMAPS, false, STORAGE>(ms, done, K, st);
     if (e != cudaSuccess) return e;
     if (launches) ++*launches;
@@ -697,6 +705,9 @@ cudaError_t launch_mipmap(const MapSet& ms, int mip_mode, cudaStream_t st, int* 
   if (mip_mode == VCT_MIP_ISO) {
     e = ms.storage == VCT_STORAGE_RGBA8 ? run_all<1, VCT_STORAGE_RGBA8>(ms, st, launches, map, status, fl)
                                         : run_all<1, VCT_STORAGE_RGBA16F>(ms, st, launches, map, status, fl);
+  } else if (mip_mode == VCT_MIP_BOTH) {
+    e = ms.storage == VCT_STORAGE_RGBA8 ? run_all<7, VCT_STORAGE_RGBA8>(ms, st, launches, map, status, fl)
+                                        : run_all<7, VCT_STORAGE_RGBA16F>(ms, st, launches, map, status, fl);
   } else {
     e = ms.storage == VCT_STORAGE_RGBA8 ? run_all<6, VCT_STORAGE_RGBA8>(ms, st, launches, map, status, fl)
                                         : run_all<6, VCT_STORAGE_RGBA16F>(ms, st, launches, map, status, fl);

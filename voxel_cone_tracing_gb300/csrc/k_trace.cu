@@ -868,7 +868,8 @@ __device__ __forceinline__ void trace_px(const SceneParams& sp, const CameraPara
     // writing; the pixel keeps the clear colour.
     if (fabsf(pos.x) < 1.0f && fabsf(pos.y) < 1.0f && fabsf(pos.z) < 1.0f) {
       if (tp.view_voxel_dir < 7) {  // voxel debug view, :253-257
-        if (tp.view_voxel_dir >= 0 && tp.view_voxel_dir <= 5) {
+        // (map 6: the isotropic chain of VCT_MIP_BOTH; no such map otherwise)
+        if (tp.view_voxel_dir >= 0 && (tp.view_voxel_dir <= 5 || (tp.view_voxel_dir == 6 && m.nmaps == 7))) {
           const float lod = fmaxf(tp.view_voxel_lod, 0.0f);
           const V3 one = v3(1.f, 0.f, 0.f);
           const int d = ISO ? 0 : tp.view_voxel_dir;

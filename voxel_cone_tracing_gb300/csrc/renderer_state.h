@@ -282,7 +282,7 @@ struct MapStore {
   vct_status alloc(uint32_t r, int mip_mode, int storage, bool alpha_chains = true) {
     release();
     const int L = std::min(kMaxLevels, ilog2(r) + 1);
-    const int nmaps = mip_mode == VCT_MIP_ISO ? 1 : 6;
+    const int nmaps = mip_mode == VCT_MIP_ISO ? 1 : (mip_mode == VCT_MIP_BOTH ? 7 : 6);
     const cudaChannelFormatDesc desc = storage == VCT_STORAGE_RGBA16F
                                            ? cudaCreateChannelDesc(16, 16, 16, 16, cudaChannelFormatKindFloat)
                                            : cudaCreateChannelDesc(8, 8, 8, 8, cudaChannelFormatKindUnsigned);
@@ -301,7 +301,7 @@ struct MapStore {
     td.mipmapFilterMode = cudaFilterModeLinear;
     VCT_CUDA(cudaCreateTextureObject(&ms.l0_tex, &rd, &td, nullptr));
     for (int d = 0; d < nmaps && L > 1; ++d) VCT_CHECK(chain(r, L, desc, td, &dir_arr[d], ms.surf[d], &ms.tex[d]));
-    if (alpha_chains && nmaps == 6 && storage == VCT_STORAGE_RGBA8 && L > 1) {
+    if (alpha_chains && nmaps >= 6 && storage == VCT_STORAGE_RGBA8 && L > 1) {
       const cudaChannelFormatDesc d4 = cudaCreateChannelDesc(8, 8, 8, 8, cudaChannelFormatKindUnsigned);
       const cudaChannelFormatDesc d2 = cudaCreateChannelDesc(8, 8, 0, 0, cudaChannelFormatKindUnsigned);
       VCT_CHECK(chain(r, L, d4, td, &alpha_arr[0], ms.alpha_surf[0], &ms.alpha_tex[0]));

@@ -12,7 +12,7 @@ namespace vct {
 constexpr int kMaxLights = 10;   // MAX_POINT_LIGHTS, voxelize.frag:40,128
 constexpr int kMaxLevels = 7;    // create_tex_3d(res,res,res,7), renderer.cpp:186
 constexpr int kBrick = 8;        // voxelizer brick edge (voxels)
-constexpr int kMaxMaps = 6;
+constexpr int kMaxMaps = 7;  // six directional maps + the isotropic one (VCT_MIP_BOTH)
 // Internal storage mode of the voxelizer: per-voxel attribute grids for
 // deferred light injection instead of shaded level-0 radiance.
 constexpr int kStorageAttr = 2;

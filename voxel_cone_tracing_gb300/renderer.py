@@ -21,7 +21,7 @@ LIB_PATH = os.path.join(_HERE, "libvct.so")
 
 INVALID_ID = (1 << 64) - 1
 VOX_REF_RASTER2X, VOX_CONSERVATIVE = 0, 1
-MIP_ANISO, MIP_ISO = 0, 1
+MIP_ANISO, MIP_ISO, MIP_BOTH = 0, 1, 2
 STORAGE_RGBA8, STORAGE_RGBA16F = 0, 1
 SAMPLER_HW, SAMPLER_EXACT = 0, 1
 CONES_REF9, CONES_SIX60 = 0, 1
