@@ -318,8 +318,10 @@ vct_status vct_mlp_gradients(vct_renderer* r, const float* samples, uint32_t n, 
                              float* dweights, float* dtable);
 /* Train on explicit rows instead of scene samples. */
 /* Kernels of the network's forward pass (inference and vct_mlp_eval):
- * 1 = tcgen05.mma with TMEM accumulators (128-row tiles), 0 = mma.sync warp
- * tiles (16 rows per warp).  Training always uses the warp tiles. */
+ * 1 = tcgen05.mma with TMEM accumulators, warp-specialised (encoder warps
+ * fill 128-row tiles, epilogue warps drain the accumulators; the default),
+ * 0 = mma.sync warp tiles (16 rows per warp).  Both give the same values.
+ * Training always uses the warp tiles. */
 vct_status vct_mlp_set_tensor_kernels(vct_renderer* r, int32_t use_tcgen05);
 vct_status vct_mlp_train_samples(vct_renderer* r, const float* samples, uint32_t n,
                                  const vct_mlp_desc* d, vct_mlp_report* report);

@@ -77,6 +77,7 @@ def test_forward_tcgen05_matches_oracle_and_warp_tiles(net, oracle):
     tc = r.mlp_eval(rows)
     r.mlp_set_tensor_kernels(False)
     ws = r.mlp_eval(rows)
+    r.mlp_set_tensor_kernels(True)  # the default
     ref = oracle.mlp_forward(_cfg(oracle), t, w, rows[:, 0:3], rows[:, 3:6], rows[:, 6:9])
     scale = np.abs(ref).max()
     print(f"tcgen05 vs oracle {np.abs(tc - ref).max() / scale:.2e}, vs warp tiles {np.abs(tc - ws).max() / scale:.2e}")
@@ -172,10 +173,10 @@ def test_learned_diffuse_replaces_cones(vct):
     r.set_diffuse_mode(vct.DIFFUSE_CONES)
     rep = r.mlp_train(vct.mlp_desc(n_max=256, seed=1, steps=600, batch=1 << 16, n_samples=1 << 20))
     r.set_diffuse_mode(vct.DIFFUSE_MLP)
+    learned_tc = frame()  # the default: tcgen05
+    r.mlp_set_tensor_kernels(False)
     learned = frame()
     r.mlp_set_tensor_kernels(True)
-    learned_tc = frame()
-    r.mlp_set_tensor_kernels(False)
     # same encoding, same BF16 products, FP32 accumulation in the same order
     np.testing.assert_array_equal(learned_tc, learned)
     q_learned = psnr(np.clip(learned, 0, 1), np.clip(cones, 0, 1))

@@ -560,174 +560,274 @@ __global__ void __launch_bounds__(256) k_mlp_eval(MlpParams p, const float* __re
 }
 
 // ---- forward on the 5th-generation tensor cores ----------------------------
-// A CTA takes tiles of 128 rows.  The activation tile (128 x 64 BF16) and
-// the weights live in shared memory in the canonical K-major layout of
-// tcgen05.mma without swizzle (8-row x 16-byte core matrices: element
-// (r, k) at (r/8)*512 + (k/8)*64 + (r%8)*8 + k%8); one thread issues the four
-// K=16 steps of a layer into a TMEM accumulator (128 lanes = rows, 64 FP32
-// columns) and commits them to an mbarrier; then every warp reads its rows
-// back with tcgen05.ld (warp w: TMEM lanes 32*(w%4)..+31, columns
-// 32*(w/4)..+31), applies ReLU, packs to BF16 and writes the tile of the next
-// layer.  The inputs are the same as the warp-tile kernels' (hash encoding,
-// normal, albedo, 1).
+// Warp-specialised, one persistent CTA per SM:
+//  * 24 encoder warps in 3 groups of 8.  A group encodes one 128-row tile at
+//    a time into a shared-memory stage (6 stages of 128 x 64 BF16): warp w of
+//    the group encodes rows 16w..16w+15 with the lane layout of the warp-tile
+//    kernels (lane (g, t): rows g and g + 8, hash levels t, t + 4, 8 + t,
+//    12 + t), so each lane gathers what it gathers there; then every encoder
+//    thread arrives on the stage's `full` barrier.  Group k takes the CTA's
+//    tiles k, k + 3, k + 6, ...; an encoder never waits for the network,
+//    only for a stage to be free again.
+//  * 8 epilogue warps (two threads per row: warp e reads TMEM lanes
+//    32(e%4)..+31, columns 32(e/4)..+31), one of whose threads issues the
+//    MMAs.  They run the
+//    network over batches of 3 tiles (one per group) with 3 TMEM
+//    accumulators: for each layer and tile, wait for that tile's MMAs, read
+//    the accumulator (tcgen05.ld), apply ReLU, pack to BF16 and write the
+//    next layer's activations over the tile's stage (its MMAs are done with
+//    it), synchronise the 128 epilogue threads, and issue the tile's next
+//    layer -- which runs while the epilogue drains the next tile.  After the
+//    last layer the stage goes back to its encoder group (`empty`).
+// Operands in shared memory in the canonical K-major layout without swizzle
+// (8-row x 16-byte core matrices: element (r, k) at (r/8)*512 + (k/8)*64 +
+// (r%8)*8 + k%8); one tcgen05.mma kind::f16 per K=16 step, M=128, N=64 (the
+// output layer N=16, 3 columns used), FP32 accumulators.  Every wait is
+// bounded: a wait that gives up sets FrameStatus::async_timeout and the CTA
+// leaves after waiting (bounded) for its MMAs still in flight.
 constexpr int kTcRows = 128;
-constexpr int kTcThreads = 256;
-constexpr uint32_t kTcCols = 64;  // TMEM columns allocated per CTA
+constexpr int kWsGroups = 3;
+constexpr int kWsEncThreads = kWsGroups * 256;
+constexpr int kWsEpiThreads = 256;
+constexpr int kWsThreads = kWsEncThreads + kWsEpiThreads;
+constexpr int kWsStages = 2 * kWsGroups;
+constexpr uint32_t kTcCols = 256;  // TMEM columns: 3 accumulators of 64
 constexpr uint32_t kCoreLbo = 128, kCoreSbo = 1024;
 
 __device__ __forceinline__ int umma_elem(int r, int k) { return (r >> 3) * 512 + (k >> 3) * 64 + (r & 7) * 8 + (k & 7); }
 
 struct TcSmem {
-  unsigned short w[4][64 * 64];   // W1..W4 (rows = outputs), canonical layout
-  unsigned short w5[16 * 64];     // W5 (16 output rows, 3 used)
-  unsigned short a[kTcRows * 64]; // activations of the current layer
-  uint64_t bar;
+  unsigned short w[4][64 * 64];                 // W1..W4 (rows = outputs), canonical layout
+  unsigned short w5[16 * 64];                   // W5 (16 output rows, 3 used)
+  unsigned short a[kWsStages][kTcRows * 64];    // per stage: a tile's inputs, then its activations
+  uint64_t full[kWsStages];                     // encoder group -> issuer (256 arrivals)
+  uint64_t empty[kWsStages];                    // issuer -> encoder group (1 arrival)
+  uint64_t mma[kWsGroups];                      // tcgen05.commit of a batch slot's layer
   uint32_t tmem;
+  int abort;
 };
 
 __device__ __forceinline__ uint4 pack8(const float* x) {
   return make_uint4(pack_bf16(x[0], x[1]), pack_bf16(x[2], x[3]), pack_bf16(x[4], x[5]), pack_bf16(x[6], x[7]));
 }
 
+// bar.sync of the epilogue threads (named barrier 1) with an OR of `v`.
+__device__ __forceinline__ bool epi_sync_or(bool v) {
+  uint32_t r;
+  asm volatile(
+      "{\n .reg .pred p, q;\n setp.ne.u32 p, %1, 0;\n barrier.cta.red.or.pred q, 1, 256, p;\n"
+      " selp.u32 %0, 1, 0, q;\n}"
+      : "=r"(r)
+      : "r"((uint32_t)v)
+      : "memory");
+  return r != 0;
+}
+
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+// Input row `row` of the batch: texture-space position, normal, albedo.
 template <bool FROM_GBUF>
-__global__ void __launch_bounds__(kTcThreads, 4)
+__device__ __forceinline__ void tc_input(const SceneParams& sp, const float4* __restrict__ gb_pos,
+                                         const float4* __restrict__ gb_nrm, const float* __restrict__ samples, int n,
+                                         float inv_cube, int r, V3& pos, V3& nrm, V3& alb, bool& valid) {
+  valid = false;
+  pos = nrm = alb = v3(0.f, 0.f, 0.f);
+  if (r >= n) return;
+  if (FROM_GBUF) {
+    const float4 a = gb_pos[r], c = gb_nrm[r];
+    if (__float_as_uint(c.w) != 0xffffffffu) {
+      valid = true;
+      pos = v3(a.x * inv_cube, a.y * inv_cube, a.z * inv_cube) * 0.5f + v3(0.5f, 0.5f, 0.5f);
+      nrm = v3(c.x, c.y, c.z);
+      const vct_material_data& m = sp.materials[__float_as_uint(a.w)];
+      alb = v3(m.diffuse[0], m.diffuse[1], m.diffuse[2]);
+    }
+  } else {
+    const float* q = samples + (size_t)r * 12;
+    valid = true;
+    pos = v3(q[0], q[1], q[2]);
+    nrm = v3(q[3], q[4], q[5]);
+    alb = v3(q[6], q[7], q[8]);
+  }
+}
+
+template <bool FROM_GBUF>
+__global__ void __launch_bounds__(kWsThreads, 1)
     k_mlp_fwd_tc(MlpParams p, SceneParams sp, const float4* __restrict__ gb_pos, const float4* __restrict__ gb_nrm,
                  const float* __restrict__ samples, int n, float4* __restrict__ out4, float* __restrict__ out3,
                  FrameStatus* status) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
   TcSmem& S = *reinterpret_cast<TcSmem*>(smem_raw + ((128u - (smem_u32(smem_raw) & 127u)) & 127u));
-  const int tid = threadIdx.x, warp = tid >> 5, row = tid & (kTcRows - 1), half = tid >> 7;
-  const unsigned short* g = reinterpret_cast<const unsigned short*>(p.w_bf);
-  for (int i = tid; i < 4 * 64 * 64; i += kTcThreads) {
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const unsigned short* gw = reinterpret_cast<const unsigned short*>(p.w_bf);
+  for (int i = tid; i < 4 * 64 * 64; i += kWsThreads) {
     const int l = i >> 12, o = (i >> 6) & 63, k = i & 63;
-    S.w[l][umma_elem(o, k)] = g[i];
+    S.w[l][umma_elem(o, k)] = gw[i];
   }
-  for (int i = tid; i < 16 * 64; i += kTcThreads) S.w5[umma_elem(i >> 6, i & 63)] = g[4 * 4096 + i];
+  for (int i = tid; i < 16 * 64; i += kWsThreads) S.w5[umma_elem(i >> 6, i & 63)] = gw[4 * 4096 + i];
   if (tid == 0) {
-    mbar_init(&S.bar, 1);
+    for (int s = 0; s < kWsStages; ++s) {
+      mbar_init(&S.full[s], 256);
+      mbar_init(&S.empty[s], 1);
+    }
+    for (int j = 0; j < kWsGroups; ++j) mbar_init(&S.mma[j], 1);
+    S.abort = 0;
     mbar_init_fence();
   }
-  __syncwarp();
-  if (warp == 0) tc_alloc(&S.tmem, kTcCols);
-  fence_async_smem();
+  const int epi_warp0 = kWsEncThreads / 32;
+  if (warp == epi_warp0) tc_alloc(&S.tmem, kTcCols);
+  fence_async_smem();  // the weights, for the tensor cores
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
-  const uint32_t tmem = S.tmem;
-  const uint32_t lane_addr = tmem + ((uint32_t)((warp & 3) * 32) << 16);
-  const float inv_cube = 1.0f / sp.cube_size;
-  uint32_t phase = 0;
-  bool ok = true;
   const int tiles = (n + kTcRows - 1) / kTcRows;
-  for (int tile = blockIdx.x; tile < tiles && ok; tile += gridDim.x) {
-    const int r = tile * kTcRows + row;
-    V3 pos = v3(0.f, 0.f, 0.f), nrm = pos, alb = pos;
-    bool valid = false;
-    if (FROM_GBUF) {
-      if (r < n) {
-        const float4 a = gb_pos[r], c = gb_nrm[r];
-        if (__float_as_uint(c.w) != 0xffffffffu) {
-          valid = true;
-          pos = v3(a.x * inv_cube, a.y * inv_cube, a.z * inv_cube) * 0.5f + v3(0.5f, 0.5f, 0.5f);
-          nrm = v3(c.x, c.y, c.z);
-          const vct_material_data& m = sp.materials[__float_as_uint(a.w)];
-          alb = v3(m.diffuse[0], m.diffuse[1], m.diffuse[2]);
-        }
-      }
-    } else if (r < n) {
-      const float* q = samples + (size_t)r * 12;
-      valid = true;
-      pos = v3(q[0], q[1], q[2]);
-      nrm = v3(q[3], q[4], q[5]);
-      alb = v3(q[6], q[7], q[8]);
-    }
-    // Inputs: half 0 the hash levels 0..7 (k 0..15), half 1 levels 8..15
-    // (k 16..31) and normal, albedo, 1, zeros (k 32..63).
-    float x[16];
-#pragma unroll
-    for (int j = 0; j < 8; ++j) {
-      const float2 f = valid ? level_features(p, 8 * half + j, pos) : make_float2(0.f, 0.f);
-      x[2 * j] = f.x;
-      x[2 * j + 1] = f.y;
-    }
-    uint4* arow = reinterpret_cast<uint4*>(S.a);
-    arow[umma_elem(row, 16 * half) / 8] = pack8(x);
-    arow[umma_elem(row, 16 * half + 8) / 8] = pack8(x + 8);
-    if (half) {
-      const V3 nn = normalize(nrm);
-      float e[32];
-#pragma unroll
-      for (int i = 0; i < 32; ++i) e[i] = 0.f;
-      if (valid) {
-        e[0] = nn.x; e[1] = nn.y; e[2] = nn.z;
-        e[3] = alb.x; e[4] = alb.y; e[5] = alb.z;
-        e[6] = 1.0f;
-      }
-#pragma unroll
-      for (int c = 0; c < 4; ++c) arow[umma_elem(row, 32 + 8 * c) / 8] = pack8(e + 8 * c);
-    }
-    fence_async_smem();
-    tc_fence_before();
-    __syncthreads();
-    for (int layer = 0; layer < 5 && ok; ++layer) {
-      const int N = layer < 4 ? 64 : 16;
-      if (tid == 0) {
-        tc_fence_after();
-        const unsigned short* W = layer < 4 ? S.w[layer] : S.w5;
-#pragma unroll
-        for (int kk = 0; kk < 4; ++kk)
-          tc_mma_bf16(tmem, tc_smem_desc(S.a + 128 * kk, kCoreLbo, kCoreSbo),
-                      tc_smem_desc(W + 128 * kk, kCoreLbo, kCoreSbo), tc_idesc_bf16(kTcRows, N), kk > 0 ? 1u : 0u);
-        tc_commit(&S.bar);
-      }
-      const bool done = mbar_wait(&S.bar, phase & 1);
-      ++phase;
-      if (__syncthreads_or(!done)) {
-        ok = false;
+  const float inv_cube = 1.0f / sp.cube_size;
+  // The CTA's it-th tile is blockIdx.x + it * gridDim.x; its stage it % 6.
+  if (tid < kWsEncThreads) {
+    // ---------------------------------------------------------- encoders --
+    const int grp = warp >> 3, wi = warp & 7, g = lane >> 2, t = lane & 3;
+    for (int it = grp;; it += kWsGroups) {
+      const int tile = blockIdx.x + it * gridDim.x;
+      if (tile >= tiles) break;
+      const int s = it % kWsStages, use = it / kWsStages;
+      if (use > 0 && !mbar_wait(&S.empty[s], (use - 1) & 1)) {
+        atomicOr(&status->async_timeout, 1u);
+        S.abort = 1;
         break;
       }
-      tc_fence_after();
-      if (layer < 4) {
-        float v[16], w[16];
-        tc_ld16(lane_addr + 32 * half, v);
-        tc_ld16(lane_addr + 32 * half + 16, w);
-        tc_wait_ld();
+      if (*(volatile int*)&S.abort) break;
+      uint32_t* a32 = reinterpret_cast<uint32_t*>(S.a[s]);
 #pragma unroll
-        for (int i = 0; i < 16; ++i) {
-          v[i] = fmaxf(v[i], 0.f);
-          w[i] = fmaxf(w[i], 0.f);
+      for (int h = 0; h < 2; ++h) {
+        const int row = 16 * wi + g + 8 * h;
+        V3 pos, nrm, alb;
+        bool valid;
+        tc_input<FROM_GBUF>(sp, gb_pos, gb_nrm, samples, n, inv_cube, tile * kTcRows + row, pos, nrm, alb, valid);
+        const int lv[4] = {t, t + 4, 8 + t, 12 + t};
+        uint32_t f[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const float2 v = valid ? level_features(p, lv[q], pos) : make_float2(0.f, 0.f);
+          f[q] = pack_bf16(v.x, v.y);
         }
-        arow[umma_elem(row, 32 * half) / 8] = pack8(v);
-        arow[umma_elem(row, 32 * half + 8) / 8] = pack8(v + 8);
-        arow[umma_elem(row, 32 * half + 16) / 8] = pack8(w);
-        arow[umma_elem(row, 32 * half + 24) / 8] = pack8(w + 8);
-        fence_async_smem();
-      } else if (half == 0) {
-        float v[16];
-        tc_ld16(lane_addr, v);
-        tc_wait_ld();
-        if (r < n) {
-          if (FROM_GBUF) out4[r] = make_float4(v[0], v[1], v[2], 0.f);
-          else {
-            out3[3 * r] = v[0];
-            out3[3 * r + 1] = v[1];
-            out3[3 * r + 2] = v[2];
+        float x0 = 0.f, x1 = 0.f;
+        if (valid) {
+          const V3 nn = normalize(nrm);
+          // x = (n.x, n.y, n.z, alb.x, alb.y, alb.z, 1, 0, 0, ...)
+          x0 = t == 0 ? nn.x : (t == 1 ? nn.z : (t == 2 ? alb.y : 1.0f));
+          x1 = t == 0 ? nn.y : (t == 1 ? alb.x : (t == 2 ? alb.z : 0.0f));
+        }
+#pragma unroll
+        for (int q = 0; q < 4; ++q) a32[umma_elem(row, 2 * lv[q]) >> 1] = f[q];
+        a32[umma_elem(row, 32 + 2 * t) >> 1] = pack_bf16(x0, x1);
+#pragma unroll
+        for (int c = 0; c < 3; ++c) a32[umma_elem(row, 40 + 8 * c + 2 * t) >> 1] = 0u;
+      }
+      fence_async_smem();
+      mbar_arrive(&S.full[s]);
+    }
+  } else {
+    // ---------------------------------------------------------- epilogue --
+    const int e = tid - kWsEncThreads, ew = e >> 5, row = 32 * (ew & 3) + lane, ch = ew >> 2;
+    const uint32_t tmem = S.tmem;
+    const uint32_t lane_addr = tmem + ((uint32_t)(32 * (ew & 3)) << 16);
+    const uint32_t idesc64 = tc_idesc_bf16(kTcRows, 64), idesc16 = tc_idesc_bf16(kTcRows, 16);
+    uint32_t mma_phase = 0;  // bit j: parity of slot j's next commit (flipped by each completed wait)
+    uint32_t pending = 0;    // bit j: an MMA group of slot j not yet waited for (issuer)
+    bool bad = false;
+    auto issue = [&](int j, int s, int layer) {  // issuer only
+      tc_fence_after();
+      const unsigned short* W = layer < 4 ? S.w[layer] : S.w5;
+#pragma unroll
+      for (int kk = 0; kk < 4; ++kk)
+        tc_mma_bf16(tmem + 64u * j, tc_smem_desc(S.a[s] + 128 * kk, kCoreLbo, kCoreSbo),
+                    tc_smem_desc(W + 128 * kk, kCoreLbo, kCoreSbo), layer < 4 ? idesc64 : idesc16, kk > 0 ? 1u : 0u);
+      tc_commit(&S.mma[j]);
+      pending |= 1u << j;
+    };
+    for (int b = 0; !bad; ++b) {
+      int nb = 0;
+      while (nb < kWsGroups && blockIdx.x + (kWsGroups * b + nb) * gridDim.x < tiles) ++nb;
+      if (nb == 0) break;
+      bool ok = true;
+      if (e == 0) {
+        for (int j = 0; j < nb && ok; ++j) {
+          const int it = kWsGroups * b + j;
+          ok = mbar_wait(&S.full[it % kWsStages], (it / kWsStages) & 1);
+          if (ok) issue(j, it % kWsStages, 0);
+        }
+      }
+      if (epi_sync_or(!ok)) {
+        bad = true;
+        break;
+      }
+      for (int layer = 0; layer < 5 && !bad; ++layer) {
+        for (int j = 0; j < nb; ++j) {
+          const int it = kWsGroups * b + j, s = it % kWsStages;
+          ok = mbar_wait(&S.mma[j], (mma_phase >> j) & 1);
+          if (ok) {
+            mma_phase ^= 1u << j;
+            pending &= ~(1u << j);
+            tc_fence_after();
+            const uint32_t acc = lane_addr + 64u * j;
+            if (layer < 4) {
+              float v[16], w[16];
+              uint4* arow = reinterpret_cast<uint4*>(S.a[s]);
+              tc_ld16(acc + 32 * ch, v);
+              tc_ld16(acc + 32 * ch + 16, w);
+              tc_wait_ld();
+#pragma unroll
+              for (int i = 0; i < 16; ++i) {
+                v[i] = fmaxf(v[i], 0.f);
+                w[i] = fmaxf(w[i], 0.f);
+              }
+              arow[umma_elem(row, 32 * ch) / 8] = pack8(v);
+              arow[umma_elem(row, 32 * ch + 8) / 8] = pack8(v + 8);
+              arow[umma_elem(row, 32 * ch + 16) / 8] = pack8(w);
+              arow[umma_elem(row, 32 * ch + 24) / 8] = pack8(w + 8);
+              fence_async_smem();
+            } else if (ch == 0) {
+              float v[16];
+              tc_ld16(acc, v);
+              tc_wait_ld();
+              const int r = (blockIdx.x + it * gridDim.x) * kTcRows + row;
+              if (r < n) {
+                if (FROM_GBUF) out4[r] = make_float4(v[0], v[1], v[2], 0.f);
+                else {
+                  out3[3 * r] = v[0];
+                  out3[3 * r + 1] = v[1];
+                  out3[3 * r + 2] = v[2];
+                }
+              }
+            }
+          }
+          tc_fence_before();
+          if (epi_sync_or(!ok)) {
+            bad = true;
+            break;
+          }
+          if (e == 0) {
+            if (layer < 4) issue(j, s, layer + 1);
+            else mbar_arrive(&S.empty[s]);  // the tile's last MMAs are done with its stage
           }
         }
       }
-      tc_fence_before();
-      __syncthreads();
     }
+    if (bad) {
+      if (e == 0) atomicOr(&status->async_timeout, 1u);
+      S.abort = 1;
+    }
+    if (e == 0)  // MMA groups still in flight
+      for (int j = 0; j < kWsGroups; ++j)
+        if ((pending >> j) & 1) mbar_wait(&S.mma[j], (mma_phase >> j) & 1);
   }
+  tc_fence_before();
   __syncthreads();
-  if (!ok && tid == 0) {
-    atomicOr(&status->async_timeout, 1u);
-    mbar_wait(&S.bar, phase & 1);  // the group still in flight, if any
-  }
-  __syncthreads();
-  if (warp == 0) {
+  if (warp == epi_warp0) {
     tc_fence_after();
-    tc_dealloc(tmem, kTcCols);
+    tc_dealloc(S.tmem, kTcCols);
   }
 }
 
@@ -776,14 +876,10 @@ cudaError_t run_fwd_tc(const MlpParams& p, const SceneParams& sp, const float4* 
   auto kern = k_mlp_fwd_tc<FROM_GBUF>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  int per_sm = 1;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kTcThreads, smem) != cudaSuccess || per_sm < 1)
-    per_sm = 1;
-  // Each resident CTA holds kTcCols of the SM's 512 TMEM columns.
-  per_sm = std::min(per_sm, (int)(512 / kTcCols));
+  // One CTA per SM (it holds kTcCols of the SM's 512 TMEM columns).
   const int tiles = (n + kTcRows - 1) / kTcRows;
-  kern<<<std::max(1, std::min(tiles, sm_count() * per_sm)), kTcThreads, smem, st>>>(p, sp, gb_pos, gb_nrm, samples, n,
-                                                                                  out4, out3, status);
+  kern<<<std::max(1, std::min(tiles, sm_count())), kWsThreads, smem, st>>>(p, sp, gb_pos, gb_nrm, samples, n, out4,
+                                                                         out3, status);
   return cudaGetLastError();
 }
 

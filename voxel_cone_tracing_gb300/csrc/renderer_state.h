@@ -128,7 +128,7 @@ using namespace vct::detail;
 struct MlpState {
   bool ready = false;  // parameters allocated and initialised
   bool trained = false;
-  bool tc = false;     // forward on tcgen05 / TMEM (else mma.sync warp tiles)
+  bool tc = true;      // forward on tcgen05 / TMEM, warp-specialised (else mma.sync warp tiles)
   int32_t levels = 16, log2_table = 19, n_min = 16, n_max = 512;
   int adam_t = 0;
   DevBuf<float> table, table_grad, table_m, table_v;  // levels * T * 2
