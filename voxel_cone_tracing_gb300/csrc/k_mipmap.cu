@@ -229,7 +229,24 @@ __device__ __forceinline__ void mip_reduce(const MapSet& ms, int src_level, int 
         occ_store<B>(ms, l, ox, oy, oz, x, y, z, r, any, occ_box + occ_off);
       }
     }
-    if (FROM_L0 && ms.skip_empty) {
+    if (!FROM_L0 && ms.skip_empty && ms.occ_raw[src_level + l]) {
+      // Tail passes: the occupancy bytes of their levels, from the source
+      // level's bytes (l = 1) and then from the region's shared copy.
+      const int S = ms.N >> src_level, cb = b * 2, dl = src_level + l, sd = ms.N >> dl;
+      for (int r = threadIdx.x; r < b3; r += kThreads) {
+        const int x = r % b, y = (r / b) % b, z = r / (b * b);
+        bool any = false;
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+          const int cx = 2 * x + c_off[k][0], cy = 2 * y + c_off[k][1], cz = 2 * z + c_off[k][2];
+          any |= l == 1 ? __ldg(ms.occ_raw[src_level] + ((size_t)(oz + cz) * S + oy + cy) * S + ox + cx) != 0
+                        : occ_box[occ_prev + (cz * cb + cy) * cb + cx] != 0;
+        }
+        occ_box[occ_off + r] = any ? 1 : 0;
+        ms.occ_raw[dl][((size_t)((oz >> l) + z) * sd + (oy >> l) + y) * sd + (ox >> l) + x] = any ? 1 : 0;
+      }
+    }
+    if (ms.skip_empty) {
       occ_prev = occ_off;
       occ_off += b3;
     }
@@ -575,6 +592,11 @@ __device__ __forceinline__ bool occ_raw_cell(const MapSet& ms, int c, int x, int
       } else if (f == 8) {
         const uint2 v = __ldg(reinterpret_cast<const uint2*>(row));  // 8-byte aligned: x * 8
         any |= v.x | v.y;
+      } else if (f >= 16) {  // 16-byte aligned: x * f, and every row of level k holds a multiple of 16 bytes
+        for (int dx = 0; dx < f; dx += 16) {
+          const uint4 v = __ldg(reinterpret_cast<const uint4*>(row + dx));
+          any |= v.x | v.y | v.z | v.w;
+        }
       } else {
         for (int dx = 0; dx < f; ++dx) any |= __ldg(row + dx);
       }
@@ -583,18 +605,22 @@ __device__ __forceinline__ bool occ_raw_cell(const MapSet& ms, int c, int x, int
 }
 
 __device__ void occ_pack_word(const MapSet& ms, int c, uint32_t w) {
-  if (c == 1 && ms.occ_k == 4) return;  // written packed by the first pass (16^3 regions)
+  if (c == 1 && ms.occ_l1_packed) return;  // written packed by the first pass (16^3 regions)
   const int s = ms.N >> c, wpr = ms.occ_wpr[c];
   const int xw = (int)(w % wpr), y = (int)((w / wpr) % s), z = (int)(w / ((uint32_t)wpr * s));
   const int x0 = xw * 32;
   uint32_t bits = 0;
   if (c <= ms.occ_k && s >= 32) {
-    const uint32_t* r = reinterpret_cast<const uint32_t*>(ms.occ_raw[c] + ((size_t)z * s + y) * s + x0);
+    // 32 bytes, 16-byte aligned (x0 and s are multiples of 32)
+    const uint4* r = reinterpret_cast<const uint4*>(ms.occ_raw[c] + ((size_t)z * s + y) * s + x0);
 #pragma unroll
-    for (int j = 0; j < 8; ++j) {
-      const uint32_t v = __ldg(r + j);
+    for (int j = 0; j < 2; ++j) {
+      const uint4 v4 = __ldg(r + j);
+      const uint32_t v[4] = {v4.x, v4.y, v4.z, v4.w};
 #pragma unroll
-      for (int q = 0; q < 4; ++q) bits |= (((v >> (8 * q)) & 0xffu) ? 1u : 0u) << (4 * j + q);
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) bits |= (((v[i] >> (8 * q)) & 0xffu) ? 1u : 0u) << (16 * j + 4 * i + q);
     }
   } else {
     for (int i = 0; i < 32 && x0 + i < s; ++i)
@@ -713,9 +739,13 @@ cudaError_t launch_mipmap(const MapSet& ms, int mip_mode, cudaStream_t st, int* 
                                         : run_all<6, VCT_STORAGE_RGBA16F>(ms, st, launches, map, status, fl);
   }
   if (e != cudaSuccess || !ms.skip_empty || ms.L < 2) return e;
-  const uint32_t total = occ_words(ms);
-  k_occupancy<false><<<(total + 255) / 256, 256, 0, st>>>(ms, total);
-  k_occupancy<true><<<(total + 255) / 256, 256, 0, st>>>(ms, total);
+  // Every level now has its occupancy bytes (first pass or brick kernel,
+  // then the tail passes).
+  MapSet mo = ms;
+  mo.occ_k = ms.L - 1;
+  const uint32_t total = occ_words(mo);
+  k_occupancy<false><<<(total + 255) / 256, 256, 0, st>>>(mo, total);
+  k_occupancy<true><<<(total + 255) / 256, 256, 0, st>>>(mo, total);
   if (launches) *launches += 2;
   return cudaGetLastError();
 }

@@ -312,10 +312,12 @@ struct MapStore {
     ms.nmaps = nmaps;
     ms.storage = storage;
     if (L > 1) {
-      // occupancy: raw bytes for the first pass's levels, dilated bits for all
+      // occupancy: raw bytes for every level (the first pass writes levels
+      // 1..occ_k, the tail passes the rest), packed and dilated bits
       ms.occ_k = std::min(L - 1, 4);
+      ms.occ_l1_packed = L - 1 >= 4 ? 1 : 0;
       size_t bytes = 0;
-      for (int c = 1; c <= ms.occ_k; ++c) bytes += (size_t)(r >> c) * (r >> c) * (r >> c);
+      for (int c = 1; c < L; ++c) bytes += (size_t)(r >> c) * (r >> c) * (r >> c);
       bytes = (bytes + 255) & ~(size_t)255;
       const size_t raw_bytes = bytes;
       for (int c = 1; c < L; ++c) {
@@ -326,7 +328,7 @@ struct MapStore {
       VCT_CUDA(cudaMalloc(&occ_mem, bytes));
       unsigned char* base = static_cast<unsigned char*>(occ_mem);
       size_t o = 0;
-      for (int c = 1; c <= ms.occ_k; ++c) {
+      for (int c = 1; c < L; ++c) {
         ms.occ_raw[c] = base + o;
         o += (size_t)(r >> c) * (r >> c) * (r >> c);
       }
@@ -769,7 +771,8 @@ struct vct_renderer {
     VCT_CUDA(cudaEventRecord(ev[1], stream));
     if (fuse) {
       MapSet m3 = ms;
-      m3.occ_k = 3;  // the levels whose occupancy bytes the brick kernel wrote
+      m3.occ_k = 3;          // the levels whose occupancy bytes the brick kernel wrote
+      m3.occ_l1_packed = 0;  // (as bytes)
       VCT_CUDA(launch_mipmap(m3, cfg.mip_mode, stream, &launches, nullptr, d_status.p, 3));
     } else {
       VCT_CUDA(launch_mipmap(ms, cfg.mip_mode, stream, &launches, have_l0_map ? &l0_map : nullptr, d_status.p));

@@ -128,6 +128,7 @@ struct MapSet {
   // one cell of floor(u * (N >> c))).
   int skip_empty;
   int occ_k;
+  int occ_l1_packed;  // level 1 written as packed bits by the first pass (16^3 regions), not as bytes
   uint8_t* occ_raw[kMaxLevels];
   uint32_t* occ_pack[kMaxLevels];  // undilated occupancy bits (same layout as occ)
   uint32_t* occ[kMaxLevels];
