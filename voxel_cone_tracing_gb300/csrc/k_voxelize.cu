@@ -873,17 +873,25 @@ __device__ __forceinline__ void brick_occ(const BrickMips& bm, int N, int level,
   bm.occ_raw[level][((size_t)z * s + y) * s + x] = any ? 1 : 0;
 }
 
+// Texel (x, y, z), map d, of the level above a cube of side s2 stored
+// [z][y][x] at src (shared memory): one out-of-line copy of the rule for
+// all three levels.
+__device__ __noinline__ uint32_t brick_mip_texel(const uint32_t* src, int s2, int x, int y, int z, int d) {
+  return aniso_rgba8_dir(d, [&](int k) { return src[mip_child(s2, x, y, z, k)]; });
+}
+
 // Levels 1-3 of brick b3 from scr.l0 ([z][y][x], written and synchronised
-// by the caller); all threads of the CTA.  Each (texel, map) item takes one
-// thread, the map a run-time index (aniso_rgba8_dir), so that the whole CTA
-// works on level 1 and the code exists once: six unrolled copies of the rule
-// made the kernel miss its instruction cache.
+// by the caller); all threads of the CTA.  Level 1 takes the whole CTA, one
+// (texel, map) item per thread with the map a run-time index, so that the
+// rule's code exists once (six unrolled copies made the kernel miss its
+// instruction cache); levels 2 and 3 (48 and 6 items) and their occupancy
+// and alpha copies are one warp's, which synchronises only itself.
 __device__ void brick_mips(const BrickMips& bm, int N, const int b3[3], BrickMipScratch& scr) {
-  static_assert(kThreads >= 128, "level 2 and its occupancy take threads 64-119");
+  static_assert(kThreads >= 96, "levels 2-3 are warp 2's");
   const int t = threadIdx.x;
   for (int i = t; i < 6 * 64; i += kThreads) {  // level 1: map i / 64 (warp-uniform), texel i % 64
     const int d = i >> 6, r = i & 63, x = r & 3, y = (r >> 2) & 3, z = r >> 4;
-    const uint32_t v = aniso_rgba8_dir(d, [&](int k) { return scr.l0[mip_child(8, x, y, z, k)]; });
+    const uint32_t v = brick_mip_texel(scr.l0, 8, x, y, z, d);
     surf3Dwrite(v, bm.surf[d][1], (b3[0] * 4 + x) * 4, b3[1] * 4 + y, b3[2] * 4 + z);
     scr.l1[d][r] = v;
   }
@@ -899,35 +907,41 @@ __device__ void brick_mips(const BrickMips& bm, int N, const int b3[3], BrickMip
   if (t < 64) {
     if (bm.has_alpha) brick_alpha(bm, 1, b3[0] * 4 + (t & 3), b3[1] * 4 + ((t >> 2) & 3), b3[2] * 4 + (t >> 4),
                                   &scr.l1[0][t], 64);
-  } else if (t < 64 + 48) {  // level 2: texel r of map d from that map's level 1
-    const int j = t - 64, d = j >> 3, r = j & 7, x = r & 1, y = (r >> 1) & 1, z = r >> 2;
-    const uint32_t v = aniso_rgba8_dir(d, [&](int k) { return scr.l1[d][mip_child(4, x, y, z, k)]; });
+    return;
+  }
+  if (t >= 96) return;
+  const int lane = t - 64;
+  for (int j = lane; j < 48; j += 32) {  // level 2: texel r of map d from that map's level 1
+    const int d = j >> 3, r = j & 7, x = r & 1, y = (r >> 1) & 1, z = r >> 2;
+    const uint32_t v = brick_mip_texel(scr.l1[d], 4, x, y, z, d);
     surf3Dwrite(v, bm.surf[d][2], (b3[0] * 2 + x) * 4, b3[1] * 2 + y, b3[2] * 2 + z);
     scr.l2[d][r] = v;
-  } else if (t < 64 + 48 + 8) {  // occupancy of level 2 from level 1's
-    const int r = t - 112, x = r & 1, y = (r >> 1) & 1, z = r >> 2;
+  }
+  if (lane < 8) {  // occupancy of level 2 from level 1's
+    const int x = lane & 1, y = (lane >> 1) & 1, z = lane >> 2;
     bool any = false;
 #pragma unroll
     for (int k = 0; k < 8; ++k) any |= scr.occ1[mip_child(4, x, y, z, k)] != 0;
-    scr.occ2[r] = any ? 1 : 0;
+    scr.occ2[lane] = any ? 1 : 0;
     brick_occ(bm, N, 2, b3[0] * 2 + x, b3[1] * 2 + y, b3[2] * 2 + z, any);
   }
-  __syncthreads();
-  if (t < 8) {
-    if (bm.has_alpha) brick_alpha(bm, 2, b3[0] * 2 + (t & 1), b3[1] * 2 + ((t >> 1) & 1), b3[2] * 2 + (t >> 2),
-                                  &scr.l2[0][t], 8);
-  } else if (t >= 32 && t < 38) {  // level 3: the brick's one texel of map d
-    const int d = t - 32;
-    const uint32_t v = aniso_rgba8_dir(d, [&](int k) { return scr.l2[d][mip_child(2, 0, 0, 0, k)]; });
+  __syncwarp();
+  if (lane < 8) {
+    if (bm.has_alpha)
+      brick_alpha(bm, 2, b3[0] * 2 + (lane & 1), b3[1] * 2 + ((lane >> 1) & 1), b3[2] * 2 + (lane >> 2),
+                  &scr.l2[0][lane], 8);
+  } else if (lane < 14) {  // level 3: the brick's one texel of map d
+    const int d = lane - 8;
+    const uint32_t v = brick_mip_texel(scr.l2[d], 2, 0, 0, 0, d);
     surf3Dwrite(v, bm.surf[d][3], b3[0] * 4, b3[1], b3[2]);
     scr.l3[d] = v;
-  } else if (t == 64) {
+  } else if (lane == 14) {
     bool any = false;
     for (int k = 0; k < 8; ++k) any |= scr.occ2[k] != 0;
     brick_occ(bm, N, 3, b3[0], b3[1], b3[2], any);
   }
-  __syncthreads();
-  if (t == 0 && bm.has_alpha) brick_alpha(bm, 3, b3[0], b3[1], b3[2], scr.l3, 1);
+  __syncwarp();
+  if (lane == 0 && bm.has_alpha) brick_alpha(bm, 3, b3[0], b3[1], b3[2], scr.l3, 1);
 }
 
 // Levels 1-3 of an empty brick: zeros (the texels and the occupancy).
