@@ -278,6 +278,7 @@ def mlp_leg(r, R, scene, ids, stream, flush, steps, plain_stages, per_pixel_trac
     trace_cones = statistics.mean(s["trace"] for s in plain_stages)
     value = statistics.mean(s["voxelize"] + s["mipmap"] + s["trace"] for s in stages)
     res = {"value": round(value, 4), "unit": UNIT, "trace_ms": round(trace_mlp, 4),
+           "infer_ms": round(statistics.mean(s["infer"] for s in stages), 4),
            "forward": "tcgen05, warp-specialised",
            "trace_ms_mma_sync_forward": round(statistics.mean(s["trace"] for s in sync_stages), 4),
            "trace_ms_cones": round(trace_cones, 4), "trace_speedup": round(trace_cones / trace_mlp, 3),

@@ -153,6 +153,8 @@ typedef struct {
                              * injection reused the attribute grids        */
   uint32_t split_bricks;    /* dense bricks (> 1024 triangle pairs) whose
                              * pairs were spread over several CTAs         */
+  float infer;              /* the learned diffuse term's inference (part of
+                             * trace; 0 without it)                        */
 } vct_stage_times;
 
 /* --------------------------------------------------- error reporting --- */

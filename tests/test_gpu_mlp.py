@@ -166,6 +166,7 @@ def test_learned_diffuse_replaces_cones(vct):
         return r.read_frame(vct.FRAME_RGBA32F).copy()
 
     cones = frame()
+    assert r.stage_times()["infer"] == 0.0
     r.mlp_init(vct.mlp_desc(n_max=256, seed=1))
     r.mlp_train(vct.mlp_desc(n_max=256, seed=1, steps=0, n_samples=1 << 12))  # 1 step: untrained baseline
     r.set_diffuse_mode(vct.DIFFUSE_MLP)
@@ -174,6 +175,8 @@ def test_learned_diffuse_replaces_cones(vct):
     rep = r.mlp_train(vct.mlp_desc(n_max=256, seed=1, steps=600, batch=1 << 16, n_samples=1 << 20))
     r.set_diffuse_mode(vct.DIFFUSE_MLP)
     learned_tc = frame()  # the default: tcgen05
+    t = r.stage_times()
+    assert 0.0 < t["infer"] <= t["trace"]  # the inference is timed, and part of the trace stage
     r.mlp_set_tensor_kernels(False)
     learned = frame()
     r.mlp_set_tensor_kernels(True)

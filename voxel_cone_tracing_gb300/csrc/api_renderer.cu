@@ -367,6 +367,7 @@ extern "C" vct_status vct_get_stage_times(vct_renderer* r, vct_stage_times* out)
   out->kernel_launches = (uint32_t)r->launches;
   out->voxelized = r->last_revoxelized ? 1u : 0u;
   out->split_bricks = r->h_status.p->heavy_total;
+  out->infer = g[1];
   return VCT_OK;
 }
 

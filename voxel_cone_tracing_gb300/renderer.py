@@ -95,7 +95,7 @@ class Config(C.Structure):
 class StageTimes(C.Structure):
     _fields_ = [("voxelize", C.c_float), ("mipmap", C.c_float), ("gbuffer", C.c_float), ("trace", C.c_float),
                 ("total", C.c_float), ("kernel_launches", C.c_uint32), ("voxelized", C.c_uint32),
-                ("split_bricks", C.c_uint32)]
+                ("split_bricks", C.c_uint32), ("infer", C.c_float)]
 
 
 class DrawObj(C.Structure):
