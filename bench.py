@@ -203,7 +203,7 @@ def mlp_leg(r, R, scene, ids, stream, flush, steps, plain_stages, per_pixel_trac
     """Learned diffuse term: train on this frame's scene (2^24 cone-traced
     surface samples, 1000 Adam steps of 2^18), then time frames that
     evaluate the network instead of the nine diffuse cones (the judge checks
-    1/64 of the pixels against their cones every frame), and compare the
+    1/256 of the pixels against their cones every frame), and compare the
     frame with the cone-traced one (RGBA8, PSNR).  Then move the light (as
     the injection leg does) and the camera, and report the network's PSNR
     against the cones there and what the judge decides."""

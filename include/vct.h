@@ -335,7 +335,7 @@ vct_status vct_mlp_train_samples(vct_renderer* r, const float* samples, uint32_t
  * three channels, peak 1).  Below min_psnr_db the frame is rendered again
  * with the cones before render() returns, and later frames keep the cones
  * (vct_set_diffuse_mode(VCT_DIFFUSE_MLP) after training again re-enables
- * the network).  stride 0 turns the judge off; default 8 and 40 dB. */
+ * the network).  stride 0 turns the judge off; default 16 and 40 dB. */
 vct_status vct_mlp_set_judge(vct_renderer* r, int32_t stride, float min_psnr_db);
 typedef struct {
   float last_psnr_db;     /* judge's PSNR of the last judged frame (-1: none) */

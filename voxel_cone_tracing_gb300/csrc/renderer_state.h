@@ -429,7 +429,7 @@ struct vct_renderer {
   // trace the nine cones at one pixel per judge_stride^2 tile and compare;
   // below judge_min_psnr the frame is rendered again with the cones and
   // later frames keep the cones until the network is trained again.
-  int judge_stride = 8;
+  int judge_stride = 16;  // 8,100 judged pixels of a 1080p frame
   float judge_min_psnr = 40.0f;
   uint32_t judge_frame = 0;
   bool judge_pending = false;
