@@ -362,12 +362,12 @@ extern "C" vct_status vct_get_stage_times(vct_renderer* r, vct_stage_times* out)
   out->voxelize = t[0];
   out->mipmap = t[1];
   out->gbuffer = g[0];
-  out->trace = tr + g[1];
+  out->trace = tr + (r->infer_ran ? g[1] : 0.0f);  // (+ the learned term's inference)
   VCT_CUDA(cudaEventElapsedTime(&out->total, r->ev_start, r->ev[4]));
   out->kernel_launches = (uint32_t)r->launches;
   out->voxelized = r->last_revoxelized ? 1u : 0u;
   out->split_bricks = r->h_status.p->heavy_total;
-  out->infer = g[1];
+  out->infer = r->infer_ran ? g[1] : 0.0f;
   return VCT_OK;
 }
 

@@ -430,6 +430,7 @@ struct vct_renderer {
   // below judge_min_psnr the frame is rendered again with the cones and
   // later frames keep the cones until the network is trained again.
   int judge_stride = 16;  // 8,100 judged pixels of a 1080p frame
+  bool infer_ran = false;  // the last frame evaluated the learned term
   float judge_min_psnr = 40.0f;
   uint32_t judge_frame = 0;
   bool judge_pending = false;
@@ -748,6 +749,7 @@ struct vct_renderer {
       tp.diffuse_in = diffuse_px.p;
     }
     VCT_CUDA(cudaEventRecord(evg[2], gs));
+    infer_ran = tp.diffuse_in != nullptr;
     if (side) VCT_CUDA(cudaEventRecord(ev_join, gb_stream));
     VCT_CUDA(cudaEventRecord(ev[0], stream));
     if (inject) {
