@@ -126,14 +126,18 @@ typedef struct {
                          * a shorter frame, longer voxelize and mipmap
                          * stages; 0 (default): one stream, one stage
                          * after the other                                */
-  int32_t far_share;    /* texture-unit sampler: 1 (default): the four
-                         * pixels of a 2x2 quad with matching normals and
-                         * positions share the coarse part (lod >= 2) of
-                         * their diffuse cones, marched once per quad by the
-                         * lanes of the warp together; 0: every pixel marches
-                         * all of its cones (the reference's rule).  The FP32
-                         * software sampler always marches per pixel       */
-  int32_t reserved[3];
+  int32_t far_share;    /* texture-unit sampler: 1 (default): the pixels of
+                         * a 4x2 group with matching normals and positions
+                         * share their diffuse cones after the first sample
+                         * (the far field, marched once per group by the
+                         * lanes of the warp together); 0: every pixel
+                         * marches all of its cones (the reference's rule).
+                         * The FP32 software sampler always marches per
+                         * pixel                                           */
+  int32_t trace_tile_rows; /* shared-far-field tracer: rows of a CTA's
+                         * 16-pixel-wide tile, 8, 16 or 32; 0 (default): 16.
+                         * The frame is the same for every value          */
+  int32_t reserved[2];
 } vct_config;
 
 typedef struct vct_renderer vct_renderer;
@@ -488,8 +492,8 @@ typedef struct {
   int32_t trace_ctas_per_sm;
   int32_t trace_dynamic;
   int32_t trace_per_scene;
-  int32_t trace_tile_rows;  /* per-scene shared-far-field trace: CTA tile 16 x 8
-                             * or 16 x 16 pixels (the same frame either way) */
+  int32_t trace_tile_rows;  /* per-scene shared-far-field trace: CTA tile 16 x 8,
+                             * 16 x 16 or 16 x 32 pixels (the same frame) */
 } vct_batch_shape;
 
 typedef struct vct_batch vct_batch;

@@ -74,7 +74,7 @@ def test_bad_config_rejected_before_device(vct):
         vct.Renderer(16, 16, mip_mode=vct.MIP_BOTH + 1)
     assert e.value.status == 1
     # every switch of vct_config is 0 or 1
-    for field in ("shadow_from_maps", "full_march", "overlap_raster", "far_share"):
+    for field in ("shadow_from_maps", "full_march", "overlap_raster", "far_share", "trace_tile_rows"):
         with pytest.raises(vct.VCTError) as e:
             vct.Renderer(16, 16, **{field: 2})
         assert e.value.status == 1, field
@@ -86,7 +86,8 @@ def test_config_defaults_of_the_engine_switches(vct):
     and shared far fields of the diffuse cones for the texture-unit sampler."""
     c = vct.default_config()
     assert (c.shadow_from_maps, c.full_march, c.overlap_raster, c.far_share) == (0, 0, 0, 1)
-    assert list(c.reserved) == [0, 0, 0]
+    assert c.trace_tile_rows == 0  # 16-row tiles
+    assert list(c.reserved) == [0, 0]
 
 
 def test_cpp_facade_header_compiles(tmp_path):

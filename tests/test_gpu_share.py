@@ -99,3 +99,18 @@ def test_shared_far_fields_off_for_exact_sampler(vct):
     a, _ = _render(vct, scene, 48, 32, 32, sampler=vct.SAMPLER_EXACT)
     b, _ = _render(vct, scene, 48, 32, 32, sampler=vct.SAMPLER_EXACT, far_share=0)
     np.testing.assert_array_equal(a.read_frame(vct.FRAME_RGBA32F), b.read_frame(vct.FRAME_RGBA32F))
+
+
+@pytest.mark.parametrize("size", [(96, 64), (83, 37)], ids=["96x64", "ragged_83x37"])
+def test_tile_rows_same_frame(vct, size):
+    """The tracer's CTA tile (16 x 8, 16 x 16 -- the default -- or 16 x 32
+    pixels) changes which warps share an SM, not what a warp computes."""
+    w, h = size
+    scene = scenes.scene_small(width=w, height=h)
+    frames = {}
+    for rows in (0, 8, 16, 32):
+        r, _ = _render(vct, scene, w, h, 64, trace_tile_rows=rows)
+        frames[rows] = r.read_frame(vct.FRAME_RGBA32F).copy()
+        r.close()
+    for rows in (8, 16, 32):
+        np.testing.assert_array_equal(frames[rows], frames[0])

@@ -618,7 +618,7 @@ extern "C" vct_status vct_batch_set_shape(vct_batch* b, const vct_batch_shape* s
   if (s->bin_ctas_per_sm < 1 || s->bin_ctas_per_sm > 32 || s->bricks_ctas_per_sm < 1 ||
       s->bricks_ctas_per_sm > 32 || s->trace_ctas_per_sm < 0 || s->trace_ctas_per_sm > 3 ||
       (s->trace_dynamic != 0 && s->trace_dynamic != 1) || (s->trace_per_scene != 0 && s->trace_per_scene != 1) ||
-      (s->trace_tile_rows != 8 && s->trace_tile_rows != 16))
+      (s->trace_tile_rows != 8 && s->trace_tile_rows != 16 && s->trace_tile_rows != 32))
     return set_error(VCT_ERR_INVALID_VALUE, "launch shape out of range");
   VCT_CHECK(b->finish());
   b->shape.bin_ctas_per_sm = s->bin_ctas_per_sm;
@@ -690,14 +690,15 @@ extern "C" vct_status vct_batch_autotune(vct_batch* b, int32_t frames, vct_batch
     return VCT_OK;
   };
   // The trace's form first, from the same starting point: one launch per
-  // scene (16x8 or, with shared far fields, 16x16 tiles), one launch with
-  // one CTA per tile, or one persistent launch (2 or 3 CTAs per SM).
+  // scene (16x8 or, with shared far fields, 16x16 or 16x32 tiles), one
+  // launch with one CTA per tile, or one persistent launch (2 or 3 CTAs
+  // per SM).
   {
     const BatchShape start = cur;
-    BatchShape forms[5];
+    BatchShape forms[6];
     int nf = 0;
-    for (int rows = 8; rows <= 16; rows += 8) {
-      if (rows == 16 && !b->cfg.far_share) continue;
+    for (int rows = 8; rows <= 32; rows *= 2) {
+      if (rows > 8 && !b->cfg.far_share) continue;
       forms[nf] = start;
       forms[nf].trace_per_scene = 1;
       forms[nf++].trace_tile_rows = rows;

@@ -93,7 +93,8 @@ static vct_status check_config(const vct_config& c) {
   if (c.vox_mode < 0 || c.vox_mode > 1 || c.mip_mode < 0 || c.mip_mode > 2 || c.storage < 0 || c.storage > 1 ||
       c.sampler < 0 || c.sampler > 1 || c.cone_set < 0 || c.cone_set > 1 || c.shadow_from_maps < 0 ||
       c.shadow_from_maps > 1 || c.full_march < 0 || c.full_march > 1 || c.overlap_raster < 0 || c.overlap_raster > 1 ||
-      c.far_share < 0 || c.far_share > 1)
+      c.far_share < 0 || c.far_share > 1 ||
+      (c.trace_tile_rows != 0 && c.trace_tile_rows != 8 && c.trace_tile_rows != 16 && c.trace_tile_rows != 32))
     return set_error(VCT_ERR_INVALID_VALUE, "config field out of range");
   return VCT_OK;
 }

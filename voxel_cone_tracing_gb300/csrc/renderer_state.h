@@ -861,7 +861,7 @@ struct vct_renderer {
     tp.mip_mode = cfg.mip_mode;
     tp.diffuse_in = nullptr;
     tp.far_share = cfg.far_share;
-    tp.tile_rows = 0;
+    tp.tile_rows = cfg.trace_tile_rows;
     return tp;
   }
 };

@@ -203,8 +203,8 @@ struct TraceParams {
   // Texture-unit sampler: pixel groups share the far fields of their diffuse
   // cones (vct_config::far_share).
   int far_share;
-  // Rows of a CTA's 16-pixel-wide tile of the shared-far-field tracer: 8
-  // (0 means 8) or 16.  The frame is the same either way.
+  // Rows of a CTA's 16-pixel-wide tile of the shared-far-field tracer: 8,
+  // 16 (0 means 16) or 32.  The frame is the same for every value.
   int tile_rows;
 };
 
@@ -284,7 +284,7 @@ struct BatchShape {
   int trace_ctas_per_sm;
   int trace_dynamic;   // 1: tiles from an atomic queue; 0: static stride
   int trace_per_scene; // 1: one launch of the one-scene trace kernel per scene
-  int trace_tile_rows; // 8 or 16: CTA tile rows of the per-scene shared-far-field trace
+  int trace_tile_rows; // 8, 16 or 32: CTA tile rows of the per-scene shared-far-field trace
 };
 
 // ---- learned diffuse term (k_mlp.cu) --------------------------------------

@@ -89,7 +89,8 @@ class Config(C.Structure):
                 ("storage", C.c_int32), ("sampler", C.c_int32), ("cone_set", C.c_int32),
                 ("keep_counts", C.c_int32), ("keep_float_frame", C.c_int32), ("radiance_max", C.c_float),
                 ("shadow_from_maps", C.c_int32), ("full_march", C.c_int32),
-                ("overlap_raster", C.c_int32), ("far_share", C.c_int32), ("reserved", C.c_int32 * 3)]
+                ("overlap_raster", C.c_int32), ("far_share", C.c_int32), ("trace_tile_rows", C.c_int32),
+                ("reserved", C.c_int32 * 2)]
 
 
 class StageTimes(C.Structure):
