@@ -1,10 +1,10 @@
 // k_trace.cu -- the ConeTracer: replaces the per-fragment cone marching of
 // voxel_cone_tracing.frag (main :246-275) over the G-buffer.
 //
-// One thread shades one visible pixel; a CTA covers a 16x8 pixel tile (each
-// warp a 16x2 strip; the batched kernel's CTAs 16x16) so that neighbouring
-// lanes march neighbouring, nearly parallel cones and hit the same
-// texture-cache lines.
+// One thread shades one visible pixel; a k_trace CTA covers a 16x8 pixel
+// tile (each warp a 16x2 strip), a shared-far-field CTA a 16x16 tile of 8x4
+// warp blocks, so that neighbouring lanes march neighbouring, nearly
+// parallel cones and hit the same texture-cache lines.
 //
 // This file is compiled with -fmad=false: a product and a sum are fused only
 // where the code says so (__fmaf_rn), so the results do not depend on how
@@ -574,9 +574,9 @@ constexpr bool kFarPipe = VCT_FAR_PIPE != 0;  // software-pipelined far-field ma
 #ifndef VCT_SHARE_GROUP_W
 #define VCT_SHARE_GROUP_W 4
 #endif
-// A sharing group is kShareW x 2 pixels of a warp's 16x2 strip.
+// A sharing group is kShareW x 2 pixels of a warp's 8x4-pixel block.
 constexpr int kShareW = VCT_SHARE_GROUP_W;
-static_assert(kShareW == 2 || kShareW == 4 || kShareW == 8, "group width divides the 16-pixel strip");
+static_assert(kShareW == 2 || kShareW == 4 || kShareW == 8, "group width divides the 8-pixel block row");
 constexpr int kShareQuads = 16 / kShareW;  // groups of a warp
 constexpr int kShareCones = 9;
 constexpr int kShareJobs = kShareQuads * kShareCones;
@@ -927,8 +927,19 @@ __global__ void __launch_bounds__(kTraceThreads, SAMPLER == VCT_SAMPLER_HW ? kTr
 #endif
 constexpr int kShareMinBlocks = VCT_SHARE_MIN_BLOCKS;
 
-// One pixel of k_trace_share: the warp (a 16x2 strip of kShareW x 2
-// groups, its rows starting at an even frame row) first picks each group's
+// The pixel of this lane in a 16-pixel-wide CTA tile at (x0, y0) of the
+// shared-far-field kernels: a warp is an 8 x 4-pixel block (lane = x + 8 y),
+// two blocks per 16-pixel row of blocks.  (Measured on the 1080p bench
+// frame, trace ms: 16 x 2 strips 1.235, 8 x 4 blocks 1.217; the same frame:
+// the groups are the same aligned kShareW x 2 pixels either way.)
+__device__ __forceinline__ void share_tile_px(int x0, int y0, int& px, int& py) {
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  px = x0 + (w & 1) * 8 + (lane & 7);
+  py = y0 + (w >> 1) * 4 + (lane >> 3);
+}
+
+// One pixel of k_trace_share: the warp (an 8x4 block of kShareW x 2
+// groups, its rows starting at a frame row divisible by 4) first picks each group's
 // representative (its first pixel, row by row, whose diffuse cones are
 // traced) and the pixels that share with it, marches the groups' far fields
 // together (far_fields), then shades its pixels as k_trace does.  Called by
@@ -953,9 +964,10 @@ __device__ __forceinline__ void trace_px_share(const SceneParams& sp, const Came
   }
   valid = valid && tp.enable_diffuse && tp.view_voxel_dir >= 7 && !tp.diffuse_in;
   const unsigned vmask = __ballot_sync(0xffffffffu, valid);
-  const int q = (lane & 15) / kShareW;
-  const unsigned gbits = (1u << kShareW) - 1u;
-  const unsigned qv = vmask & ((gbits << (kShareW * q)) | (gbits << (16 + kShareW * q)));
+  // this lane's group: columns kShareW * gx .., rows 2 gy and 2 gy + 1 of the block
+  const int gx = (lane & 7) / kShareW, gy = lane >> 4;
+  const unsigned grow = ((1u << kShareW) - 1u) << (kShareW * gx);
+  const unsigned qv = vmask & ((grow << (16 * gy)) | (grow << (16 * gy + 8)));
   const int rep = qv ? __ffs(qv) - 1 : lane;
   const V3 rpos = v3(__shfl_sync(0xffffffffu, pos.x, rep), __shfl_sync(0xffffffffu, pos.y, rep),
                      __shfl_sync(0xffffffffu, pos.z, rep));
@@ -992,15 +1004,16 @@ __device__ __forceinline__ void trace_px_share(const SceneParams& sp, const Came
 }
 
 // k_trace with shared far fields: a CTA shades a 16 x ROWS tile (8 or 16
-// rows: the same warps, 16x2 strips, so the same frame either way).
+// rows: the same warps, 8x4 blocks, so the same frame either way).
 template <bool ISO, int ROWS>
 __global__ void __launch_bounds__(16 * ROWS, kShareMinBlocks * 8 / ROWS)
     k_trace_share(SceneParams sp, CameraParams cp, MapSet m, TraceParams tp, const float4* __restrict__ gb_pos,
                   const float4* __restrict__ gb_nrm, uchar4* __restrict__ frame, float4* __restrict__ frame_f32) {
-  static_assert(ROWS % 2 == 0, "whole 16x2 warps");
+  static_assert(ROWS % 4 == 0, "whole 8x4 warps");
   __shared__ FarWarp s_far[ROWS / 2];
-  trace_px_share<ISO>(sp, cp, m, tp, gb_pos, gb_nrm, frame, frame_f32, blockIdx.x * 16 + (threadIdx.x & 15),
-                      blockIdx.y * ROWS + (threadIdx.x >> 4), s_far[threadIdx.x >> 5]);
+  int px, py;
+  share_tile_px(blockIdx.x * 16, blockIdx.y * ROWS, px, py);
+  trace_px_share<ISO>(sp, cp, m, tp, gb_pos, gb_nrm, frame, frame_f32, px, py, s_far[threadIdx.x >> 5]);
 }
 
 // One pixel of a batch scene.  Called, not inlined, from the tile loop of
@@ -1083,7 +1096,7 @@ __global__ void __launch_bounds__(256, kTraceBatchMinBlocks) k_trace_batch(Batch
 }
 
 // k_trace_batch with shared far fields (the batch's far_share): every 16x16
-// tile is eight 16x2 warps, as in k_trace_share, so each scene's frame equals
+// tile is eight 8x4 warps, as in k_trace_share, so each scene's frame equals
 // a Renderer's with far_share 1.  Anisotropic maps (the batch's).
 #ifndef VCT_TRACE_BATCH_SHARE_MIN_BLOCKS
 #define VCT_TRACE_BATCH_SHARE_MIN_BLOCKS 4
@@ -1118,8 +1131,9 @@ __global__ void __launch_bounds__(256, kTraceBatchShareMinBlocks) k_trace_batch_
       if (threadIdx.x == 0) s_cur = s;
     }
     const uint32_t lt = g - __ldg(w.prefix + s), tiles_x = (uint32_t)(s_sc.W + 15) / 16;
-    trace_batch_px_share(bb.rb.gb_pos + s_sc.px_base, bb.rb.gb_nrm + s_sc.px_base, bb.frame + s_sc.px_base,
-                         (int)(lt % tiles_x) * 16 + (threadIdx.x & 15), (int)(lt / tiles_x) * 16 + (threadIdx.x >> 4),
+    int px, py;
+    share_tile_px((int)(lt % tiles_x) * 16, (int)(lt / tiles_x) * 16, px, py);
+    trace_batch_px_share(bb.rb.gb_pos + s_sc.px_base, bb.rb.gb_nrm + s_sc.px_base, bb.frame + s_sc.px_base, px, py,
                          s_far[threadIdx.x >> 5]);
     if (w.queue) {
       __syncthreads();  // every thread has read s_next
@@ -1153,7 +1167,8 @@ __global__ void __launch_bounds__(256, SHARE ? kTraceBatchShareMinBlocks : kTrac
     reinterpret_cast<uint32_t*>(&s_cam)[i] = __ldg(csrc + i);
   __syncthreads();
   const uint32_t lt = g - __ldg(w.prefix + s), tiles_x = (uint32_t)(s_sc.W + 15) / 16;
-  const int px = (int)(lt % tiles_x) * 16 + (threadIdx.x & 15), py = (int)(lt / tiles_x) * 16 + (threadIdx.x >> 4);
+  int px, py;
+  share_tile_px((int)(lt % tiles_x) * 16, (int)(lt / tiles_x) * 16, px, py);
   const float4* gp = bb.rb.gb_pos + s_sc.px_base;
   const float4* gn = bb.rb.gb_nrm + s_sc.px_base;
   uchar4* fr = bb.frame + s_sc.px_base;
