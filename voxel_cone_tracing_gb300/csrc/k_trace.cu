@@ -928,18 +928,25 @@ __global__ void __launch_bounds__(kTraceThreads, SAMPLER == VCT_SAMPLER_HW ? kTr
 constexpr int kShareMinBlocks = VCT_SHARE_MIN_BLOCKS;
 
 // The pixel of this lane in a 16-pixel-wide CTA tile at (x0, y0) of the
-// shared-far-field kernels: a warp is an 8 x 4-pixel block (lane = x + 8 y),
-// two blocks per 16-pixel row of blocks.  (Measured on the 1080p bench
-// frame, trace ms: 16 x 2 strips 1.235, 8 x 4 blocks 1.217; the same frame:
-// the groups are the same aligned kShareW x 2 pixels either way.)
+// shared-far-field kernels: a warp is a kShareWarpW x (32 / kShareWarpW)
+// block (lane = x + kShareWarpW y), 16 / kShareWarpW blocks per row of
+// blocks.  (Measured on the 1080p bench frame, trace ms: 16 x 2 strips
+// 1.235, 8 x 4 blocks 1.217, 4 x 8 blocks 1.221; the same frame: the
+// groups are the same aligned kShareW x 2 pixels whatever the block.)
+#ifndef VCT_SHARE_WARP_W
+#define VCT_SHARE_WARP_W 8
+#endif
+constexpr int kShareWarpW = VCT_SHARE_WARP_W;
+static_assert((kShareWarpW == 4 || kShareWarpW == 8 || kShareWarpW == 16) && kShareWarpW % kShareW == 0,
+              "a warp block holds whole groups");
 __device__ __forceinline__ void share_tile_px(int x0, int y0, int& px, int& py) {
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  px = x0 + (w & 1) * 8 + (lane & 7);
-  py = y0 + (w >> 1) * 4 + (lane >> 3);
+  px = x0 + (w % (16 / kShareWarpW)) * kShareWarpW + lane % kShareWarpW;
+  py = y0 + (w / (16 / kShareWarpW)) * (32 / kShareWarpW) + lane / kShareWarpW;
 }
 
-// One pixel of k_trace_share: the warp (an 8x4 block of kShareW x 2
-// groups, its rows starting at a frame row divisible by 4) first picks each group's
+// One pixel of k_trace_share: the warp (a block of kShareW x 2 groups, its
+// rows starting at an even frame row; share_tile_px) first picks each group's
 // representative (its first pixel, row by row, whose diffuse cones are
 // traced) and the pixels that share with it, marches the groups' far fields
 // together (far_fields), then shades its pixels as k_trace does.  Called by
@@ -965,9 +972,9 @@ __device__ __forceinline__ void trace_px_share(const SceneParams& sp, const Came
   valid = valid && tp.enable_diffuse && tp.view_voxel_dir >= 7 && !tp.diffuse_in;
   const unsigned vmask = __ballot_sync(0xffffffffu, valid);
   // this lane's group: columns kShareW * gx .., rows 2 gy and 2 gy + 1 of the block
-  const int gx = (lane & 7) / kShareW, gy = lane >> 4;
+  const int gx = (lane % kShareWarpW) / kShareW, gy = lane / (2 * kShareWarpW);
   const unsigned grow = ((1u << kShareW) - 1u) << (kShareW * gx);
-  const unsigned qv = vmask & ((grow << (16 * gy)) | (grow << (16 * gy + 8)));
+  const unsigned qv = vmask & ((grow << (2 * kShareWarpW * gy)) | (grow << (2 * kShareWarpW * gy + kShareWarpW)));
   const int rep = qv ? __ffs(qv) - 1 : lane;
   const V3 rpos = v3(__shfl_sync(0xffffffffu, pos.x, rep), __shfl_sync(0xffffffffu, pos.y, rep),
                      __shfl_sync(0xffffffffu, pos.z, rep));
@@ -1009,7 +1016,7 @@ template <bool ISO, int ROWS>
 __global__ void __launch_bounds__(16 * ROWS, kShareMinBlocks * 8 / ROWS)
     k_trace_share(SceneParams sp, CameraParams cp, MapSet m, TraceParams tp, const float4* __restrict__ gb_pos,
                   const float4* __restrict__ gb_nrm, uchar4* __restrict__ frame, float4* __restrict__ frame_f32) {
-  static_assert(ROWS % 4 == 0, "whole 8x4 warps");
+  static_assert(ROWS % (32 / kShareWarpW) == 0 && ROWS % 2 == 0, "whole warp blocks");
   __shared__ FarWarp s_far[ROWS / 2];
   int px, py;
   share_tile_px(blockIdx.x * 16, blockIdx.y * ROWS, px, py);
