@@ -380,7 +380,9 @@ struct vct_renderer {
   bool have_last = false;
   // GPU state
   cudaStream_t own_stream = nullptr, stream = nullptr;
-  cudaStream_t gb_stream = nullptr;  // G-buffer raster + learned diffuse term
+  cudaStream_t gb_stream = nullptr;  // G-buffer raster + learned diffuse term (lowest priority)
+  cudaStream_t vx_stream = nullptr;  // voxelize + mipmap beside it (highest priority)
+  cudaEvent_t ev_vjoin = nullptr;
   cudaEvent_t ev_start = nullptr;
   cudaEvent_t ev[5] = {};
   cudaEvent_t evg[3] = {};
@@ -444,6 +446,7 @@ struct vct_renderer {
 
   ~vct_renderer() {
     if (gb_stream) cudaStreamSynchronize(gb_stream);
+    if (vx_stream) cudaStreamSynchronize(vx_stream);
     if (stream) cudaStreamSynchronize(stream);
     free_maps();
     for (auto& e : ev)
@@ -452,9 +455,11 @@ struct vct_renderer {
       if (e) cudaEventDestroy(e);
     if (ev_start) cudaEventDestroy(ev_start);
     if (ev_join) cudaEventDestroy(ev_join);
+    if (ev_vjoin) cudaEventDestroy(ev_vjoin);
     if (ev_staged) cudaEventDestroy(ev_staged);
     if (ev_done) cudaEventDestroy(ev_done);
     if (gb_stream) cudaStreamDestroy(gb_stream);
+    if (vx_stream) cudaStreamDestroy(vx_stream);
     if (own_stream) cudaStreamDestroy(own_stream);
   }
 
@@ -513,6 +518,7 @@ struct vct_renderer {
   // mip levels.  Here: level 0 once + one chain (levels 1..L-1) per map.
   vct_status alloc_maps(uint32_t r) {
     if (gb_stream) VCT_CUDA(cudaStreamSynchronize(gb_stream));
+    if (vx_stream) VCT_CUDA(cudaStreamSynchronize(vx_stream));
     if (stream) VCT_CUDA(cudaStreamSynchronize(stream));
     free_inj();
     VCT_CHECK(maps.alloc(r, cfg.mip_mode, cfg.storage, cfg.shadow_from_maps == 0 && cfg.sampler == VCT_SAMPLER_HW));
@@ -548,7 +554,15 @@ struct vct_renderer {
     std::memcpy(proj, kIdentity, sizeof(proj));
     VCT_CUDA(cudaStreamCreateWithFlags(&own_stream, cudaStreamNonBlocking));
     stream = own_stream;
-    VCT_CUDA(cudaStreamCreateWithFlags(&gb_stream, cudaStreamNonBlocking));
+    // With overlap_raster the G-buffer raster fills what voxelize and
+    // mipmap leave idle: their stream has the highest priority, the
+    // raster's the lowest, so the stages that the metric times are delayed
+    // as little as possible.
+    int prio_least = 0, prio_greatest = 0;
+    VCT_CUDA(cudaDeviceGetStreamPriorityRange(&prio_least, &prio_greatest));
+    VCT_CUDA(cudaStreamCreateWithPriority(&gb_stream, cudaStreamNonBlocking, prio_least));
+    VCT_CUDA(cudaStreamCreateWithPriority(&vx_stream, cudaStreamNonBlocking, prio_greatest));
+    VCT_CUDA(cudaEventCreateWithFlags(&ev_vjoin, cudaEventDisableTiming));
     for (auto& e : ev) VCT_CUDA(cudaEventCreate(&e));
     for (auto& e : evg) VCT_CUDA(cudaEventCreate(&e));
     VCT_CUDA(cudaEventCreate(&ev_start));
@@ -751,7 +765,9 @@ struct vct_renderer {
     VCT_CUDA(cudaEventRecord(evg[2], gs));
     infer_ran = tp.diffuse_in != nullptr;
     if (side) VCT_CUDA(cudaEventRecord(ev_join, gb_stream));
-    VCT_CUDA(cudaEventRecord(ev[0], stream));
+    cudaStream_t vs = side ? vx_stream : stream;  // voxelize + mipmap
+    if (side) VCT_CUDA(cudaStreamWaitEvent(vx_stream, ev_start, 0));
+    VCT_CUDA(cudaEventRecord(ev[0], vs));
     if (inject) {
       // Re-voxelize the attribute grids only when the geometry changed;
       // light changes cost one injection pass.
@@ -759,28 +775,32 @@ struct vct_renderer {
       last_revoxelized = !inj_valid || key != inj_key;
       if (last_revoxelized) {
         if (!inj_arr[0]) VCT_CHECK(alloc_inj());
-        VCT_CUDA(launch_voxelize(sp, (int)res, cfg.vox_mode, cfg.storage, vb, ms.l0_surf, stream, &launches,
+        VCT_CUDA(launch_voxelize(sp, (int)res, cfg.vox_mode, cfg.storage, vb, ms.l0_surf, vs, &launches,
                                  &inj_g));
         inj_key.swap(key);
         inj_valid = true;
       }
-      VCT_CUDA(launch_inject(sp, (int)res, inj_g, ms.l0_surf, have_l0_map ? (uchar4*)l0_lin.p : nullptr, stream,
+      VCT_CUDA(launch_inject(sp, (int)res, inj_g, ms.l0_surf, have_l0_map ? (uchar4*)l0_lin.p : nullptr, vs,
                              &launches));
     } else {
       last_revoxelized = true;
-      VCT_CUDA(launch_voxelize(sp, (int)res, cfg.vox_mode, cfg.storage, vb, ms.l0_surf, stream, &launches));
+      VCT_CUDA(launch_voxelize(sp, (int)res, cfg.vox_mode, cfg.storage, vb, ms.l0_surf, vs, &launches));
     }
-    VCT_CUDA(cudaEventRecord(ev[1], stream));
+    VCT_CUDA(cudaEventRecord(ev[1], vs));
     if (fuse) {
       MapSet m3 = ms;
       m3.occ_k = 3;          // the levels whose occupancy bytes the brick kernel wrote
       m3.occ_l1_packed = 0;  // (as bytes)
-      VCT_CUDA(launch_mipmap(m3, cfg.mip_mode, stream, &launches, nullptr, d_status.p, 3));
+      VCT_CUDA(launch_mipmap(m3, cfg.mip_mode, vs, &launches, nullptr, d_status.p, 3));
     } else {
-      VCT_CUDA(launch_mipmap(ms, cfg.mip_mode, stream, &launches, have_l0_map ? &l0_map : nullptr, d_status.p));
+      VCT_CUDA(launch_mipmap(ms, cfg.mip_mode, vs, &launches, have_l0_map ? &l0_map : nullptr, d_status.p));
     }
-    VCT_CUDA(cudaEventRecord(ev[2], stream));
-    if (side) VCT_CUDA(cudaStreamWaitEvent(stream, ev_join, 0));
+    VCT_CUDA(cudaEventRecord(ev[2], vs));
+    if (side) {
+      VCT_CUDA(cudaEventRecord(ev_vjoin, vx_stream));
+      VCT_CUDA(cudaStreamWaitEvent(stream, ev_vjoin, 0));
+      VCT_CUDA(cudaStreamWaitEvent(stream, ev_join, 0));
+    }
     VCT_CUDA(cudaEventRecord(ev[3], stream));
     VCT_CUDA(launch_trace(sp, cp, ms, tp, gb_pos.p, gb_nrm.p, frame.p, cfg.keep_float_frame ? frame_f32.p : nullptr,
                           stream, &launches));
