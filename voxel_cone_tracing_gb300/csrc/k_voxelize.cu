@@ -1048,7 +1048,7 @@ __device__ __forceinline__ void brick_unit(const SceneParams& sp, int N, uint32_
                                            FrameStatus* st, AccT<STORAGE>& acc, SetupOf<MODE> (&setup)[kSetupSlots],
                                            int (&excl)[kExclSlots], const InjGrids& inj, void* l0_lin,
                                            const HeavyBricks* hb, uint32_t slot_index, uint32_t chunk, bool item,
-                                           const BrickMips* bm = nullptr) {
+                                           const BrickMips* bm = nullptr, uint8_t* dirty = nullptr) {
   static_assert(sizeof(BrickMipScratch) <= sizeof(setup), "fused mips fit in the triangle setups' memory");
   __shared__ uint32_t s_last;
   int b3[3];
@@ -1057,11 +1057,13 @@ __device__ __forceinline__ void brick_unit(const SceneParams& sp, int N, uint32_
   if (beg0 == end) {
     // No triangle touches this brick (most of the grid): store cleared texels
     // without the accumulator or its barriers -- unless they are zero already
-    // (BrickMips::dirty; the per-voxel counts are not tracked by it).
-    if (bm && bm->dirty && !counts) {
-      if (!bm->dirty[brick]) return;  // CTA-uniform
-      __syncthreads();                // every thread has read the flag
-      if (threadIdx.x == 0) bm->dirty[brick] = 0;
+    // (`dirty`: per brick, 1 when its texels -- level 0, its linear copy and
+    // any fused levels -- may be non-zero; the per-voxel counts are not
+    // tracked by it).
+    if (dirty && !counts) {
+      if (!dirty[brick]) return;  // CTA-uniform
+      __syncthreads();            // every thread has read the flag
+      if (threadIdx.x == 0) dirty[brick] = 0;
     }
     for (int i = threadIdx.x; i < kBrickVox; i += kThreads) {
       const int x = b3[0] * kBrick + (i & 7), y = b3[1] * kBrick + ((i >> 3) & 7), z = b3[2] * kBrick + (i >> 6);
@@ -1106,7 +1108,7 @@ __device__ __forceinline__ void brick_unit(const SceneParams& sp, int N, uint32_
     __syncthreads();
   }
   // (the triangle setups are done with: their memory holds the fused mips)
-  if (bm && bm->dirty && threadIdx.x == 0) bm->dirty[brick] = 1;
+  if (dirty && threadIdx.x == 0) dirty[brick] = 1;
   brick_finalize<STORAGE>(sp, N, b3, acc, l0, counts, st, inj, l0_lin, bm,
                           reinterpret_cast<BrickMipScratch*>(&setup[0]));
 }
@@ -1146,7 +1148,7 @@ __global__ void __launch_bounds__(kThreads, FUSE ? 7 : brick_min_blocks<MODE>())
       chunk = w.y;
     }
     brick_unit<MODE, STORAGE>(sp, N, brick, offset, list, cap, l0, counts, st, acc, setup, excl, inj, l0_lin, &hb,
-                              brick, chunk, extra, FUSE ? &bm : nullptr);
+                              brick, chunk, extra, FUSE ? &bm : nullptr, bm.dirty);
     __syncthreads();  // done with acc
   }
 }
@@ -1385,6 +1387,7 @@ cudaError_t launch_voxelize(const SceneParams& sp, int N, int mode, int storage,
   BrickMips bm;
   std::memset(&bm, 0, sizeof(bm));
   if (fuse_mips) bm = *vb.mips;
+  bm.dirty = inj ? nullptr : vb.dirty;  // (kernel parameter of every brick kernel)
   // Before the bricks: two CTAs per SM that run the extra chunks.
   const uint32_t n_extra = hb.slot ? std::min<uint32_t>(hb.item_cap, (uint32_t)(sms * std::min(fit, 2))) : 0u;
   dispatch_bricks(mode, storage, inj != nullptr, [&](auto mode_tag, auto storage_tag) {

@@ -716,17 +716,21 @@ struct vct_renderer {
       for (int k = 0; k < 2 && bm.has_alpha; ++k)
         for (int l = 1; l <= 3; ++l) bm.alpha[k][l] = ms.alpha_surf[k][l];
       for (int l = 1; l <= 3 && ms.skip_empty; ++l) bm.occ_raw[l] = ms.occ_raw[l];
-      if (dirty_unknown) {  // new maps, or another writer touched them: every brick writes
-        const size_t nb = (size_t)(res / kBrick) * (res / kBrick) * (res / kBrick);
-        VCT_CUDA(cudaMemsetAsync(brick_dirty.p, 1, nb, stream));
-        dirty_unknown = false;
-      }
-      bm.dirty = brick_dirty.p;
       vb.mips = &bm;
       vb.level0_lin = nullptr;  // no TMA-staged first pass to read it
     } else {
       vb.mips = nullptr;
-      dirty_unknown = true;  // this frame writes every level without the flags
+    }
+    if (!inject) {
+      if (dirty_unknown) {  // new maps, or light injection wrote level 0: every brick writes
+        const size_t nb = (size_t)(res / kBrick) * (res / kBrick) * (res / kBrick);
+        VCT_CUDA(cudaMemsetAsync(brick_dirty.p, 1, nb, stream));
+        dirty_unknown = false;
+      }
+      vb.dirty = brick_dirty.p;
+    } else {
+      vb.dirty = nullptr;
+      dirty_unknown = true;
     }
 
     RasterBuffers rb;

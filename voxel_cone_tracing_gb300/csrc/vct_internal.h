@@ -147,10 +147,7 @@ struct BrickMips {
   cudaSurfaceObject_t surf[6][4];   // [map][level 1..3]
   cudaSurfaceObject_t alpha[2][4];  // [chain][level 1..3] (has_alpha)
   uint8_t* occ_raw[4];              // [level 1..3] (null: no occupancy)
-  // Per brick: 1 when its level-0 texels, levels 1-3 or occupancy bytes may
-  // hold non-zero data from an earlier frame.  A brick that is empty in this
-  // frame and not dirty holds zeros already and writes nothing.
-  uint8_t* dirty;
+  uint8_t* dirty;  // (set by launch_voxelize from VoxBuffers::dirty)
   int has_alpha;
 };
 
@@ -171,6 +168,11 @@ struct VoxBuffers {
   uint2* bin_rec;          // per triangle: the counting pass's bricks, replayed
                            // by the filling pass (total_tris; null: recompute)
   const BrickMips* mips;   // RGBA8: the brick kernel writes levels 1-3 too (null: off)
+  // Per brick: 1 when its level-0 texels (and linear copy, and fused levels
+  // 1-3 and occupancy bytes) may hold non-zero data from an earlier frame;
+  // a brick empty in this frame and not dirty holds zeros already and
+  // writes nothing.  Null: every brick writes.
+  uint8_t* dirty;
 };
 
 struct RasterBuffers {
