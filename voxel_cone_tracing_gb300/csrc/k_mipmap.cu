@@ -77,25 +77,11 @@ __device__ __forceinline__ uint32_t iso_rgba8(const uint32_t* ch) {
   return out;
 }
 
-__device__ __forceinline__ float4 h2f(uint2 t) {
-  __half2 a = *reinterpret_cast<__half2*>(&t.x), b = *reinterpret_cast<__half2*>(&t.y);
-  float2 fa = __half22float2(a), fb = __half22float2(b);
-  return make_float4(fa.x, fa.y, fb.x, fb.y);
-}
-__device__ __forceinline__ uint2 f2h(float4 v) {
-  __half2 a = __floats2half2_rn(v.x, v.y), b = __floats2half2_rn(v.z, v.w);
-  return make_uint2(*reinterpret_cast<uint32_t*>(&a), *reinterpret_cast<uint32_t*>(&b));
-}
-
 __device__ __forceinline__ uint2 aniso_rgba16f(const uint2* ch, int d) {
   float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
-  for (int q = 0; q < 4; ++q) {
-    const float4 f = h2f(ch[c_pairs[d][q][0]]), b = h2f(ch[c_pairs[d][q][1]]);
-    const float k = 1.0f - f.w;
-    acc.x += f.x + k * b.x; acc.y += f.y + k * b.y; acc.z += f.z + k * b.z; acc.w += f.w + k * b.w;
-  }
-  return f2h(make_float4(acc.x * 0.25f, acc.y * 0.25f, acc.z * 0.25f, acc.w * 0.25f));
+  for (int q = 0; q < 4; ++q) blend16(acc, h2f(ch[c_pairs[d][q][0]]), h2f(ch[c_pairs[d][q][1]]));
+  return finish16(acc);
 }
 
 __device__ __forceinline__ uint2 iso_rgba16f(const uint2* ch) {
@@ -122,12 +108,8 @@ __device__ __forceinline__ void aniso6_rgba16f(const uint2* ch, uint2* out) {
   for (int d = 0; d < 6; ++d) {
     float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
-    for (int p = 0; p < 4; ++p) {
-      const float4 f = c[c_pairs_h[d][p][0]], b = c[c_pairs_h[d][p][1]];
-      const float k = 1.0f - f.w;
-      acc.x += f.x + k * b.x; acc.y += f.y + k * b.y; acc.z += f.z + k * b.z; acc.w += f.w + k * b.w;
-    }
-    out[d] = f2h(make_float4(acc.x * 0.25f, acc.y * 0.25f, acc.z * 0.25f, acc.w * 0.25f));
+    for (int p = 0; p < 4; ++p) blend16(acc, c[c_pairs_h[d][p][0]], c[c_pairs_h[d][p][1]]);
+    out[d] = finish16(acc);
   }
 }
 

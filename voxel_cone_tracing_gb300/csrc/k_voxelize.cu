@@ -844,21 +844,27 @@ __device__ __forceinline__ void brick_accumulate(const SceneParams& sp, int N, c
   __syncthreads();
 }
 
-// ---- fused mip levels 1-3 (RGBA8, six maps; BrickMips) ----------------------
+// ---- fused mip levels 1-3 (six maps, RGBA8 or RGBA16F; BrickMips) ---------
 // The brick holds whole 4^3, 2^3 and 1^3 blocks of levels 1-3, so its CTA
 // writes them from its level-0 texels in shared memory with the MipBuilder's
-// exact rule (vct_mip.cuh), plus the alpha-only chains and the occupancy
-// bytes of those levels (a cell is occupied when its block of level 0 holds a
+// rule (vct_mip.cuh: exact integers for RGBA8, one fixed FP32 evaluation for
+// RGBA16F), plus the alpha-only chains (RGBA8) and the occupancy bytes of
+// those levels (a cell is occupied when its block of level 0 holds a
 // non-zero texel); the MipBuilder then starts from level 3.  This replaces
 // the first pass's re-read of level 0 (and the linear copy it read).
-struct BrickMipScratch {
-  uint32_t l0[kBrick * kBrick * kBrick];
-  uint32_t l1[6][64];
-  uint32_t l2[6][8];
-  uint32_t l3[6];
+template <int STORAGE>
+struct BrickMipScratchT {
+  typedef typename std::conditional<STORAGE == VCT_STORAGE_RGBA16F, uint2, uint32_t>::type T;
+  T l0[kBrick * kBrick * kBrick];
+  T l1[6][64];
+  T l2[6][8];
+  T l3[6];
   uint8_t occ1[64];
   uint8_t occ2[8];
 };
+typedef BrickMipScratchT<VCT_STORAGE_RGBA8> BrickMipScratch;
+__device__ __forceinline__ bool texel_nonzero(uint32_t v) { return v != 0u; }
+__device__ __forceinline__ bool texel_nonzero(uint2 v) { return (v.x | v.y) != 0u; }
 
 __device__ __forceinline__ void brick_alpha(const BrickMips& bm, int level, int x, int y, int z, const uint32_t* v,
                                             int stride) {
@@ -879,6 +885,9 @@ __device__ __forceinline__ void brick_occ(const BrickMips& bm, int N, int level,
 __device__ __noinline__ uint32_t brick_mip_texel(const uint32_t* src, int s2, int x, int y, int z, int d) {
   return aniso_rgba8_dir(d, [&](int k) { return src[mip_child(s2, x, y, z, k)]; });
 }
+__device__ __noinline__ uint2 brick_mip_texel(const uint2* src, int s2, int x, int y, int z, int d) {
+  return aniso_rgba16f_dir(d, [&](int k) { return src[mip_child(s2, x, y, z, k)]; });
+}
 
 // Levels 1-3 of brick b3 from scr.l0 ([z][y][x], written and synchronised
 // by the caller); all threads of the CTA.  Level 1 takes the whole CTA, one
@@ -886,35 +895,39 @@ __device__ __noinline__ uint32_t brick_mip_texel(const uint32_t* src, int s2, in
 // rule's code exists once (six unrolled copies made the kernel miss its
 // instruction cache); levels 2 and 3 (48 and 6 items) and their occupancy
 // and alpha copies are one warp's, which synchronises only itself.
-__device__ void brick_mips(const BrickMips& bm, int N, const int b3[3], BrickMipScratch& scr) {
+template <int STORAGE>
+__device__ void brick_mips(const BrickMips& bm, int N, const int b3[3], BrickMipScratchT<STORAGE>& scr) {
   static_assert(kThreads >= 96, "levels 2-3 are warp 2's");
+  typedef typename BrickMipScratchT<STORAGE>::T T;
+  constexpr int kB = sizeof(T);  // bytes per texel
   const int t = threadIdx.x;
   for (int i = t; i < 6 * 64; i += kThreads) {  // level 1: map i / 64 (warp-uniform), texel i % 64
     const int d = i >> 6, r = i & 63, x = r & 3, y = (r >> 2) & 3, z = r >> 4;
-    const uint32_t v = brick_mip_texel(scr.l0, 8, x, y, z, d);
-    surf3Dwrite(v, bm.surf[d][1], (b3[0] * 4 + x) * 4, b3[1] * 4 + y, b3[2] * 4 + z);
+    const T v = brick_mip_texel(scr.l0, 8, x, y, z, d);
+    surf3Dwrite(v, bm.surf[d][1], (b3[0] * 4 + x) * kB, b3[1] * 4 + y, b3[2] * 4 + z);
     scr.l1[d][r] = v;
   }
   if (t < 64) {  // occupancy of level 1: the texel's block of level 0
     const int x = t & 3, y = (t >> 2) & 3, z = t >> 4;
     bool any = false;
 #pragma unroll
-    for (int k = 0; k < 8; ++k) any |= scr.l0[mip_child(8, x, y, z, k)] != 0u;
+    for (int k = 0; k < 8; ++k) any |= texel_nonzero(scr.l0[mip_child(8, x, y, z, k)]);
     scr.occ1[t] = any ? 1 : 0;
     brick_occ(bm, N, 1, b3[0] * 4 + x, b3[1] * 4 + y, b3[2] * 4 + z, any);
   }
   __syncthreads();
   if (t < 64) {
-    if (bm.has_alpha) brick_alpha(bm, 1, b3[0] * 4 + (t & 3), b3[1] * 4 + ((t >> 2) & 3), b3[2] * 4 + (t >> 4),
-                                  &scr.l1[0][t], 64);
+    if constexpr (STORAGE == VCT_STORAGE_RGBA8)
+      if (bm.has_alpha) brick_alpha(bm, 1, b3[0] * 4 + (t & 3), b3[1] * 4 + ((t >> 2) & 3), b3[2] * 4 + (t >> 4),
+                                    &scr.l1[0][t], 64);
     return;
   }
   if (t >= 96) return;
   const int lane = t - 64;
   for (int j = lane; j < 48; j += 32) {  // level 2: texel r of map d from that map's level 1
     const int d = j >> 3, r = j & 7, x = r & 1, y = (r >> 1) & 1, z = r >> 2;
-    const uint32_t v = brick_mip_texel(scr.l1[d], 4, x, y, z, d);
-    surf3Dwrite(v, bm.surf[d][2], (b3[0] * 2 + x) * 4, b3[1] * 2 + y, b3[2] * 2 + z);
+    const T v = brick_mip_texel(scr.l1[d], 4, x, y, z, d);
+    surf3Dwrite(v, bm.surf[d][2], (b3[0] * 2 + x) * kB, b3[1] * 2 + y, b3[2] * 2 + z);
     scr.l2[d][r] = v;
   }
   if (lane < 8) {  // occupancy of level 2 from level 1's
@@ -927,13 +940,14 @@ __device__ void brick_mips(const BrickMips& bm, int N, const int b3[3], BrickMip
   }
   __syncwarp();
   if (lane < 8) {
-    if (bm.has_alpha)
-      brick_alpha(bm, 2, b3[0] * 2 + (lane & 1), b3[1] * 2 + ((lane >> 1) & 1), b3[2] * 2 + (lane >> 2),
-                  &scr.l2[0][lane], 8);
+    if constexpr (STORAGE == VCT_STORAGE_RGBA8)
+      if (bm.has_alpha)
+        brick_alpha(bm, 2, b3[0] * 2 + (lane & 1), b3[1] * 2 + ((lane >> 1) & 1), b3[2] * 2 + (lane >> 2),
+                    &scr.l2[0][lane], 8);
   } else if (lane < 14) {  // level 3: the brick's one texel of map d
     const int d = lane - 8;
-    const uint32_t v = brick_mip_texel(scr.l2[d], 2, 0, 0, 0, d);
-    surf3Dwrite(v, bm.surf[d][3], b3[0] * 4, b3[1], b3[2]);
+    const T v = brick_mip_texel(scr.l2[d], 2, 0, 0, 0, d);
+    surf3Dwrite(v, bm.surf[d][3], b3[0] * kB, b3[1], b3[2]);
     scr.l3[d] = v;
   } else if (lane == 14) {
     bool any = false;
@@ -941,10 +955,12 @@ __device__ void brick_mips(const BrickMips& bm, int N, const int b3[3], BrickMip
     brick_occ(bm, N, 3, b3[0], b3[1], b3[2], any);
   }
   __syncwarp();
-  if (lane == 0 && bm.has_alpha) brick_alpha(bm, 3, b3[0], b3[1], b3[2], scr.l3, 1);
+  if constexpr (STORAGE == VCT_STORAGE_RGBA8)
+    if (lane == 0 && bm.has_alpha) brick_alpha(bm, 3, b3[0], b3[1], b3[2], scr.l3, 1);
 }
 
 // Levels 1-3 of an empty brick: zeros (the texels and the occupancy).
+template <int STORAGE>
 __device__ void brick_mips_zero(const BrickMips& bm, int N, const int b3[3]) {
   const int t = threadIdx.x;
   const uint32_t zero[6] = {0u, 0u, 0u, 0u, 0u, 0u};
@@ -967,8 +983,12 @@ __device__ void brick_mips_zero(const BrickMips& bm, int N, const int b3[3]) {
   }
   if (!level) return;
 #pragma unroll
-  for (int d = 0; d < 6; ++d) surf3Dwrite(0u, bm.surf[d][level], x * 4, y, z);
-  if (bm.has_alpha) brick_alpha(bm, level, x, y, z, zero, 1);
+  for (int d = 0; d < 6; ++d) {
+    if constexpr (STORAGE == VCT_STORAGE_RGBA16F) surf3Dwrite(make_uint2(0u, 0u), bm.surf[d][level], x * 8, y, z);
+    else surf3Dwrite(0u, bm.surf[d][level], x * 4, y, z);
+  }
+  if constexpr (STORAGE == VCT_STORAGE_RGBA8)
+    if (bm.has_alpha) brick_alpha(bm, level, x, y, z, zero, 1);
   brick_occ(bm, N, level, x, y, z, false);
 }
 
@@ -979,7 +999,9 @@ template <int STORAGE>
 __device__ __forceinline__ void brick_finalize(const SceneParams& sp, int N, const int b3[3], const AccT<STORAGE>& acc,
                                                cudaSurfaceObject_t l0, uint32_t* __restrict__ counts,
                                                FrameStatus* st, const InjGrids& inj, void* l0_lin,
-                                               const BrickMips* bm = nullptr, BrickMipScratch* scr = nullptr) {
+                                               const BrickMips* bm = nullptr, void* scr_raw = nullptr) {
+  using Scr = BrickMipScratchT<STORAGE == VCT_STORAGE_RGBA16F ? VCT_STORAGE_RGBA16F : VCT_STORAGE_RGBA8>;
+  Scr* scr = static_cast<Scr*>(scr_raw);
   for (int i = threadIdx.x; i < kBrickVox; i += kThreads) {
     const uint32_t n = acc.n[i];
     const int lx = i & 7, ly = (i >> 3) & 7, lz = i >> 6;
@@ -1014,13 +1036,14 @@ __device__ __forceinline__ void brick_finalize(const SceneParams& sp, int N, con
       }
       surf3Dwrite(o, l0, x * 8, y, z);
       if (l0_lin) static_cast<ushort4*>(l0_lin)[((size_t)z * N + y) * N + x] = o;
+      if (bm) scr->l0[i] = make_uint2((uint32_t)o.x | (uint32_t)o.y << 16, (uint32_t)o.z | (uint32_t)o.w << 16);
     }
     if (counts) counts[((size_t)z * N + y) * N + x] = n;
   }
-  if constexpr (STORAGE == VCT_STORAGE_RGBA8) {
+  if constexpr (STORAGE == VCT_STORAGE_RGBA8 || STORAGE == VCT_STORAGE_RGBA16F) {
     if (bm) {
       __syncthreads();
-      brick_mips(*bm, N, b3, *scr);
+      brick_mips<STORAGE>(*bm, N, b3, *scr);
     }
   }
 }
@@ -1049,7 +1072,8 @@ __device__ __forceinline__ void brick_unit(const SceneParams& sp, int N, uint32_
                                            int (&excl)[kExclSlots], const InjGrids& inj, void* l0_lin,
                                            const HeavyBricks* hb, uint32_t slot_index, uint32_t chunk, bool item,
                                            const BrickMips* bm = nullptr, uint8_t* dirty = nullptr) {
-  static_assert(sizeof(BrickMipScratch) <= sizeof(setup), "fused mips fit in the triangle setups' memory");
+  static_assert(sizeof(BrickMipScratchT<VCT_STORAGE_RGBA16F>) <= sizeof(setup),
+                "fused mips fit in the triangle setups' memory");
   __shared__ uint32_t s_last;
   int b3[3];
   brick_coords(N, brick, b3);
@@ -1080,7 +1104,8 @@ __device__ __forceinline__ void brick_unit(const SceneParams& sp, int N, uint32_
       }
       if (counts) counts[((size_t)z * N + y) * N + x] = 0u;
     }
-    if (bm) brick_mips_zero(*bm, N, b3);
+    if constexpr (STORAGE == VCT_STORAGE_RGBA8 || STORAGE == VCT_STORAGE_RGBA16F)
+      if (bm) brick_mips_zero<STORAGE>(*bm, N, b3);
     return;
   }
   // Only a dense brick looks up its slot.
@@ -1109,8 +1134,7 @@ __device__ __forceinline__ void brick_unit(const SceneParams& sp, int N, uint32_
   }
   // (the triangle setups are done with: their memory holds the fused mips)
   if (dirty && threadIdx.x == 0) dirty[brick] = 1;
-  brick_finalize<STORAGE>(sp, N, b3, acc, l0, counts, st, inj, l0_lin, bm,
-                          reinterpret_cast<BrickMipScratch*>(&setup[0]));
+  brick_finalize<STORAGE>(sp, N, b3, acc, l0, counts, st, inj, l0_lin, bm, &setup[0]);
 }
 
 // One CTA per brick, after `n_extra` CTAs that run the extra chunks of
@@ -1383,7 +1407,7 @@ cudaError_t launch_voxelize(const SceneParams& sp, int N, int mode, int storage,
   }
   const InjGrids g = inj ? *inj : InjGrids{};
   void* lin = inj ? nullptr : vb.level0_lin;
-  const bool fuse_mips = vb.mips && !inj && storage == VCT_STORAGE_RGBA8;
+  const bool fuse_mips = vb.mips && !inj && (storage == VCT_STORAGE_RGBA8 || storage == VCT_STORAGE_RGBA16F);
   BrickMips bm;
   std::memset(&bm, 0, sizeof(bm));
   if (fuse_mips) bm = *vb.mips;
@@ -1392,7 +1416,7 @@ cudaError_t launch_voxelize(const SceneParams& sp, int N, int mode, int storage,
   const uint32_t n_extra = hb.slot ? std::min<uint32_t>(hb.item_cap, (uint32_t)(sms * std::min(fit, 2))) : 0u;
   dispatch_bricks(mode, storage, inj != nullptr, [&](auto mode_tag, auto storage_tag) {
     constexpr int M = decltype(mode_tag)::value, S = decltype(storage_tag)::value;
-    if constexpr (S == VCT_STORAGE_RGBA8) {
+    if constexpr (S == VCT_STORAGE_RGBA8 || S == VCT_STORAGE_RGBA16F) {
       if (fuse_mips) {
         k_bricks<M, S, true><<<(unsigned)(n_extra + n_bricks), kThreads, 0, st>>>(
             sp, N, vb.brick_offset, vb.pair_list, vb.pair_cap, l0, vb.counts, vb.status, g, lin, hb, n_extra, bm);

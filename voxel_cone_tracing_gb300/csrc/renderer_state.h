@@ -703,12 +703,11 @@ struct vct_renderer {
     vb.level0_lin = have_l0_map ? (void*)l0_lin.p : nullptr;
     vb.heavy = kHeavySplit ? heavy.view() : HeavyBricks{};
     vb.bin_rec = bin_rec.p;
-    // RGBA8 anisotropic maps: the brick kernel writes mip levels 1-3 itself
-    // (not for light injection, whose level 0 comes from k_inject).
+    // Anisotropic maps: the brick kernel writes mip levels 1-3 itself (not
+    // for light injection, whose level 0 comes from k_inject).
     BrickMips bm;
     std::memset(&bm, 0, sizeof(bm));
-    const bool fuse = kFuseBrickMips && !inject && cfg.storage == VCT_STORAGE_RGBA8 &&
-                      cfg.mip_mode == VCT_MIP_ANISO && ms.L >= 4;
+    const bool fuse = kFuseBrickMips && !inject && cfg.mip_mode == VCT_MIP_ANISO && ms.L >= 4;
     if (fuse) {
       for (int d = 0; d < 6; ++d)
         for (int l = 1; l <= 3; ++l) bm.surf[d][l] = ms.surf[d][l];

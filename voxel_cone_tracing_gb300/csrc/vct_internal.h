@@ -167,7 +167,7 @@ struct VoxBuffers {
   HeavyBricks heavy;       // dense-brick splitting (heavy.slot null: off)
   uint2* bin_rec;          // per triangle: the counting pass's bricks, replayed
                            // by the filling pass (total_tris; null: recompute)
-  const BrickMips* mips;   // RGBA8: the brick kernel writes levels 1-3 too (null: off)
+  const BrickMips* mips;   // anisotropic maps: the brick kernel writes levels 1-3 too (null: off)
   // Per brick: 1 when its level-0 texels (and linear copy, and fused levels
   // 1-3 and occupancy bytes) may hold non-zero data from an earlier frame;
   // a brick empty in this frame and not dirty holds zeros already and

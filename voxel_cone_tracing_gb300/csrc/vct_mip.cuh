@@ -9,6 +9,8 @@
 // unorm8 as imageStore does.
 #pragma once
 
+#include <cuda_fp16.h>
+
 #include <cstdint>
 
 namespace vct {
@@ -81,6 +83,48 @@ __device__ __forceinline__ uint32_t aniso_rgba8_dir(int d, Child child) {
     o |= (v > 255u ? 255u : v) << (8 * q);
   }
   return o;
+}
+
+// ---- RGBA16F (half texels): the mean of the four blend(front, back) pairs
+// in FP32, rounded to half -- one definition, each operation rounded once
+// in a fixed order, so that the MipBuilder and the brick kernel's fused
+// levels give the same bits.
+__device__ __forceinline__ float4 h2f(uint2 t) {
+  __half2 a = *reinterpret_cast<__half2*>(&t.x), b = *reinterpret_cast<__half2*>(&t.y);
+  float2 fa = __half22float2(a), fb = __half22float2(b);
+  return make_float4(fa.x, fa.y, fb.x, fb.y);
+}
+__device__ __forceinline__ uint2 f2h(float4 v) {
+  __half2 a = __floats2half2_rn(v.x, v.y), b = __floats2half2_rn(v.z, v.w);
+  return make_uint2(*reinterpret_cast<uint32_t*>(&a), *reinterpret_cast<uint32_t*>(&b));
+}
+// acc += f + (1 - f.a) * b
+__device__ __forceinline__ void blend16(float4& acc, float4 f, float4 b) {
+  const float k = __fsub_rn(1.0f, f.w);
+  acc.x = __fadd_rn(acc.x, __fmaf_rn(k, b.x, f.x));
+  acc.y = __fadd_rn(acc.y, __fmaf_rn(k, b.y, f.y));
+  acc.z = __fadd_rn(acc.z, __fmaf_rn(k, b.z, f.z));
+  acc.w = __fadd_rn(acc.w, __fmaf_rn(k, b.w, f.w));
+}
+__device__ __forceinline__ uint2 finish16(float4 acc) {
+  return f2h(make_float4(__fmul_rn(acc.x, 0.25f), __fmul_rn(acc.y, 0.25f), __fmul_rn(acc.z, 0.25f),
+                         __fmul_rn(acc.w, 0.25f)));
+}
+// Direction d (run-time) of one destination texel whose children come from
+// child(k), the pairs summed in the order of c_pairs_h[d] (the order matters
+// in floating point: for the y maps the table takes its last two pairs the
+// other way round).
+template <class Child>
+__device__ __forceinline__ uint2 aniso_rgba16f_dir(int d, Child child) {
+  const int bit = 4 >> (d >> 1), sel = (d & 1) ? bit : 0;
+  float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+  for (int p = 0; p < 4; ++p) {
+    const int pp = bit == 2 ? (p ^ (p >> 1)) : p;
+    const int k = ((pp & (bit - 1)) | ((pp & ~(bit - 1)) << 1)) | sel;
+    blend16(acc, h2f(child(k)), h2f(child(k ^ bit)));
+  }
+  return finish16(acc);
 }
 
 }  // namespace vct
