@@ -70,6 +70,7 @@ struct vct_batch {
   size_t total_px = 0;
   // batch-wide work arrays
   DevBuf<uint32_t> brick_count, brick_offset, brick_cursor, pair_list, scan_tmp, bin_big_count, queue;
+  DevBuf<uint8_t> brick_dirty;  // BatchBuffers::dirty
   DevBuf<BinRec> bin_big;
   DevBuf<uint2> bin_rec;  // per padded batch triangle (counting -> filling pass)
   uint32_t bin_big_cap = 0;
@@ -135,6 +136,7 @@ struct vct_batch {
     bb.frame = frame.p;
     bb.heavy = kHeavySplit ? heavy.view() : HeavyBricks{};
     bb.bin_rec = bin_rec.p;
+    bb.dirty = brick_dirty.p;
     return bb;
   }
 
@@ -456,6 +458,8 @@ vct_status build_batch(vct_batch* b, const vct_batch_scene* descs, uint32_t n) {
   VCT_CHECK(b->brick_count.ensure(nbk));
   VCT_CHECK(b->brick_offset.ensure(nbk + 1));
   VCT_CHECK(b->brick_cursor.ensure(nbk));
+  VCT_CHECK(b->brick_dirty.ensure(nbk));
+  VCT_CUDA(cudaMemsetAsync(b->brick_dirty.p, 1, nbk, b->stream));  // the new maps: every brick writes once
   VCT_CHECK(b->heavy.reserve(nbk, 1024, 65536, b->stream));
   VCT_CHECK(b->scan_tmp.ensure(scan_tmp_words(nbk)));
   VCT_CHECK(b->pair_list.ensure((size_t)std::min<uint64_t>(0xffffff00ull, 4ull * total_tris + 65536ull)));
@@ -472,6 +476,7 @@ vct_status build_batch(vct_batch* b, const vct_batch_scene* descs, uint32_t n) {
   VCT_CHECK(b->d_status.ensure(1));
   VCT_CHECK(b->h_status.ensure(1));
   std::memset(b->h_status.p, 0, sizeof(FrameStatus));
+  VCT_CUDA(cudaStreamSynchronize(b->stream));  // (the set-up memsets, before the caller may change streams)
   return VCT_OK;
 }
 

@@ -1211,7 +1211,7 @@ __global__ void __launch_bounds__(kThreads, brick_min_blocks<MODE>()) k_bricks_b
     const BatchScene& S = w.scenes[s];
     brick_unit<MODE, STORAGE>(S.sp, S.N, g - __ldg(w.prefix + s), bb.brick_offset + S.brick_base, bb.pair_list,
                               bb.pair_cap, S.ms.l0_surf, nullptr, bb.status, acc, setup, excl, InjGrids{}, nullptr,
-                              &hb, g, chunk, item);
+                              &hb, g, chunk, item, nullptr, bb.dirty ? bb.dirty + S.brick_base : nullptr);
     __syncthreads();  // done with acc
   }
 }

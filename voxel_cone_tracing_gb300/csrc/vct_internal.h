@@ -277,6 +277,7 @@ struct BatchBuffers {
   uchar4* frame;
   HeavyBricks heavy;      // over the batch-wide (global) brick indices
   uint2* bin_rec;         // per (padded) batch triangle, as VoxBuffers::bin_rec
+  uint8_t* dirty;         // per batch brick (global index), as VoxBuffers::dirty
 };
 
 // Tunable launch shapes of the batched kernels (chosen by the autotuner).
