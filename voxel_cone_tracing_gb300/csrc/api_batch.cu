@@ -64,7 +64,11 @@ struct vct_batch {
   DevBuf<BatchScene> d_scenes;
   HostBuf<CameraParams> h_cams;
   DevBuf<CameraParams> d_cams;
-  Prefix tris, bricks, regions, tail5, tail6, tiles, occw;
+  Prefix tris, bricks, regions, tail4, tail5, tail6, tiles, occw;
+  // The brick kernel writes mip levels 1-3 (per-scene targets in d_mips);
+  // the mip pass then runs the tail levels from level 4.
+  bool fused = false;
+  DevBuf<BrickMips> d_mips;
   std::vector<uint32_t> brick_base;
   std::vector<size_t> px_base;
   size_t total_px = 0;
@@ -137,6 +141,7 @@ struct vct_batch {
     bb.heavy = kHeavySplit ? heavy.view() : HeavyBricks{};
     bb.bin_rec = bin_rec.p;
     bb.dirty = brick_dirty.p;
+    bb.mips = fused ? d_mips.p : nullptr;
     return bb;
   }
 
@@ -195,8 +200,15 @@ struct vct_batch {
     VCT_CUDA(launch_voxelize_batch(work(tris), wb, bricks.total(), cfg.vox_mode, VCT_STORAGE_RGBA8, bb,
                                    scan_tmp.p, shape, sms, stream, &launches));
     VCT_CUDA(record(1));
-    const BatchWork tail[2] = {work(tail5), work(tail6)};
-    VCT_CUDA(launch_mipmap_batch(work(regions), tail, 2, VCT_STORAGE_RGBA8, stream, &launches));
+    if (fused) {
+      BatchWork none = work(regions);
+      none.total = 0;
+      const BatchWork tail[3] = {work(tail4), work(tail5), work(tail6)};
+      VCT_CUDA(launch_mipmap_batch(none, tail, 3, 4, VCT_STORAGE_RGBA8, stream, &launches));
+    } else {
+      const BatchWork tail[2] = {work(tail5), work(tail6)};
+      VCT_CUDA(launch_mipmap_batch(work(regions), tail, 2, 5, VCT_STORAGE_RGBA8, stream, &launches));
+    }
     VCT_CUDA(launch_occupancy_batch(work(occw), stream, &launches));
     VCT_CUDA(record(2));
     VCT_CUDA(launch_gbuffer_batch(work(tris), work(tiles), total_px, bb, sms, stream, &launches));
@@ -401,7 +413,7 @@ vct_status build_batch(vct_batch* b, const vct_batch_scene* descs, uint32_t n) {
     VCT_CUDA(cudaStreamCreateWithFlags(&b->side[k], cudaStreamNonBlocking));
     VCT_CUDA(cudaEventCreateWithFlags(&b->join_ev[k], cudaEventDisableTiming));
   }
-  std::vector<uint32_t> c_tris, c_bricks, c_regions, c_tail5, c_tail6, c_tiles, c_occw;
+  std::vector<uint32_t> c_tris, c_bricks, c_regions, c_tail4, c_tail5, c_tail6, c_tiles, c_occw;
   uint64_t total_tris = 0;
   for (uint32_t i = 0; i < n; ++i) {
     b->scenes.emplace_back(new SceneRes());
@@ -412,7 +424,9 @@ vct_status build_batch(vct_batch* b, const vct_batch_scene* descs, uint32_t n) {
     c_bricks.push_back(nb * nb * nb);
     const uint32_t rg = (uint32_t)(r.N / 16);
     c_regions.push_back(rg * rg * rg);
+    const uint32_t s4 = r.L > 4 ? (uint32_t)(r.N >> 4) : 0u;
     const uint32_t s5 = r.L > 5 ? (uint32_t)(r.N >> 5) : 0u, s6 = r.L > 6 ? (uint32_t)(r.N >> 6) : 0u;
+    c_tail4.push_back(s4 * s4 * s4);
     c_tail5.push_back(s5 * s5 * s5);  // texels; a thread computes all six maps
     c_tail6.push_back(s6 * s6 * s6);
     c_tiles.push_back((uint32_t)((r.W + 15) / 16) * (uint32_t)((r.H + 15) / 16));
@@ -422,10 +436,29 @@ vct_status build_batch(vct_batch* b, const vct_batch_scene* descs, uint32_t n) {
   VCT_CHECK(make_prefix(b->tris, c_tris));
   VCT_CHECK(make_prefix(b->bricks, c_bricks));
   VCT_CHECK(make_prefix(b->regions, c_regions));
+  VCT_CHECK(make_prefix(b->tail4, c_tail4));
   VCT_CHECK(make_prefix(b->tail5, c_tail5));
   VCT_CHECK(make_prefix(b->tail6, c_tail6));
   VCT_CHECK(make_prefix(b->occw, c_occw));
   VCT_CHECK(make_prefix(b->tiles, c_tiles));
+  // fused mip levels 1-3 (every scene: RGBA8 anisotropic maps of >= 4 levels)
+  b->fused = kFuseBrickMips;
+  for (uint32_t i = 0; i < n && b->fused; ++i) b->fused = b->scenes[i]->maps.ms.L >= 4;
+  if (b->fused) {
+    std::vector<BrickMips> hm(n);
+    for (uint32_t i = 0; i < n; ++i) {
+      const MapSet& ms = b->scenes[i]->maps.ms;
+      BrickMips& bm = hm[i];
+      std::memset(&bm, 0, sizeof(bm));
+      for (int d = 0; d < 6; ++d)
+        for (int l = 1; l <= 3; ++l) bm.surf[d][l] = ms.surf[d][l];
+      bm.has_alpha = ms.alpha_tex[0] != 0;
+      for (int k = 0; k < 2 && bm.has_alpha; ++k)
+        for (int l = 1; l <= 3; ++l) bm.alpha[k][l] = ms.alpha_surf[k][l];
+      for (int l = 1; l <= 3 && ms.skip_empty; ++l) bm.occ_raw[l] = ms.occ_raw[l];
+    }
+    VCT_CHECK(upload(b->d_mips, hm.data(), hm.size()));
+  }
   // scene descriptors
   std::vector<BatchScene> hs(n);
   size_t px = 0;
@@ -435,6 +468,10 @@ vct_status build_batch(vct_batch* b, const vct_batch_scene* descs, uint32_t n) {
     std::memset(&s, 0, sizeof(s));
     s.sp = r.sp;
     s.ms = r.maps.ms;
+    if (b->fused) {  // occupancy bytes of levels 1-3 from the brick kernel; coarser ones ORed from level 3's
+      s.ms.occ_k = 3;
+      s.ms.occ_l1_packed = 0;
+    }
     s.tp = r.tp;
     s.N = r.N;
     s.W = r.W;

@@ -438,7 +438,8 @@ __global__ void __launch_bounds__(kThreads) k_mip_level_batch(BatchWork w, int l
 }
 
 template <int NMAPS, int STORAGE>
-cudaError_t run_batch(const BatchWork& regions, const BatchWork* tail, int n_tail, cudaStream_t st, int* launches) {
+cudaError_t run_batch(const BatchWork& regions, const BatchWork* tail, int n_tail, int first_tail, cudaStream_t st,
+                      int* launches) {
   typedef typename Texel<STORAGE>::T T;
   constexpr int B = 16;
   size_t smem = (size_t)B * B * B * sizeof(T);
@@ -460,7 +461,7 @@ cudaError_t run_batch(const BatchWork& regions, const BatchWork* tail, int n_tai
   for (int t = 0; t < n_tail; ++t) {
     if (!tail[t].total) continue;
     const unsigned grid = (unsigned)std::min<uint32_t>((tail[t].total + kThreads - 1) / kThreads, (uint32_t)sms * 8);
-    k_mip_level_batch<NMAPS, STORAGE><<<grid, kThreads, 0, st>>>(tail[t], 5 + t);
+    k_mip_level_batch<NMAPS, STORAGE><<<grid, kThreads, 0, st>>>(tail[t], first_tail + t);
     if (launches) ++*launches;
   }
   return cudaGetLastError();
@@ -742,12 +743,14 @@ cudaError_t launch_occupancy_batch(const BatchWork& words, cudaStream_t st, int*
 
 uint32_t occupancy_words(const MapSet& ms) { return ms.skip_empty && ms.L > 1 ? occ_words(ms) : 0u; }
 
-cudaError_t launch_mipmap_batch(const BatchWork& regions, const BatchWork* tail, int n_tail, int storage,
-                                cudaStream_t st, int* launches) {
+cudaError_t launch_mipmap_batch(const BatchWork& regions, const BatchWork* tail, int n_tail, int first_tail,
+                                int storage, cudaStream_t st, int* launches) {
   // Every scene of a batch is anisotropic (6 maps); levels 1..4 in the first
-  // launch, levels 5 and 6 (where a scene has them) in one launch each.
-  return storage == VCT_STORAGE_RGBA8 ? run_batch<6, VCT_STORAGE_RGBA8>(regions, tail, n_tail, st, launches)
-                                      : run_batch<6, VCT_STORAGE_RGBA16F>(regions, tail, n_tail, st, launches);
+  // launch (unless the brick kernel wrote 1-3), the tail levels (where a
+  // scene has them) in one launch each.
+  return storage == VCT_STORAGE_RGBA8
+             ? run_batch<6, VCT_STORAGE_RGBA8>(regions, tail, n_tail, first_tail, st, launches)
+             : run_batch<6, VCT_STORAGE_RGBA16F>(regions, tail, n_tail, first_tail, st, launches);
 }
 
 cudaError_t launch_fill_rgba8(cudaSurfaceObject_t s, int w, int h, int d, uchar4 v, cudaStream_t st) {

@@ -1181,8 +1181,9 @@ __global__ void __launch_bounds__(kThreads, FUSE ? 7 : brick_min_blocks<MODE>())
 // from the atomic counter w.queue (brick costs range from an empty brick to
 // thousands of triangle samples).  The queue hands out the extra chunks of
 // the split bricks first (global brick indices), then the bricks.
-template <int MODE, int STORAGE>
-__global__ void __launch_bounds__(kThreads, brick_min_blocks<MODE>()) k_bricks_batch(BatchWork w, BatchBuffers bb) {
+template <int MODE, int STORAGE, bool FUSE = false>
+__global__ void __launch_bounds__(kThreads, FUSE ? 7 : brick_min_blocks<MODE>())
+    k_bricks_batch(BatchWork w, BatchBuffers bb) {
   __shared__ AccT<STORAGE> acc;
   __shared__ SetupOf<MODE> setup[kSetupSlots];
   __shared__ int excl[kExclSlots];
@@ -1211,7 +1212,8 @@ __global__ void __launch_bounds__(kThreads, brick_min_blocks<MODE>()) k_bricks_b
     const BatchScene& S = w.scenes[s];
     brick_unit<MODE, STORAGE>(S.sp, S.N, g - __ldg(w.prefix + s), bb.brick_offset + S.brick_base, bb.pair_list,
                               bb.pair_cap, S.ms.l0_surf, nullptr, bb.status, acc, setup, excl, InjGrids{}, nullptr,
-                              &hb, g, chunk, item, nullptr, bb.dirty ? bb.dirty + S.brick_base : nullptr);
+                              &hb, g, chunk, item, FUSE ? bb.mips + s : nullptr,
+                              bb.dirty ? bb.dirty + S.brick_base : nullptr);
     __syncthreads();  // done with acc
   }
 }
@@ -1450,9 +1452,13 @@ cudaError_t launch_voxelize_batch(const BatchWork& tris, const BatchWork& bricks
   const HeavyBricks& hb = bb.heavy;
   // The persistent brick grid (bricks + at most item_cap extra chunks).
   unsigned grid = 1;
+  const bool fuse_mips = bb.mips != nullptr && storage == VCT_STORAGE_RGBA8;
   dispatch_bricks(mode, storage, false, [&](auto mode_tag, auto storage_tag) {
-    grid = resident_grid(k_bricks_batch<decltype(mode_tag)::value, decltype(storage_tag)::value>, kThreads, 0, sms,
-                         shape.bricks_ctas_per_sm, bricks.total + (hb.slot ? hb.item_cap : 0u));
+    constexpr int M = decltype(mode_tag)::value, S = decltype(storage_tag)::value;
+    grid = fuse_mips ? resident_grid(k_bricks_batch<M, S, true>, kThreads, 0, sms, shape.bricks_ctas_per_sm,
+                                bricks.total + (hb.slot ? hb.item_cap : 0u))
+                : resident_grid(k_bricks_batch<M, S>, kThreads, 0, sms, shape.bricks_ctas_per_sm,
+                                bricks.total + (hb.slot ? hb.item_cap : 0u));
   });
   cudaError_t e = cudaMemsetAsync(bb.brick_count, 0, (size_t)total_bricks * sizeof(uint32_t), st);
   if (e != cudaSuccess) return e;
@@ -1488,7 +1494,9 @@ cudaError_t launch_voxelize_batch(const BatchWork& tris, const BatchWork& bricks
   e = cudaMemsetAsync(bricks.queue, 0, sizeof(uint32_t), st);
   if (e != cudaSuccess) return e;
   dispatch_bricks(mode, storage, false, [&](auto mode_tag, auto storage_tag) {
-    k_bricks_batch<decltype(mode_tag)::value, decltype(storage_tag)::value><<<grid, kThreads, 0, st>>>(bricks, bb);
+    constexpr int M = decltype(mode_tag)::value, S = decltype(storage_tag)::value;
+    if (fuse_mips) k_bricks_batch<M, S, true><<<grid, kThreads, 0, st>>>(bricks, bb);
+    else k_bricks_batch<M, S><<<grid, kThreads, 0, st>>>(bricks, bb);
   });
   ++nl;
   if (launches) *launches += nl;

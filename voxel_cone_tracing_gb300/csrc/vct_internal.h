@@ -278,6 +278,7 @@ struct BatchBuffers {
   HeavyBricks heavy;      // over the batch-wide (global) brick indices
   uint2* bin_rec;         // per (padded) batch triangle, as VoxBuffers::bin_rec
   uint8_t* dirty;         // per batch brick (global index), as VoxBuffers::dirty
+  const BrickMips* mips;  // per scene: the brick kernel writes levels 1-3 too (null: off)
 };
 
 // Tunable launch shapes of the batched kernels (chosen by the autotuner).
@@ -395,8 +396,11 @@ cudaError_t launch_voxelize_batch(const BatchWork& tris, const BatchWork& bricks
 // their batch pass (one work item per word of every scene).
 uint32_t occupancy_words(const MapSet& ms);
 cudaError_t launch_occupancy_batch(const BatchWork& words, cudaStream_t st, int* launches);
-cudaError_t launch_mipmap_batch(const BatchWork& regions, const BatchWork* tail, int n_tail, int storage,
-                                cudaStream_t st, int* launches);
+// regions: the first pass's 16^3 regions of level 0 (levels 1-4; empty when
+// the brick kernel wrote levels 1-3); tail[t]: the texels of level
+// first_tail + t of every scene.
+cudaError_t launch_mipmap_batch(const BatchWork& regions, const BatchWork* tail, int n_tail, int first_tail,
+                                int storage, cudaStream_t st, int* launches);
 cudaError_t launch_gbuffer_batch(const BatchWork& tris, const BatchWork& tiles, size_t total_px,
                                  const BatchBuffers& bb, int sms, cudaStream_t st, int* launches);
 // share: every scene shares the far fields of its diffuse cones (the batch's
