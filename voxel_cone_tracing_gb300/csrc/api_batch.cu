@@ -59,7 +59,7 @@ struct vct_batch {
   vct_batch_config cfg;
   std::vector<std::unique_ptr<SceneRes>> scenes;
   int sms = 148;
-  BatchShape shape = {8, 8, 3, 1, 1, 8};
+  BatchShape shape = {8, 8, 3, 1, 1, 16};  // (16-row trace tiles, as a Renderer's)
   // device descriptors
   DevBuf<BatchScene> d_scenes;
   HostBuf<CameraParams> h_cams;
