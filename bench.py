@@ -78,34 +78,54 @@ def _dist():
 
 
 class ClockSampler:
-    """nvidia-smi clock / throttle-reason samples during the timed region."""
+    """nvidia-smi clock / throttle-reason samples around the timed region.
+
+    The sampler starts before the warm-up and waits for nvidia-smi's first
+    line (its start-up takes longer than a short timed region), then polls
+    every ``interval_ms``; ``start()`` and
+    ``stop()`` mark the timed region on the host clock, and the summary keeps
+    the samples that arrived inside it (plus one polling interval after it,
+    the sample taken while its last frame ran)."""
 
     FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
-    def __init__(self, gpu_index: int):
+    def __init__(self, gpu_index: int, interval_ms: int = 20):
         self.gpu = gpu_index
+        self.interval = interval_ms
         self.proc = None
         self.lines = []
+        self.t0 = self.t1 = None
 
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
-                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+                 "-lms", str(self.interval)], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
+            deadline = time.perf_counter() + 5.0   # first line before the warm-up starts
+            while not self.lines and self.proc.poll() is None and time.perf_counter() < deadline:
+                time.sleep(0.005)
         except Exception:
             self.proc = None
         return self
 
     def _read(self):
         for line in self.proc.stdout:
-            self.lines.append(line.strip())
+            self.lines.append((time.perf_counter(), line.strip()))
+
+    def start(self):
+        self.t0 = time.perf_counter()
+
+    def stop(self):
+        self.t1 = time.perf_counter()
 
     def __exit__(self, *a):
         if self.proc is not None:
+            if self.t1 is not None:  # let the sample that covers the region's end arrive
+                time.sleep(max(0.0, self.t1 + 3 * self.interval / 1000.0 - time.perf_counter()))
             self.proc.terminate()
             try:
                 self.proc.wait(timeout=5)
@@ -115,7 +135,11 @@ class ClockSampler:
     def summary(self):
         sm, mx, reasons = [], None, set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in self.lines:
+        lo = self.t0 if self.t0 is not None else float("-inf")
+        hi = self.t1 + self.interval / 1000.0 if self.t1 is not None else float("inf")
+        for t, ln in list(self.lines):
+            if not lo <= t <= hi:
+                continue
             f = [x.strip() for x in ln.split(",")]
             if len(f) < 8:
                 continue
@@ -129,7 +153,11 @@ class ClockSampler:
                     reasons.add(name)
         if not sm:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
-        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+        out = {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm),
+               "interval_ms": self.interval}
+        if self.t0 is not None and self.t1 is not None:
+            out["region_ms"] = round((self.t1 - self.t0) * 1000.0, 1)
+        return out
 
 
 def _scene():
@@ -557,16 +585,17 @@ def run_ours(args):
         R.queue_scene(r, scene, ids)
         r.render()
 
-    for _ in range(max(args.warmup, 3)):
-        frame()
-    r.synchronize()
-    if pg:
-        pg.barrier()
-    torch.cuda.synchronize()
     starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     stages = []
     with ClockSampler(local) as clk:
+        for _ in range(max(args.warmup, 3)):
+            frame()
+        r.synchronize()
+        if pg:
+            pg.barrier()
+        torch.cuda.synchronize()
+        clk.start()
         for k in range(args.steps):
             with torch.cuda.stream(stream):
                 flush.zero_()          # L2 flush, outside the timed pair
@@ -576,6 +605,7 @@ def run_ours(args):
             r.synchronize()
             stages.append(r.stage_times())
         torch.cuda.synchronize()
+        clk.stop()
     if pg:
         pg.barrier()
     frame_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]

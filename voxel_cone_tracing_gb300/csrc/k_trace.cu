@@ -2,8 +2,7 @@
 // voxel_cone_tracing.frag (main :246-275) over the G-buffer.
 //
 // One thread shades one visible pixel; a k_trace CTA covers a 16x8 pixel
-// tile (each warp a 16x2 strip), a shared-far-field CTA a 16x16 tile of 8x4
-// warp blocks, so that neighbouring lanes march neighbouring, nearly
+// tile of 8x4 warp blocks, a shared-far-field CTA a 16x16 tile of them, so that neighbouring lanes march neighbouring, nearly
 // parallel cones and hit the same texture-cache lines.
 //
 // This file is compiled with -fmad=false: a product and a sum are fused only
@@ -49,16 +48,23 @@ __device__ __forceinline__ float4 fma4(float4 a, float s, float4 c) {
 #ifndef VCT_TRACE_MIN_BLOCKS
 #define VCT_TRACE_MIN_BLOCKS 12
 #endif
-// A k_trace CTA shades a 16 x kTraceRows pixel tile (each warp a 16x2
-// strip); the texture-unit variant is compiled for kTraceMinBlocks resident
+// A k_trace CTA shades a 16 x kTraceRows pixel tile (each warp a
+// kTraceWarpW x (32 / kTraceWarpW) block); the texture-unit variant is compiled for kTraceMinBlocks resident
 // CTAs per SM (register budget 65536 / (16 * rows * blocks) per thread).
 // Measured on the 1080p bench frame (trace ms): 128 threads x 12 CTAs (40
 // registers, 48 warps per SM) 2.59; x 9 (56 registers) 2.64; 256 threads
 // x 4 (64 registers) 2.71, x 6 (40) 2.62; 32 registers 3.77 (spills);
-// 64-thread CTAs x 22 2.98.
+// 64-thread CTAs x 22 2.98. Warps of 8x4 pixels instead of 16x2 strips:
+// 2.536 vs 2.543 (the same frame bit for bit).
 constexpr int kTraceRows = VCT_TRACE_ROWS;
 constexpr int kTraceThreads = 16 * kTraceRows;
 constexpr int kTraceMinBlocks = VCT_TRACE_MIN_BLOCKS;
+#ifndef VCT_TRACE_WARP_W
+#define VCT_TRACE_WARP_W 8
+#endif
+constexpr int kTraceWarpW = VCT_TRACE_WARP_W;
+static_assert((kTraceWarpW == 8 || kTraceWarpW == 16) && kTraceRows % (32 / kTraceWarpW) == 0,
+              "a k_trace tile holds whole warp blocks");
 #ifndef VCT_TRACE_BATCH_MIN_BLOCKS
 #define VCT_TRACE_BATCH_MIN_BLOCKS 3
 #endif
@@ -918,8 +924,11 @@ template <int SAMPLER, bool ISO, int STORAGE>
 __global__ void __launch_bounds__(kTraceThreads, SAMPLER == VCT_SAMPLER_HW ? kTraceMinBlocks : 1)
     k_trace(SceneParams sp, CameraParams cp, MapSet m, TraceParams tp, const float4* __restrict__ gb_pos,
             const float4* __restrict__ gb_nrm, uchar4* __restrict__ frame, float4* __restrict__ frame_f32) {
-  trace_px<SAMPLER, ISO, STORAGE>(sp, cp, m, tp, gb_pos, gb_nrm, frame, frame_f32, blockIdx.x * 16 + (threadIdx.x & 15),
-                                  blockIdx.y * kTraceRows + (threadIdx.x >> 4));
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  trace_px<SAMPLER, ISO, STORAGE>(
+      sp, cp, m, tp, gb_pos, gb_nrm, frame, frame_f32,
+      blockIdx.x * 16 + (w % (16 / kTraceWarpW)) * kTraceWarpW + lane % kTraceWarpW,
+      blockIdx.y * kTraceRows + (w / (16 / kTraceWarpW)) * (32 / kTraceWarpW) + lane / kTraceWarpW);
 }
 
 #ifndef VCT_SHARE_MIN_BLOCKS
