@@ -341,10 +341,10 @@ __global__ void __launch_bounds__(kThreads, STORAGE == VCT_STORAGE_RGBA8 ? VCT_M
   typedef typename Texel<STORAGE>::T T;
   constexpr int B3 = kTmaBox * kTmaBox * kTmaBox;
   constexpr uint32_t kBytes = B3 * sizeof(T);
-  extern __shared__ __align__(128) unsigned char smem_raw[];
+  extern __shared__ __align__(128) unsigned char smem_tma[];
   __shared__ __align__(8) uint64_t bar[2];
   // Copy destinations 128-byte aligned (the launch adds 128 bytes of slack).
-  unsigned char* base = smem_raw + ((128u - (smem_u32(smem_raw) & 127u)) & 127u);
+  unsigned char* base = smem_tma + ((128u - (smem_u32(smem_tma) & 127u)) & 127u);
   T* stage[2] = {reinterpret_cast<T*>(base), reinterpret_cast<T*>(base + kBytes)};
   T* lvl = reinterpret_cast<T*>(base + 2 * kBytes);
   const int nbx = ms.N / kTmaBox;

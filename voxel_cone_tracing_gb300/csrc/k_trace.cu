@@ -714,47 +714,47 @@ __device__ void far_fields(const MapSet& m, FarWarp& fw, int cone_set, int nq, f
         }
       }
     }
-    return;
-  }
-  for (;;) {
-    const unsigned need = __ballot_sync(0xffffffffu, !active);
-    if (need && next < n_jobs) {
-      const int job = next + __popc(need & ((1u << lane) - 1u));
-      if (!active && job < n_jobs) {
-        const int k = job / nq, q = job - k * nq;
-        res = q * K + k;
-        const float4 jb = fw.job[job];
-        dir = v3(jb.x, jb.y, jb.z);
-        stop = jb.w;
-        origin = v3(fw.origin[q][0], fw.origin[q][1], fw.origin[q][2]);
-        ix = dir.x < 0.0f ? 0 : 1;
-        iy = dir.y < 0.0f ? 2 : 3;
-        iz = dir.z < 0.0f ? 4 : 5;
-        ad = vabs(dir);
-        dist = dist1;
-        diam = diam1;
-        check = !march_sane(origin, dir, stop);
-        acc = f4(0.f, 0.f, 0.f, 0.f);
-        active = dist < stop;
-        if (!active) fw.far[res] = acc;
+  } else {
+    for (;;) {
+      const unsigned need = __ballot_sync(0xffffffffu, !active);
+      if (need && next < n_jobs) {
+        const int job = next + __popc(need & ((1u << lane) - 1u));
+        if (!active && job < n_jobs) {
+          const int k = job / nq, q = job - k * nq;
+          res = q * K + k;
+          const float4 jb = fw.job[job];
+          dir = v3(jb.x, jb.y, jb.z);
+          stop = jb.w;
+          origin = v3(fw.origin[q][0], fw.origin[q][1], fw.origin[q][2]);
+          ix = dir.x < 0.0f ? 0 : 1;
+          iy = dir.y < 0.0f ? 2 : 3;
+          iz = dir.z < 0.0f ? 4 : 5;
+          ad = vabs(dir);
+          dist = dist1;
+          diam = diam1;
+          check = !march_sane(origin, dir, stop);
+          acc = f4(0.f, 0.f, 0.f, 0.f);
+          active = dist < stop;
+          if (!active) fw.far[res] = acc;
+        }
+        next += __popc(need);
       }
-      next += __popc(need);
-    }
-    if (!__any_sync(0xffffffffu, active)) break;
-    if (active) {
-      const V3 sp = march_pos(origin, dir, dist);
-      const float mip = cone_lod(diam * cube_res);
-      if (!(kSkipEmptyRGBA && m.skip_empty && mip < kSkipMaxLod && sample_empty(m, sp, mip)) &&
-          !(check && !u_sane(sp))) {
-        const float4 smp = sample_voxel<VCT_SAMPLER_HW, ISO, VCT_STORAGE_RGBA8, false>(m, sp, ix, iy, iz, ad, mip);
-        acc = fma4(smp, 1.0f - acc.w, acc);
-      }
-      const float step = fmaxf(diam * 0.5f, voxel_size);
-      dist += step;
-      diam = dist * ap;
-      if (!(acc.w < 1.0f) || !(dist < stop)) {
-        fw.far[res] = acc;
-        active = false;
+      if (!__any_sync(0xffffffffu, active)) break;
+      if (active) {
+        const V3 sp = march_pos(origin, dir, dist);
+        const float mip = cone_lod(diam * cube_res);
+        if (!(kSkipEmptyRGBA && m.skip_empty && mip < kSkipMaxLod && sample_empty(m, sp, mip)) &&
+            !(check && !u_sane(sp))) {
+          const float4 smp = sample_voxel<VCT_SAMPLER_HW, ISO, VCT_STORAGE_RGBA8, false>(m, sp, ix, iy, iz, ad, mip);
+          acc = fma4(smp, 1.0f - acc.w, acc);
+        }
+        const float step = fmaxf(diam * 0.5f, voxel_size);
+        dist += step;
+        diam = dist * ap;
+        if (!(acc.w < 1.0f) || !(dist < stop)) {
+          fw.far[res] = acc;
+          active = false;
+        }
       }
     }
   }

@@ -803,45 +803,45 @@ __device__ __forceinline__ void brick_accumulate(const SceneParams& sp, int N, c
       }
       __syncthreads();  // the round's setups and offsets are free again
     }
-    return;
-  }
-  // Rounds of up to kWarps * 32 pairs, split evenly between the warps (a
-  // brick with a few dozen pairs keeps every warp busy expanding samples).
-  for (uint32_t b0 = beg; b0 < end; b0 += kWarps * 32) {
-    const uint32_t n = min((uint32_t)(kWarps * 32), end - b0);
-    const uint32_t q = (n + kWarps - 1) / kWarps;
-    const uint32_t k = warp * q + lane;
-    const uint32_t e = b0 + k;
-    int cnt = 0;
-    if (lane < q && k < n) {
-      if (MODE == VCT_VOX_CONSERVATIVE)
-        cnt = setup_sat(sp, N, __ldg(list + e), b3, reinterpret_cast<SetupSat&>(setup[warp * 32 + lane]));
-      else
-        cnt = setup_ref(sp, N, __ldg(list + e), b3, reinterpret_cast<SetupRef&>(setup[warp * 32 + lane]));
-    }
-    int incl = cnt;
-    for (int o = 1; o < 32; o <<= 1) {
-      int v = __shfl_up_sync(0xffffffffu, incl, o);
-      if (lane >= o) incl += v;
-    }
-    excl[warp * 33 + lane] = incl - cnt;
-    const int total = __shfl_sync(0xffffffffu, incl, 31);
-    __syncwarp();
-    for (int it = lane; it < total; it += 32) {
-      int lo = 0, hi = 31;  // owner = last lane with excl <= it
-      while (lo < hi) {
-        int mid = (lo + hi + 1) >> 1;
-        if (excl[warp * 33 + mid] <= it) lo = mid; else hi = mid - 1;
+  } else {
+    // Rounds of up to kWarps * 32 pairs, split evenly between the warps (a
+    // brick with a few dozen pairs keeps every warp busy expanding samples).
+    for (uint32_t b0 = beg; b0 < end; b0 += kWarps * 32) {
+      const uint32_t n = min((uint32_t)(kWarps * 32), end - b0);
+      const uint32_t q = (n + kWarps - 1) / kWarps;
+      const uint32_t k = warp * q + lane;
+      const uint32_t e = b0 + k;
+      int cnt = 0;
+      if (lane < q && k < n) {
+        if (MODE == VCT_VOX_CONSERVATIVE)
+          cnt = setup_sat(sp, N, __ldg(list + e), b3, reinterpret_cast<SetupSat&>(setup[warp * 32 + lane]));
+        else
+          cnt = setup_ref(sp, N, __ldg(list + e), b3, reinterpret_cast<SetupRef&>(setup[warp * 32 + lane]));
       }
-      const int local = it - excl[warp * 33 + lo];
-      if (MODE == VCT_VOX_CONSERVATIVE)
-        item_sat(sp, N, b3, reinterpret_cast<const SetupSat&>(setup[warp * 32 + lo]), local, acc);
-      else
-        item_ref(sp, N, b3, reinterpret_cast<const SetupRef&>(setup[warp * 32 + lo]), local, acc);
+      int incl = cnt;
+      for (int o = 1; o < 32; o <<= 1) {
+        int v = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += v;
+      }
+      excl[warp * 33 + lane] = incl - cnt;
+      const int total = __shfl_sync(0xffffffffu, incl, 31);
+      __syncwarp();
+      for (int it = lane; it < total; it += 32) {
+        int lo = 0, hi = 31;  // owner = last lane with excl <= it
+        while (lo < hi) {
+          int mid = (lo + hi + 1) >> 1;
+          if (excl[warp * 33 + mid] <= it) lo = mid; else hi = mid - 1;
+        }
+        const int local = it - excl[warp * 33 + lo];
+        if (MODE == VCT_VOX_CONSERVATIVE)
+          item_sat(sp, N, b3, reinterpret_cast<const SetupSat&>(setup[warp * 32 + lo]), local, acc);
+        else
+          item_ref(sp, N, b3, reinterpret_cast<const SetupRef&>(setup[warp * 32 + lo]), local, acc);
+      }
+      __syncwarp();
     }
-    __syncwarp();
+    __syncthreads();
   }
-  __syncthreads();
 }
 
 // ---- fused mip levels 1-3 (six maps, RGBA8 or RGBA16F; BrickMips) ---------
