@@ -55,7 +55,7 @@ __device__ __forceinline__ float4 fma4(float4 a, float s, float4 c) {
 // registers, 48 warps per SM) 2.59; x 9 (56 registers) 2.64; 256 threads
 // x 4 (64 registers) 2.71, x 6 (40) 2.62; 32 registers 3.77 (spills);
 // 64-thread CTAs x 22 2.98. Warps of 8x4 pixels instead of 16x2 strips:
-// 2.536 vs 2.543 (the same frame bit for bit).
+// 2.536 vs 2.543 alternating on one GPU, within noise across GPUs (same frame).
 constexpr int kTraceRows = VCT_TRACE_ROWS;
 constexpr int kTraceThreads = 16 * kTraceRows;
 constexpr int kTraceMinBlocks = VCT_TRACE_MIN_BLOCKS;
