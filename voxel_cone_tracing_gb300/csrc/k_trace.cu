@@ -587,11 +587,20 @@ constexpr int kShareQuads = 16 / kShareW;  // groups of a warp
 constexpr int kShareCones = 9;
 constexpr int kShareJobs = kShareQuads * kShareCones;
 
+// Order of a warp's far-field jobs: 1 = the jobs that start after the
+// first 32 (the last lanes to finish wait for them) are those with the
+// shortest exit distance, so the warp's tail is short; 0 = cone-major order.
+#ifndef VCT_FAR_SHORT_TAIL
+#define VCT_FAR_SHORT_TAIL 1
+#endif
+constexpr bool kFarShortTail = VCT_FAR_SHORT_TAIL != 0;
+
 struct FarWarp {
   float4 far[kShareJobs];   // far field of cone k of group slot q at q * K + k
   float4 job[kShareJobs];   // job j = k * nq + q: unit direction, exit distance
   float origin[kShareQuads][3];  // representative's texture-space position
   float normal[kShareQuads][3];  // and normal
+  uint8_t order[kShareJobs];     // the job handed out n-th
 };
 
 // Direction (unnormalised) and aperture of diffuse cone k, as trace_diffuse
@@ -637,6 +646,44 @@ __device__ void far_fields(const MapSet& m, FarWarp& fw, int cone_set, int nq, f
     fw.job[j] = f4(d.x, d.y, d.z, exit_distance(m, o, d, kMaxDistance));
   }
   __syncwarp();
+  {
+    // Jobs 0..31 start together; the n_jobs - 32 handed out after them
+    // (kShareJobs - 32 at most) are swapped for the jobs of shortest exit
+    // distance -- the cones that reach least far, nearly always the shortest
+    // marches -- picked by warp min-reductions of (distance, job) keys.
+    // Which lane marches a job changes nothing in its result.
+    static_assert(kShareJobs <= 64, "job index in 6 bits");
+    const int n_tail = n_jobs - 32;
+    uint64_t tail = 0;  // warp-uniform: the jobs chosen for the tail
+    if (kFarShortTail && n_tail > 0) {
+      auto key = [&](int j) {
+        return j < n_jobs ? (__float_as_uint(fmaxf(fw.job[j].w, 0.0f)) & ~63u) | (unsigned)j : ~0u;
+      };
+      unsigned k0 = key(lane), k1 = key(lane + 32);
+      for (int t = 0; t < n_tail; ++t) {
+        const unsigned mn = __reduce_min_sync(0xffffffffu, min(k0, k1));
+        tail |= 1ull << (mn & 63u);
+        if (k0 == mn) k0 = ~0u;
+        if (k1 == mn) k1 = ~0u;
+      }
+    }
+    // chosen jobs among 0..31 trade places, in order, with the jobs at 32..
+    // that were not chosen
+    // (no choice made: a = b = 0, every job keeps its place)
+    const uint32_t a = (uint32_t)tail;
+    const uint32_t b = tail ? ~(uint32_t)(tail >> 32) & ((1u << n_tail) - 1u) : 0u;
+    auto nth = [](uint32_t mask, int i) {  // the i-th set bit of mask
+      for (; i > 0; --i) mask &= mask - 1u;
+      return __ffs(mask) - 1;
+    };
+    for (int j = lane; j < n_jobs; j += 32) {
+      int o = j;
+      if (j < 32 && ((a >> j) & 1u)) o = 32 + nth(b, __popc(a & ((1u << j) - 1u)));
+      if (j >= 32 && ((b >> (j - 32)) & 1u)) o = nth(a, __popc(b & ((1u << (j - 32)) - 1u)));
+      fw.order[j] = (uint8_t)o;
+    }
+  }
+  __syncwarp();
   const float ap = cone_set == VCT_CONES_SIX60 ? 1.15470053838f : kTan22_5;
   const float cube_res = (float)m.N;
   const float voxel_size = 1.0f / cube_res;
@@ -663,9 +710,10 @@ __device__ void far_fields(const MapSet& m, FarWarp& fw, int cone_set, int nq, f
       if (need && next < n_jobs) {
         const int job = next + __popc(need & ((1u << lane) - 1u));
         if (!active && job < n_jobs) {
-          const int k = job / nq, q = job - k * nq;
+          const int jo = fw.order[job];
+          const int k = jo / nq, q = jo - k * nq;
           res = q * K + k;
-          const float4 jb = fw.job[job];
+          const float4 jb = fw.job[jo];
           dir = v3(jb.x, jb.y, jb.z);
           stop = jb.w;
           origin = v3(fw.origin[q][0], fw.origin[q][1], fw.origin[q][2]);
@@ -720,9 +768,10 @@ __device__ void far_fields(const MapSet& m, FarWarp& fw, int cone_set, int nq, f
       if (need && next < n_jobs) {
         const int job = next + __popc(need & ((1u << lane) - 1u));
         if (!active && job < n_jobs) {
-          const int k = job / nq, q = job - k * nq;
+          const int jo = fw.order[job];
+          const int k = jo / nq, q = jo - k * nq;
           res = q * K + k;
-          const float4 jb = fw.job[job];
+          const float4 jb = fw.job[jo];
           dir = v3(jb.x, jb.y, jb.z);
           stop = jb.w;
           origin = v3(fw.origin[q][0], fw.origin[q][1], fw.origin[q][2]);
